@@ -1,0 +1,262 @@
+/*
+ * cassia_gb300 — GB300-native (sm_103a) surpass/mold rasterize -> sort -> paint.
+ *
+ * C ABI.  Plain pointers and sizes only.  Every call returns a cgb_status.
+ * A composition handle is single-threaded; distinct handles may be used from
+ * distinct threads.  Caller-owned arrays are copied during the call.
+ *
+ * The entry points mirror the reference's two seams:
+ *   - mold's Composition / Layer / Path / Props API
+ *     (mold/src/composition.rs:26-329, mold/src/layer.rs:145-244,
+ *      mold/src/path/mod.rs:25-179, surpass/src/painter/style.rs:189-432),
+ *     which drives surpass's LinesBuilder::build -> Rasterizer::rasterize ->
+ *     Rasterizer::sort -> BufferLayout::print;
+ *   - cassia's headless consumer of sorted pixel segments
+ *     (cassia/src/Cassia.h:25-41).
+ * Each declaration cites the reference interface it replaces.
+ */
+#ifndef CASSIA_GB300_H
+#define CASSIA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(_WIN32)
+#define CGB_EXPORT __declspec(dllexport)
+#else
+#define CGB_EXPORT __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ----------------------------------------------------------- */
+typedef int32_t cgb_status;
+#define CGB_OK 0
+#define CGB_ERR_INVALID_ARG 1    /* bad pointer, size, id or enum value */
+#define CGB_ERR_OUT_OF_MEMORY 2  /* cudaMalloc / host allocation failed */
+#define CGB_ERR_OVER_BUDGET 3    /* the handle's HBM budget would be exceeded */
+#define CGB_ERR_LAYER_LIMIT 4    /* more layers / tiles than the segment format holds */
+#define CGB_ERR_DEVICE_TIMEOUT 5 /* a bounded device-side wait expired (no hang) */
+#define CGB_ERR_DEVICE 6         /* a CUDA runtime error */
+#define CGB_ERR_NO_DEVICE 7      /* no CUDA device visible */
+#define CGB_ERR_CAPACITY 8       /* caller's output array is too small (size reported) */
+#define CGB_ERR_NOT_FOUND 9      /* unknown layer id / cache id */
+#define CGB_ERR_SCALE 10         /* mold Layer::set_transform scale check (mold/src/layer.rs:186-190) */
+
+/* ---- enums (values are the reference's enum order) -------------------------- */
+/* surpass FillRule (surpass/src/painter/style.rs:10-13) */
+#define CGB_FILL_NONZERO 0u
+#define CGB_FILL_EVENODD 1u
+/* surpass BlendMode (surpass/src/painter/style.rs:190-203) */
+#define CGB_BLEND_OVER 0u
+#define CGB_BLEND_MULTIPLY 1u
+#define CGB_BLEND_SCREEN 2u
+#define CGB_BLEND_OVERLAY 3u
+#define CGB_BLEND_DARKEN 4u
+#define CGB_BLEND_LIGHTEN 5u
+#define CGB_BLEND_COLOR_DODGE 6u
+#define CGB_BLEND_COLOR_BURN 7u
+#define CGB_BLEND_HARD_LIGHT 8u
+#define CGB_BLEND_SOFT_LIGHT 9u
+#define CGB_BLEND_DIFFERENCE 10u
+#define CGB_BLEND_EXCLUSION 11u
+/* surpass painter Func (surpass/src/painter/mod.rs:125-129) */
+#define CGB_FUNC_DRAW 0u
+#define CGB_FUNC_CLIP 1u
+/* surpass Fill (surpass/src/painter/style.rs:177-181) */
+#define CGB_FILL_SOLID 0u
+#define CGB_FILL_GRADIENT 1u
+/* surpass GradientType (surpass/src/painter/style.rs:21-25) */
+#define CGB_GRADIENT_LINEAR 0u
+#define CGB_GRADIENT_RADIAL 1u
+
+/* mold PathCommand (mold/src/path/mod.rs:13-21).  Floats per command, in the
+ * argument order of mold's Path methods (mold/src/path/mod.rs:53-170):
+ *   LINE      4: x0 y0 x1 y1
+ *   QUAD      6: x0 y0 x1 y1 x2 y2
+ *   RAT_QUAD  9: x0 y0 w0 x1 y1 w1 x2 y2 w2     (points are NOT pre-weighted)
+ *   CUBIC     8: x0 y0 .. x3 y3
+ *   RAT_CUBIC 12: x0 y0 w0 .. x3 y3 w3
+ *   CLOSE     0 */
+#define CGB_CMD_LINE 0u
+#define CGB_CMD_QUAD 1u
+#define CGB_CMD_RAT_QUAD 2u
+#define CGB_CMD_CUBIC 3u
+#define CGB_CMD_RAT_CUBIC 4u
+#define CGB_CMD_CLOSE 5u
+
+/* composition flags */
+/* Widened segment format: layer field 17 bits (131,072 orders) in place of the
+ * reference's is_none bit; every other field keeps its width and order.  Used
+ * for scenes with more than 65,536 layer orders (the reference's u16 limit,
+ * mold/src/layer.rs:13, surpass/src/rasterizer/raster_segment.rs:148). */
+#define CGB_COMPOSITION_WIDE_LAYERS 1u
+
+/* layer transform flags */
+/* Skip mold's per-axis scale <= ~1 check (mold/src/layer.rs:186-190) and store
+ * the affine directly in surpass::Layer::affine_transform
+ * (surpass/src/layer.rs:8), which has no such limit. */
+#define CGB_TRANSFORM_UNCHECKED 1u
+
+/* pixel_segments ordering */
+#define CGB_SORT_CANONICAL 0u /* ascending by the full u64 (a refinement of the reference order) */
+#define CGB_SORT_KEY 1u       /* ascending by u64 >> 22, ties in rasterizer order (stable) */
+
+/* ---- plain-data types ---------------------------------------------------------- */
+
+/* surpass painter Props { fill_rule, func: Draw(Style) | Clip(usize) }
+ * (surpass/src/painter/mod.rs:125-141) with Style { fill_rule, is_clipped,
+ * fill: Solid([f32;4]) | Gradient, blend_mode } (style.rs:427-432).
+ * Gradient stops are (r, g, b, a, stop) tuples; a stop < 0 (or -0.0) means
+ * "no stop" and is spread evenly as GradientBuilder::build does
+ * (style.rs:66-84). */
+typedef struct cgb_props {
+    uint32_t fill_rule;     /* CGB_FILL_NONZERO | CGB_FILL_EVENODD */
+    uint32_t func;          /* CGB_FUNC_DRAW | CGB_FUNC_CLIP */
+    uint32_t clip_layers;   /* Func::Clip(n) */
+    uint32_t is_clipped;    /* Style::is_clipped */
+    uint32_t blend_mode;    /* CGB_BLEND_* */
+    uint32_t fill_kind;     /* CGB_FILL_SOLID | CGB_FILL_GRADIENT */
+    float color[4];         /* Fill::Solid, linear RGBA */
+    uint32_t gradient_type; /* CGB_GRADIENT_* */
+    uint32_t n_stops;
+    float gradient_start[2];
+    float gradient_end[2];
+    const float* stops; /* n_stops * 5 floats; copied by the call */
+} cgb_props;
+
+/* Output buffer (mold Buffer, mold/src/buffer.rs:19-25): `height` rows of
+ * `width_stride` RGBA8 pixels of which the first `width` are painted. */
+#define CGB_MEMORY_HOST 0u
+#define CGB_MEMORY_DEVICE 1u
+typedef struct cgb_buffer {
+    uint8_t* pixels;
+    uint64_t width;
+    uint64_t height;
+    uint64_t width_stride; /* 0 means width */
+    int32_t layer_cache;   /* BufferLayerCache id, or -1 */
+    uint32_t memory;       /* CGB_MEMORY_HOST | CGB_MEMORY_DEVICE */
+} cgb_buffer;
+
+/* surpass painter Rect (surpass/src/painter/buffer_layout.rs:37-50), in
+ * pixels; rounded out to whole tiles as Rect::new does. */
+typedef struct cgb_rect {
+    uint64_t x0, x1, y0, y1;
+} cgb_rect;
+
+/* Per-frame sizes and device stage times of the last render / pixel_segments. */
+typedef struct cgb_stats {
+    uint64_t lines;            /* lines in the builder (L) */
+    uint64_t steps;            /* pixel steps, S = sum of line lengths */
+    uint64_t segments;         /* real pixel segments, P (the reference emits 2*S slots) */
+    uint64_t painted_segments; /* segments inside the canvas rows/tiles (painter input) */
+    uint64_t tile_layers;      /* (tile, layer) groups that hold segments */
+    uint64_t work_items;       /* (tile, layer) pairs painted, incl. cover-carry-only pairs */
+    uint32_t sort_passes;      /* radix passes of the segment sort */
+    uint32_t item_sort_passes; /* radix passes of the work-item sort */
+    float build_ms, rasterize_ms, sort_ms, carry_ms, paint_ms, total_ms;
+} cgb_stats;
+
+/* Autotuned knobs (0 keeps the current value). */
+typedef struct cgb_tuning {
+    uint32_t radix_bits;     /* digit width of the segment sort: 6, 7 or 8 */
+    uint32_t raster_block;   /* threads per rasterizer block: 128..1024 */
+    uint32_t steps_per_block;/* pixel steps per rasterizer block */
+    uint32_t paint_warps;    /* warps (tiles) per painter block */
+} cgb_tuning;
+
+typedef struct cgb_composition cgb_composition;
+
+/* ---- library --------------------------------------------------------------------- */
+
+/* Version string and the last error message of this thread. */
+CGB_EXPORT const char* cgb_version(void);
+CGB_EXPORT const char* cgb_last_error(void);
+
+/* ---- mold::Composition ------------------------------------------------------------ */
+
+/* Composition::new (mold/src/composition.rs:36-48).  `hbm_budget_bytes` caps the
+ * device memory the handle may hold (0 = unlimited).  Binds the current device. */
+CGB_EXPORT cgb_status cgb_composition_new(uint32_t flags, uint64_t hbm_budget_bytes,
+                                          cgb_composition** out);
+CGB_EXPORT cgb_status cgb_composition_free(cgb_composition* c);
+
+/* Composition::create_layer (mold/src/composition.rs:54-56), IdSet::acquire
+ * (mold/src/layer.rs:61-72).  Ids are handed out lowest-free-first. */
+CGB_EXPORT cgb_status cgb_create_layer(cgb_composition* c, uint32_t* out_layer_id);
+
+/* Composition::insert_in_layer / insert_in_layer_transformed
+ * (mold/src/composition.rs:58-94): flattens the path on the GPU
+ * (PathSegments, mold/src/path/segments.rs) and pushes the lines.
+ * `transform9` may be NULL. */
+CGB_EXPORT cgb_status cgb_insert_in_layer(cgb_composition* c, uint32_t layer_id,
+                                          const uint32_t* kinds, size_t n_cmds,
+                                          const float* points, size_t n_point_floats,
+                                          const float* transform9);
+
+/* Batched insert_in_layer over many paths: path k owns commands
+ * [cmd_offsets[k], cmd_offsets[k+1]) and floats [point_offsets[k],
+ * point_offsets[k+1]); `transforms9` is NULL or 9 floats per path, used where
+ * has_transform[k] != 0. */
+CGB_EXPORT cgb_status cgb_insert_paths(cgb_composition* c, size_t n_paths,
+                                       const uint32_t* layer_ids, const uint64_t* cmd_offsets,
+                                       const uint32_t* kinds, const uint64_t* point_offsets,
+                                       const float* points, const float* transforms9,
+                                       const uint8_t* has_transform);
+
+/* LinesBuilder::push (surpass/src/segment.rs:47-53) of already-flattened lines
+ * (x0 y0 x1 y1 per line) into a layer, with insert_segments' bookkeeping. */
+CGB_EXPORT cgb_status cgb_insert_lines(cgb_composition* c, uint32_t layer_id,
+                                       const float* segments, size_t n_lines);
+
+/* Layer setters (mold/src/layer.rs:158-231).  set_transform(NULL) = identity. */
+CGB_EXPORT cgb_status cgb_layer_set_enabled(cgb_composition* c, uint32_t layer_id, int enabled);
+CGB_EXPORT cgb_status cgb_layer_set_transform(cgb_composition* c, uint32_t layer_id,
+                                              const float* affine6, uint32_t flags);
+CGB_EXPORT cgb_status cgb_layer_set_order(cgb_composition* c, uint32_t layer_id, uint32_t order);
+CGB_EXPORT cgb_status cgb_layer_set_props(cgb_composition* c, uint32_t layer_id,
+                                          const cgb_props* props);
+/* Batched set_transform for n layers (6 floats each); flags as above. */
+CGB_EXPORT cgb_status cgb_layers_set_transforms(cgb_composition* c, size_t n,
+                                                const uint32_t* layer_ids, const float* affine6,
+                                                uint32_t flags);
+
+/* Composition::remove_disabled (mold/src/composition.rs:124-142). */
+CGB_EXPORT cgb_status cgb_remove_disabled(cgb_composition* c);
+/* LinesBuilder::len and Composition::actual_len (composition.rs:116-121). */
+CGB_EXPORT cgb_status cgb_lines_len(cgb_composition* c, uint64_t* builder_len,
+                                    uint64_t* actual_len);
+
+/* Composition::create_buffer_layer_cache (composition.rs:144-151) and the
+ * BufferLayerCache drop (mold/src/buffer.rs:62-71). */
+CGB_EXPORT cgb_status cgb_create_buffer_layer_cache(cgb_composition* c, int32_t* out_cache_id);
+CGB_EXPORT cgb_status cgb_release_buffer_layer_cache(cgb_composition* c, int32_t cache_id);
+
+/* Composition::render (mold/src/composition.rs:212-329): build lines,
+ * rasterize, sort and paint on the GPU into `buffer` (host or device memory).
+ * `background` is linear RGBA; `crop` may be NULL. */
+CGB_EXPORT cgb_status cgb_render(cgb_composition* c, const cgb_buffer* buffer,
+                                 const float background[4], const cgb_rect* crop);
+
+/* Composition::pixel_segments (mold/src/composition.rs:153-188): the real
+ * pixel segments after build + rasterize + sort, copied to the host array
+ * `out` (capacity `cap` u64).  `*out_len` receives P even when cap < P (then
+ * CGB_ERR_CAPACITY).  `*out_none` receives the NONE slots (2*S - P) that the
+ * reference's array ends with.  `order` is CGB_SORT_CANONICAL or CGB_SORT_KEY. */
+CGB_EXPORT cgb_status cgb_pixel_segments(cgb_composition* c, uint64_t* out, size_t cap,
+                                         uint64_t* out_len, uint64_t* out_none, uint32_t order);
+
+/* Sizes and stage times of the last render / pixel_segments. */
+CGB_EXPORT cgb_status cgb_get_stats(cgb_composition* c, cgb_stats* out);
+CGB_EXPORT cgb_status cgb_set_tuning(cgb_composition* c, const cgb_tuning* tuning);
+CGB_EXPORT cgb_status cgb_get_tuning(cgb_composition* c, cgb_tuning* out);
+
+/* Synchronize the handle's stream (device buffers written by render are ready). */
+CGB_EXPORT cgb_status cgb_synchronize(cgb_composition* c);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CASSIA_GB300_H */
