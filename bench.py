@@ -1,0 +1,369 @@
+#!/usr/bin/env python3
+"""Benchmark: Msegments/s of the surpass/mold rasterize -> sort -> paint frame.
+
+Workload (default): the mixed 100,000-layer scene on a 2560x1600 canvas
+(star/convex polygons and closed cubic paths, random affine per layer, 12
+blend modes, NonZero/EvenOdd; ~7.6M lines, ~65M pixel segments), seeded and
+synthetic.  Lines are flattened once on the GPU and stay resident in HBM; one
+step is one frame: LinesBuilder::build -> rasterize -> sort -> paint into an
+RGBA8 device buffer.  value = pixel segments / second over all ranks.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the CPU restatement of the reference path (the
+oracle, std::thread-parallel over the host cores) on the same workload,
+each step a bounded sample of it.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "mixed100k": dict(kind="mixed", n_layers=100_000, width=2560, height=1600, seed=2),
+    "mixed65k": dict(kind="mixed", n_layers=65_535, width=2560, height=1600, seed=2),
+    "circles": dict(kind="circles", n_layers=1000, width=1024, height=1024, seed=1),
+    "glyphs": dict(kind="glyphs", n_layers=50_000, width=3840, height=2160, seed=3),
+}
+
+
+def make_scene(name):
+    from cassia_gb300 import scenes
+    w = WORKLOADS[name]
+    if w["kind"] == "mixed":
+        return scenes.mixed(seed=w["seed"], n_layers=w["n_layers"], width=w["width"], height=w["height"])
+    if w["kind"] == "circles":
+        return scenes.circles(seed=w["seed"], n_layers=w["n_layers"], size=w["width"])
+    return scenes.glyphs(seed=w["seed"], n_layers=w["n_layers"], width=w["width"], height=w["height"])
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def stage_bytes(st, scene):
+    """Algorithmic bytes per stage: each stage reads its input once and
+    writes its output once; one sort pass is one read + one write."""
+    L, P, N = st["lines"], st["segments"], scene.n_layers
+    return {
+        "rasterize": 18 * L + 8 * P,
+        "sort": 16 * st["painted_segments"],
+        "paint": 8 * st["painted_segments"] + 32 * N + 4 * scene.width * scene.height,
+    }
+
+
+STAGE_KERNELS = {
+    "build": "k_build_lines + scan",
+    "rasterize": "k_rasterize (count + write)",
+    "sort": "k_radix_hist + k_onesweep",
+    "carry": "k_tl_* + k_items_* + item sort",
+    "paint": "k_paint",
+}
+
+
+def cpu_reference(scene, steps, warmup, budget_s=150.0):
+    """Times the oracle's full frame (build, rasterize, sort, paint) on the
+    host cores.  Each step renders a bounded sample: the first fraction of the
+    scene's layers, sized so that all steps fit the time budget."""
+    import oracle
+    from cassia_gb300 import scenes as sc_mod
+    threads = os.cpu_count() or 1
+
+    def sub_scene(frac):
+        n = max(1, int(scene.n_layers * frac))
+        k = int(np.searchsorted(scene.path_layer, n))
+        s = sc_mod.Scene(scene.name, scene.width, scene.height, scene.background, scene.wide, n,
+                         scene.path_layer[:k], scene.cmd_offsets[:k + 1], scene.kinds[:int(scene.cmd_offsets[k])],
+                         scene.point_offsets[:k + 1], scene.points[:int(scene.point_offsets[k])],
+                         None if scene.transforms is None else scene.transforms[:n], scene.fill_rule[:n],
+                         scene.blend_mode[:n], scene.color[:n])
+        return s
+
+    def frame(s, comp, img):
+        t0 = time.perf_counter()
+        comp.render(img, s.width, s.background, threads=threads)
+        dt = time.perf_counter() - t0
+        return dt, comp.stats()["segments"]
+
+    img = np.zeros((scene.height, scene.width, 4), np.uint8)
+    # calibrate on 5% of the layers
+    s = sub_scene(0.05)
+    comp = oracle.Composition(wide=scene.wide)
+    sc_mod.load(s, comp)
+    dt, _ = frame(s, comp, img)
+    per_step = budget_s / max(1, steps + warmup)
+    frac = min(1.0, 0.05 * per_step / max(dt, 1e-3))
+    if frac < 1.0:
+        s = sub_scene(frac)
+    else:
+        s = scene
+    comp = oracle.Composition(wide=scene.wide)
+    sc_mod.load(s, comp)
+    for _ in range(warmup):
+        frame(s, comp, img)
+    times, segs = [], 0
+    for _ in range(steps):
+        dt, segs = frame(s, comp, img)
+        times.append(dt)
+    t = sum(times) / len(times)
+    sample = (f"{s.n_layers} of {scene.n_layers} layers ({100.0 * s.n_layers / scene.n_layers:.1f}%), "
+              f"full {scene.width}x{scene.height} canvas, {segs} segments per frame")
+    return {"value": segs / t / 1e6, "unit": "Msegments/s", "cores": threads, "kind": "port", "sample": sample,
+            "ms_per_step": t * 1e3, "frames_per_s": 1.0 / t}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    scene = make_scene(args.workload)
+    r = cpu_reference(scene, args.steps, args.warmup)
+    line = {
+        "metric": "Msegments/s", "value": r["value"], "unit": "Msegments/s", "impl": "reference",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+int (fixed point)",
+        "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "canvas": [scene.width, scene.height], "layers": scene.n_layers},
+        "frames_per_s": r["frames_per_s"],
+        "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": r["value"], "unit": "Msegments/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="mixed100k", choices=list(WORKLOADS))
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quiet", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    if args.impl == "reference":
+        rc = run_reference(args, rank, world)
+        if dist:
+            dist.destroy_process_group()
+        return rc
+
+    torch.cuda.set_device(local)
+    from cassia_gb300 import Composition, scenes
+    from cassia_gb300.composition import kernel_launches
+
+    t0 = time.time()
+    scene = make_scene(args.workload)
+    gen_s = time.time() - t0
+    comp = Composition(wide=scene.wide)
+    t0 = time.time()
+    scenes.load(scene, comp)
+    load_s = time.time() - t0
+    H, W = scene.height, scene.width
+    out = torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.ExternalStream(comp.stream())
+
+    def frame():
+        comp.render(out.data_ptr(), W, scene.background, height=H)
+
+    for _ in range(args.warmup):
+        frame()
+    comp.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    stats = []
+    launches0 = kernel_launches()
+    with ClockSampler(local) as clk:
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            frame()
+            stats.append(comp.stats())
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = kernel_launches() - launches0
+    if dist:
+        dist.barrier()
+    ms_total = ev0.elapsed_time(ev1)
+    ms_step = ms_total / args.steps
+    if dist:
+        t = torch.tensor([ms_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    st = stats[-1]
+    segs = st["segments"]
+    value = world * segs / (ms_step / 1e3) / 1e6
+
+    # stage times (device events on the launching stream), averaged over the timed steps
+    stage_ms = {k: statistics.mean(s[k + "_ms"] for s in stats) for k in
+                ("build", "rasterize", "sort", "carry", "paint", "total")}
+    peak, peak_kind = load_peaks()
+    sb = stage_bytes(st, scene)
+    dom = max(("rasterize", "sort", "paint"), key=lambda k: stage_ms[k])
+    achieved = sb[dom] / (stage_ms[dom] / 1e3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        try:
+            with open(tfile) as f:
+                tr = json.load(f).get(args.workload, {}).get(dom)
+            traffic = tr
+        except Exception:
+            traffic = None
+    frame_bytes = 18 * st["lines"] + 32 * segs + 32 * scene.n_layers + 4 * W * H
+
+    # e2e through the public API with host buffers: every step uploads all
+    # layer transforms from pinned host memory (the per-frame input of a
+    # retained scene) and reads the RGBA8 frame back into pinned host memory.
+    e2e = None
+    if args.e2e_steps > 0:
+        host_img = torch.zeros((H, W, 4), dtype=torch.uint8).pin_memory().numpy()
+        ids = np.arange(scene.n_layers, dtype=np.uint32)
+        tr = torch.from_numpy(scene.transforms if scene.transforms is not None
+                              else np.tile(np.array([[1, 0, 0, 1, 0, 0]], np.float32), (scene.n_layers, 1)))
+        tr = tr.pin_memory().numpy()
+        comp.set_transforms(ids, tr)
+        comp.render(host_img, W, scene.background)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for k in range(args.e2e_steps):
+            tr[:, 4] += np.float32(0.25 if k % 2 == 0 else -0.25)  # a new placement each frame
+            comp.set_transforms(ids, tr)
+            comp.render(host_img, W, scene.background)
+        torch.cuda.synchronize()
+        e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+        if dist:
+            t = torch.tensor([e2e_s], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        h2d = scene.n_layers * (6 * 4)
+        e2e = {"value": world * comp.stats()["segments"] / e2e_s / 1e6, "unit": "Msegments/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": W * H * 4, "ms_per_step": e2e_s * 1e3}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            r = cpu_reference(scene, steps=1, warmup=0, budget_s=45.0)
+            cpu = {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        except Exception as e:  # report, do not hide
+            cpu = {"value": None, "error": repr(e)}
+
+    if rank == 0:
+        line = {
+            "metric": "Msegments/s", "value": value, "unit": "Msegments/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+int (fixed point)", "data": "synthetic (seeded)",
+            "config": {"workload": args.workload, "canvas": [W, H], "layers": scene.n_layers,
+                       "lines": st["lines"], "segments_per_frame": segs,
+                       "painted_segments": st["painted_segments"], "work_items": st["work_items"],
+                       "segment_format": "wide (17-bit layer)" if scene.wide else "reference u16",
+                       "l2": "inputs larger than L2 (lines %d MB, segments %d MB)" % (
+                           st["lines"] * 20 // 2**20, segs * 8 // 2**20),
+                       "parallelism": f"replicas x{world}"},
+            "frames_per_s": world * 1e3 / ms_step,
+            "stage_ms": stage_ms,
+            "roofline": {"bound": "hbm", "kernel": STAGE_KERNELS[dom], "stage": dom, "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": traffic, "algorithmic_bytes": sb[dom]},
+            "frame_roofline": {"algorithmic_bytes": frame_bytes,
+                               "achieved": frame_bytes / (ms_step / 1e3) / 1e9,
+                               "frac": frame_bytes / (ms_step / 1e3) / 1e9 / peak},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "setup_s": {"scene_gen": gen_s, "load_insert_paths": load_s},
+        }
+        print(json.dumps(line))
+    comp.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

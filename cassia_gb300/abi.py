@@ -149,6 +149,7 @@ def _declare(lib):
         "cgb_layer_set_order": ([handle, u32, u32], i32),
         "cgb_layer_set_props": ([handle, u32, P(CgbProps)], i32),
         "cgb_layers_set_transforms": ([handle, sz, P(u32), fp, u32], i32),
+        "cgb_layers_set_props": ([handle, sz, P(u32), P(CgbProps)], i32),
         "cgb_remove_disabled": ([handle], i32),
         "cgb_lines_len": ([handle, P(u64), P(u64)], i32),
         "cgb_create_buffer_layer_cache": ([handle, P(i32)], i32),
@@ -159,6 +160,9 @@ def _declare(lib):
         "cgb_set_tuning": ([handle, P(CgbTuning)], i32),
         "cgb_get_tuning": ([handle, P(CgbTuning)], i32),
         "cgb_synchronize": ([handle], i32),
+        "cgb_get_stream": ([handle, P(vp)], i32),
+        "cgb_kernel_launches": ([], u64),
+        "cgb_composition_clear": ([handle], i32),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

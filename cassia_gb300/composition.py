@@ -1,0 +1,213 @@
+"""mold::Composition over the CUDA library's C ABI (include/cassia_gb300.h).
+
+Composition mirrors mold/src/composition.rs:26-329: create_layer,
+insert_in_layer(_transformed), layer setters (mold/src/layer.rs:145-244),
+render into a Buffer, pixel_segments, remove_disabled and buffer layer
+caches.  Every call goes through the native library; there is no CPU path.
+"""
+import ctypes
+from typing import Optional
+
+import numpy as np
+
+from . import abi
+from .types import Path, Props, transform_array
+
+
+def _check(lib, st, where):
+    if st != abi.OK:
+        msg = lib.cgb_last_error()
+        raise abi.CassiaError(st, where, msg.decode() if msg else "")
+
+
+def _u32p(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+
+
+def _u64p(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+
+
+def _fp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def kernel_launches() -> int:
+    """Kernels launched by the native library in this process."""
+    return int(abi.load_library().cgb_kernel_launches())
+
+
+class Composition:
+    """mold::Composition on the GPU.  `wide=True` selects the 17-bit layer
+    segment format for more than 65,536 layer orders; `hbm_budget` caps the
+    device memory the handle may hold (bytes, 0 = unlimited)."""
+
+    def __init__(self, wide: bool = False, hbm_budget: int = 0):
+        self._lib = abi.load_library()
+        h = ctypes.c_void_p()
+        flags = abi.COMPOSITION_WIDE_LAYERS if wide else 0
+        _check(self._lib, self._lib.cgb_composition_new(flags, hbm_budget, ctypes.byref(h)), "Composition::new")
+        self._h = h
+        self.wide = wide
+
+    def close(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h:
+            self._lib.cgb_composition_free(h)
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- layers -------------------------------------------------------------
+    def create_layer(self) -> Optional[int]:
+        out = ctypes.c_uint32()
+        st = self._lib.cgb_create_layer(self._h, ctypes.byref(out))
+        return None if st else out.value
+
+    def insert_in_layer(self, layer_id: int, path: Path, transform9=None):
+        k, p = path.c_arrays()
+        st = self._lib.cgb_insert_in_layer(self._h, layer_id, k, len(path.kinds), p, len(path.points),
+                                           transform_array(transform9, 9))
+        _check(self._lib, st, "insert_in_layer")
+        return self
+
+    def insert_paths(self, scene, transforms9=None, has_transform=None):
+        """Batched insert_in_layer of every path of a scene (cassia_gb300.scenes.Scene)."""
+        s = scene
+        t9 = None if transforms9 is None else np.ascontiguousarray(transforms9, np.float32)
+        ht = None if has_transform is None else np.ascontiguousarray(has_transform, np.uint8)
+        st = self._lib.cgb_insert_paths(
+            self._h, s.n_paths, _u32p(s.path_layer), _u64p(s.cmd_offsets), _u32p(s.kinds), _u64p(s.point_offsets),
+            _fp(s.points), None if t9 is None else _fp(t9),
+            None if ht is None else ht.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+        _check(self._lib, st, "insert_paths")
+
+    def insert_lines(self, layer_id: int, segs):
+        segs = np.ascontiguousarray(np.asarray(segs, np.float32).reshape(-1, 4))
+        _check(self._lib, self._lib.cgb_insert_lines(self._h, layer_id, _fp(segs), len(segs)), "insert_lines")
+
+    def set_enabled(self, layer_id: int, enabled: bool):
+        _check(self._lib, self._lib.cgb_layer_set_enabled(self._h, layer_id, int(bool(enabled))), "set_enabled")
+
+    def set_transform(self, layer_id: int, affine6, unchecked: bool = False):
+        st = self._lib.cgb_layer_set_transform(self._h, layer_id, transform_array(affine6, 6),
+                                               abi.TRANSFORM_UNCHECKED if unchecked else 0)
+        _check(self._lib, st, "set_transform")
+
+    def set_transforms(self, ids, affine6, unchecked: bool = True):
+        ids = np.ascontiguousarray(ids, np.uint32)
+        t = np.ascontiguousarray(affine6, np.float32)
+        st = self._lib.cgb_layers_set_transforms(self._h, len(ids), _u32p(ids), _fp(t),
+                                                 abi.TRANSFORM_UNCHECKED if unchecked else 0)
+        _check(self._lib, st, "set_transforms")
+
+    def set_order(self, layer_id: int, order: int):
+        _check(self._lib, self._lib.cgb_layer_set_order(self._h, layer_id, order), "set_order")
+
+    def set_props(self, layer_id: int, props: Props):
+        p, keep = props.to_c()
+        _check(self._lib, self._lib.cgb_layer_set_props(self._h, layer_id, ctypes.byref(p)), "set_props")
+
+    def set_layers_solid(self, ids, fill_rules, blend_modes, colors):
+        ids = np.ascontiguousarray(ids, np.uint32)
+        n = len(ids)
+        arr = (abi.CgbProps * max(n, 1))()
+        fr = np.asarray(fill_rules, np.uint32)
+        bm = np.asarray(blend_modes, np.uint32)
+        col = np.asarray(colors, np.float32).reshape(-1, 4)
+        # fill the struct array through a numpy view of its bytes
+        view = np.frombuffer(arr, dtype=np.uint8).reshape(max(n, 1), ctypes.sizeof(abi.CgbProps))
+        u32 = view[:, :40].view(np.uint32)
+        u32[:n, 0] = fr
+        u32[:n, 1] = abi.FUNC_DRAW
+        u32[:n, 4] = bm
+        u32[:n, 5] = abi.FILL_SOLID
+        view[:n, 24:40].view(np.float32)[:] = col
+        st = self._lib.cgb_layers_set_props(self._h, n, _u32p(ids), arr)
+        _check(self._lib, st, "set_layers_solid")
+
+    def remove_disabled(self):
+        _check(self._lib, self._lib.cgb_remove_disabled(self._h), "remove_disabled")
+
+    def lens(self):
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(self._lib, self._lib.cgb_lines_len(self._h, ctypes.byref(a), ctypes.byref(b)), "lines_len")
+        return a.value, b.value
+
+    def create_buffer_layer_cache(self) -> Optional[int]:
+        out = ctypes.c_int32()
+        st = self._lib.cgb_create_buffer_layer_cache(self._h, ctypes.byref(out))
+        return None if st else out.value
+
+    def release_buffer_layer_cache(self, cache_id: int):
+        _check(self._lib, self._lib.cgb_release_buffer_layer_cache(self._h, cache_id), "release_cache")
+
+    # ---- frames -----------------------------------------------------------------
+    def render(self, pixels, width, background, crop=None, layer_cache=-1, width_stride=None, height=None):
+        """Composition::render.  `pixels` is a host uint8 numpy array of shape
+        (height, width_stride, 4), or a device pointer (int) with `height` given."""
+        stride = width_stride or width
+        b = abi.CgbBuffer()
+        if isinstance(pixels, np.ndarray):
+            assert pixels.dtype == np.uint8 and pixels.flags.c_contiguous
+            b.pixels = pixels.ctypes.data
+            b.height = pixels.size // (4 * stride)
+            b.memory = abi.MEMORY_HOST
+        else:
+            b.pixels = int(pixels)
+            b.height = int(height)
+            b.memory = abi.MEMORY_DEVICE
+        b.width = width
+        b.width_stride = stride
+        b.layer_cache = -1 if layer_cache is None else layer_cache
+        bg = (ctypes.c_float * 4)(*background)
+        cr = None
+        if crop is not None:
+            cr = abi.CgbRect(*crop)
+        st = self._lib.cgb_render(self._h, ctypes.byref(b), bg, None if cr is None else ctypes.byref(cr))
+        _check(self._lib, st, "render")
+        return pixels
+
+    def pixel_segments(self, canonical: bool = True):
+        """Composition::pixel_segments: (sorted real segments, NONE count)."""
+        n, none = ctypes.c_uint64(), ctypes.c_uint64()
+        order = abi.SORT_CANONICAL if canonical else abi.SORT_KEY
+        st = self._lib.cgb_pixel_segments(self._h, None, 0, ctypes.byref(n), ctypes.byref(none), order)
+        if st not in (abi.OK, abi.ERR_CAPACITY):
+            _check(self._lib, st, "pixel_segments")
+        out = np.zeros(max(1, n.value), np.uint64)
+        st = self._lib.cgb_pixel_segments(self._h, _u64p(out), n.value, ctypes.byref(n), ctypes.byref(none), order)
+        _check(self._lib, st, "pixel_segments")
+        return out[:n.value], none.value
+
+    def stats(self) -> dict:
+        s = abi.CgbStats()
+        _check(self._lib, self._lib.cgb_get_stats(self._h, ctypes.byref(s)), "get_stats")
+        return s.as_dict()
+
+    def tuning(self) -> dict:
+        t = abi.CgbTuning()
+        _check(self._lib, self._lib.cgb_get_tuning(self._h, ctypes.byref(t)), "get_tuning")
+        return {k: getattr(t, k) for k, _ in t._fields_}
+
+    def set_tuning(self, **kw):
+        t = abi.CgbTuning(**kw)
+        _check(self._lib, self._lib.cgb_set_tuning(self._h, ctypes.byref(t)), "set_tuning")
+
+    def stream(self) -> int:
+        """The cudaStream_t (as an int) the handle launches on."""
+        out = ctypes.c_void_p()
+        _check(self._lib, self._lib.cgb_get_stream(self._h, ctypes.byref(out)), "get_stream")
+        return out.value or 0
+
+    def clear(self):
+        _check(self._lib, self._lib.cgb_composition_clear(self._h), "clear")
+
+    def synchronize(self):
+        _check(self._lib, self._lib.cgb_synchronize(self._h), "synchronize")

@@ -1,0 +1,254 @@
+// Internal declarations shared by the CUDA translation units of cassia_gb300.
+//
+// All device arithmetic reproduces the reference (Rust, surpass/mold) bit for
+// bit: the library is compiled with -fmad=false so that no a*b+c is
+// contracted, and every `mul_add` of the reference is an explicit __fmaf_rn.
+// Float->int conversions use the saturating round-toward-zero cvt (NaN -> 0),
+// which is Rust's `as`; roundf is round-half-away-from-zero, as f32::round.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/cassia_gb300.h"
+
+namespace cgb {
+
+// surpass/src/lib.rs:18-33
+constexpr int PIXEL_WIDTH = 16;
+constexpr int PIXEL_SHIFT = 4;
+constexpr int PIXEL_MASK = 15;
+constexpr int TILE_SHIFT = 3;
+constexpr int TILE_MASK = 7;
+
+// ---------------------------------------------------------------------------
+// device records
+// ---------------------------------------------------------------------------
+
+// surpass::Layer (surpass/src/layer.rs:5-20) indexed by layer id.
+struct LayerRec {
+    uint32_t flags;  // LAYER_PRESENT | LAYER_ENABLED | LAYER_HAS_TRANSFORM
+    uint32_t order;  // Layer::order (defaults to the id when LAYER_HAS_ORDER is clear)
+    float t[6];      // affine_transform
+};
+constexpr uint32_t LAYER_PRESENT = 1u;
+constexpr uint32_t LAYER_ENABLED = 2u;
+constexpr uint32_t LAYER_HAS_TRANSFORM = 4u;
+constexpr uint32_t LAYER_HAS_ORDER = 8u;
+
+// Output of LinesBuilder::build for one line (surpass/src/segment.rs:208-219),
+// packed into 32 bytes.  `length` lives in a separate array (it is scanned).
+struct LineRec {
+    int32_t start;
+    float start_f32, end_f32;
+    float slope, slope_recip, py_slope_px, px_slope_recip_py;
+    uint32_t order_octant;  // order << 3 | octant
+};
+
+// Painter-side props of one order (LayerProps::get, painter/mod.rs:143-146).
+struct PaintProps {
+    uint32_t fill_rule;
+    uint32_t blend_mode;
+    uint32_t flags;  // PROPS_*
+    uint32_t pad;
+    float color[4];
+};
+constexpr uint32_t PROPS_SOLID = 1u;        // Fill::Solid
+constexpr uint32_t PROPS_OPAQUE_OVER = 2u;  // Fill::Solid, BlendMode::Over, alpha == 1.0
+constexpr uint32_t PROPS_DRAW = 4u;         // Func::Draw
+constexpr uint32_t PROPS_PRESENT = 8u;      // an enabled layer holds this order
+
+// Segment formats.
+struct SegFormat {
+    uint32_t wide;  // 0: reference CompactSegment; 1: D5 widened layer field
+};
+
+// Render-mode key geometry: key = ((j * n_orders + order) * (row_len + 1) + (i + 1)).
+struct RenderGeom {
+    uint32_t rows, row_len;  // tile rows / tiles per row of the canvas
+    uint32_t n_orders;       // max order + 1
+    uint32_t key_bits;       // bits of the largest key
+};
+
+// ---------------------------------------------------------------------------
+// Rust-semantics numerics
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int32_t wadd(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
+__device__ __forceinline__ int32_t wsub(int32_t a, int32_t b) { return (int32_t)((uint32_t)a - (uint32_t)b); }
+__device__ __forceinline__ int32_t wmul(int32_t a, int32_t b) { return (int32_t)((uint32_t)a * (uint32_t)b); }
+__device__ __forceinline__ int32_t wabs(int32_t a) { return a < 0 ? wsub(0, a) : a; }
+
+// `v as i32`: truncation, saturation, NaN -> 0 (cvt.rzi.s32.f32).
+__device__ __forceinline__ int32_t f2i32(float v) { return __float2int_rz(v); }
+// `v as u8`
+__device__ __forceinline__ uint32_t f2u8(float v) { return min(__float2uint_rz(v), 255u); }
+// `v as usize` for the small positive values of curve subdivision counts.
+__device__ __forceinline__ uint64_t f2usize(float v) { return __float2ull_rz(v); }
+
+// segment.rs:13-16
+__device__ __forceinline__ int32_t to_sub_pixel(float v) {
+    return f2i32(__fmaf_rn(v, (float)PIXEL_WIDTH, copysignf(0.5f, v)));
+}
+
+// Sign-extend the low `bits` of v.
+__device__ __forceinline__ int32_t sext(uint64_t v, int bits) {
+    uint64_t m = 1ull << (bits - 1);
+    v &= (1ull << bits) - 1;
+    return (int32_t)(int64_t)((v ^ m) - m);
+}
+
+// CompactSegment packing (raster_segment.rs:142-154) and the D5 layout.
+__device__ __forceinline__ uint64_t pack_segment(uint32_t wide, int32_t tile_j, int32_t tile_i_stored, uint32_t layer,
+                                                 uint32_t ty, uint32_t tx, int32_t area, int32_t cover) {
+    uint64_t v;
+    if (!wide) {
+        v = ((uint64_t)(uint32_t)tile_j & 0xFFF);
+        v = (v << 13) | ((uint64_t)(uint32_t)tile_i_stored & 0x1FFF);
+        v = (v << 16) | ((uint64_t)layer & 0xFFFF);
+    } else {
+        v = ((uint64_t)(uint32_t)tile_j & 0xFFF);
+        v = (v << 13) | ((uint64_t)(uint32_t)tile_i_stored & 0x1FFF);
+        v = (v << 17) | ((uint64_t)layer & 0x1FFFF);
+    }
+    v = (v << 3) | (ty & 7);
+    v = (v << 3) | (tx & 7);
+    v = (v << 10) | ((uint64_t)(uint32_t)area & 0x3FF);
+    v = (v << 6) | ((uint64_t)(uint32_t)cover & 0x3F);
+    return v;
+}
+__device__ __forceinline__ int32_t seg_tile_j(uint32_t wide, uint64_t s) { return sext(s >> (wide ? 52 : 51), 12); }
+__device__ __forceinline__ int32_t seg_tile_i_stored(uint32_t wide, uint64_t s) { return sext(s >> (wide ? 39 : 38), 13); }
+__device__ __forceinline__ uint32_t seg_layer(uint32_t wide, uint64_t s) {
+    return wide ? (uint32_t)((s >> 22) & 0x1FFFF) : (uint32_t)((s >> 22) & 0xFFFF);
+}
+__device__ __forceinline__ uint32_t low_tile_y(uint32_t low) { return (low >> 19) & 7; }
+__device__ __forceinline__ uint32_t low_tile_x(uint32_t low) { return (low >> 16) & 7; }
+__device__ __forceinline__ int32_t low_area(uint32_t low) { return sext(low >> 6, 10); }
+__device__ __forceinline__ int32_t low_cover(uint32_t low) { return sext(low, 6); }
+
+// 8 x i8 cover lanes packed in a u64 (lane y = byte y); lane-wise wrapping add.
+__device__ __forceinline__ uint64_t cover_add(uint64_t a, uint64_t b) {
+    const uint64_t H = 0x8080808080808080ull;
+    return ((a & ~H) + (b & ~H)) ^ ((a ^ b) & H);
+}
+__device__ __forceinline__ int32_t cover_lane(uint64_t c, int y) { return (int32_t)(int8_t)(uint8_t)(c >> (8 * y)); }
+__device__ __forceinline__ int32_t abs8(int32_t v) {  // wrapping i8 abs
+    return (int32_t)(int8_t)(uint8_t)(v < 0 ? (uint32_t)(-v) : (uint32_t)v);
+}
+// Cover::is_empty / is_full (painter/mod.rs:164-189, D2)
+__device__ __forceinline__ bool cover_is_empty(uint64_t c, uint32_t fill_rule) {
+    if (fill_rule == CGB_FILL_NONZERO) return c == 0;
+#pragma unroll
+    for (int y = 0; y < 8; y++)
+        if ((abs8(cover_lane(c, y)) & 31) != 0) return false;
+    return true;
+}
+__device__ __forceinline__ bool cover_is_full(uint64_t c, uint32_t fill_rule) {
+#pragma unroll
+    for (int y = 0; y < 8; y++) {
+        int32_t a = abs8(cover_lane(c, y));
+        if (fill_rule == CGB_FILL_NONZERO ? a != PIXEL_WIDTH : (a & 31) != 16) return false;
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// host-side launchers (defined in the .cu files)
+// ---------------------------------------------------------------------------
+
+// A grow-only device buffer accounted against the handle's HBM budget.
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    template <class T>
+    T* as() const { return (T*)p; }
+};
+
+// Device scratch shared by the stages of one composition handle.
+struct Scratch {
+    size_t budget = 0;  // 0 = unlimited
+    size_t used = 0;    // bytes held by all DevBufs of the handle
+    bool over_budget = false;
+    // Grows `b` to at least `bytes` (geometric growth).  Fails with
+    // cudaErrorMemoryAllocation (and sets over_budget) past the budget.
+    cudaError_t ensure(DevBuf& b, size_t bytes);
+    void release(DevBuf& b);
+    DevBuf scan_sums;  // u64 per-block sums of scan_u32
+    DevBuf sort_hist, sort_lookback, sort_counter;
+    uint64_t* pinned = nullptr;  // small pinned host area for readbacks
+};
+
+// Process-wide count of kernels launched by this library.
+void count_launches(uint64_t n);
+
+// k_lines.cu
+cudaError_t launch_flatten(int write, const uint32_t* kinds, const float* points, const uint64_t* cmd_off,
+                           const uint64_t* pt_off, const float* transforms9, const uint8_t* has_t,
+                           const uint32_t* path_layer, uint32_t n_paths, uint32_t* counts, const uint32_t* out_off,
+                           float* p0x, float* p0y, float* p1x, float* p1y, uint32_t* lids, cudaStream_t st);
+cudaError_t launch_build_lines(const float* p0x, const float* p0y, const float* p1x, const float* p1y,
+                               const uint32_t* lids, uint32_t n, const LayerRec* layers, uint32_t n_layer_recs,
+                               const float* default_t, LineRec* recs, uint32_t* lengths, cudaStream_t st);
+// mode: 0 = count, 1 = write.  render != 0 selects the culled, re-keyed
+// render format; else the reference format (SegFormat).
+cudaError_t launch_rasterize(int mode, const LineRec* recs, const uint32_t* step_off, uint32_t n_lines,
+                             uint64_t n_steps, uint32_t steps_per_block, uint32_t block, SegFormat fmt, int render,
+                             RenderGeom geom, uint32_t* block_counts, uint32_t* block_totals,
+                             const uint32_t* block_off, uint64_t* out, cudaStream_t st);
+cudaError_t launch_compact_lines(const float* in4[4], const uint32_t* lid_in, uint32_t n, const LayerRec* layers,
+                                 uint32_t n_layer_recs, float* out4[4], uint32_t* lid_out, uint32_t* flags,
+                                 uint32_t* offsets, Scratch* s, cudaStream_t st, uint32_t* n_out_host);
+
+// k_sort.cu
+// Exclusive scan of n u32 values; out has n+1 entries (out[n] = total mod 2^32).
+// *total_host receives the exact 64-bit total (synchronizes).
+cudaError_t scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, Scratch* s, cudaStream_t st,
+                     uint64_t* total_host);
+// Sort n u64 keys by bits [bit_lo, bit_hi).  `keys` and `tmp` hold n keys;
+// on return *result points at the sorted array (keys or tmp).
+cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo, int bit_hi, int digit_bits,
+                           Scratch* s, uint32_t* err_flag, cudaStream_t st, uint64_t** result, int* passes);
+size_t radix_sort_scratch_bytes(uint32_t n, int bit_lo, int bit_hi, int digit_bits);
+size_t scan_scratch_bytes(uint32_t n);
+
+// k_paint.cu
+struct PaintParams {
+    RenderGeom geom;
+    uint32_t width, height, stride;  // pixels
+    float clear[4];
+    uint8_t* out;  // device RGBA8
+    const PaintProps* props;
+    const uint8_t* unchanged;  // per order, or null (no layer cache)
+    int32_t* prev_layers;      // per tile, or null
+    uint32_t crop_h0, crop_h1, crop_v0, crop_v1;  // in tiles
+};
+struct CarryBuffers {
+    uint32_t* tl_start;   // [G + 1]
+    uint64_t* tl_cover;   // [G]
+    uint64_t* tl_carry;   // [G]
+    uint32_t* tl_flags;   // per-segment / per-TL scratch
+    uint32_t* item_count; // [G]
+    uint32_t* item_off;   // [G + 1]
+    uint64_t* items;      // [W]
+    uint64_t* items_tmp;  // [W]
+    uint32_t* tile_start; // [tiles + 1]
+};
+cudaError_t launch_tl_heads(int mode, const uint64_t* segs, uint32_t n, uint32_t* block_counts, const uint32_t* block_off,
+                            uint32_t* tl_start, cudaStream_t st);
+cudaError_t launch_tl_reduce_scan(const uint64_t* segs, uint32_t n_segs, uint32_t G, const RenderGeom& geom,
+                                  CarryBuffers& cb, Scratch* s, cudaStream_t st);
+cudaError_t launch_items(int mode, const uint64_t* segs, uint32_t G, const RenderGeom& geom, const PaintProps* props,
+                         CarryBuffers& cb, int idx_bits, cudaStream_t st);
+cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_tiles, int shift, uint32_t n_orders,
+                               uint32_t* tile_start, cudaStream_t st);
+cudaError_t launch_paint(const PaintParams& p, const uint64_t* segs, const uint64_t* items, int idx_bits,
+                         const uint32_t* tile_start, const CarryBuffers& cb, uint32_t warps_per_block,
+                         cudaStream_t st);
+
+// Generic block-count compaction helper: scan of per-block counts.
+cudaError_t scan_block_counts(const uint32_t* counts, uint32_t* offsets, uint32_t n_blocks, Scratch* s,
+                              cudaStream_t st, uint64_t* total_host);
+
+}  // namespace cgb

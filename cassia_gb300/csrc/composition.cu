@@ -1,0 +1,987 @@
+// C ABI of cassia_gb300: mold's Composition / Layer / Props API
+// (mold/src/composition.rs, mold/src/layer.rs) over the GPU pipeline
+//   build lines -> rasterize -> radix sort -> carries / work items -> paint.
+//
+// Host state mirrors mold: layers by id (FxHashMap<u16, Layer> in the
+// reference), an IdSet of free ids, orders_to_layers, per-cache layer counts.
+// Lines live on the device (the LinesBuilder SoA, surpass/src/segment.rs:30-89)
+// and are garbage-collected by the reference's rule (composition.rs:124-142).
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "cgb_internal.cuh"
+
+namespace cgb {
+uint32_t raster_grid(uint64_t n_steps, uint32_t block);
+uint32_t tl_heads_grid(uint32_t n);
+cudaError_t launch_items_crop(int mode, const uint64_t* segs, uint32_t G, const RenderGeom& geom,
+                              const PaintParams& pp, CarryBuffers& cb, int idx_bits, cudaStream_t st);
+}  // namespace cgb
+
+using namespace cgb;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+cgb_status fail(cgb_status st, const std::string& msg) {
+    g_last_error = msg;
+    return st;
+}
+
+cgb_status from_cuda(cudaError_t e, const char* where) {
+    if (e == cudaSuccess) return CGB_OK;
+    std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return fail(CGB_ERR_OUT_OF_MEMORY, m);
+    return fail(CGB_ERR_DEVICE, m);
+}
+
+#define CK(expr)                                                  \
+    do {                                                          \
+        cudaError_t _e = (expr);                                  \
+        if (_e != cudaSuccess) return c->cuda_fail(_e, #expr);   \
+    } while (0)
+
+int bits_for(uint64_t max_value) {  // bits to hold values in [0, max_value]
+    int b = 0;
+    while (b < 64 && (max_value >> b) != 0) b++;
+    return std::max(b, 1);
+}
+
+struct HostProps {
+    cgb_props c{};
+    std::vector<float> stops;
+    bool operator==(const HostProps& o) const {
+        if (c.fill_rule != o.c.fill_rule || c.func != o.c.func) return false;
+        if (c.func == CGB_FUNC_CLIP) return c.clip_layers == o.c.clip_layers;
+        if (c.is_clipped != o.c.is_clipped || c.blend_mode != o.c.blend_mode || c.fill_kind != o.c.fill_kind)
+            return false;
+        if (c.fill_kind == CGB_FILL_SOLID) return std::memcmp(c.color, o.c.color, sizeof(c.color)) == 0;
+        return c.gradient_type == o.c.gradient_type && c.n_stops == o.c.n_stops &&
+               std::memcmp(c.gradient_start, o.c.gradient_start, 8) == 0 &&
+               std::memcmp(c.gradient_end, o.c.gradient_end, 8) == 0 && stops == o.stops;
+    }
+};
+
+HostProps default_props() {
+    HostProps p;
+    p.c.fill_rule = CGB_FILL_NONZERO;
+    p.c.func = CGB_FUNC_DRAW;
+    p.c.blend_mode = CGB_BLEND_OVER;
+    p.c.fill_kind = CGB_FILL_SOLID;
+    p.c.color[3] = 1.0f;  // Fill::default (style.rs:183-187)
+    return p;
+}
+
+struct HostLayer {
+    bool enabled = true;
+    bool has_transform = false;
+    float t[6] = {1, 0, 0, 1, 0, 0};
+    bool has_order = false;
+    uint32_t order = 0;
+    HostProps props = default_props();
+    uint32_t unchanged = 0;  // SmallBitSet of cache ids (mold/src/layer.rs:101-142)
+    uint64_t len = 0;
+};
+
+struct CacheState {
+    DevBuf prev;  // int32 per tile, -1 = None
+    uint64_t tiles = 0;
+};
+
+}  // namespace
+
+struct cgb_composition {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool wide = false;
+    uint32_t max_ids = 1u << 16;
+    Scratch s;
+    cgb_tuning tuning{8, 256, 2048, 4};
+    cgb_stats stats{};
+
+    // LinesBuilder (device SoA)
+    DevBuf p0x, p0y, p1x, p1y, lids;
+    uint64_t n_lines = 0, line_cap = 0;
+    bool has_default_transform = false;
+    float default_transform[6] = {1, 0, 0, 1, 0, 0};
+
+    std::map<uint32_t, HostLayer> layers;
+    std::set<uint32_t> used_ids;
+    std::map<uint32_t, uint32_t> orders_to_layers;
+    bool layers_dirty = true;
+    DevBuf d_layers;
+    uint32_t n_layer_recs = 0;
+
+    // frame buffers
+    DevBuf recs, lengths, step_off, bcounts, btotals, boff, btoff, segs_a, segs_b;
+    DevBuf tl_start, tl_cover, tl_carry, tl_flags, item_count, item_off, items_a, items_b, tile_start;
+    DevBuf d_props, d_unchanged, out_rgba, err, dflt_t;
+    // flatten staging
+    DevBuf f_kinds, f_points, f_cmd_off, f_pt_off, f_t9, f_has_t, f_path_layer, f_counts, f_off;
+    // GC staging
+    DevBuf g_flags, g_off, g_tmp[5];
+
+    uint32_t caches_used = 0;
+    std::map<int32_t, CacheState> caches;
+
+    cudaEvent_t ev[8] = {};
+
+    cgb_status cuda_fail(cudaError_t e, const char* where) {
+        if (e == cudaErrorMemoryAllocation && s.over_budget) {
+            s.over_budget = false;
+            return fail(CGB_ERR_OVER_BUDGET, std::string(where) + ": HBM budget exceeded");
+        }
+        return from_cuda(e, where);
+    }
+};
+
+namespace cgb {
+
+static std::atomic<uint64_t> g_launches{0};
+void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+cudaError_t Scratch::ensure(DevBuf& b, size_t bytes) {
+    if (bytes <= b.cap) return cudaSuccess;
+    size_t want = std::max(bytes, b.cap + b.cap / 4);
+    want = (want + 255) & ~(size_t)255;
+    if (budget && used - b.cap + want > budget) {
+        want = bytes;
+        if (used - b.cap + want > budget) {
+            over_budget = true;
+            return cudaErrorMemoryAllocation;
+        }
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return e;
+    }
+    if (b.p) cudaFree(b.p);
+    used = used - b.cap + want;
+    b.p = p;
+    b.cap = want;
+    return cudaSuccess;
+}
+
+void Scratch::release(DevBuf& b) {
+    if (b.p) cudaFree(b.p);
+    used -= b.cap;
+    b.p = nullptr;
+    b.cap = 0;
+}
+
+}  // namespace cgb
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+// Grows a device buffer while keeping its first `keep` bytes.
+cudaError_t grow_keep(cgb_composition* c, DevBuf& b, size_t bytes, size_t keep) {
+    if (bytes <= b.cap) return cudaSuccess;
+    DevBuf nb;
+    size_t want = std::max(bytes, b.cap * 2);
+    Scratch tmp = c->s;
+    (void)tmp;
+    cudaError_t e = c->s.ensure(nb, want);
+    if (e != cudaSuccess) {
+        e = c->s.ensure(nb, bytes);
+        if (e != cudaSuccess) return e;
+    }
+    if (keep && b.p) {
+        e = cudaMemcpyAsync(nb.p, b.p, keep, cudaMemcpyDeviceToDevice, c->stream);
+        if (e != cudaSuccess) return e;
+        e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return e;
+    }
+    c->s.release(b);
+    b = nb;
+    return cudaSuccess;
+}
+
+cudaError_t ensure_lines(cgb_composition* c, uint64_t n) {
+    if (n <= c->line_cap) return cudaSuccess;
+    uint64_t cap = std::max<uint64_t>(n, c->line_cap * 2);
+    cap = std::max<uint64_t>(cap, 1024);
+    DevBuf* arrs[5] = {&c->p0x, &c->p0y, &c->p1x, &c->p1y, &c->lids};
+    for (DevBuf* a : arrs) {
+        cudaError_t e = grow_keep(c, *a, cap * 4, c->n_lines * 4);
+        if (e != cudaSuccess) return e;
+    }
+    c->line_cap = cap;
+    return cudaSuccess;
+}
+
+HostLayer* find_layer(cgb_composition* c, uint32_t id) {
+    auto it = c->layers.find(id);
+    return it == c->layers.end() ? nullptr : &it->second;
+}
+
+// insert_segments bookkeeping (mold/src/composition.rs:58-79)
+void insert_bookkeeping(cgb_composition* c, uint32_t id, uint64_t n) {
+    HostLayer& l = c->layers[id];
+    l.has_order = true;
+    l.order = id;
+    l.enabled = true;
+    l.len += n;
+    c->used_ids.insert(id);
+    c->layers_dirty = true;
+}
+
+uint64_t actual_len(cgb_composition* c) {
+    uint64_t s = 0;
+    for (auto& kv : c->layers)
+        if (kv.second.enabled) s += kv.second.len;
+    return s;
+}
+
+cgb_status upload_layers(cgb_composition* c) {
+    if (!c->layers_dirty) return CGB_OK;
+    uint32_t n = 0;
+    for (auto& kv : c->layers) n = std::max(n, kv.first + 1);
+    std::vector<LayerRec> recs(std::max<uint32_t>(n, 1));
+    std::memset(recs.data(), 0, recs.size() * sizeof(LayerRec));
+    for (auto& kv : c->layers) {
+        LayerRec& r = recs[kv.first];
+        const HostLayer& l = kv.second;
+        r.flags = LAYER_PRESENT | (l.enabled ? LAYER_ENABLED : 0u) | (l.has_transform ? LAYER_HAS_TRANSFORM : 0u) |
+                  (l.has_order ? LAYER_HAS_ORDER : 0u);
+        r.order = l.order;
+        std::memcpy(r.t, l.t, sizeof(r.t));
+    }
+    CK(c->s.ensure(c->d_layers, recs.size() * sizeof(LayerRec)));
+    CK(cudaMemcpyAsync(c->d_layers.p, recs.data(), recs.size() * sizeof(LayerRec), cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->n_layer_recs = n;
+    c->layers_dirty = false;
+    return CGB_OK;
+}
+
+// Composition::remove_disabled (mold/src/composition.rs:124-142)
+cgb_status remove_disabled(cgb_composition* c) {
+    if (c->n_lines < actual_len(c) * 2) return CGB_OK;
+    cgb_status st = upload_layers(c);
+    if (st) return st;
+    uint32_t n = (uint32_t)c->n_lines;
+    if (n > 0) {
+        CK(c->s.ensure(c->g_flags, (size_t)n * 4));
+        CK(c->s.ensure(c->g_off, ((size_t)n + 1) * 4));
+        for (int k = 0; k < 5; k++) CK(c->s.ensure(c->g_tmp[k], (size_t)n * 4));
+        const float* in4[4] = {c->p0x.as<float>(), c->p0y.as<float>(), c->p1x.as<float>(), c->p1y.as<float>()};
+        float* out4[4] = {c->g_tmp[0].as<float>(), c->g_tmp[1].as<float>(), c->g_tmp[2].as<float>(),
+                          c->g_tmp[3].as<float>()};
+        uint32_t kept = 0;
+        CK(launch_compact_lines(in4, c->lids.as<uint32_t>(), n, c->d_layers.as<LayerRec>(), c->n_layer_recs, out4,
+                                c->g_tmp[4].as<uint32_t>(), c->g_flags.as<uint32_t>(), c->g_off.as<uint32_t>(), &c->s,
+                                c->stream, &kept));
+        DevBuf* arrs[5] = {&c->p0x, &c->p0y, &c->p1x, &c->p1y, &c->lids};
+        for (int k = 0; k < 5; k++)
+            CK(cudaMemcpyAsync(arrs[k]->p, c->g_tmp[k].p, (size_t)kept * 4, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        c->n_lines = kept;
+    }
+    for (auto it = c->layers.begin(); it != c->layers.end();) {
+        if (!it->second.enabled) {
+            c->used_ids.erase(it->first);
+            it = c->layers.erase(it);
+        } else {
+            ++it;
+        }
+    }
+    c->layers_dirty = true;
+    return CGB_OK;
+}
+
+// Validates a command stream; returns the float count or -1.
+int64_t count_floats(const uint32_t* kinds, size_t n) {
+    int64_t f = 0;
+    for (size_t i = 0; i < n; i++) {
+        switch (kinds[i]) {
+            case CGB_CMD_LINE: f += 4; break;
+            case CGB_CMD_QUAD: f += 6; break;
+            case CGB_CMD_RAT_QUAD: f += 9; break;
+            case CGB_CMD_CUBIC: f += 8; break;
+            case CGB_CMD_RAT_CUBIC: f += 12; break;
+            case CGB_CMD_CLOSE: break;
+            default: return -1;
+        }
+    }
+    return f;
+}
+
+cgb_status insert_paths(cgb_composition* c, size_t n_paths, const uint32_t* layer_ids, const uint64_t* cmd_offsets,
+                        const uint32_t* kinds, const uint64_t* point_offsets, const float* points,
+                        const float* transforms9, const uint8_t* has_transform) {
+    if (n_paths == 0) return CGB_OK;
+    if (!layer_ids || !cmd_offsets || !kinds || !point_offsets || !points)
+        return fail(CGB_ERR_INVALID_ARG, "insert_paths: null array");
+    for (size_t k = 0; k < n_paths; k++) {
+        if (layer_ids[k] >= c->max_ids) return fail(CGB_ERR_LAYER_LIMIT, "insert_paths: layer id out of range");
+        if (cmd_offsets[k + 1] < cmd_offsets[k] || point_offsets[k + 1] < point_offsets[k])
+            return fail(CGB_ERR_INVALID_ARG, "insert_paths: offsets not monotone");
+        int64_t f = count_floats(kinds + cmd_offsets[k], cmd_offsets[k + 1] - cmd_offsets[k]);
+        if (f < 0) return fail(CGB_ERR_INVALID_ARG, "insert_paths: unknown command kind");
+        if ((uint64_t)f != point_offsets[k + 1] - point_offsets[k])
+            return fail(CGB_ERR_INVALID_ARG, "insert_paths: point count does not match the commands");
+    }
+    if (n_paths >= (1u << 31)) return fail(CGB_ERR_INVALID_ARG, "insert_paths: too many paths");
+    const uint64_t n_cmds = cmd_offsets[n_paths] - cmd_offsets[0];
+    const uint64_t n_floats = point_offsets[n_paths] - point_offsets[0];
+    // rebase offsets to the uploaded slices
+    std::vector<uint64_t> co(n_paths + 1), po(n_paths + 1);
+    for (size_t k = 0; k <= n_paths; k++) {
+        co[k] = cmd_offsets[k] - cmd_offsets[0];
+        po[k] = point_offsets[k] - point_offsets[0];
+    }
+    CK(c->s.ensure(c->f_kinds, std::max<size_t>(n_cmds, 1) * 4));
+    CK(c->s.ensure(c->f_points, std::max<size_t>(n_floats, 1) * 4));
+    CK(c->s.ensure(c->f_cmd_off, (n_paths + 1) * 8));
+    CK(c->s.ensure(c->f_pt_off, (n_paths + 1) * 8));
+    CK(c->s.ensure(c->f_path_layer, n_paths * 4));
+    CK(c->s.ensure(c->f_counts, n_paths * 4));
+    CK(c->s.ensure(c->f_off, (n_paths + 1) * 4));
+    cudaStream_t st = c->stream;
+    CK(cudaMemcpyAsync(c->f_kinds.p, kinds + cmd_offsets[0], n_cmds * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->f_points.p, points + point_offsets[0], n_floats * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->f_cmd_off.p, co.data(), (n_paths + 1) * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->f_pt_off.p, po.data(), (n_paths + 1) * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->f_path_layer.p, layer_ids, n_paths * 4, cudaMemcpyHostToDevice, st));
+    const float* dt = nullptr;
+    const uint8_t* dh = nullptr;
+    if (transforms9 && has_transform) {
+        CK(c->s.ensure(c->f_t9, n_paths * 9 * 4));
+        CK(c->s.ensure(c->f_has_t, n_paths));
+        CK(cudaMemcpyAsync(c->f_t9.p, transforms9, n_paths * 9 * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(c->f_has_t.p, has_transform, n_paths, cudaMemcpyHostToDevice, st));
+        dt = c->f_t9.as<float>();
+        dh = c->f_has_t.as<uint8_t>();
+    }
+    CK(launch_flatten(0, c->f_kinds.as<uint32_t>(), c->f_points.as<float>(), c->f_cmd_off.as<uint64_t>(),
+                      c->f_pt_off.as<uint64_t>(), dt, dh, c->f_path_layer.as<uint32_t>(), (uint32_t)n_paths,
+                      c->f_counts.as<uint32_t>(), nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, st));
+    uint64_t total = 0;
+    CK(scan_u32(c->f_counts.as<uint32_t>(), c->f_off.as<uint32_t>(), (uint32_t)n_paths, &c->s, st, &total));
+    if (c->n_lines + total >= (1ull << 32)) return fail(CGB_ERR_LAYER_LIMIT, "insert_paths: more than 2^32 lines");
+    CK(ensure_lines(c, c->n_lines + total));
+    const uint64_t base = c->n_lines;
+    CK(launch_flatten(1, c->f_kinds.as<uint32_t>(), c->f_points.as<float>(), c->f_cmd_off.as<uint64_t>(),
+                      c->f_pt_off.as<uint64_t>(), dt, dh, c->f_path_layer.as<uint32_t>(), (uint32_t)n_paths, nullptr,
+                      c->f_off.as<uint32_t>(), c->p0x.as<float>() + base, c->p0y.as<float>() + base,
+                      c->p1x.as<float>() + base, c->p1y.as<float>() + base, c->lids.as<uint32_t>() + base, st));
+    std::vector<uint32_t> counts(n_paths);
+    CK(cudaMemcpyAsync(counts.data(), c->f_counts.p, n_paths * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    c->n_lines += total;
+    for (size_t k = 0; k < n_paths; k++) insert_bookkeeping(c, layer_ids[k], counts[k]);
+    return CGB_OK;
+}
+
+struct FrameGeom {
+    uint32_t width, height, stride, rows, row_len;
+};
+
+// LinesBuilder::build + Rasterizer::rasterize (+ re-keying / culling in
+// render mode).  Leaves n_segs keys in segs_a.
+cgb_status build_and_rasterize(cgb_composition* c, int render, const RenderGeom& geom, uint64_t* n_segs,
+                               uint64_t* n_total) {
+    cudaStream_t st = c->stream;
+    const uint32_t L = (uint32_t)c->n_lines;
+    c->stats.lines = L;
+    CK(c->s.ensure(c->recs, std::max<size_t>(L, 1) * sizeof(LineRec)));
+    CK(c->s.ensure(c->lengths, std::max<size_t>(L, 1) * 4));
+    CK(c->s.ensure(c->step_off, ((size_t)L + 1) * 4));
+    const float* dflt = nullptr;
+    if (c->has_default_transform) {
+        CK(c->s.ensure(c->dflt_t, 6 * 4));
+        CK(cudaMemcpyAsync(c->dflt_t.p, c->default_transform, 24, cudaMemcpyHostToDevice, st));
+        dflt = c->dflt_t.as<float>();
+    }
+    CK(cudaEventRecord(c->ev[0], st));
+    CK(launch_build_lines(c->p0x.as<float>(), c->p0y.as<float>(), c->p1x.as<float>(), c->p1y.as<float>(),
+                          c->lids.as<uint32_t>(), L, c->d_layers.as<LayerRec>(), c->n_layer_recs, dflt,
+                          c->recs.as<LineRec>(), c->lengths.as<uint32_t>(), st));
+    uint64_t S = 0;
+    CK(scan_u32(c->lengths.as<uint32_t>(), c->step_off.as<uint32_t>(), L, &c->s, st, &S));
+    CK(cudaEventRecord(c->ev[1], st));
+    if (S >= (1ull << 32)) return fail(CGB_ERR_LAYER_LIMIT, "more than 2^32 pixel steps");
+    c->stats.steps = S;
+    const uint32_t block = c->tuning.raster_block;
+    const uint32_t grid = raster_grid(S, block);
+    CK(c->s.ensure(c->bcounts, ((size_t)grid + 1) * 4));
+    CK(c->s.ensure(c->btotals, ((size_t)grid + 1) * 4));
+    CK(c->s.ensure(c->boff, ((size_t)grid + 1) * 4));
+    CK(c->s.ensure(c->btoff, ((size_t)grid + 1) * 4));
+    SegFormat fmt{c->wide ? 1u : 0u};
+    CK(launch_rasterize(0, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, S, 0, block, fmt, render, geom,
+                        c->bcounts.as<uint32_t>(), c->btotals.as<uint32_t>(), nullptr, nullptr, st));
+    uint64_t P = 0, PT = 0;
+    CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid, &c->s, st, &P));
+    CK(scan_u32(c->btotals.as<uint32_t>(), c->btoff.as<uint32_t>(), grid, &c->s, st, &PT));
+    if (P >= (1ull << 30)) return fail(CGB_ERR_LAYER_LIMIT, "more than 2^30 pixel segments");
+    CK(c->s.ensure(c->segs_a, std::max<size_t>(P, 1) * 8));
+    CK(c->s.ensure(c->segs_b, std::max<size_t>(P, 1) * 8));
+    CK(launch_rasterize(1, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, S, 0, block, fmt, render, geom,
+                        nullptr, nullptr, c->boff.as<uint32_t>(), c->segs_a.as<uint64_t>(), st));
+    CK(cudaEventRecord(c->ev[2], st));
+    *n_segs = P;
+    *n_total = PT;
+    c->stats.segments = PT;
+    return CGB_OK;
+}
+
+cgb_status check_device_error(cgb_composition* c) {
+    uint32_t v = 0;
+    CK(cudaMemcpyAsync(&v, c->err.p, 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (v) {
+        CK(cudaMemsetAsync(c->err.p, 0, 4, c->stream));
+        return fail(CGB_ERR_DEVICE_TIMEOUT, "a bounded device-side wait expired");
+    }
+    return CGB_OK;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+        cudaGetLastError();
+        return 0.0f;
+    }
+    return ms;
+}
+
+cgb_status render(cgb_composition* c, const cgb_buffer* buf, const float bg[4], const cgb_rect* crop) {
+    if (!buf || !bg || !buf->pixels || buf->width == 0 || buf->height == 0)
+        return fail(CGB_ERR_INVALID_ARG, "render: empty buffer");
+    const uint64_t stride = buf->width_stride ? buf->width_stride : buf->width;
+    if (stride < buf->width || buf->width > (1u << 20) || buf->height > (1u << 20))
+        return fail(CGB_ERR_INVALID_ARG, "render: bad width/stride/height");
+    cudaStream_t st = c->stream;
+    FrameGeom fg{(uint32_t)buf->width, (uint32_t)buf->height, (uint32_t)stride, (uint32_t)((buf->height + 7) / 8),
+                 (uint32_t)((buf->width + 7) / 8)};
+    const uint64_t n_tiles = (uint64_t)fg.rows * fg.row_len;
+    CacheState* cache = nullptr;
+    if (buf->layer_cache >= 0) {
+        auto it = c->caches.find(buf->layer_cache);
+        if (it == c->caches.end()) return fail(CGB_ERR_NOT_FOUND, "render: unknown layer cache");
+        cache = &it->second;
+        if (cache->tiles != n_tiles) {  // composition.rs:218-225
+            CK(c->s.ensure(cache->prev, n_tiles * 4));
+            CK(cudaMemsetAsync(cache->prev.p, 0xFF, n_tiles * 4, st));
+            cache->tiles = n_tiles;
+        }
+    }
+    cgb_status s0 = remove_disabled(c);
+    if (s0) return s0;
+    for (auto& kv : c->layers)
+        if (kv.second.enabled) c->orders_to_layers[kv.second.order] = kv.first;
+    // LayerProps by order (composition.rs:247-284)
+    uint32_t n_orders = 1;
+    for (auto& kv : c->layers)
+        if (kv.second.enabled) n_orders = std::max(n_orders, kv.second.order + 1);
+    std::vector<PaintProps> props(n_orders);
+    std::vector<uint8_t> unchanged(cache ? n_orders : 0, 0);
+    for (uint32_t o = 0; o < n_orders; o++) {
+        PaintProps& pp = props[o];
+        pp = PaintProps{CGB_FILL_NONZERO, CGB_BLEND_OVER, PROPS_SOLID | PROPS_DRAW | PROPS_OPAQUE_OVER, 0, {0, 0, 0, 1}};
+    }
+    for (auto& kv : c->orders_to_layers) {
+        if (kv.first >= n_orders) continue;
+        HostLayer* l = find_layer(c, kv.second);
+        if (!l || !l->enabled) continue;
+        const cgb_props& p = l->props.c;
+        if (p.func != CGB_FUNC_DRAW || p.is_clipped)
+            return fail(CGB_ERR_INVALID_ARG, "render: clip layers are not supported by the GPU painter");
+        if (p.fill_kind != CGB_FILL_SOLID)
+            return fail(CGB_ERR_INVALID_ARG, "render: gradient fills are not supported by the GPU painter");
+        PaintProps& pp = props[kv.first];
+        pp.fill_rule = p.fill_rule;
+        pp.blend_mode = p.blend_mode;
+        pp.flags = PROPS_SOLID | PROPS_DRAW | PROPS_PRESENT;
+        if (p.blend_mode == CGB_BLEND_OVER && p.color[3] == 1.0f) pp.flags |= PROPS_OPAQUE_OVER;
+        std::memcpy(pp.color, p.color, sizeof(pp.color));
+        if (cache) unchanged[kv.first] = (l->unchanged >> buf->layer_cache) & 1;
+    }
+    RenderGeom geom{fg.rows, fg.row_len, n_orders, 0};
+    geom.key_bits = bits_for((uint64_t)fg.rows * n_orders * (fg.row_len + 1) - 1);
+    if (geom.key_bits > 42) return fail(CGB_ERR_LAYER_LIMIT, "render: canvas x orders too large for the segment key");
+    cgb_status s1 = upload_layers(c);
+    if (s1) return s1;
+    CK(c->s.ensure(c->d_props, props.size() * sizeof(PaintProps)));
+    CK(cudaMemcpyAsync(c->d_props.p, props.data(), props.size() * sizeof(PaintProps), cudaMemcpyHostToDevice, st));
+    if (cache) {
+        CK(c->s.ensure(c->d_unchanged, unchanged.size()));
+        CK(cudaMemcpyAsync(c->d_unchanged.p, unchanged.data(), unchanged.size(), cudaMemcpyHostToDevice, st));
+    }
+
+    uint64_t P = 0, PT = 0;
+    cgb_status s2 = build_and_rasterize(c, 1, geom, &P, &PT);
+    if (s2) return s2;
+    c->stats.painted_segments = P;
+    // sort by (row, order, tile column)
+    uint64_t* sorted = c->segs_a.as<uint64_t>();
+    int passes = 0;
+    CK(radix_sort_u64(c->segs_a.as<uint64_t>(), c->segs_b.as<uint64_t>(), (uint32_t)P, 22, 22 + (int)geom.key_bits,
+                      (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &sorted, &passes));
+    c->stats.sort_passes = passes;
+    CK(cudaEventRecord(c->ev[3], st));
+
+    // tile-layer groups, carries, work items
+    CarryBuffers cb{};
+    const uint32_t hg = tl_heads_grid((uint32_t)P);
+    CK(c->s.ensure(c->bcounts, ((size_t)hg + 1) * 4));
+    CK(c->s.ensure(c->boff, ((size_t)hg + 1) * 4));
+    CK(launch_tl_heads(0, sorted, (uint32_t)P, c->bcounts.as<uint32_t>(), nullptr, nullptr, st));
+    uint64_t G = 0;
+    if (P) CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), hg, &c->s, st, &G));
+    c->stats.tile_layers = G;
+    CK(c->s.ensure(c->tl_start, (G + 1) * 4));
+    CK(c->s.ensure(c->tl_cover, std::max<uint64_t>(G, 1) * 8));
+    CK(c->s.ensure(c->tl_carry, std::max<uint64_t>(G, 1) * 8));
+    CK(c->s.ensure(c->tl_flags, std::max<uint64_t>(G, 1) * 4));
+    CK(c->s.ensure(c->item_count, std::max<uint64_t>(G, 1) * 4));
+    CK(c->s.ensure(c->item_off, (G + 1) * 4));
+    cb.tl_start = c->tl_start.as<uint32_t>();
+    cb.tl_cover = c->tl_cover.as<uint64_t>();
+    cb.tl_carry = c->tl_carry.as<uint64_t>();
+    cb.tl_flags = c->tl_flags.as<uint32_t>();
+    cb.item_count = c->item_count.as<uint32_t>();
+    cb.item_off = c->item_off.as<uint32_t>();
+    CK(launch_tl_heads(1, sorted, (uint32_t)P, nullptr, c->boff.as<uint32_t>(), cb.tl_start, st));
+    uint32_t P32 = (uint32_t)P;
+    CK(cudaMemcpyAsync(cb.tl_start + G, &P32, 4, cudaMemcpyHostToDevice, st));
+    CK(launch_tl_reduce_scan(sorted, (uint32_t)P, (uint32_t)G, geom, cb, &c->s, st));
+
+    PaintParams pp{};
+    pp.geom = geom;
+    pp.width = fg.width;
+    pp.height = fg.height;
+    pp.stride = fg.stride;
+    std::memcpy(pp.clear, bg, sizeof(pp.clear));
+    pp.props = c->d_props.as<PaintProps>();
+    pp.unchanged = cache ? c->d_unchanged.as<uint8_t>() : nullptr;
+    pp.prev_layers = cache ? cache->prev.as<int32_t>() : nullptr;
+    pp.crop_h0 = 0;
+    pp.crop_h1 = fg.row_len;
+    pp.crop_v0 = 0;
+    pp.crop_v1 = fg.rows;
+    if (crop) {  // Rect::new (buffer_layout.rs:43-50)
+        pp.crop_h0 = (uint32_t)std::min<uint64_t>(crop->x0 / 8, fg.row_len);
+        pp.crop_h1 = (uint32_t)std::min<uint64_t>((crop->x1 + 7) / 8, fg.row_len);
+        pp.crop_v0 = (uint32_t)std::min<uint64_t>(crop->y0 / 8, fg.rows);
+        pp.crop_v1 = (uint32_t)std::min<uint64_t>((crop->y1 + 7) / 8, fg.rows);
+    }
+    CK(launch_items_crop(0, sorted, (uint32_t)G, geom, pp, cb, 0, st));
+    uint64_t W = 0;
+    if (G) CK(scan_u32(cb.item_count, cb.item_off, (uint32_t)G, &c->s, st, &W));
+    c->stats.work_items = W;
+    const int idx_bits = bits_for(std::max<uint64_t>(G, 1) - 1);
+    const int item_key_bits = bits_for(n_tiles * n_orders * 2 - 1);
+    if (idx_bits + item_key_bits > 64 || W >= (1ull << 30))
+        return fail(CGB_ERR_LAYER_LIMIT, "render: too many tile x layer work items");
+    CK(c->s.ensure(c->items_a, std::max<uint64_t>(W, 1) * 8));
+    CK(c->s.ensure(c->items_b, std::max<uint64_t>(W, 1) * 8));
+    CK(c->s.ensure(c->tile_start, (n_tiles + 1) * 4));
+    cb.items = c->items_a.as<uint64_t>();
+    cb.items_tmp = c->items_b.as<uint64_t>();
+    cb.tile_start = c->tile_start.as<uint32_t>();
+    CK(launch_items_crop(1, sorted, (uint32_t)G, geom, pp, cb, idx_bits, st));
+    uint64_t* items_sorted = cb.items;
+    int ipasses = 0;
+    CK(radix_sort_u64(cb.items, cb.items_tmp, (uint32_t)W, idx_bits + 1, idx_bits + item_key_bits,
+                      (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &items_sorted, &ipasses));
+    c->stats.item_sort_passes = ipasses;
+    CK(launch_tile_ranges(items_sorted, (uint32_t)W, (uint32_t)n_tiles, idx_bits + 1, n_orders, cb.tile_start, st));
+    CK(cudaEventRecord(c->ev[4], st));
+
+    // output
+    const bool host = buf->memory == CGB_MEMORY_HOST;
+    uint8_t* out = buf->pixels;
+    if (host) {
+        CK(c->s.ensure(c->out_rgba, (size_t)fg.height * fg.stride * 4));
+        out = c->out_rgba.as<uint8_t>();
+        if (cache || crop)  // tiles that are not repainted keep the caller's pixels
+            CK(cudaMemcpy2DAsync(out, (size_t)fg.stride * 4, buf->pixels, (size_t)fg.stride * 4,
+                                 (size_t)fg.width * 4, fg.height, cudaMemcpyHostToDevice, st));
+    }
+    pp.out = out;
+    CK(launch_paint(pp, sorted, items_sorted, idx_bits, cb.tile_start, cb, c->tuning.paint_warps, st));
+    CK(cudaEventRecord(c->ev[5], st));
+    if (host)
+        CK(cudaMemcpy2DAsync(buf->pixels, (size_t)fg.stride * 4, out, (size_t)fg.stride * 4, (size_t)fg.width * 4,
+                             fg.height, cudaMemcpyDeviceToHost, st));
+    cgb_status s3 = check_device_error(c);
+    if (s3) return s3;
+    c->stats.build_ms = elapsed(c->ev[0], c->ev[1]);
+    c->stats.rasterize_ms = elapsed(c->ev[1], c->ev[2]);
+    c->stats.sort_ms = elapsed(c->ev[2], c->ev[3]);
+    c->stats.carry_ms = elapsed(c->ev[3], c->ev[4]);
+    c->stats.paint_ms = elapsed(c->ev[4], c->ev[5]);
+    c->stats.total_ms = elapsed(c->ev[0], c->ev[5]);
+    if (cache)  // composition.rs:322-327
+        for (auto& kv : c->layers) {
+            if (kv.second.enabled) kv.second.unchanged |= 1u << buf->layer_cache;
+            else kv.second.unchanged &= ~(1u << buf->layer_cache);
+        }
+    return CGB_OK;
+}
+
+}  // namespace
+
+#define HANDLE_CHECK()                                                      \
+    if (!c) return fail(CGB_ERR_INVALID_ARG, "null composition handle");   \
+    DeviceGuard _guard(c->device)
+
+extern "C" {
+
+CGB_EXPORT const char* cgb_version(void) { return "cassia_gb300 0.1.0 (sm_103a)"; }
+CGB_EXPORT const char* cgb_last_error(void) { return g_last_error.c_str(); }
+
+CGB_EXPORT cgb_status cgb_composition_new(uint32_t flags, uint64_t hbm_budget_bytes, cgb_composition** out) {
+    if (!out) return fail(CGB_ERR_INVALID_ARG, "null out");
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(CGB_ERR_NO_DEVICE, "no CUDA device");
+    }
+    cgb_composition* c = new cgb_composition();
+    cudaGetDevice(&c->device);
+    c->wide = (flags & CGB_COMPOSITION_WIDE_LAYERS) != 0;
+    c->max_ids = c->wide ? (1u << 17) : (1u << 16);
+    c->s.budget = hbm_budget_bytes;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->s.pinned, 64);
+    for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
+    if (e == cudaSuccess) e = c->s.ensure(c->err, 256);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->err.p, 0, 4, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        cgb_status st = c->cuda_fail(e, "cgb_composition_new");
+        cgb_composition_free(c);
+        return st;
+    }
+    *out = c;
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_composition_free(cgb_composition* c) {
+    if (!c) return CGB_OK;
+    DeviceGuard g(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    DevBuf* bufs[] = {&c->p0x, &c->p0y, &c->p1x, &c->p1y, &c->lids, &c->d_layers, &c->recs, &c->lengths,
+                      &c->step_off, &c->bcounts, &c->btotals, &c->boff, &c->btoff, &c->segs_a, &c->segs_b,
+                      &c->tl_start, &c->tl_cover, &c->tl_carry, &c->tl_flags, &c->item_count, &c->item_off,
+                      &c->items_a, &c->items_b, &c->tile_start, &c->d_props, &c->d_unchanged, &c->out_rgba, &c->err,
+                      &c->dflt_t, &c->f_kinds, &c->f_points, &c->f_cmd_off, &c->f_pt_off, &c->f_t9, &c->f_has_t,
+                      &c->f_path_layer, &c->f_counts, &c->f_off, &c->g_flags, &c->g_off, &c->s.scan_sums,
+                      &c->s.sort_hist, &c->s.sort_lookback, &c->s.sort_counter};
+    for (DevBuf* b : bufs) c->s.release(*b);
+    for (auto& b : c->g_tmp) c->s.release(b);
+    for (auto& kv : c->caches) c->s.release(kv.second.prev);
+    for (auto& e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->s.pinned) cudaFreeHost(c->s.pinned);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_create_layer(cgb_composition* c, uint32_t* out_layer_id) {
+    if (!c || !out_layer_id) return fail(CGB_ERR_INVALID_ARG, "null argument");
+    uint32_t cand = 0;
+    for (uint32_t u : c->used_ids) {
+        if (u != cand) break;
+        cand++;
+    }
+    if (cand >= c->max_ids) return fail(CGB_ERR_LAYER_LIMIT, "create_layer: no free layer id");
+    c->used_ids.insert(cand);
+    *out_layer_id = cand;
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_insert_in_layer(cgb_composition* c, uint32_t layer_id, const uint32_t* kinds,
+                                          size_t n_cmds, const float* points, size_t n_point_floats,
+                                          const float* transform9) {
+    HANDLE_CHECK();
+    uint64_t co[2] = {0, n_cmds}, po[2] = {0, n_point_floats};
+    uint8_t has = transform9 ? 1 : 0;
+    float zero = 0.0f;
+    return insert_paths(c, 1, &layer_id, co, kinds, po, points ? points : &zero, transform9, transform9 ? &has : nullptr);
+}
+
+CGB_EXPORT cgb_status cgb_insert_paths(cgb_composition* c, size_t n_paths, const uint32_t* layer_ids,
+                                       const uint64_t* cmd_offsets, const uint32_t* kinds,
+                                       const uint64_t* point_offsets, const float* points, const float* transforms9,
+                                       const uint8_t* has_transform) {
+    HANDLE_CHECK();
+    return insert_paths(c, n_paths, layer_ids, cmd_offsets, kinds, point_offsets, points, transforms9, has_transform);
+}
+
+CGB_EXPORT cgb_status cgb_insert_lines(cgb_composition* c, uint32_t layer_id, const float* segments, size_t n_lines) {
+    HANDLE_CHECK();
+    if (layer_id >= c->max_ids) return fail(CGB_ERR_LAYER_LIMIT, "insert_lines: layer id out of range");
+    if (n_lines && !segments) return fail(CGB_ERR_INVALID_ARG, "insert_lines: null segments");
+    if (c->n_lines + n_lines >= (1ull << 32)) return fail(CGB_ERR_LAYER_LIMIT, "insert_lines: too many lines");
+    CK(ensure_lines(c, c->n_lines + n_lines));
+    if (n_lines) {
+        std::vector<float> soa(4 * n_lines);
+        std::vector<uint32_t> ids(n_lines, layer_id);
+        for (size_t i = 0; i < n_lines; i++)
+            for (int k = 0; k < 4; k++) soa[k * n_lines + i] = segments[4 * i + k];
+        DevBuf* arrs[4] = {&c->p0x, &c->p0y, &c->p1x, &c->p1y};
+        for (int k = 0; k < 4; k++)
+            CK(cudaMemcpyAsync(arrs[k]->as<float>() + c->n_lines, soa.data() + k * n_lines, n_lines * 4,
+                               cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->lids.as<uint32_t>() + c->n_lines, ids.data(), n_lines * 4, cudaMemcpyHostToDevice,
+                           c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    c->n_lines += n_lines;
+    insert_bookkeeping(c, layer_id, n_lines);
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_layer_set_enabled(cgb_composition* c, uint32_t layer_id, int enabled) {
+    if (!c) return fail(CGB_ERR_INVALID_ARG, "null composition handle");
+    HostLayer* l = find_layer(c, layer_id);
+    if (!l) return fail(CGB_ERR_NOT_FOUND, "set_enabled: unknown layer");
+    if (l->enabled != (enabled != 0)) c->layers_dirty = true;
+    l->enabled = enabled != 0;
+    return CGB_OK;
+}
+
+static cgb_status set_transform(cgb_composition* c, uint32_t layer_id, const float* t, uint32_t flags) {
+    HostLayer* l = find_layer(c, layer_id);
+    if (!l) return fail(CGB_ERR_NOT_FOUND, "set_transform: unknown layer");
+    // Layer::set_transform (mold/src/layer.rs:182-201)
+    static const float I[6] = {1, 0, 0, 1, 0, 0};
+    const bool identity = !t || std::memcmp(t, I, sizeof(I)) == 0 ||
+                          (t[0] == 1 && t[1] == 0 && t[2] == 0 && t[3] == 1 && t[4] == 0 && t[5] == 0);
+    const bool has = !identity;
+    if (has && !(flags & CGB_TRANSFORM_UNCHECKED) &&
+        (t[0] * t[0] + t[2] * t[2] > 1.001f || t[1] * t[1] + t[3] * t[3] > 1.001f))
+        return fail(CGB_ERR_SCALE, "set_transform: Layer's scaling on each axis must be between -1.0 and 1.0");
+    bool changed = has != l->has_transform;
+    if (!changed && has)
+        for (int i = 0; i < 6; i++) changed |= l->t[i] != t[i];
+    if (changed) {
+        l->unchanged = 0;
+        l->has_transform = has;
+        if (has) std::memcpy(l->t, t, sizeof(l->t));
+        c->layers_dirty = true;
+    }
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_layer_set_transform(cgb_composition* c, uint32_t layer_id, const float* affine6,
+                                              uint32_t flags) {
+    if (!c) return fail(CGB_ERR_INVALID_ARG, "null composition handle");
+    return set_transform(c, layer_id, affine6, flags);
+}
+
+CGB_EXPORT cgb_status cgb_layers_set_transforms(cgb_composition* c, size_t n, const uint32_t* layer_ids,
+                                                const float* affine6, uint32_t flags) {
+    if (!c || (n && (!layer_ids || !affine6))) return fail(CGB_ERR_INVALID_ARG, "null argument");
+    for (size_t i = 0; i < n; i++) {
+        cgb_status st = set_transform(c, layer_ids[i], affine6 + 6 * i, flags);
+        if (st) return st;
+    }
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_layer_set_order(cgb_composition* c, uint32_t layer_id, uint32_t order) {
+    if (!c) return fail(CGB_ERR_INVALID_ARG, "null composition handle");
+    HostLayer* l = find_layer(c, layer_id);
+    if (!l) return fail(CGB_ERR_NOT_FOUND, "set_order: unknown layer");
+    if (order >= c->max_ids) return fail(CGB_ERR_LAYER_LIMIT, "set_order: order out of range");
+    if (!(l->has_order && l->order == order)) {
+        l->unchanged = 0;
+        l->has_order = true;
+        l->order = order;
+        c->layers_dirty = true;
+    }
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_layer_set_props(cgb_composition* c, uint32_t layer_id, const cgb_props* props) {
+    if (!c || !props) return fail(CGB_ERR_INVALID_ARG, "null argument");
+    HostLayer* l = find_layer(c, layer_id);
+    if (!l) return fail(CGB_ERR_NOT_FOUND, "set_props: unknown layer");
+    if (props->fill_rule > 1 || props->func > 1 || props->blend_mode > 11 || props->fill_kind > 1)
+        return fail(CGB_ERR_INVALID_ARG, "set_props: enum out of range");
+    HostProps hp;
+    hp.c = *props;
+    hp.c.stops = nullptr;
+    if (props->fill_kind == CGB_FILL_GRADIENT) {
+        if (props->n_stops < 2 || !props->stops) return fail(CGB_ERR_INVALID_ARG, "set_props: gradient needs 2 stops");
+        hp.stops.assign(props->stops, props->stops + 5 * (size_t)props->n_stops);
+    }
+    if (!(l->props == hp)) {
+        l->unchanged = 0;
+        l->props = hp;
+    }
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_layers_set_props(cgb_composition* c, size_t n, const uint32_t* layer_ids,
+                                           const cgb_props* props) {
+    if (!c || (n && (!layer_ids || !props))) return fail(CGB_ERR_INVALID_ARG, "null argument");
+    for (size_t i = 0; i < n; i++) {
+        cgb_status st = cgb_layer_set_props(c, layer_ids[i], props + i);
+        if (st) return st;
+    }
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_remove_disabled(cgb_composition* c) {
+    HANDLE_CHECK();
+    return remove_disabled(c);
+}
+
+CGB_EXPORT cgb_status cgb_lines_len(cgb_composition* c, uint64_t* builder_len, uint64_t* actual) {
+    if (!c || !builder_len || !actual) return fail(CGB_ERR_INVALID_ARG, "null argument");
+    *builder_len = c->n_lines;
+    *actual = actual_len(c);
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_create_buffer_layer_cache(cgb_composition* c, int32_t* out_cache_id) {
+    if (!c || !out_cache_id) return fail(CGB_ERR_INVALID_ARG, "null argument");
+    int slot = 0;  // SmallBitSet::first_empty_slot (mold/src/layer.rs:137-141)
+    while (slot < 32 && ((c->caches_used >> slot) & 1)) slot++;
+    if (slot >= 32) return fail(CGB_ERR_LAYER_LIMIT, "create_buffer_layer_cache: 32 caches in use");
+    c->caches_used |= 1u << slot;
+    c->caches[slot] = CacheState{};
+    *out_cache_id = slot;
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_release_buffer_layer_cache(cgb_composition* c, int32_t cache_id) {
+    HANDLE_CHECK();
+    auto it = c->caches.find(cache_id);
+    if (it == c->caches.end()) return fail(CGB_ERR_NOT_FOUND, "release_buffer_layer_cache: unknown cache");
+    c->s.release(it->second.prev);
+    c->caches.erase(it);
+    c->caches_used &= ~(1u << cache_id);
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_render(cgb_composition* c, const cgb_buffer* buffer, const float background[4],
+                                 const cgb_rect* crop) {
+    HANDLE_CHECK();
+    return render(c, buffer, background, crop);
+}
+
+CGB_EXPORT cgb_status cgb_pixel_segments(cgb_composition* c, uint64_t* out, size_t cap, uint64_t* out_len,
+                                         uint64_t* out_none, uint32_t order) {
+    HANDLE_CHECK();
+    if (!out_len || !out_none || order > 1) return fail(CGB_ERR_INVALID_ARG, "pixel_segments: bad argument");
+    cgb_status s0 = remove_disabled(c);
+    if (s0) return s0;
+    cgb_status s1 = upload_layers(c);
+    if (s1) return s1;
+    uint64_t P = 0, PT = 0;
+    RenderGeom geom{};
+    cgb_status s2 = build_and_rasterize(c, 0, geom, &P, &PT);
+    if (s2) return s2;
+    uint64_t* sorted = c->segs_a.as<uint64_t>();
+    int passes = 0;
+    const int lo = order == CGB_SORT_CANONICAL ? 0 : 22;
+    CK(radix_sort_u64(c->segs_a.as<uint64_t>(), c->segs_b.as<uint64_t>(), (uint32_t)P, lo, 64,
+                      (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), c->stream, &sorted, &passes));
+    c->stats.sort_passes = passes;
+    CK(cudaEventRecord(c->ev[3], c->stream));
+    *out_len = P;
+    *out_none = 2 * c->stats.steps - P;
+    if (cap < P) {
+        cgb_status s3 = check_device_error(c);
+        return s3 ? s3 : fail(CGB_ERR_CAPACITY, "pixel_segments: output array too small");
+    }
+    if (P) CK(cudaMemcpyAsync(out, sorted, P * 8, cudaMemcpyDeviceToHost, c->stream));
+    cgb_status s3 = check_device_error(c);
+    if (s3) return s3;
+    c->stats.build_ms = elapsed(c->ev[0], c->ev[1]);
+    c->stats.rasterize_ms = elapsed(c->ev[1], c->ev[2]);
+    c->stats.sort_ms = elapsed(c->ev[2], c->ev[3]);
+    c->stats.total_ms = elapsed(c->ev[0], c->ev[3]);
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_get_stats(cgb_composition* c, cgb_stats* out) {
+    if (!c || !out) return fail(CGB_ERR_INVALID_ARG, "null argument");
+    *out = c->stats;
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_set_tuning(cgb_composition* c, const cgb_tuning* t) {
+    if (!c || !t) return fail(CGB_ERR_INVALID_ARG, "null argument");
+    if (t->radix_bits) {
+        if (t->radix_bits < 4 || t->radix_bits > 8) return fail(CGB_ERR_INVALID_ARG, "radix_bits must be 4..8");
+        c->tuning.radix_bits = t->radix_bits;
+    }
+    if (t->raster_block) {
+        if (t->raster_block % 32 || t->raster_block > 256)
+            return fail(CGB_ERR_INVALID_ARG, "raster_block must be a multiple of 32, <= 256");
+        c->tuning.raster_block = t->raster_block;
+    }
+    if (t->steps_per_block) c->tuning.steps_per_block = t->steps_per_block;
+    if (t->paint_warps) {
+        if (t->paint_warps > 8) return fail(CGB_ERR_INVALID_ARG, "paint_warps must be <= 8");
+        c->tuning.paint_warps = t->paint_warps;
+    }
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_get_tuning(cgb_composition* c, cgb_tuning* out) {
+    if (!c || !out) return fail(CGB_ERR_INVALID_ARG, "null argument");
+    *out = c->tuning;
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_get_stream(cgb_composition* c, void** out_stream) {
+    if (!c || !out_stream) return fail(CGB_ERR_INVALID_ARG, "null argument");
+    *out_stream = (void*)c->stream;
+    return CGB_OK;
+}
+
+CGB_EXPORT uint64_t cgb_kernel_launches(void) { return g_launches.load(); }
+
+CGB_EXPORT cgb_status cgb_composition_clear(cgb_composition* c) {
+    if (!c) return fail(CGB_ERR_INVALID_ARG, "null composition handle");
+    c->n_lines = 0;
+    c->layers.clear();
+    c->used_ids.clear();
+    c->orders_to_layers.clear();
+    c->layers_dirty = true;
+    for (auto& kv : c->caches) kv.second.tiles = 0;
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_synchronize(cgb_composition* c) {
+    HANDLE_CHECK();
+    CK(cudaStreamSynchronize(c->stream));
+    return CGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,650 @@
+// Line expansion and rasterization kernels.
+//
+//   k_flatten      mold PathSegments (mold/src/path/segments.rs:97-263) with
+//                  Transform (mold/src/path/transform.rs:56-94): one thread per
+//                  path; a count pass, a scan of the counts, a write pass.
+//   k_build_lines  LinesBuilder::build (surpass/src/segment.rs:91-237): one
+//                  thread per line; writes a packed 32-byte LineRec + length.
+//   k_rasterize    Rasterizer::rasterize (surpass/src/rasterizer/mod.rs:214-285):
+//                  each thread walks 8 consecutive pixel steps; a count pass
+//                  sizes every block's output, a write pass block-scans the
+//                  per-thread counts, stages the segments in shared memory and
+//                  stores each block's run with coalesced 128-bit stores.  No
+//                  NONE slots are materialized.
+#include "cgb_internal.cuh"
+
+namespace cgb {
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// path flattening
+// ---------------------------------------------------------------------------
+
+struct Pt {
+    float x, y;
+};
+__device__ __forceinline__ Pt pmul(Pt p, float s) { return {p.x * s, p.y * s}; }
+__device__ __forceinline__ Pt padd(Pt a, Pt b) { return {a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ Pt plerp(float t, Pt p0, Pt p1) { return padd(pmul(p0, 1.0f - t), pmul(p1, t)); }
+__device__ __forceinline__ float lerp1(float t, float a, float b) { return a * (1.0f - t) + b * t; }
+__device__ __forceinline__ Pt from_weighted(float x, float y, float w) {
+    float r = 1.0f / w;
+    return {x * r, y * r};
+}
+__device__ __forceinline__ bool approx_eq(Pt a, Pt b) {
+    const float eps = 1.1920929e-7f;
+    return fabsf(a.x - b.x) < eps && fabsf(a.y - b.y) < eps;
+}
+
+struct Cmd {
+    uint32_t kind;
+    Pt p[4];
+    float w[4];
+};
+
+__device__ __forceinline__ int cmd_floats(uint32_t kind) {
+    switch (kind) {
+        case CGB_CMD_LINE: return 4;
+        case CGB_CMD_QUAD: return 6;
+        case CGB_CMD_RAT_QUAD: return 9;
+        case CGB_CMD_CUBIC: return 8;
+        case CGB_CMD_RAT_CUBIC: return 12;
+        default: return 0;
+    }
+}
+
+// Path::line/quad/rat_quad/cubic/rat_cubic storage (mold/src/path/mod.rs:53-143).
+__device__ Cmd load_cmd(uint32_t kind, const float* f) {
+    Cmd c;
+    c.kind = kind;
+    switch (kind) {
+        case CGB_CMD_LINE:
+        case CGB_CMD_QUAD:
+        case CGB_CMD_CUBIC: {
+            int np = kind == CGB_CMD_LINE ? 2 : kind == CGB_CMD_QUAD ? 3 : 4;
+            for (int k = 0; k < np; k++) c.p[k] = {f[2 * k], f[2 * k + 1]};
+            break;
+        }
+        case CGB_CMD_RAT_QUAD:
+        case CGB_CMD_RAT_CUBIC: {
+            int np = kind == CGB_CMD_RAT_QUAD ? 3 : 4;
+            for (int k = 0; k < np; k++) {
+                float w = f[3 * k + 2];
+                c.p[k] = pmul(Pt{f[3 * k], f[3 * k + 1]}, w);
+                c.w[k] = w;
+            }
+            break;
+        }
+        default: break;
+    }
+    return c;
+}
+
+struct DTransform {
+    float t[9];
+    bool persp;
+};
+
+__device__ DTransform make_transform(const float* t9) {
+    DTransform r;
+    float rc = 1.0f / t9[8];
+    for (int i = 0; i < 9; i++) r.t[i] = t9[i] * rc;
+    const float eps = 1.1920929e-7f;
+    r.persp = fabsf(r.t[6]) > eps || fabsf(r.t[7]) > eps;
+    return r;
+}
+
+// Transform::transform (transform.rs:71-93)
+__device__ Cmd apply_transform(const DTransform& T, const Cmd& c) {
+    Cmd r = c;
+    const float* t = T.t;
+    int np = c.kind == CGB_CMD_LINE ? 2 : (c.kind == CGB_CMD_QUAD || c.kind == CGB_CMD_RAT_QUAD) ? 3 : 4;
+    if (c.kind == CGB_CMD_CLOSE) return r;
+    bool rational = c.kind == CGB_CMD_RAT_QUAD || c.kind == CGB_CMD_RAT_CUBIC;
+    if (c.kind == CGB_CMD_LINE || (!rational && !T.persp)) {
+        for (int k = 0; k < np; k++) {
+            float x = c.p[k].x, y = c.p[k].y;
+            if (!T.persp) {
+                r.p[k] = {t[0] * x + t[1] * y + t[2], t[3] * x + t[4] * y + t[5]};
+            } else {
+                float o0 = t[0] * x + t[1] * y + t[2] * 1.0f;
+                float o1 = t[3] * x + t[4] * y + t[5] * 1.0f;
+                float o2 = t[6] * x + t[7] * y + t[8] * 1.0f;
+                r.p[k] = from_weighted(o0, o1, o2);
+            }
+        }
+        return r;
+    }
+    for (int k = 0; k < np; k++) {
+        float w = rational ? c.w[k] : 1.0f;
+        float x = c.p[k].x, y = c.p[k].y;
+        r.p[k] = {t[0] * x + t[1] * y + t[2] * w, t[3] * x + t[4] * y + t[5] * w};
+        r.w[k] = t[6] * x + t[7] * y + t[8] * w;
+    }
+    if (c.kind == CGB_CMD_QUAD) r.kind = CGB_CMD_RAT_QUAD;
+    if (c.kind == CGB_CMD_CUBIC) r.kind = CGB_CMD_RAT_CUBIC;
+    return r;
+}
+
+__device__ Pt eval_curve(const Cmd& c, float tt) {
+    switch (c.kind) {
+        case CGB_CMD_QUAD: return plerp(tt, plerp(tt, c.p[0], c.p[1]), plerp(tt, c.p[1], c.p[2]));
+        case CGB_CMD_CUBIC: {
+            Pt a = plerp(tt, plerp(tt, c.p[0], c.p[1]), plerp(tt, c.p[1], c.p[2]));
+            Pt b = plerp(tt, plerp(tt, c.p[1], c.p[2]), plerp(tt, c.p[2], c.p[3]));
+            return plerp(tt, a, b);
+        }
+        case CGB_CMD_RAT_QUAD: {
+            Pt b = plerp(tt, plerp(tt, c.p[0], c.p[1]), plerp(tt, c.p[1], c.p[2]));
+            float w = lerp1(tt, lerp1(tt, c.w[0], c.w[1]), lerp1(tt, c.w[1], c.w[2]));
+            return pmul(b, 1.0f / w);
+        }
+        default: {  // RAT_CUBIC
+            Pt a = plerp(tt, plerp(tt, c.p[0], c.p[1]), plerp(tt, c.p[1], c.p[2]));
+            Pt b = plerp(tt, plerp(tt, c.p[1], c.p[2]), plerp(tt, c.p[2], c.p[3]));
+            Pt bz = plerp(tt, a, b);
+            float wa = lerp1(tt, lerp1(tt, c.w[0], c.w[1]), lerp1(tt, c.w[1], c.w[2]));
+            float wb = lerp1(tt, lerp1(tt, c.w[1], c.w[2]), lerp1(tt, c.w[2], c.w[3]));
+            return pmul(bz, 1.0f / lerp1(tt, wa, wb));
+        }
+    }
+}
+
+__device__ __forceinline__ float dev3(float a, float b, float c) { return a + c - 2.0f * b; }
+__device__ __forceinline__ float dev4(float a, float b, float c, float d) {
+    return fmaxf(fabsf(a + c - 2.0f * b), fabsf(b + d - 2.0f * c));
+}
+
+// Output side of PathSegments::line (segments.rs:106-114): tracks the
+// closing and last points and counts or stores each emitted segment.
+struct LineSink {
+    bool has_last = false, has_closing = false;
+    Pt last_point{0, 0}, closing_point{0, 0};
+    uint32_t n = 0;
+    bool write = false;
+    uint32_t o = 0, lid = 0;
+    float *p0x = nullptr, *p0y = nullptr, *p1x = nullptr, *p1y = nullptr;
+    uint32_t* lids = nullptr;
+
+    __device__ void line(Pt a, Pt b) {
+        if (!has_closing) {
+            has_closing = true;
+            closing_point = a;
+        }
+        has_last = true;
+        last_point = b;
+        if (write) {
+            p0x[o] = a.x;
+            p0y[o] = a.y;
+            p1x[o] = b.x;
+            p1y[o] = b.y;
+            lids[o] = lid;
+            o++;
+        }
+        n++;
+    }
+};
+
+// Flattens one path (PathSegments as an iterator, segments.rs:233-262), each
+// curve run to completion with the incremental-t sampler of next_segment.
+__device__ void flatten_path(const uint32_t* kinds, uint32_t n_cmds, const float* pts, const float* t9,
+                             LineSink& sink) {
+    DTransform T;
+    const bool has_t = t9 != nullptr;
+    if (has_t) T = make_transform(t9);
+    const float PIXEL_ACCURACY = 0.5f / (float)PIXEL_WIDTH;
+    uint64_t po = 0;
+    for (uint32_t ci = 0; ci < n_cmds; ci++) {
+        const uint32_t kind = kinds[ci];
+        if (kind == CGB_CMD_CLOSE) {
+            // close (segments.rs:208-223)
+            if (sink.has_closing && sink.has_last) {
+                if (!approx_eq(sink.closing_point, sink.last_point)) sink.line(sink.last_point, sink.closing_point);
+                sink.has_closing = false;
+            }
+            continue;
+        }
+        Cmd c = load_cmd(kind, pts + po);
+        po += cmd_floats(kind);
+        if (has_t) c = apply_transform(T, c);
+        if (c.kind == CGB_CMD_LINE) {
+            sink.line(c.p[0], c.p[1]);
+            continue;
+        }
+        Pt first, last;
+        float dx, dy;
+        if (c.kind == CGB_CMD_QUAD) {
+            first = c.p[0];
+            last = c.p[2];
+            dx = dev3(c.p[0].x, c.p[1].x, c.p[2].x);
+            dy = dev3(c.p[0].y, c.p[1].y, c.p[2].y);
+        } else if (c.kind == CGB_CMD_CUBIC) {
+            first = c.p[0];
+            last = c.p[3];
+            dx = dev4(c.p[0].x, c.p[1].x, c.p[2].x, c.p[3].x);
+            dy = dev4(c.p[0].y, c.p[1].y, c.p[2].y, c.p[3].y);
+        } else if (c.kind == CGB_CMD_RAT_QUAD) {
+            Pt p0 = from_weighted(c.p[0].x, c.p[0].y, c.w[0]);
+            Pt p1 = from_weighted(c.p[1].x, c.p[1].y, c.w[1]);
+            Pt p2 = from_weighted(c.p[2].x, c.p[2].y, c.w[2]);
+            first = p0;
+            last = p2;
+            dx = dev3(p0.x, p1.x, p2.x);
+            dy = dev3(p0.y, p1.y, p2.y);
+        } else {
+            Pt p0 = from_weighted(c.p[0].x, c.p[0].y, c.w[0]);
+            Pt p1 = from_weighted(c.p[1].x, c.p[1].y, c.w[1]);
+            Pt p2 = from_weighted(c.p[2].x, c.p[2].y, c.w[2]);
+            Pt p3 = from_weighted(c.p[3].x, c.p[3].y, c.w[3]);
+            first = p0;
+            last = p3;
+            dx = dev4(p0.x, p1.x, p2.x, p3.x);
+            dy = dev4(p0.y, p1.y, p2.y, p3.y);
+        }
+        // subdivisions (segments.rs:51-72) then next_segment (:116-157)
+        const float dev2 = dx * dx + dy * dy;
+        uint64_t subs = 0;
+        if (!(dev2 < PIXEL_ACCURACY)) {
+            uint64_t count = f2usize(ceilf(sqrtf(sqrtf(dev2) * 2.0f / (8.0f * PIXEL_ACCURACY))));
+            subs = (count > 1 ? count : 1) - 1;
+        }
+        if (subs == 0) {
+            sink.line(first, last);
+            continue;
+        }
+        const float increment = 1.0f / (float)subs;
+        float t = 0.0f;
+        Pt point = first;
+        for (uint64_t left = subs; left > 1; left--) {
+            t += increment;
+            Pt np = eval_curve(c, t);
+            sink.line(point, np);
+            point = np;
+        }
+        sink.line(point, last);
+    }
+}
+
+__global__ void k_flatten(int write, const uint32_t* __restrict__ kinds, const float* __restrict__ points,
+                          const uint64_t* __restrict__ cmd_off, const uint64_t* __restrict__ pt_off,
+                          const float* __restrict__ transforms9, const uint8_t* __restrict__ has_t,
+                          const uint32_t* __restrict__ path_layer, uint32_t n_paths, uint32_t* __restrict__ counts,
+                          const uint32_t* __restrict__ out_off, float* __restrict__ p0x, float* __restrict__ p0y,
+                          float* __restrict__ p1x, float* __restrict__ p1y, uint32_t* __restrict__ lids) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_paths) return;
+    const float* t9 = (transforms9 && has_t && has_t[k]) ? transforms9 + 9 * (uint64_t)k : nullptr;
+    const uint64_t c0 = cmd_off[k], c1 = cmd_off[k + 1];
+    LineSink sink;
+    if (write) {
+        sink.write = true;
+        sink.o = out_off[k];
+        sink.lid = path_layer[k];
+        sink.p0x = p0x;
+        sink.p0y = p0y;
+        sink.p1x = p1x;
+        sink.p1y = p1y;
+        sink.lids = lids;
+    }
+    flatten_path(kinds + c0, (uint32_t)(c1 - c0), points + pt_off[k], t9, sink);
+    if (!write) counts[k] = sink.n;
+}
+
+// ---------------------------------------------------------------------------
+// LinesBuilder::build
+// ---------------------------------------------------------------------------
+
+__global__ void k_build_lines(const float* __restrict__ p0xs, const float* __restrict__ p0ys,
+                              const float* __restrict__ p1xs, const float* __restrict__ p1ys,
+                              const uint32_t* __restrict__ lids, uint32_t n, const LayerRec* __restrict__ layers,
+                              uint32_t n_layer_recs, const float* __restrict__ default_t, LineRec* __restrict__ recs,
+                              uint32_t* __restrict__ lengths) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float p0x = p0xs[i], p0y = p0ys[i], p1x = p1xs[i], p1y = p1ys[i];
+    uint32_t lid = lids[i];
+    LineRec r{0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0u};
+    uint32_t length = 0;
+    uint32_t flags = 0, lorder = 0;
+    if (lid < n_layer_recs) {
+        flags = layers[lid].flags;
+        lorder = layers[lid].order;
+    }
+    const bool present = (flags & LAYER_PRESENT) != 0;
+    if (!(present && !(flags & LAYER_ENABLED))) {
+        const uint32_t order = (present && (flags & LAYER_HAS_ORDER)) ? lorder : lid;
+        // the layer's affine, else the builder's default (segment.rs:130-142)
+        bool has_t = false;
+        float t0 = 0.f, t1 = 0.f, t2 = 0.f, t3 = 0.f, t4 = 0.f, t5 = 0.f;
+        if (present && (flags & LAYER_HAS_TRANSFORM)) {
+            const float* tr = layers[lid].t;
+            t0 = tr[0], t1 = tr[1], t2 = tr[2], t3 = tr[3], t4 = tr[4], t5 = tr[5];
+            has_t = true;
+        } else if (default_t) {
+            t0 = default_t[0], t1 = default_t[1], t2 = default_t[2], t3 = default_t[3], t4 = default_t[4],
+            t5 = default_t[5];
+            has_t = true;
+        }
+        if (has_t) {
+            float a = __fmaf_rn(t0, p0x, __fmaf_rn(t1, p0y, t4));
+            float b = __fmaf_rn(t2, p0x, __fmaf_rn(t3, p0y, t5));
+            float c = __fmaf_rn(t0, p1x, __fmaf_rn(t1, p1y, t4));
+            float d = __fmaf_rn(t2, p1x, __fmaf_rn(t3, p1y, t5));
+            p0x = a;
+            p0y = b;
+            p1x = c;
+            p1y = d;
+        }
+        int32_t p0x_sub = to_sub_pixel(p0x), p0y_sub = to_sub_pixel(p0y);
+        int32_t p1x_sub = to_sub_pixel(p1x), p1y_sub = to_sub_pixel(p1y);
+        if (p0y_sub != p1y_sub) {
+            int32_t dx = wsub(p1x_sub, p0x_sub), dy = wsub(p1y_sub, p0y_sub);
+            bool dx_dy = wabs(dx) > wabs(dy);
+            bool sum_0 = wadd(dx, dy) > 0 || (dx == wsub(0, dy) && dx < dy);
+            int32_t start_sub = dx_dy ? (sum_0 ? p0x_sub : p1x_sub) : (sum_0 ? p0y_sub : p1y_sub);
+            int32_t end_sub = dx_dy ? (sum_0 ? p1x_sub : p0x_sub) : (sum_0 ? p1y_sub : p0y_sub);
+            int32_t start = start_sub >> PIXEL_SHIFT;
+            int32_t end = (end_sub & PIXEL_MASK) == 0 ? end_sub >> PIXEL_SHIFT : (end_sub >> PIXEL_SHIFT) + 1;
+            length = (uint32_t)wsub(end, start);
+            const float rcp = 1.0f / (float)PIXEL_WIDTH;
+            float fp0x = (float)p0x_sub * rcp, fp0y = (float)p0y_sub * rcp;
+            float px = dx_dy ? fp0x : fp0y, py = dx_dy ? fp0y : fp0x;
+            float slope = dx_dy ? (float)dy / (float)dx : (float)dx / (float)dy;
+            float slope_recip = 1.0f / slope;
+            bool xp = dx > 0, yp = dy > 0;
+            uint32_t oct = dx_dy ? (xp ? (yp ? 0u : 7u) : (yp ? 3u : 4u)) : (xp ? (yp ? 1u : 6u) : (yp ? 2u : 5u));
+            r.start = start;
+            r.start_f32 = (float)start_sub * rcp;
+            r.end_f32 = (float)end_sub * rcp;
+            r.slope = slope;
+            r.slope_recip = slope_recip;
+            r.py_slope_px = __fmaf_rn(slope, -px, py);
+            r.px_slope_recip_py = __fmaf_rn(slope_recip, -py, px);
+            r.order_octant = (order << 3) | oct;
+        }
+    }
+    recs[i] = r;
+    lengths[i] = length;
+}
+
+// ---------------------------------------------------------------------------
+// rasterization
+// ---------------------------------------------------------------------------
+
+// tiles + area_cover + CompactSegment::new (rasterizer/mod.rs:134-189)
+__device__ __forceinline__ uint64_t make_segment(uint32_t wide, uint32_t layer, int32_t x0, int32_t x1, int32_t y0,
+                                                 int32_t y1, int32_t bx, int32_t by, uint32_t oct) {
+    if (oct == 1 || oct == 2 || oct == 5 || oct == 6) {
+        int32_t t = bx;
+        bx = by;
+        by = t;
+    }
+    int32_t ti = (int16_t)(bx >> TILE_SHIFT);
+    int32_t tj = (int16_t)(by >> TILE_SHIFT);
+    uint32_t tx = (uint32_t)(bx & TILE_MASK), ty = (uint32_t)(by & TILE_MASK);
+    int32_t a0 = x0, a1 = x1, b0 = y0, b1 = y1;
+    switch (oct) {
+        case 1: a0 = y0; a1 = y1; b0 = x0; b1 = x1; break;
+        case 2: a0 = y1; a1 = y0; b0 = x0; b1 = x1; break;
+        case 3:
+        case 4: b0 = y1; b1 = y0; break;
+        case 5: a0 = y0; a1 = y1; b0 = x1; b1 = x0; break;
+        case 6: a0 = y1; a1 = y0; b0 = x1; b1 = x0; break;
+        default: break;
+    }
+    int32_t border = wadd(a0 & ~PIXEL_MASK, PIXEL_WIDTH);
+    int32_t height = wsub(b1, b0);
+    int32_t triangle = (int16_t)(wmul(height, wsub(a1, a0)) / 2);
+    int32_t rectangle = (int16_t)wmul(height, wsub(border, a1));
+    int32_t area = (int16_t)(uint16_t)((uint32_t)triangle + (uint32_t)rectangle);
+    int32_t cover = (int8_t)height;
+    int32_t tis = (int16_t)(uint16_t)((uint32_t)(ti > -1 ? ti : -1) + 256u);
+    return pack_segment(wide, tj, tis, layer, ty, tx, area, cover);
+}
+
+__device__ __forceinline__ bool intersects_y_border(int32_t y0, int32_t y1) {
+    return (y0 & PIXEL_MASK) != 0 && (y1 & PIXEL_MASK) != 0 && (y0 >> PIXEL_SHIFT) != (y1 >> PIXEL_SHIFT);
+}
+
+// One pixel step (rasterizer/mod.rs:233-281); returns 1 or 2 segments.
+__device__ __forceinline__ int raster_step(uint32_t wide, const LineRec& l, int32_t pi, uint64_t out[2]) {
+    const uint32_t oct = l.order_octant & 7, layer = l.order_octant >> 3;
+    int32_t x0i = wadd(l.start, pi);
+    int32_t x1i = wadd(x0i, 1);
+    int32_t border_x = x0i;
+    float x0 = fmaxf((float)x0i, l.start_f32);
+    float x1 = fminf((float)x1i, l.end_f32);
+    float y0 = __fmaf_rn(l.slope, x0, l.py_slope_px);
+    float y1 = __fmaf_rn(l.slope, x1, l.py_slope_px);
+    int32_t x0s = to_sub_pixel(x0), x1s = to_sub_pixel(x1), y0s = to_sub_pixel(y0), y1s = to_sub_pixel(y1);
+    if (intersects_y_border(y0s, y1s)) {
+        int32_t y = max(y0s, y1s) >> PIXEL_SHIFT;
+        int32_t ys = (int32_t)((uint32_t)y << PIXEL_SHIFT);
+        float x = __fmaf_rn(l.slope_recip, (float)y, l.px_slope_recip_py);
+        int32_t xs = to_sub_pixel(x);
+        out[0] = make_segment(wide, layer, x0s, xs, y0s, ys, border_x, min(ys, y0s) >> PIXEL_SHIFT, oct);
+        out[1] = make_segment(wide, layer, xs, x1s, ys, y1s, border_x, min(ys, y1s) >> PIXEL_SHIFT, oct);
+        return 2;
+    }
+    out[0] = make_segment(wide, layer, x0s, x1s, y0s, y1s, border_x, min(y0s, y1s) >> PIXEL_SHIFT, oct);
+    return 1;
+}
+
+// Render format: culls segments the painter never reads (rows outside the
+// canvas, tiles right of it, 13-bit tile_i wrap) and re-keys the rest by
+// (tile row, order, tile column + 1) above the reference's low 22 bits.
+__device__ __forceinline__ bool render_key(uint32_t wide, const RenderGeom& g, uint64_t seg, uint64_t& out) {
+    int32_t tj = seg_tile_j(wide, seg);
+    int32_t ti = seg_tile_i_stored(wide, seg) - 256;
+    if (tj < 0 || tj >= (int32_t)g.rows || ti < -1 || ti >= (int32_t)g.row_len) return false;
+    uint64_t key = ((uint64_t)tj * g.n_orders + seg_layer(wide, seg)) * (g.row_len + 1) + (uint64_t)(ti + 1);
+    out = (key << 22) | (seg & 0x3FFFFFull);
+    return true;
+}
+
+constexpr int RASTER_ITEMS = 8;  // consecutive pixel steps per thread
+
+__device__ __forceinline__ uint32_t find_line(const uint32_t* __restrict__ off, uint32_t n_lines, uint64_t s) {
+    // largest l with off[l] <= s (off has n_lines + 1 entries, off[0] = 0)
+    uint32_t lo = 0, hi = n_lines;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if ((uint64_t)off[mid] <= s) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <int MODE, int RENDER>
+__global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ recs, const uint32_t* __restrict__ off,
+                                                   uint32_t n_lines, uint64_t n_steps, uint32_t wide, RenderGeom geom,
+                                                   uint32_t* __restrict__ block_counts,
+                                                   uint32_t* __restrict__ block_totals,
+                                                   const uint32_t* __restrict__ block_off,
+                                                   uint64_t* __restrict__ out) {
+    extern __shared__ uint64_t s_out[];  // 2 * RASTER_ITEMS * blockDim.x (write mode)
+    const uint64_t s0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * RASTER_ITEMS;
+    uint64_t segs[2 * RASTER_ITEMS];
+    int n = 0, total = 0;
+    if (s0 < n_steps) {
+        uint32_t l = find_line(off, n_lines, s0);
+        uint32_t next = off[l + 1];
+        LineRec rec = recs[l];
+#pragma unroll
+        for (int k = 0; k < RASTER_ITEMS; k++) {
+            uint64_t s = s0 + k;
+            if (s < n_steps) {
+                while (s >= next) {
+                    l++;
+                    next = off[l + 1];
+                    rec = recs[l];
+                }
+                uint64_t o[2];
+                int m = raster_step(wide, rec, (int32_t)(s - off[l]), o);
+                total += m;
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    if (q < m) {
+                        uint64_t v = o[q];
+                        bool keep = true;
+                        if (RENDER) keep = render_key(wide, geom, o[q], v);
+                        if (keep) segs[n++] = v;
+                    }
+                }
+            }
+        }
+    }
+    // block-wide exclusive scan of the per-thread counts
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t warp_tot[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t inc = n;
+    uint32_t tinc = total;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t a = __shfl_up_sync(0xffffffffu, inc, o);
+        uint32_t b = __shfl_up_sync(0xffffffffu, tinc, o);
+        if (lane >= o) {
+            inc += a;
+            tinc += b;
+        }
+    }
+    if (lane == 31) {
+        warp_sums[warp] = inc;
+        warp_tot[warp] = tinc;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < nw ? warp_sums[lane] : 0, wt = lane < nw ? warp_tot[lane] : 0;
+        uint32_t wi = w, wti = wt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t a = __shfl_up_sync(0xffffffffu, wi, o);
+            uint32_t b = __shfl_up_sync(0xffffffffu, wti, o);
+            if (lane >= o) {
+                wi += a;
+                wti += b;
+            }
+        }
+        if (lane < nw) warp_sums[lane] = wi - w;
+        if (lane == 31) {
+            if (MODE == 0) {
+                block_counts[blockIdx.x] = wi;
+                block_totals[blockIdx.x] = wti;
+            } else {
+                warp_tot[0] = wi;  // block total
+            }
+        }
+    }
+    __syncthreads();
+    if (MODE == 0) return;
+    const uint32_t local = warp_sums[warp] + inc - n;
+    const uint32_t btotal = warp_tot[0];
+    for (int q = 0; q < n; q++) s_out[local + q] = segs[q];
+    __syncthreads();
+    uint64_t* dst = out + block_off[blockIdx.x];
+    for (uint32_t i = threadIdx.x; i < btotal; i += blockDim.x) dst[i] = s_out[i];
+}
+
+__global__ void k_keep_flags(const uint32_t* __restrict__ lids, uint32_t n, const LayerRec* __restrict__ layers,
+                             uint32_t n_layer_recs, uint32_t* __restrict__ flags) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t lid = lids[i];
+    uint32_t f = lid < n_layer_recs ? layers[lid].flags : 0u;
+    flags[i] = ((f & LAYER_PRESENT) && (f & LAYER_ENABLED)) ? 1u : 0u;
+}
+
+__global__ void k_scatter_lines(const float* __restrict__ a, const float* __restrict__ b, const float* __restrict__ c,
+                                const float* __restrict__ d, const uint32_t* __restrict__ lid_in, uint32_t n,
+                                const uint32_t* __restrict__ flags, const uint32_t* __restrict__ off,
+                                float* __restrict__ oa, float* __restrict__ ob, float* __restrict__ oc,
+                                float* __restrict__ od, uint32_t* __restrict__ lid_out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !flags[i]) return;
+    uint32_t o = off[i];
+    oa[o] = a[i];
+    ob[o] = b[i];
+    oc[o] = c[i];
+    od[o] = d[i];
+    lid_out[o] = lid_in[i];
+}
+
+}  // namespace
+
+cudaError_t launch_flatten(int write, const uint32_t* kinds, const float* points, const uint64_t* cmd_off,
+                           const uint64_t* pt_off, const float* transforms9, const uint8_t* has_t,
+                           const uint32_t* path_layer, uint32_t n_paths, uint32_t* counts, const uint32_t* out_off,
+                           float* p0x, float* p0y, float* p1x, float* p1y, uint32_t* lids, cudaStream_t st) {
+    if (n_paths == 0) return cudaSuccess;
+    count_launches(1);
+    k_flatten<<<(n_paths + 127) / 128, 128, 0, st>>>(write, kinds, points, cmd_off, pt_off, transforms9, has_t,
+                                                     path_layer, n_paths, counts, out_off, p0x, p0y, p1x, p1y, lids);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_lines(const float* p0x, const float* p0y, const float* p1x, const float* p1y,
+                               const uint32_t* lids, uint32_t n, const LayerRec* layers, uint32_t n_layer_recs,
+                               const float* default_t, LineRec* recs, uint32_t* lengths, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    count_launches(1);
+    k_build_lines<<<(n + 255) / 256, 256, 0, st>>>(p0x, p0y, p1x, p1y, lids, n, layers, n_layer_recs, default_t,
+                                                   recs, lengths);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rasterize(int mode, const LineRec* recs, const uint32_t* step_off, uint32_t n_lines,
+                             uint64_t n_steps, uint32_t steps_per_block, uint32_t block, SegFormat fmt, int render,
+                             RenderGeom geom, uint32_t* block_counts, uint32_t* block_totals,
+                             const uint32_t* block_off, uint64_t* out, cudaStream_t st) {
+    (void)steps_per_block;
+    if (n_steps == 0) return cudaSuccess;
+    block = block ? block : 256;
+    uint64_t per_block = (uint64_t)block * RASTER_ITEMS;
+    uint32_t grid = (uint32_t)((n_steps + per_block - 1) / per_block);
+    size_t smem = mode ? (size_t)2 * per_block * sizeof(uint64_t) : 0;
+    count_launches(1);
+    if (mode == 0) {
+        if (render)
+            k_rasterize<0, 1><<<grid, block, 0, st>>>(recs, step_off, n_lines, n_steps, fmt.wide, geom, block_counts,
+                                                      block_totals, block_off, out);
+        else
+            k_rasterize<0, 0><<<grid, block, 0, st>>>(recs, step_off, n_lines, n_steps, fmt.wide, geom, block_counts,
+                                                      block_totals, block_off, out);
+    } else {
+        if (render)
+            k_rasterize<1, 1><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, fmt.wide, geom,
+                                                         block_counts, block_totals, block_off, out);
+        else
+            k_rasterize<1, 0><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, fmt.wide, geom,
+                                                         block_counts, block_totals, block_off, out);
+    }
+    return cudaGetLastError();
+}
+
+uint32_t raster_grid(uint64_t n_steps, uint32_t block) {
+    block = block ? block : 256;
+    uint64_t per_block = (uint64_t)block * RASTER_ITEMS;
+    return (uint32_t)((n_steps + per_block - 1) / per_block);
+}
+
+cudaError_t launch_compact_lines(const float* in4[4], const uint32_t* lid_in, uint32_t n, const LayerRec* layers,
+                                 uint32_t n_layer_recs, float* out4[4], uint32_t* lid_out, uint32_t* flags,
+                                 uint32_t* offsets, Scratch* s, cudaStream_t st, uint32_t* n_out_host) {
+    if (n == 0) {
+        *n_out_host = 0;
+        return cudaSuccess;
+    }
+    count_launches(2);
+    k_keep_flags<<<(n + 255) / 256, 256, 0, st>>>(lid_in, n, layers, n_layer_recs, flags);
+    uint64_t total = 0;
+    cudaError_t e = scan_u32(flags, offsets, n, s, st, &total);
+    if (e != cudaSuccess) return e;
+    k_scatter_lines<<<(n + 255) / 256, 256, 0, st>>>(in4[0], in4[1], in4[2], in4[3], lid_in, n, flags, offsets,
+                                                     out4[0], out4[1], out4[2], out4[3], lid_out);
+    *n_out_host = (uint32_t)total;
+    return cudaGetLastError();
+}
+
+}  // namespace cgb

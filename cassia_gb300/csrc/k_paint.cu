@@ -1,0 +1,566 @@
+// Cover carries, per-tile work items and the tile painter.
+//
+// The reference paints each tile row sequentially (Painter::paint_tile_row,
+// surpass/src/painter/mod.rs:495-596) and carries each layer's per-row cover
+// from tile to tile through LayerWorkbench's queue
+// (surpass/src/painter/layer_workbench.rs:134-198, 430-486).  Here the segments
+// arrive sorted by (tile row j, order L, tile column i), so every (j, L) run of
+// "tile-layer" groups (TLs) is contiguous and the carry into a TL is an
+// exclusive prefix of the runs' cover sums (8 x i8 lanes, wrapping).
+//
+// A layer L is painted in tile i of row j (is in the workbench's `ids`) iff
+//   - L has segments in (j, i), or
+//   - i is the first painted tile of the row and L has segments left of it
+//     (the initial queue is pushed without an emptiness test,
+//     painter/mod.rs:507-550, layer_workbench.rs:134-137), or
+//   - the cumulative cover of L entering tile i is non-empty for L's fill rule
+//     (the queue only keeps non-empty carries, layer_workbench.rs:194, 475).
+// The exact cumulative cover equals the reference's queued cover up to
+// multiples of 32 for EvenOdd (whose tests are mod 32) and exactly for NonZero,
+// so every decision and coverage below is bit-identical.
+//
+// Work items are (tile, order) pairs, sorted by (tile, order) with the radix
+// sort.  The painter gives each tile one warp (2 pixels per lane), replicates
+// tile_unchanged_pass and skip_fully_covered_layers (:200-222, :310-388),
+// paints the surviving layers bottom-up in f32 with the reference's vector
+// blend formulas, and writes RGBA8 with 128-bit stores.
+#include "cgb_internal.cuh"
+
+namespace cgb {
+
+namespace {
+
+constexpr int HEAD_THREADS = 256;
+constexpr int HEAD_ITEMS = 8;
+
+__global__ void __launch_bounds__(HEAD_THREADS) k_tl_heads(int mode, const uint64_t* __restrict__ segs, uint32_t n,
+                                                           uint32_t* __restrict__ block_counts,
+                                                           const uint32_t* __restrict__ block_off,
+                                                           uint32_t* __restrict__ tl_start) {
+    const uint64_t s0 = ((uint64_t)blockIdx.x * HEAD_THREADS + threadIdx.x) * HEAD_ITEMS;
+    uint32_t flags = 0, cnt = 0;
+    if (s0 < n) {
+        uint64_t prev = s0 == 0 ? ~0ull : (segs[s0 - 1] >> 22);
+#pragma unroll
+        for (int k = 0; k < HEAD_ITEMS; k++) {
+            uint64_t s = s0 + k;
+            if (s < n) {
+                uint64_t key = segs[s] >> 22;
+                if (key != prev) {
+                    flags |= 1u << k;
+                    cnt++;
+                }
+                prev = key;
+            }
+        }
+    }
+    __shared__ uint32_t warp_sums[HEAD_THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t inc = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t a = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += a;
+    }
+    if (lane == 31) warp_sums[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < HEAD_THREADS / 32 ? warp_sums[lane] : 0, wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t a = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += a;
+        }
+        if (lane < HEAD_THREADS / 32) warp_sums[lane] = wi - w;
+        if (lane == 31 && mode == 0) block_counts[blockIdx.x] = wi;
+    }
+    __syncthreads();
+    if (mode == 0) return;
+    uint32_t o = block_off[blockIdx.x] + warp_sums[warp] + inc - cnt;
+#pragma unroll
+    for (int k = 0; k < HEAD_ITEMS; k++)
+        if (flags & (1u << k)) tl_start[o++] = (uint32_t)(s0 + k);
+}
+
+// Per TL: cover sums per tile row (8 x i8 lanes) and the run-start flag.
+__global__ void k_tl_reduce(const uint64_t* __restrict__ segs, uint32_t G, const uint32_t* __restrict__ tl_start,
+                            uint32_t row_len, uint64_t* __restrict__ tl_cover, uint32_t* __restrict__ tl_flags) {
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= G) return;
+    const uint32_t b = tl_start[g], e = tl_start[g + 1];
+    int32_t c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t s = b; s < e; s++) {
+        uint32_t low = (uint32_t)segs[s];
+        c[low_tile_y(low)] += low_cover(low);
+    }
+    uint64_t packed = 0;
+#pragma unroll
+    for (int y = 0; y < 8; y++) packed |= (uint64_t)(uint8_t)c[y] << (8 * y);
+    tl_cover[g] = packed;
+    const uint64_t run = (segs[b] >> 22) / (row_len + 1);
+    const bool start = g == 0 || ((segs[tl_start[g - 1]] >> 22) / (row_len + 1)) != run;
+    tl_flags[g] = start ? 1u : 0u;
+}
+
+// Exclusive prefix of the cover sums along each (j, L) run: one thread walks
+// each run (runs are a layer's few tile groups in one tile row).
+__global__ void k_tl_carry(uint32_t G, const uint64_t* __restrict__ tl_cover, const uint32_t* __restrict__ tl_flags,
+                           uint64_t* __restrict__ tl_carry) {
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= G || !tl_flags[g]) return;
+    uint64_t acc = 0;
+    uint32_t h = g;
+    do {
+        tl_carry[h] = acc;
+        acc = cover_add(acc, tl_cover[h]);
+        h++;
+    } while (h < G && !tl_flags[h]);
+}
+
+struct ItemGeom {
+    RenderGeom geom;
+    uint32_t h0, h1, v0, v1;  // crop in tiles
+};
+
+// Items of TL g: its own (tile, L) pair and the cover-carry-only tiles up to
+// the next TL of the run.  Returns the count; `emit(tile, carry_only)` is
+// called for each when non-null.
+template <class Emit>
+__device__ __forceinline__ uint32_t tl_items(uint32_t g, uint32_t G, const uint64_t* __restrict__ segs,
+                                             const uint32_t* __restrict__ tl_start, const uint32_t* __restrict__ tl_flags,
+                                             const uint64_t* __restrict__ tl_cover,
+                                             const uint64_t* __restrict__ tl_carry, const ItemGeom& ig,
+                                             const PaintProps* __restrict__ props, Emit emit) {
+    const RenderGeom& geo = ig.geom;
+    const uint64_t key = segs[tl_start[g]] >> 22;
+    const uint32_t rl1 = geo.row_len + 1;
+    const int32_t i = (int32_t)(key % rl1) - 1;
+    const uint64_t run = key / rl1;
+    const uint32_t L = (uint32_t)(run % geo.n_orders);
+    const uint32_t j = (uint32_t)(run / geo.n_orders);
+    if (j < ig.v0 || j >= ig.v1) return 0;
+    int32_t next = (int32_t)geo.row_len;
+    if (g + 1 < G && !tl_flags[g + 1]) next = (int32_t)((segs[tl_start[g + 1]] >> 22) % rl1) - 1;
+    const int32_t h0 = (int32_t)ig.h0, h1 = (int32_t)ig.h1;
+    if (next > h1) next = h1;
+    uint32_t cnt = 0;
+    if (i >= h0 && i < h1) {
+        emit(i, 0u);
+        cnt++;
+    }
+    if (next <= i + 1) return cnt;
+    const uint64_t carry_out = cover_add(tl_carry[g], tl_cover[g]);
+    const bool nonempty = !cover_is_empty(carry_out, props[L].fill_rule);
+    int32_t t = i + 1;
+    if (i < h0) {
+        // the first painted tile of the row holds every layer with segments
+        // to its left, empty or not
+        if (next <= h0) return cnt;
+        emit(h0, 1u);
+        cnt++;
+        t = h0 + 1;
+    }
+    if (nonempty)
+        for (; t < next; t++) {
+            emit(t, 1u);
+            cnt++;
+        }
+    return cnt;
+}
+
+__global__ void k_items_count(const uint64_t* __restrict__ segs, uint32_t G, const uint32_t* __restrict__ tl_start,
+                              const uint32_t* __restrict__ tl_flags, const uint64_t* __restrict__ tl_cover,
+                              const uint64_t* __restrict__ tl_carry, ItemGeom ig, const PaintProps* __restrict__ props,
+                              uint32_t* __restrict__ counts) {
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= G) return;
+    counts[g] = tl_items(g, G, segs, tl_start, tl_flags, tl_cover, tl_carry, ig, props, [](int32_t, uint32_t) {});
+}
+
+__global__ void k_items_write(const uint64_t* __restrict__ segs, uint32_t G, const uint32_t* __restrict__ tl_start,
+                              const uint32_t* __restrict__ tl_flags, const uint64_t* __restrict__ tl_cover,
+                              const uint64_t* __restrict__ tl_carry, ItemGeom ig, const PaintProps* __restrict__ props,
+                              const uint32_t* __restrict__ off, int idx_bits, uint64_t* __restrict__ items) {
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= G) return;
+    const uint64_t key = segs[tl_start[g]] >> 22;
+    const uint32_t rl1 = ig.geom.row_len + 1;
+    const uint64_t run = key / rl1;
+    const uint64_t L = run % ig.geom.n_orders;
+    const uint64_t j = run / ig.geom.n_orders;
+    uint32_t o = off[g];
+    tl_items(g, G, segs, tl_start, tl_flags, tl_cover, tl_carry, ig, props, [&](int32_t t, uint32_t carry_only) {
+        uint64_t tile = j * ig.geom.row_len + (uint64_t)t;
+        uint64_t k = ((tile * ig.geom.n_orders + L) << 1) | carry_only;
+        items[o++] = (k << idx_bits) | g;
+    });
+}
+
+__global__ void k_tile_ranges(const uint64_t* __restrict__ items, uint32_t W, uint32_t n_tiles, int shift,
+                              uint32_t n_orders, uint32_t* __restrict__ tile_start) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > W) return;
+    int64_t cur = k < W ? (int64_t)((items[k] >> shift) / n_orders) : (int64_t)n_tiles;
+    int64_t prev = k > 0 ? (int64_t)((items[k - 1] >> shift) / n_orders) : -1;
+    for (int64_t t = prev + 1; t <= cur; t++) tile_start[t] = k;
+}
+
+// ---------------------------------------------------------------------------
+// painter numerics (surpass/src/painter/mod.rs:53-123, style.rs:206-418)
+// ---------------------------------------------------------------------------
+
+// from_area (painter/mod.rs:53-71)
+__device__ __forceinline__ float from_area(int32_t area, uint32_t fill_rule) {
+    if (fill_rule == CGB_FILL_NONZERO) return fminf(fabsf((float)area * (1.0f / 256.0f)), 1.0f);
+    float capped = (float)(area & 255) * (1.0f / 256.0f);
+    return ((area >> 8) & 1) == 0 ? capped : 1.0f - capped;
+}
+
+// blend_function! per lane (style.rs:288-418)
+__device__ __forceinline__ float blend_vec(uint32_t mode, float d, float s) {
+    switch (mode) {
+        case CGB_BLEND_OVER: return s;
+        case CGB_BLEND_MULTIPLY: return d * s;
+        case CGB_BLEND_SCREEN: return __fmaf_rn(d, -s, d) + s;
+        case CGB_BLEND_OVERLAY: return s <= 0.5f ? (d * s * 2.0f) : 2.0f * (s + d - __fmaf_rn(s, d, 0.5f));
+        case CGB_BLEND_DARKEN: return fminf(d, s);
+        case CGB_BLEND_LIGHTEN: return fmaxf(d, s);
+        case CGB_BLEND_COLOR_DODGE: return s == 0.0f ? 0.0f : fminf(1.0f, s / (1.0f - d));
+        case CGB_BLEND_COLOR_BURN: return s == 1.0f ? 1.0f : 1.0f - fminf(1.0f, (1.0f - s) / d);
+        case CGB_BLEND_HARD_LIGHT: return d <= 0.5f ? (d * s * 2.0f) : 2.0f * (s + d - __fmaf_rn(s, d, 0.5f));
+        case CGB_BLEND_SOFT_LIGHT: {
+            float dd = s <= 0.25f ? __fmaf_rn(__fmaf_rn(16.0f, s, -12.0f), s, 4.0f) * s : sqrtf(s);
+            float k = __fmaf_rn(2.0f, d, -1.0f);
+            return d <= 0.5f ? __fmaf_rn(s * (1.0f - s), k, s) : __fmaf_rn(dd - s, k, s);
+        }
+        case CGB_BLEND_DIFFERENCE: return fabsf(d - s);
+        default: return __fmaf_rn(-2.0f * d, s, d) + s;  // EXCLUSION
+    }
+}
+
+// BlendMode::blend_fn (style.rs:206-267)
+__device__ float blend_fn(uint32_t mode, float dst, float src) {
+    switch (mode) {
+        case CGB_BLEND_OVER: return src;
+        case CGB_BLEND_MULTIPLY: return dst * src;
+        case CGB_BLEND_SCREEN: return dst + src - (dst * src);
+        case CGB_BLEND_OVERLAY:
+            return src <= 0.5f ? (2.0f * src) * dst : (2.0f * src - 1.0f) + dst - ((2.0f * src - 1.0f) * dst);
+        case CGB_BLEND_DARKEN: return fminf(dst, src);
+        case CGB_BLEND_LIGHTEN: return fmaxf(dst, src);
+        case CGB_BLEND_COLOR_DODGE:
+            if (src == 0.0f) return 0.0f;
+            if (dst == 1.0f) return 1.0f;
+            return fminf(1.0f, src / (1.0f - dst));
+        case CGB_BLEND_COLOR_BURN:
+            if (src == 1.0f) return 1.0f;
+            if (dst == 0.0f) return 0.0f;
+            return 1.0f - fminf(1.0f, (1.0f - src) / dst);
+        case CGB_BLEND_HARD_LIGHT:
+            return dst <= 0.5f ? (2.0f * dst) * src : (2.0f * dst - 1.0f) + src - ((2.0f * dst - 1.0f) * src);
+        case CGB_BLEND_SOFT_LIGHT: {
+            float d = src <= 0.25f ? ((16.0f * src - 12.0f) * src + 4.0f) * src : sqrtf(src);
+            if (dst <= 0.5f) return src - (1.0f - 2.0f * dst) * src * (1.0f - src);
+            return src + (2.0f * dst - 1.0f) * (d - src);
+        }
+        case CGB_BLEND_DIFFERENCE: return fabsf(dst - src);
+        default: return dst + src - 2.0f * dst * src;
+    }
+}
+
+// linear_to_srgb_approx[_simd] (painter/mod.rs:73-106)
+__device__ __forceinline__ float linear_to_srgb(float l) {
+    float s = sqrtf(l);
+    float s3 = l * s;
+    float n = __fmaf_rn(0.20101772f, s3, __fmaf_rn(-0.51280147f, l, __fmaf_rn(1.344401f, s, -0.030656587f)));
+    return l <= 0.0031308f ? l * 12.92f : n;
+}
+__device__ __forceinline__ uint32_t round_u8(float v) { return f2u8(roundf(v)); }
+__device__ __forceinline__ uint32_t to_byte(float n) { return f2u8(__fmaf_rn(n, 255.0f, 0.5f)); }
+
+// compute_srgb for one pixel (painter/mod.rs:418-453)
+__device__ __forceinline__ uint32_t pixel_bytes(float c0, float c1, float c2, float a) {
+    uint32_t r = round_u8((linear_to_srgb(c0) * a) * 255.0f);
+    uint32_t g = round_u8((linear_to_srgb(c1) * a) * 255.0f);
+    uint32_t b = round_u8((linear_to_srgb(c2) * a) * 255.0f);
+    uint32_t al = round_u8(__fmaf_rn(a, 255.0f, 0.5f));
+    return r | (g << 8) | (b << 16) | (al << 24);
+}
+
+// to_bytes (painter/mod.rs:108-123)
+__device__ __forceinline__ uint32_t solid_bytes(const float c[4]) {
+    float ar = 1.0f / c[3];
+    return to_byte(linear_to_srgb(c[0] * ar)) | (to_byte(linear_to_srgb(c[1] * ar)) << 8) |
+           (to_byte(linear_to_srgb(c[2] * ar)) << 16) | (to_byte(c[3]) << 24);
+}
+
+__device__ __forceinline__ void item_decode(uint64_t item, int idx_bits, uint32_t n_orders, uint32_t& L,
+                                            uint32_t& carry_only, uint32_t& g) {
+    g = (uint32_t)(item & ((1ull << idx_bits) - 1));
+    uint64_t k = item >> idx_bits;
+    carry_only = (uint32_t)(k & 1);
+    L = (uint32_t)((k >> 1) % n_orders);
+}
+
+struct PaintArgs {
+    PaintParams p;
+    const uint64_t* segs;
+    const uint64_t* items;
+    int idx_bits;
+    const uint32_t* tile_start;
+    const uint32_t* tl_start;
+    const uint64_t* tl_cover;
+    const uint64_t* tl_carry;
+};
+
+__global__ void __launch_bounds__(256) k_paint(PaintArgs a) {
+    const PaintParams& p = a.p;
+    const int lane = threadIdx.x & 31;
+    const uint32_t n_tiles = p.geom.rows * p.geom.row_len;
+    const uint32_t t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (t >= n_tiles) return;
+    const uint32_t j = t / p.geom.row_len, i = t % p.geom.row_len;
+    if (i < p.crop_h0 || i >= p.crop_h1 || j < p.crop_v0 || j >= p.crop_v1) return;
+    const uint32_t b = a.tile_start[t], e = a.tile_start[t + 1];
+    const uint32_t n_orders = p.geom.n_orders;
+
+    // tile_unchanged_pass (layer_workbench.rs:200-222)
+    if (p.prev_layers) {
+        const int32_t layers = (int32_t)((e - b) & 0xFFFF);
+        const int32_t old = p.prev_layers[t];
+        __syncwarp();
+        if (lane == 0) p.prev_layers[t] = layers;
+        if (old >= 0 && old == layers) {
+            bool all = true;
+            for (uint32_t k = b + lane; k < e; k += 32) {
+                uint32_t L, co, g;
+                item_decode(a.items[k], a.idx_bits, n_orders, L, co, g);
+                all &= p.unchanged[L] != 0;
+            }
+            if (__all_sync(0xffffffffu, all)) return;  // TileWriteOp::None
+        }
+    }
+
+    // skip_fully_covered_layers (layer_workbench.rs:310-388), top-down.
+    int64_t k_op = -1;
+    int first = 0;  // 0 none, 1 opaque, 2 incomplete
+    for (int64_t c0 = (int64_t)e - 1; c0 >= (int64_t)b; c0 -= 32) {
+        const int64_t idx = c0 - lane;
+        bool inc = false, op = false;
+        if (idx >= (int64_t)b) {
+            uint32_t L, co, g;
+            item_decode(a.items[idx], a.idx_bits, n_orders, L, co, g);
+            const PaintProps pp = a.p.props[L];
+            bool full = co && cover_is_full(cover_add(a.tl_carry[g], a.tl_cover[g]), pp.fill_rule);
+            inc = !full;
+            op = full && (pp.flags & PROPS_OPAQUE_OVER);
+        }
+        const uint32_t bi = __ballot_sync(0xffffffffu, inc), bo = __ballot_sync(0xffffffffu, op);
+        if (first == 0 && (bi | bo)) first = ((bo & -(int32_t)(bi | bo)) != 0) ? 1 : 2;  // lowest lane = topmost item
+        if (bo) {
+            k_op = c0 - (__ffs(bo) - 1);
+            break;
+        }
+    }
+
+    const uint32_t y = lane & 7, xg = lane >> 3;
+    const uint32_t x0 = 2 * xg;
+    uint32_t px0, px1;
+    bool painted = true;
+    if (first != 2) {
+        // Solid: fold the scalar blend over the (full) layers above the opaque one.
+        float dst[4];
+        uint32_t from;
+        if (first == 1) {
+            uint32_t L, co, g;
+            item_decode(a.items[k_op], a.idx_bits, n_orders, L, co, g);
+            const PaintProps pp = a.p.props[L];
+            for (int q = 0; q < 4; q++) dst[q] = pp.color[q];
+            from = (uint32_t)k_op + 1;
+        } else {
+            for (int q = 0; q < 4; q++) dst[q] = p.clear[q];
+            from = b;
+        }
+        bool ok = true;
+        for (uint32_t k = from; k < e; k++) {
+            uint32_t L, co, g;
+            item_decode(a.items[k], a.idx_bits, n_orders, L, co, g);
+            const PaintProps pp = a.p.props[L];
+            if (!(pp.flags & PROPS_SOLID)) {
+                ok = false;
+                break;
+            }
+            // BlendMode::blend (style.rs:269-285)
+            const float al = pp.color[3], inv = 1.0f - al;
+            float o0 = __fmaf_rn(dst[0], inv, blend_fn(pp.blend_mode, dst[0], pp.color[0]) * al);
+            float o1 = __fmaf_rn(dst[1], inv, blend_fn(pp.blend_mode, dst[1], pp.color[1]) * al);
+            float o2 = __fmaf_rn(dst[2], inv, blend_fn(pp.blend_mode, dst[2], pp.color[2]) * al);
+            float o3 = __fmaf_rn(dst[3], inv, al);
+            dst[0] = o0;
+            dst[1] = o1;
+            dst[2] = o2;
+            dst[3] = o3;
+        }
+        if (ok) {
+            px0 = px1 = solid_bytes(dst);
+            painted = false;
+        }
+    }
+    if (painted) {
+        // ColorBuffer: paint the unculled layers bottom-up (drive_tile_painting, :449-481).
+        float c[2][4];
+#pragma unroll
+        for (int h = 0; h < 2; h++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) c[h][q] = p.clear[q];
+        const uint32_t start = k_op >= 0 ? (uint32_t)k_op : b;
+        for (uint32_t k = start; k < e; k++) {
+            uint32_t L, co, g;
+            item_decode(a.items[k], a.idx_bits, n_orders, L, co, g);
+            const PaintProps pp = a.p.props[L];
+            float cov[2];
+            if (co) {
+                const uint64_t carry = cover_add(a.tl_carry[g], a.tl_cover[g]);
+                cov[0] = cov[1] = from_area(PIXEL_WIDTH * cover_lane(carry, y), pp.fill_rule);
+            } else {
+                const int32_t cy = cover_lane(a.tl_carry[g], y);
+                int32_t ar0 = 0, ar1 = 0, cv0 = 0, cv1 = 0;
+                const uint32_t sb = a.tl_start[g], se = a.tl_start[g + 1];
+                for (uint32_t base = sb; base < se; base += 32) {
+                    const uint32_t mine = base + lane < se ? (uint32_t)a.segs[base + lane] : 0u;
+                    const uint32_t m = min(32u, se - base);
+                    for (uint32_t q = 0; q < m; q++) {
+                        const uint32_t low = __shfl_sync(0xffffffffu, mine, q);
+                        if (low_tile_y(low) == y) {
+                            const uint32_t tx = low_tile_x(low);
+                            const int32_t ar = low_area(low), cv = low_cover(low);
+                            if (tx == x0) ar0 += ar;
+                            if (tx == x0 + 1) ar1 += ar;
+                            if (tx < x0) cv0 += cv;
+                            if (tx < x0 + 1) cv1 += cv;
+                        }
+                    }
+                }
+                // compute_areas (painter/mod.rs:347-362): 16 * i8 cover + i16 area
+                cov[0] = from_area(PIXEL_WIDTH * (int32_t)(int8_t)(cy + cv0) + (int32_t)(int16_t)ar0, pp.fill_rule);
+                cov[1] = from_area(PIXEL_WIDTH * (int32_t)(int8_t)(cy + cv1) + (int32_t)(int16_t)ar1, pp.fill_rule);
+            }
+            // A column is blended when any of its 8 coverages is non-zero
+            // (painter/mod.rs:287-289).
+            const uint32_t b0 = __ballot_sync(0xffffffffu, cov[0] != 0.0f);
+            const uint32_t b1 = __ballot_sync(0xffffffffu, cov[1] != 0.0f);
+            const bool col[2] = {((b0 >> (8 * xg)) & 0xFFu) != 0, ((b1 >> (8 * xg)) & 0xFFu) != 0};
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                if (!col[h]) continue;
+                // blend_at (painter/mod.rs:364-400)
+                const float al = pp.color[3] * cov[h];
+                const float inv = 1.0f - al;
+                const float f0 = blend_vec(pp.blend_mode, c[h][0], pp.color[0]) * al;
+                const float f1 = blend_vec(pp.blend_mode, c[h][1], pp.color[1]) * al;
+                const float f2 = blend_vec(pp.blend_mode, c[h][2], pp.color[2]) * al;
+                c[h][0] = __fmaf_rn(c[h][0], inv, f0);
+                c[h][1] = __fmaf_rn(c[h][1], inv, f1);
+                c[h][2] = __fmaf_rn(c[h][2], inv, f2);
+                c[h][3] = __fmaf_rn(c[h][3], inv, al);
+            }
+        }
+        px0 = pixel_bytes(c[0][0], c[0][1], c[0][2], c[0][3]);
+        px1 = pixel_bytes(c[1][0], c[1][1], c[1][2], c[1][3]);
+    }
+
+    // RGBA8 store: a full tile goes out as 16 x 16-byte rows halves.
+    const uint32_t gx = i * 8 + x0, gy = j * 8 + y;
+    const bool full_tile = (i * 8 + 8 <= p.width) && (j * 8 + 8 <= p.height) && ((p.stride & 3) == 0) &&
+                           ((((uintptr_t)p.out) & 15) == 0);
+    if (full_tile) {
+        const uint32_t q0 = __shfl_down_sync(0xffffffffu, px0, 8);
+        const uint32_t q1 = __shfl_down_sync(0xffffffffu, px1, 8);
+        if ((xg & 1) == 0) {
+            uint4 v = make_uint4(px0, px1, q0, q1);
+            *reinterpret_cast<uint4*>(p.out + ((size_t)gy * p.stride + gx) * 4) = v;
+        }
+    } else if (gy < p.height) {
+        uint32_t* row = reinterpret_cast<uint32_t*>(p.out + (size_t)gy * p.stride * 4);
+        if (gx < p.width) row[gx] = px0;
+        if (gx + 1 < p.width) row[gx + 1] = px1;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_tl_heads(int mode, const uint64_t* segs, uint32_t n, uint32_t* block_counts,
+                            const uint32_t* block_off, uint32_t* tl_start, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    uint32_t per = HEAD_THREADS * HEAD_ITEMS;
+    count_launches(1);
+    k_tl_heads<<<(n + per - 1) / per, HEAD_THREADS, 0, st>>>(mode, segs, n, block_counts, block_off, tl_start);
+    return cudaGetLastError();
+}
+
+uint32_t tl_heads_grid(uint32_t n) { return (n + HEAD_THREADS * HEAD_ITEMS - 1) / (HEAD_THREADS * HEAD_ITEMS); }
+
+cudaError_t launch_tl_reduce_scan(const uint64_t* segs, uint32_t n_segs, uint32_t G, const RenderGeom& geom,
+                                  CarryBuffers& cb, Scratch* s, cudaStream_t st) {
+    (void)n_segs;
+    (void)s;
+    if (G == 0) return cudaSuccess;
+    count_launches(2);
+    k_tl_reduce<<<(G + 255) / 256, 256, 0, st>>>(segs, G, cb.tl_start, geom.row_len, cb.tl_cover, cb.tl_flags);
+    k_tl_carry<<<(G + 255) / 256, 256, 0, st>>>(G, cb.tl_cover, cb.tl_flags, cb.tl_carry);
+    return cudaGetLastError();
+}
+
+static ItemGeom item_geom(const RenderGeom& geom, const PaintParams* pp) {
+    ItemGeom ig;
+    ig.geom = geom;
+    ig.h0 = pp ? pp->crop_h0 : 0;
+    ig.h1 = pp ? pp->crop_h1 : geom.row_len;
+    ig.v0 = pp ? pp->crop_v0 : 0;
+    ig.v1 = pp ? pp->crop_v1 : geom.rows;
+    return ig;
+}
+
+cudaError_t launch_items_crop(int mode, const uint64_t* segs, uint32_t G, const RenderGeom& geom,
+                              const PaintParams& pp, CarryBuffers& cb, int idx_bits, cudaStream_t st) {
+    if (G == 0) return cudaSuccess;
+    ItemGeom ig = item_geom(geom, &pp);
+    count_launches(1);
+    if (mode == 0)
+        k_items_count<<<(G + 255) / 256, 256, 0, st>>>(segs, G, cb.tl_start, cb.tl_flags, cb.tl_cover, cb.tl_carry, ig,
+                                                       pp.props, cb.item_count);
+    else
+        k_items_write<<<(G + 255) / 256, 256, 0, st>>>(segs, G, cb.tl_start, cb.tl_flags, cb.tl_cover, cb.tl_carry, ig,
+                                                       pp.props, cb.item_off, idx_bits, cb.items);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_items(int mode, const uint64_t* segs, uint32_t G, const RenderGeom& geom, const PaintProps* props,
+                         CarryBuffers& cb, int idx_bits, cudaStream_t st) {
+    PaintParams pp{};
+    pp.props = props;
+    pp.crop_h1 = geom.row_len;
+    pp.crop_v1 = geom.rows;
+    return launch_items_crop(mode, segs, G, geom, pp, cb, idx_bits, st);
+}
+
+cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_tiles, int shift, uint32_t n_orders,
+                               uint32_t* tile_start, cudaStream_t st) {
+    count_launches(1);
+    k_tile_ranges<<<(W + 1 + 255) / 256, 256, 0, st>>>(items, W, n_tiles, shift, n_orders, tile_start);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_paint(const PaintParams& p, const uint64_t* segs, const uint64_t* items, int idx_bits,
+                         const uint32_t* tile_start, const CarryBuffers& cb, uint32_t warps_per_block,
+                         cudaStream_t st) {
+    uint32_t n_tiles = p.geom.rows * p.geom.row_len;
+    if (n_tiles == 0) return cudaSuccess;
+    warps_per_block = warps_per_block ? warps_per_block : 4;
+    PaintArgs a{p, segs, items, idx_bits, tile_start, cb.tl_start, cb.tl_cover, cb.tl_carry};
+    count_launches(1);
+    k_paint<<<(n_tiles + warps_per_block - 1) / warps_per_block, 32 * warps_per_block, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace cgb

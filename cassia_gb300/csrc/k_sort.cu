@@ -1,0 +1,393 @@
+// Device-wide scan and the onesweep LSD radix sort of 64-bit pixel-segment keys.
+//
+// Replaces Rasterizer::sort (surpass/src/rasterizer/mod.rs:287-290), a rayon
+// par_sort_unstable_by_key over `segment >> 22`.  The GPU sort is an LSD radix
+// sort over a caller-chosen bit range with one "onesweep" kernel per digit:
+// each CTA ranks a tile of keys in shared memory (warp match_any multi-split),
+// publishes its digit counts, resolves its global digit offsets with a
+// decoupled look-back over the preceding tiles, and scatters the tile through
+// shared memory so that each digit run is written contiguously.  The sort is
+// stable, so sorting bits [22, 64) keeps rasterizer order among equal keys.
+//
+// Every spin on a predecessor's status is bounded: past the limit the kernel
+// sets the handle's error flag and stops waiting (the host reports
+// CGB_ERR_DEVICE_TIMEOUT), so a failed GPU never hangs on it.
+#include <algorithm>
+
+#include "cgb_internal.cuh"
+
+namespace cgb {
+
+namespace {
+
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+template <class T>
+__device__ __forceinline__ T warp_inclusive_scan(T v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        T n = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += n;
+    }
+    return v;
+}
+
+// Block-wide exclusive scan (blockDim.x a multiple of 32, <= 1024).  Every
+// thread of the block must call it.
+template <class T>
+__device__ T block_exclusive_scan(T v, T* total) {
+    __shared__ T warp_sums[32];
+    __shared__ T s_total;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    T inc = warp_inclusive_scan(v);
+    if (lane == 31) warp_sums[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        T w = lane < nw ? warp_sums[lane] : T(0);
+        T wi = warp_inclusive_scan(w);
+        if (lane < nw) warp_sums[lane] = wi - w;
+        if (lane == 31) s_total = wi;
+    }
+    __syncthreads();
+    T res = warp_sums[warp] + inc - v;
+    if (total) *total = s_total;
+    __syncthreads();
+    return res;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t* __restrict__ in, uint32_t n,
+                                                             uint64_t* __restrict__ sums) {
+    uint64_t s = 0;
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        uint64_t i = base + (uint64_t)k * SCAN_THREADS + threadIdx.x;
+        if (i < n) s += in[i];
+    }
+    __shared__ uint64_t red[32];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint64_t v = threadIdx.x < (SCAN_THREADS >> 5) ? red[threadIdx.x] : 0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) sums[blockIdx.x] = v;
+    }
+}
+
+// Exclusive scan of nb u64 block sums in place; sums[nb] = total; out_tail = total (u32).
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_sums(uint64_t* sums, uint32_t nb, uint32_t* out_tail) {
+    __shared__ uint64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t b0 = 0; b0 < nb; b0 += SCAN_THREADS) {
+        uint32_t i = b0 + threadIdx.x;
+        uint64_t v = i < nb ? sums[i] : 0;
+        uint64_t tot;
+        uint64_t ex = block_exclusive_scan<uint64_t>(v, &tot);
+        uint64_t c = carry;
+        if (i < nb) sums[i] = c + ex;
+        __syncthreads();
+        if (threadIdx.x == 0) carry = c + tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        sums[nb] = carry;
+        if (out_tail) *out_tail = (uint32_t)carry;
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const uint32_t* __restrict__ in, uint32_t n,
+                                                            const uint64_t* __restrict__ sums,
+                                                            uint32_t* __restrict__ out) {
+    // Blocked arrangement: thread t owns elements [t*ITEMS, (t+1)*ITEMS) of the tile.
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS];
+    uint64_t s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        uint64_t i = base + k;
+        v[k] = i < n ? in[i] : 0;
+        s += v[k];
+    }
+    uint64_t ex = block_exclusive_scan<uint64_t>(s, nullptr) + sums[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        uint64_t i = base + k;
+        if (i < n) out[i] = (uint32_t)ex;
+        ex += v[k];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// radix sort
+// ---------------------------------------------------------------------------
+
+constexpr int RADIX = 256;
+constexpr int MAX_PASSES = 11;
+constexpr int SORT_THREADS = 512;
+constexpr int SORT_WARPS = SORT_THREADS / 32;
+constexpr int SORT_ITEMS = 8;
+constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;  // 4096 keys per CTA
+constexpr uint32_t ST_AGG = 1u << 30;
+constexpr uint32_t ST_INC = 2u << 30;
+constexpr uint32_t ST_VAL = (1u << 30) - 1;
+constexpr uint32_t SPIN_LIMIT = 1u << 22;  // ~ a second with the back-off below
+
+struct PassPlan {
+    int n;
+    int shift[MAX_PASSES];
+    int bits[MAX_PASSES];
+};
+
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// One pass over the keys that histograms every digit of every pass.
+__global__ void __launch_bounds__(512) k_radix_hist(const uint64_t* __restrict__ keys, uint32_t n, PassPlan plan,
+                                                    uint32_t* __restrict__ hist) {
+    __shared__ uint32_t sh[MAX_PASSES][RADIX];
+    for (int i = threadIdx.x; i < plan.n * RADIX; i += blockDim.x) (&sh[0][0])[i] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint64_t k = keys[i];
+        for (int p = 0; p < plan.n; p++) {
+            uint32_t d = (uint32_t)(k >> plan.shift[p]) & ((1u << plan.bits[p]) - 1);
+            atomicAdd(&sh[p][d], 1u);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < plan.n * RADIX; i += blockDim.x) {
+        uint32_t v = (&sh[0][0])[i];
+        if (v) atomicAdd(&hist[i], v);
+    }
+}
+
+// Exclusive scan of each pass's 256 bins (one CTA of 256 threads per pass).
+__global__ void __launch_bounds__(RADIX) k_radix_hist_scan(uint32_t* hist) {
+    uint32_t* h = hist + blockIdx.x * RADIX;
+    uint32_t v = h[threadIdx.x];
+    uint32_t ex = block_exclusive_scan<uint32_t>(v, nullptr);
+    h[threadIdx.x] = ex;
+}
+
+__global__ void __launch_bounds__(SORT_THREADS) k_onesweep(const uint64_t* __restrict__ in, uint64_t* __restrict__ out,
+                                                           uint32_t n, int shift, int bits,
+                                                           const uint32_t* __restrict__ global_off,
+                                                           uint32_t* lookback, uint32_t* tile_counter,
+                                                           uint32_t* err) {
+    __shared__ uint16_t s_hist[SORT_WARPS][RADIX];  // per-warp counts, then offsets (< 4096)
+    __shared__ uint32_t s_count[RADIX];
+    __shared__ uint32_t s_start[RADIX];
+    __shared__ uint32_t s_base[RADIX];
+    __shared__ uint64_t s_keys[SORT_TILE];
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_abort;
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t mask = (1u << bits) - 1;
+    if (tid == 0) {
+        s_tile = atomicAdd(tile_counter, 1u);
+        s_abort = 0;
+    }
+    for (int i = tid; i < SORT_WARPS * RADIX; i += SORT_THREADS) (&s_hist[0][0])[i] = 0;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint64_t base = (uint64_t)tile * SORT_TILE;
+
+    uint64_t key[SORT_ITEMS];
+    uint32_t dig[SORT_ITEMS];
+    uint32_t rank[SORT_ITEMS];
+#pragma unroll
+    for (int k = 0; k < SORT_ITEMS; k++) {
+        uint64_t idx = base + (uint64_t)warp * 32 * SORT_ITEMS + k * 32 + lane;
+        bool valid = idx < n;
+        key[k] = valid ? in[idx] : 0;
+        dig[k] = valid ? ((uint32_t)(key[k] >> shift) & mask) : RADIX;
+    }
+    // Warp-level multi-split ranking, in key order within the warp (stable).
+    const uint32_t lt = lanemask_lt();
+#pragma unroll
+    for (int k = 0; k < SORT_ITEMS; k++) {
+        uint32_t d = dig[k];
+        uint32_t peers = __match_any_sync(0xffffffffu, d);
+        uint32_t r = __popc(peers & lt);
+        uint32_t cnt = d < RADIX ? s_hist[warp][d] : 0;
+        __syncwarp();
+        if (d < RADIX && r == 0) s_hist[warp][d] = (uint16_t)(cnt + __popc(peers));
+        __syncwarp();
+        rank[k] = cnt + r;
+    }
+    __syncthreads();
+    // Per digit: exclusive offsets across warps and the tile's count.
+    for (int d = tid; d < RADIX; d += SORT_THREADS) {
+        uint32_t sum = 0;
+#pragma unroll
+        for (int w = 0; w < SORT_WARPS; w++) {
+            uint32_t v = s_hist[w][d];
+            s_hist[w][d] = (uint16_t)sum;
+            sum += v;
+        }
+        s_count[d] = sum;
+    }
+    __syncthreads();
+    // Decoupled look-back for the tile's global digit offsets.
+    if (tid < RADIX) {
+        const int d = tid;
+        const uint32_t cnt = s_count[d];
+        uint32_t excl = 0;
+        uint32_t* mine = lookback + (uint64_t)tile * RADIX + d;
+        if (tile == 0) {
+            st_relaxed(mine, ST_INC | cnt);
+        } else {
+            st_relaxed(mine, ST_AGG | cnt);
+            int64_t t = (int64_t)tile - 1;
+            uint32_t spins = 0;
+            while (t >= 0) {
+                uint32_t v = ld_relaxed(lookback + (uint64_t)t * RADIX + d);
+                uint32_t stt = v & ~ST_VAL;
+                if (stt == 0) {
+                    if (++spins > SPIN_LIMIT) {
+                        atomicExch(err, 1u);
+                        s_abort = 1;
+                        break;
+                    }
+                    __nanosleep(64);
+                    continue;
+                }
+                excl += v & ST_VAL;
+                if (stt == ST_INC) break;
+                t--;
+            }
+            st_relaxed(mine, ST_INC | ((excl + cnt) & ST_VAL));
+        }
+        s_base[d] = global_off[d] + excl;
+    }
+    // Tile-local digit starts: exclusive scan of s_count over the 256 digits.
+    {
+        uint32_t v = tid < RADIX ? s_count[tid] : 0;
+        uint32_t ex = block_exclusive_scan<uint32_t>(v, nullptr);
+        if (tid < RADIX) s_start[tid] = ex;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < SORT_ITEMS; k++) {
+        uint32_t d = dig[k];
+        if (d < RADIX) s_keys[s_start[d] + s_hist[warp][d] + rank[k]] = key[k];
+    }
+    __syncthreads();
+    if (s_abort) return;  // a predecessor never published: leave the output, the host reports the timeout
+    const uint32_t valid = (n - base) < (uint64_t)SORT_TILE ? (uint32_t)(n - base) : (uint32_t)SORT_TILE;
+    for (uint32_t i = tid; i < valid; i += SORT_THREADS) {
+        uint64_t k = s_keys[i];
+        uint32_t d = (uint32_t)(k >> shift) & mask;
+        uint32_t pos = s_base[d] + (i - s_start[d]);
+        if (pos < n) out[pos] = k;
+    }
+}
+
+}  // namespace
+
+size_t scan_scratch_bytes(uint32_t n) { return ((size_t)n / SCAN_TILE + 2) * sizeof(uint64_t); }
+
+cudaError_t scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, Scratch* s, cudaStream_t st,
+                     uint64_t* total_host) {
+    uint32_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    cudaError_t e = s->ensure(s->scan_sums, ((size_t)nb + 1) * sizeof(uint64_t));
+    if (e != cudaSuccess) return e;
+    uint64_t* sums = s->scan_sums.as<uint64_t>();
+    count_launches(nb > 0 ? 3 : 1);
+    if (nb > 0) k_scan_reduce<<<nb, SCAN_THREADS, 0, st>>>(in, n, sums);
+    k_scan_sums<<<1, SCAN_THREADS, 0, st>>>(sums, nb, out + n);
+    if (nb > 0) k_scan_apply<<<nb, SCAN_THREADS, 0, st>>>(in, n, sums, out);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if (total_host) {
+        e = cudaMemcpyAsync(s->pinned, sums + nb, sizeof(uint64_t), cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) return e;
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return e;
+        *total_host = s->pinned[0];
+    }
+    return cudaSuccess;
+}
+
+cudaError_t scan_block_counts(const uint32_t* counts, uint32_t* offsets, uint32_t n_blocks, Scratch* s,
+                              cudaStream_t st, uint64_t* total_host) {
+    return scan_u32(counts, offsets, n_blocks, s, st, total_host);
+}
+
+static PassPlan make_plan(int bit_lo, int bit_hi, int digit_bits) {
+    PassPlan p{};
+    int bits = std::max(0, bit_hi - bit_lo);
+    digit_bits = std::min(8, std::max(1, digit_bits));
+    p.n = (bits + digit_bits - 1) / digit_bits;
+    if (p.n > MAX_PASSES) p.n = MAX_PASSES;
+    int sh = bit_lo;
+    for (int i = 0; i < p.n; i++) {
+        int b = bits / p.n + (i < bits % p.n ? 1 : 0);  // even split, e.g. 42 bits -> 6 x 7
+        p.shift[i] = sh;
+        p.bits[i] = b;
+        sh += b;
+    }
+    return p;
+}
+
+size_t radix_sort_scratch_bytes(uint32_t n, int bit_lo, int bit_hi, int digit_bits) {
+    PassPlan p = make_plan(bit_lo, bit_hi, digit_bits);
+    size_t tiles = ((size_t)n + SORT_TILE - 1) / SORT_TILE;
+    return (size_t)p.n * RADIX * 4 + tiles * RADIX * 4 + 64;
+}
+
+cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo, int bit_hi, int digit_bits,
+                           Scratch* s, uint32_t* err_flag, cudaStream_t st, uint64_t** result, int* passes) {
+    PassPlan plan = make_plan(bit_lo, bit_hi, digit_bits);
+    *result = keys;
+    if (passes) *passes = plan.n;
+    if (n <= 1 || plan.n == 0) return cudaSuccess;
+    if (n >= ST_VAL) return cudaErrorInvalidValue;
+    uint32_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
+    cudaError_t e;
+    if ((e = s->ensure(s->sort_hist, (size_t)MAX_PASSES * RADIX * 4)) != cudaSuccess) return e;
+    if ((e = s->ensure(s->sort_lookback, (size_t)tiles * RADIX * 4)) != cudaSuccess) return e;
+    if ((e = s->ensure(s->sort_counter, MAX_PASSES * 4)) != cudaSuccess) return e;
+    uint32_t* hist = s->sort_hist.as<uint32_t>();
+    uint32_t* lb = s->sort_lookback.as<uint32_t>();
+    uint32_t* ctr = s->sort_counter.as<uint32_t>();
+    if ((e = cudaMemsetAsync(hist, 0, (size_t)plan.n * RADIX * 4, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(ctr, 0, MAX_PASSES * 4, st)) != cudaSuccess) return e;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    uint32_t hist_blocks = std::min<uint32_t>((n + 511) / 512, (uint32_t)sms * 4);
+    count_launches(2 + plan.n);
+    k_radix_hist<<<hist_blocks, 512, 0, st>>>(keys, n, plan, hist);
+    k_radix_hist_scan<<<plan.n, RADIX, 0, st>>>(hist);
+    uint64_t* src = keys;
+    uint64_t* dst = tmp;
+    for (int p = 0; p < plan.n; p++) {
+        if ((e = cudaMemsetAsync(lb, 0, (size_t)tiles * RADIX * 4, st)) != cudaSuccess) return e;
+        k_onesweep<<<tiles, SORT_THREADS, 0, st>>>(src, dst, n, plan.shift[p], plan.bits[p], hist + p * RADIX, lb,
+                                                   ctr + p, err_flag);
+        std::swap(src, dst);
+    }
+    *result = src;
+    return cudaGetLastError();
+}
+
+}  // namespace cgb

@@ -218,6 +218,9 @@ CGB_EXPORT cgb_status cgb_layer_set_transform(cgb_composition* c, uint32_t layer
 CGB_EXPORT cgb_status cgb_layer_set_order(cgb_composition* c, uint32_t layer_id, uint32_t order);
 CGB_EXPORT cgb_status cgb_layer_set_props(cgb_composition* c, uint32_t layer_id,
                                           const cgb_props* props);
+/* Batched set_props: props[k] applies to layer_ids[k]. */
+CGB_EXPORT cgb_status cgb_layers_set_props(cgb_composition* c, size_t n, const uint32_t* layer_ids,
+                                           const cgb_props* props);
 /* Batched set_transform for n layers (6 floats each); flags as above. */
 CGB_EXPORT cgb_status cgb_layers_set_transforms(cgb_composition* c, size_t n,
                                                 const uint32_t* layer_ids, const float* affine6,
@@ -255,6 +258,17 @@ CGB_EXPORT cgb_status cgb_get_tuning(cgb_composition* c, cgb_tuning* out);
 
 /* Synchronize the handle's stream (device buffers written by render are ready). */
 CGB_EXPORT cgb_status cgb_synchronize(cgb_composition* c);
+
+/* The cudaStream_t the handle launches on (for callers that order their own
+ * work or timing events after a render). */
+CGB_EXPORT cgb_status cgb_get_stream(cgb_composition* c, void** out_stream);
+
+/* Kernels this library has launched in the process (all handles). */
+CGB_EXPORT uint64_t cgb_kernel_launches(void);
+
+/* Drops every layer and line, as Lines::cleared does for the builder
+ * (surpass/src/segment.rs:282-301); device buffers are kept for reuse. */
+CGB_EXPORT cgb_status cgb_composition_clear(cgb_composition* c);
 
 #ifdef __cplusplus
 }

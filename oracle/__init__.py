@@ -58,6 +58,10 @@ def lib():
             "orc_comp_create_layer": ([vp, P(u32)], ctypes.c_int),
             "orc_comp_insert_path": ([vp, u32, P(u32), sz, fp, fp], ctypes.c_int),
             "orc_comp_insert_lines": ([vp, u32, fp, sz], ctypes.c_int),
+            "orc_comp_insert_paths": ([vp, sz, P(u32), P(u64), P(u32), P(u64), fp, fp, P(ctypes.c_uint8)],
+                                      ctypes.c_int),
+            "orc_layers_set_solid": ([vp, sz, P(u32), P(u32), P(u32), fp], ctypes.c_int),
+            "orc_layers_set_transforms": ([vp, sz, P(u32), fp, u32], ctypes.c_int),
             "orc_layer_set_enabled": ([vp, u32, ctypes.c_int], ctypes.c_int),
             "orc_layer_set_transform": ([vp, u32, fp, u32], ctypes.c_int),
             "orc_layer_set_order": ([vp, u32, u32], ctypes.c_int),
@@ -198,6 +202,34 @@ class Composition:
     def insert_lines(self, layer_id, segs):
         segs = np.ascontiguousarray(np.asarray(segs, np.float32).reshape(-1, 4))
         _check(self._L.orc_comp_insert_lines(self._h, layer_id, _fptr(segs), len(segs)), "insert_lines")
+
+    def insert_paths(self, scene):
+        P = ctypes.POINTER
+        s = scene
+        st = self._L.orc_comp_insert_paths(
+            self._h, s.n_paths, s.path_layer.ctypes.data_as(P(ctypes.c_uint32)),
+            s.cmd_offsets.ctypes.data_as(P(ctypes.c_uint64)), s.kinds.ctypes.data_as(P(ctypes.c_uint32)),
+            s.point_offsets.ctypes.data_as(P(ctypes.c_uint64)), _fptr(s.points), None, None)
+        _check(st, "insert_paths")
+
+    def set_layers_solid(self, ids, fill_rules, blend_modes, colors):
+        P = ctypes.POINTER
+        ids = np.ascontiguousarray(ids, np.uint32)
+        fr = np.ascontiguousarray(fill_rules, np.uint32)
+        bm = np.ascontiguousarray(blend_modes, np.uint32)
+        col = np.ascontiguousarray(colors, np.float32)
+        st = self._L.orc_layers_set_solid(self._h, len(ids), ids.ctypes.data_as(P(ctypes.c_uint32)),
+                                          fr.ctypes.data_as(P(ctypes.c_uint32)),
+                                          bm.ctypes.data_as(P(ctypes.c_uint32)), _fptr(col))
+        _check(st, "set_layers_solid")
+
+    def set_transforms(self, ids, affine6, unchecked=True):
+        P = ctypes.POINTER
+        ids = np.ascontiguousarray(ids, np.uint32)
+        t = np.ascontiguousarray(affine6, np.float32)
+        st = self._L.orc_layers_set_transforms(self._h, len(ids), ids.ctypes.data_as(P(ctypes.c_uint32)), _fptr(t),
+                                               abi.TRANSFORM_UNCHECKED if unchecked else 0)
+        _check(st, "set_transforms")
 
     def set_enabled(self, layer_id, enabled):
         _check(self._L.orc_layer_set_enabled(self._h, layer_id, int(bool(enabled))), "set_enabled")

@@ -1668,6 +1668,18 @@ int orc_comp_insert_lines(orc_composition* c, uint32_t layer_id, const float* se
     return CGB_OK;
 }
 
+int orc_comp_insert_paths(orc_composition* c, size_t n_paths, const uint32_t* layer_ids, const uint64_t* cmd_offsets,
+                          const uint32_t* kinds, const uint64_t* point_offsets, const float* points,
+                          const float* transforms9, const uint8_t* has_transform) {
+    for (size_t k = 0; k < n_paths; k++) {
+        const float* t = (transforms9 && has_transform && has_transform[k]) ? transforms9 + 9 * k : nullptr;
+        int st = orc_comp_insert_path(c, layer_ids[k], kinds + cmd_offsets[k], cmd_offsets[k + 1] - cmd_offsets[k],
+                                      points + point_offsets[k], t);
+        if (st) return st;
+    }
+    return CGB_OK;
+}
+
 static MLayer* find_layer(orc_composition* c, uint32_t id) {
     auto it = c->c.layers.find(id);
     return it == c->c.layers.end() ? nullptr : &it->second;
@@ -1722,6 +1734,30 @@ int orc_layer_set_props(orc_composition* c, uint32_t id, const cgb_props* props)
     if (!(l->props == p)) {
         l->unchanged = 0;
         l->props = p;
+    }
+    return CGB_OK;
+}
+
+int orc_layers_set_solid(orc_composition* c, size_t n, const uint32_t* ids, const uint32_t* fill_rules,
+                         const uint32_t* blend_modes, const float* colors) {
+    for (size_t i = 0; i < n; i++) {
+        cgb_props p{};
+        p.fill_rule = fill_rules[i];
+        p.func = CGB_FUNC_DRAW;
+        p.blend_mode = blend_modes[i];
+        p.fill_kind = CGB_FILL_SOLID;
+        for (int k = 0; k < 4; k++) p.color[k] = colors[4 * i + k];
+        int st = orc_layer_set_props(c, ids[i], &p);
+        if (st) return st;
+    }
+    return CGB_OK;
+}
+
+int orc_layers_set_transforms(orc_composition* c, size_t n, const uint32_t* ids, const float* affine6,
+                              uint32_t flags) {
+    for (size_t i = 0; i < n; i++) {
+        int st = orc_layer_set_transform(c, ids[i], affine6 + 6 * i, flags);
+        if (st) return st;
     }
     return CGB_OK;
 }

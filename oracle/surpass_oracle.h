@@ -67,6 +67,16 @@ int orc_comp_create_layer(orc_composition* c, uint32_t* out_id);
 int orc_comp_insert_path(orc_composition* c, uint32_t layer_id, const uint32_t* kinds,
                          size_t n_cmds, const float* points, const float* transform9);
 int orc_comp_insert_lines(orc_composition* c, uint32_t layer_id, const float* segments, size_t n);
+/* Batched insert_in_layer (same layout as cgb_insert_paths). */
+int orc_comp_insert_paths(orc_composition* c, size_t n_paths, const uint32_t* layer_ids,
+                          const uint64_t* cmd_offsets, const uint32_t* kinds,
+                          const uint64_t* point_offsets, const float* points,
+                          const float* transforms9, const uint8_t* has_transform);
+/* Batched set_props with Fill::Solid styles, and batched set_transform. */
+int orc_layers_set_solid(orc_composition* c, size_t n, const uint32_t* ids, const uint32_t* fill_rules,
+                         const uint32_t* blend_modes, const float* colors);
+int orc_layers_set_transforms(orc_composition* c, size_t n, const uint32_t* ids, const float* affine6,
+                              uint32_t flags);
 int orc_layer_set_enabled(orc_composition* c, uint32_t id, int enabled);
 int orc_layer_set_transform(orc_composition* c, uint32_t id, const float* affine6, uint32_t flags);
 int orc_layer_set_order(orc_composition* c, uint32_t id, uint32_t order);

@@ -1,0 +1,231 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+Integer and byte results must be bit-exact: sorted pixel segments (canonical
+full-u64 order and the reference's key order), NONE counts and RGBA8 pixels.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from cassia_gb300 import scenes
+from cassia_gb300.types import BlendMode, FillRule, Path, Props, Style, solid
+
+from . import test_oracle_kats as kats
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(params=[False, True], ids=["u16", "wide"])
+def gpu_comp(request, gpu_lib):
+    from cassia_gb300 import Composition
+    c = Composition(wide=request.param)
+    yield c
+    c.close()
+
+
+# ---- the reference's render KATs, through the GPU ----------------------------------
+
+KAT_NAMES = ["background_color_clear", "one_pixel", "two_pixels_same_layer", "one_pixel_translated",
+             "one_pixel_rotated", "remove_and_resize", "remove_twice", "render_change_layers_only",
+             "clear_emptied_tiles", "separate_layer_caches", "even_odd"]
+
+
+def _make_kat(name):
+    fn = getattr(kats, "test_" + name)
+
+    def t(gpu_comp):
+        fn(gpu_comp)
+
+    t.__name__ = "test_gpu_kat_" + name
+    return t
+
+
+for _n in KAT_NAMES:
+    globals()["test_gpu_kat_" + _n] = _make_kat(_n)
+
+
+# ---- seeded scenes -------------------------------------------------------------------------
+
+def _load_both(scene, wide=None):
+    from cassia_gb300 import Composition
+    wide = scene.wide if wide is None else wide
+    g = Composition(wide=wide)
+    o = oracle.Composition(wide=wide)
+    scenes.load(scene, g)
+    scenes.load(scene, o)
+    return g, o
+
+
+def _assert_same_image(a, b):
+    if not np.array_equal(a, b):
+        diff = np.argwhere(np.any(a != b, axis=-1))
+        y, x = diff[0]
+        raise AssertionError(f"{len(diff)} pixels differ; first at (x={x}, y={y}): gpu={a[y, x]} oracle={b[y, x]}")
+
+
+def _render_both(scene, g, o, **kw):
+    img_g = np.zeros((scene.height, scene.width, 4), np.uint8)
+    img_o = np.zeros_like(img_g)
+    g.render(img_g, scene.width, scene.background, **kw)
+    o.render(img_o, scene.width, scene.background, threads=8, **kw)
+    return img_g, img_o
+
+
+SMALL_SCENES = {
+    "circles": lambda: scenes.circles(seed=11, n_layers=300, size=256),
+    "mixed": lambda: scenes.mixed(seed=12, n_layers=400, width=320, height=200),
+    "glyphs": lambda: scenes.glyphs(seed=13, n_layers=600, width=480, height=270),
+}
+
+
+@pytest.mark.parametrize("name", list(SMALL_SCENES))
+def test_pixel_segments_bit_exact(name):
+    sc = SMALL_SCENES[name]()
+    g, o = _load_both(sc)
+    gs, gnone = g.pixel_segments(canonical=True)
+    os_, onone = o.pixel_segments(threads=8)
+    assert gnone == onone
+    assert len(gs) == len(os_)
+    assert np.array_equal(gs, os_)
+
+
+@pytest.mark.parametrize("name", list(SMALL_SCENES))
+def test_pixel_segments_key_order(name):
+    # CGB_SORT_KEY: the reference's order (u64 >> 22), a permutation of the same multiset
+    sc = SMALL_SCENES[name]()
+    g, o = _load_both(sc)
+    gs, _ = g.pixel_segments(canonical=False)
+    os_, _ = o.pixel_segments(threads=8)
+    keys = gs >> np.uint64(22)
+    assert np.all(keys[1:] >= keys[:-1])
+    assert np.array_equal(np.sort(gs), os_)
+
+
+@pytest.mark.parametrize("name", list(SMALL_SCENES))
+def test_render_bit_exact(name):
+    sc = SMALL_SCENES[name]()
+    g, o = _load_both(sc)
+    a, b = _render_both(sc, g, o)
+    _assert_same_image(a, b)
+
+
+def test_render_wide_format_matches_u16():
+    sc = SMALL_SCENES["mixed"]()
+    g, o = _load_both(sc, wide=True)
+    a, b = _render_both(sc, g, o)
+    _assert_same_image(a, b)
+    g2, _ = _load_both(sc, wide=False)
+    c = np.zeros_like(a)
+    g2.render(c, sc.width, sc.background)
+    _assert_same_image(a, c)
+
+
+def test_render_all_blend_modes_and_fill_rules():
+    sc = scenes.mixed(seed=21, n_layers=600, width=256, height=160)
+    sc.blend_mode[:] = np.arange(sc.n_layers) % 12
+    sc.fill_rule[:] = (np.arange(sc.n_layers) // 12) % 2
+    g, o = _load_both(sc)
+    a, b = _render_both(sc, g, o)
+    _assert_same_image(a, b)
+
+
+def test_render_opaque_layers_cull_and_solid_tiles():
+    # opaque Over layers exercise skip_fully_covered_layers and the Solid path
+    sc = scenes.mixed(seed=22, n_layers=500, width=256, height=256)
+    sc.blend_mode[:] = np.where(np.arange(sc.n_layers) % 3 == 0, 0, sc.blend_mode)
+    sc.color[::2, 3] = 1.0
+    sc.blend_mode[::2] = BlendMode.Over
+    g, o = _load_both(sc)
+    a, b = _render_both(sc, g, o)
+    _assert_same_image(a, b)
+
+
+@pytest.mark.parametrize("w,h", [(250, 131), (9, 9), (1, 1), (7, 300)])
+def test_render_partial_tiles(w, h):
+    sc = scenes.mixed(seed=23, n_layers=200, width=w, height=h)
+    g, o = _load_both(sc)
+    a, b = _render_both(sc, g, o)
+    _assert_same_image(a, b)
+
+
+def test_render_stride_and_crop():
+    sc = scenes.mixed(seed=24, n_layers=300, width=200, height=120)
+    g, o = _load_both(sc)
+    stride = 232
+    a = np.full((sc.height, stride, 4), 7, np.uint8)
+    b = a.copy()
+    g.render(a, sc.width, sc.background, width_stride=stride)
+    o.render(b, sc.width, sc.background, width_stride=stride, threads=4)
+    _assert_same_image(a, b)
+    a[...] = 9
+    b[...] = 9
+    crop = (37, 150, 20, 90)
+    g.render(a, sc.width, sc.background, width_stride=stride, crop=crop)
+    o.render(b, sc.width, sc.background, width_stride=stride, crop=crop, threads=4)
+    _assert_same_image(a, b)
+
+
+def test_render_empty_and_offcanvas():
+    from cassia_gb300 import Composition
+    g, o = Composition(), oracle.Composition()
+    for c in (g, o):
+        # a layer entirely left of the canvas (its covers cancel per row) and one above it
+        lid = c.create_layer()
+        c.insert_in_layer(lid, kats.pixel_path(-20, 3))
+        c.set_props(lid, solid((1.0, 0.0, 0.0, 0.5)))
+        lid = c.create_layer()
+        c.insert_in_layer(lid, kats.pixel_path(3, -40))
+        c.set_props(lid, solid((0.0, 0.0, 1.0, 1.0)))
+    a = np.zeros((20, 24, 4), np.uint8)
+    b = np.zeros_like(a)
+    g.render(a, 24, (0.25, 0.5, 0.75, 1.0))
+    o.render(b, 24, (0.25, 0.5, 0.75, 1.0))
+    _assert_same_image(a, b)
+
+
+def test_render_left_of_canvas_carry():
+    # shapes that straddle the left edge: their left-of-canvas covers seed the row's carry
+    from cassia_gb300 import Composition
+    g, o = Composition(), oracle.Composition()
+    for c in (g, o):
+        for k, (x, fr) in enumerate([(-30, FillRule.NonZero), (-9, FillRule.EvenOdd), (-1, FillRule.NonZero)]):
+            lid = c.create_layer()
+            p = Path().line((x, 2 + k), (x + 40.3, 5 + k)).line((x + 40.3, 5 + k), (x + 12.0, 19.7 + k)).close()
+            c.insert_in_layer(lid, p)
+            c.set_props(lid, Props(fill_rule=fr, func=Style(fill=(0.2 * k, 0.5, 1.0 - 0.2 * k, 0.8))))
+    a = np.zeros((32, 40, 4), np.uint8)
+    b = np.zeros_like(a)
+    g.render(a, 40, (1.0, 1.0, 1.0, 1.0))
+    o.render(b, 40, (1.0, 1.0, 1.0, 1.0))
+    _assert_same_image(a, b)
+
+
+def test_render_layer_cache_sequence():
+    sc = scenes.mixed(seed=25, n_layers=150, width=160, height=96)
+    g, o = _load_both(sc)
+    cg, co = g.create_buffer_layer_cache(), o.create_buffer_layer_cache()
+    a = np.zeros((sc.height, sc.width, 4), np.uint8)
+    b = np.zeros_like(a)
+    rng = np.random.default_rng(5)
+    for frame in range(4):
+        ids = rng.choice(sc.n_layers, size=10, replace=False).astype(np.uint32)
+        t = sc.transforms[ids].copy()
+        t[:, 4] += rng.uniform(-5, 5, size=len(ids)).astype(np.float32)
+        for c in (g, o):
+            c.set_transforms(ids, t)
+        a[...] = 3
+        b[...] = 3
+        g.render(a, sc.width, sc.background, layer_cache=cg)
+        o.render(b, sc.width, sc.background, layer_cache=co, threads=4)
+        _assert_same_image(a, b)
+
+
+def test_disable_and_gc_matches_oracle():
+    sc = scenes.mixed(seed=26, n_layers=200, width=128, height=128)
+    g, o = _load_both(sc)
+    for c in (g, o):
+        for lid in range(0, 200, 3):
+            c.set_enabled(lid, False)
+    a, b = _render_both(sc, g, o)
+    _assert_same_image(a, b)
+    assert g.lens() == o.lens()
