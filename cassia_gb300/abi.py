@@ -163,6 +163,7 @@ def _declare(lib):
         "cgb_get_stream": ([handle, P(vp)], i32),
         "cgb_kernel_launches": ([], u64),
         "cgb_composition_clear": ([handle], i32),
+        "cgb_sort_keys_noalloc": ([vp, vp, sz, u32, u32, vp], i32),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

@@ -13,6 +13,7 @@
 // sets the handle's error flag and stops waiting (the host reports
 // CGB_ERR_DEVICE_TIMEOUT), so a failed GPU never hangs on it.
 #include <algorithm>
+#include <mutex>
 
 #include "cgb_internal.cuh"
 
@@ -391,3 +392,108 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo
 }
 
 }  // namespace cgb
+
+// ---------------------------------------------------------------------------
+// Allocation-free sort entry point.
+//
+// For callers that cannot allocate device memory while they run: a render
+// thread that has reserved its memory up front, or a host process whose
+// device memory is owned by another allocator (a framework's caching pool),
+// where a cudaMalloc either fails or, like cudaFree, synchronizes the whole
+// device and stalls every other stream.  The sort's scratch (digit
+// histograms, tile counters, the look-back table and the error flag) lives in
+// one file-scope device array instead, sized for at most
+// NOALLOC_MAX_KEYS keys; every GPU that loads this library holds it (about
+// 4 MB) until the process exits.  Every call shares that array and leaves its
+// contents behind: each call clears what must start at zero, and calls whose
+// work overlaps on the GPU (two streams, or two host threads) race on it.
+// ---------------------------------------------------------------------------
+
+namespace cgb {
+namespace {
+
+constexpr uint32_t NOALLOC_MAX_KEYS = 1u << 24;                    // 16,777,216 keys
+constexpr uint32_t NOALLOC_TILES = NOALLOC_MAX_KEYS / SORT_TILE;    // 4,096 onesweep tiles
+constexpr uint32_t NOALLOC_HIST_WORDS = MAX_PASSES * RADIX;
+constexpr uint32_t NOALLOC_CTR_OFF = NOALLOC_HIST_WORDS;            // MAX_PASSES tile counters
+constexpr uint32_t NOALLOC_ERR_OFF = NOALLOC_CTR_OFF + 64;          // error flag
+constexpr uint32_t NOALLOC_LB_OFF = NOALLOC_ERR_OFF + 64;           // look-back table
+constexpr uint32_t NOALLOC_WORDS = NOALLOC_LB_OFF + NOALLOC_TILES * RADIX;
+
+static __device__ __align__(256) uint32_t g_noalloc_scratch[NOALLOC_WORDS];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+uint32_t* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the array's name is only a host-side stand-in).
+cudaError_t noalloc_scratch(uint32_t** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[dev] = (uint32_t*)p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return cudaSuccess;
+}
+
+}  // namespace
+
+}  // namespace cgb
+
+extern "C" CGB_EXPORT cgb_status cgb_sort_keys_noalloc(uint64_t* keys, uint64_t* out, size_t n, uint32_t bit_lo,
+                                                       uint32_t bit_hi, void* stream) {
+    using namespace cgb;
+    if (n > NOALLOC_MAX_KEYS) return CGB_ERR_CAPACITY;
+    if (bit_lo >= bit_hi || bit_hi > 64) return CGB_ERR_INVALID_ARG;
+    if (n > 0 && (!keys || !out || keys == out)) return CGB_ERR_INVALID_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n <= 1) {
+        if (n == 1 && cudaMemcpyAsync(out, keys, 8, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+            return CGB_ERR_DEVICE;
+        return cudaStreamSynchronize(st) == cudaSuccess ? CGB_OK : CGB_ERR_DEVICE;
+    }
+    uint32_t* scratch = nullptr;
+    if (noalloc_scratch(&scratch) != cudaSuccess) return CGB_ERR_DEVICE;
+    uint32_t* hist = scratch;
+    uint32_t* ctr = scratch + NOALLOC_CTR_OFF;
+    uint32_t* err = scratch + NOALLOC_ERR_OFF;
+    uint32_t* lb = scratch + NOALLOC_LB_OFF;
+    const PassPlan plan = make_plan((int)bit_lo, (int)bit_hi, 8);
+    const uint32_t nn = (uint32_t)n;
+    const uint32_t tiles = (nn + SORT_TILE - 1) / SORT_TILE;
+    cudaError_t e = cudaMemsetAsync(scratch, 0, (size_t)NOALLOC_LB_OFF * 4, st);  // hist, counters, error flag
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint32_t hist_blocks = std::min<uint32_t>((nn + 511) / 512, (uint32_t)sms * 4);
+    if (e == cudaSuccess) {
+        k_radix_hist<<<hist_blocks, 512, 0, st>>>(keys, nn, plan, hist);
+        k_radix_hist_scan<<<plan.n, RADIX, 0, st>>>(hist);
+        e = cudaGetLastError();
+    }
+    // Ping-pong between the caller's two buffers; the result must end in `out`.
+    uint64_t* src = keys;
+    uint64_t* dst = out;
+    for (int p = 0; p < plan.n && e == cudaSuccess; p++) {
+        e = cudaMemsetAsync(lb, 0, (size_t)tiles * RADIX * 4, st);
+        if (e != cudaSuccess) break;
+        k_onesweep<<<tiles, SORT_THREADS, 0, st>>>(src, dst, nn, plan.shift[p], plan.bits[p], hist + p * RADIX, lb,
+                                                   ctr + p, err);
+        e = cudaGetLastError();
+        std::swap(src, dst);
+    }
+    if (e == cudaSuccess && src != out) e = cudaMemcpyAsync(out, src, (size_t)nn * 8, cudaMemcpyDeviceToDevice, st);
+    uint32_t flag = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, err, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return CGB_ERR_DEVICE;
+    return flag ? CGB_ERR_DEVICE_TIMEOUT : CGB_OK;
+}

@@ -266,6 +266,24 @@ CGB_EXPORT cgb_status cgb_get_stream(cgb_composition* c, void** out_stream);
 /* Kernels this library has launched in the process (all handles). */
 CGB_EXPORT uint64_t cgb_kernel_launches(void);
 
+/* Sorts n u64 keys in device memory by bits [bit_lo, bit_hi) with the same
+ * onesweep radix sort the pipeline uses, without allocating any memory.  This
+ * entry point has no counterpart in the reference.  It is for callers that
+ * cannot allocate device memory while they run (memory reserved up front by a
+ * render loop, or owned by another allocator, where cudaMalloc fails or, like
+ * cudaFree, synchronizes the device).  `keys` (input, n u64) is overwritten:
+ * the sort ping-pongs between it and `out` (n u64), which receives the sorted
+ * keys; both are on the current device and must not overlap.  At most
+ * 16,777,216 keys (larger n returns CGB_ERR_CAPACITY before any work).  The
+ * scratch is one static device array of about 4 MB held by every GPU that
+ * loads the library; the first call on a device looks up its address, so make
+ * that first call before any stream capture.  Calls share the array: calls
+ * whose work overlaps on the GPU race, so serialize them.  Runs on `stream`
+ * (a cudaStream_t, NULL for the default stream) and returns once the sort is
+ * complete. */
+CGB_EXPORT cgb_status cgb_sort_keys_noalloc(uint64_t* keys, uint64_t* out, size_t n, uint32_t bit_lo,
+                                            uint32_t bit_hi, void* stream);
+
 /* Drops every layer and line, as Lines::cleared does for the builder
  * (surpass/src/segment.rs:282-301); device buffers are kept for reuse. */
 CGB_EXPORT cgb_status cgb_composition_clear(cgb_composition* c);
