@@ -31,6 +31,7 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     "mixed100k": dict(kind="mixed", n_layers=100_000, width=2560, height=1600, seed=2),
     "mixed65k": dict(kind="mixed", n_layers=65_535, width=2560, height=1600, seed=2),
+    "mixed20k": dict(kind="mixed", n_layers=20_000, width=2560, height=1600, seed=2),
     "circles": dict(kind="circles", n_layers=1000, width=1024, height=1024, seed=1),
     "glyphs": dict(kind="glyphs", n_layers=50_000, width=3840, height=2160, seed=3),
 }

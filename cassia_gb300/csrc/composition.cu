@@ -82,6 +82,7 @@ HostProps default_props() {
 }
 
 struct HostLayer {
+    bool present = false;  // the layer exists in mold's `layers` map
     bool enabled = true;
     bool has_transform = false;
     float t[6] = {1, 0, 0, 1, 0, 0};
@@ -114,12 +115,25 @@ struct cgb_composition {
     bool has_default_transform = false;
     float default_transform[6] = {1, 0, 0, 1, 0, 0};
 
-    std::map<uint32_t, HostLayer> layers;
-    std::set<uint32_t> used_ids;
-    std::map<uint32_t, uint32_t> orders_to_layers;
-    bool layers_dirty = true;
+    // mold's `layers: FxHashMap<u16, Layer>` as a dense array by id, and its
+    // IdSet as a used-flag array, the freed ids below next_fresh, and next_fresh.
+    std::vector<HostLayer> layers;
+    std::vector<uint8_t> used;
+    std::set<uint32_t> released;
+    uint32_t next_fresh = 0;
+    uint64_t enabled_len = 0;            // Composition::actual_len, kept incrementally
+    std::vector<LayerRec> layer_recs;    // host mirror of the device layer table
+    uint32_t dirty_lo = UINT32_MAX, dirty_hi = 0;
+    bool layers_grew = true;
     DevBuf d_layers;
     uint32_t n_layer_recs = 0;
+    // LayerProps by order (orders_to_layers + Layer::props), rebuilt when dirty
+    bool props_dirty = true;
+    std::vector<PaintProps> props_host;
+    std::vector<uint32_t> order_layer;
+    uint32_t n_orders = 1;
+    uint32_t unsupported = 0;  // enabled layers whose props the GPU painter does not take
+    uint64_t props_version = 1, props_uploaded = 0;
 
     // frame buffers
     DevBuf recs, lengths, step_off, bcounts, btotals, boff, btoff, segs_a, segs_b;
@@ -234,49 +248,112 @@ cudaError_t ensure_lines(cgb_composition* c, uint64_t n) {
 }
 
 HostLayer* find_layer(cgb_composition* c, uint32_t id) {
-    auto it = c->layers.find(id);
-    return it == c->layers.end() ? nullptr : &it->second;
+    return id < c->layers.size() && c->layers[id].present ? &c->layers[id] : nullptr;
+}
+
+// Refreshes the device-table record of layer `id` and marks it for upload.
+void touch(cgb_composition* c, uint32_t id) {
+    if (id >= c->layer_recs.size()) {
+        c->layer_recs.resize((size_t)id + 1);
+        c->layers_grew = true;
+    }
+    const HostLayer& l = c->layers[id];
+    LayerRec& r = c->layer_recs[id];
+    r.flags = l.present ? (LAYER_PRESENT | (l.enabled ? LAYER_ENABLED : 0u) | (l.has_transform ? LAYER_HAS_TRANSFORM : 0u) |
+                           (l.has_order ? LAYER_HAS_ORDER : 0u))
+                        : 0u;
+    r.order = l.order;
+    std::memcpy(r.t, l.t, sizeof(r.t));
+    c->dirty_lo = std::min(c->dirty_lo, id);
+    c->dirty_hi = std::max(c->dirty_hi, id + 1);
+}
+
+void mark_used(cgb_composition* c, uint32_t id) {
+    if (id >= c->used.size()) c->used.resize((size_t)id + 1, 0);
+    if (!c->used[id]) {
+        c->used[id] = 1;
+        c->released.erase(id);
+    }
+}
+
+// IdSet::release (mold/src/layer.rs:74-98)
+void release_id(cgb_composition* c, uint32_t id) {
+    if (id < c->used.size()) c->used[id] = 0;
+    if (id < c->next_fresh) c->released.insert(id);
 }
 
 // insert_segments bookkeeping (mold/src/composition.rs:58-79)
 void insert_bookkeeping(cgb_composition* c, uint32_t id, uint64_t n) {
+    if (id >= c->layers.size()) c->layers.resize((size_t)id + 1);
     HostLayer& l = c->layers[id];
+    if (!l.present) {
+        l = HostLayer();
+        l.present = true;
+    }
+    const uint64_t before = l.enabled ? l.len : 0;
     l.has_order = true;
     l.order = id;
     l.enabled = true;
     l.len += n;
-    c->used_ids.insert(id);
-    c->layers_dirty = true;
+    c->enabled_len += l.len - before;
+    mark_used(c, id);
+    touch(c, id);
+    c->props_dirty = true;
 }
 
-uint64_t actual_len(cgb_composition* c) {
-    uint64_t s = 0;
-    for (auto& kv : c->layers)
-        if (kv.second.enabled) s += kv.second.len;
-    return s;
-}
+uint64_t actual_len(cgb_composition* c) { return c->enabled_len; }
 
 cgb_status upload_layers(cgb_composition* c) {
-    if (!c->layers_dirty) return CGB_OK;
-    uint32_t n = 0;
-    for (auto& kv : c->layers) n = std::max(n, kv.first + 1);
-    std::vector<LayerRec> recs(std::max<uint32_t>(n, 1));
-    std::memset(recs.data(), 0, recs.size() * sizeof(LayerRec));
-    for (auto& kv : c->layers) {
-        LayerRec& r = recs[kv.first];
-        const HostLayer& l = kv.second;
-        r.flags = LAYER_PRESENT | (l.enabled ? LAYER_ENABLED : 0u) | (l.has_transform ? LAYER_HAS_TRANSFORM : 0u) |
-                  (l.has_order ? LAYER_HAS_ORDER : 0u);
-        r.order = l.order;
-        std::memcpy(r.t, l.t, sizeof(r.t));
+    if (c->dirty_lo >= c->dirty_hi && !c->layers_grew) return CGB_OK;
+    const size_t n = std::max<size_t>(c->layer_recs.size(), 1);
+    if (c->layer_recs.empty()) c->layer_recs.resize(1);
+    size_t lo = c->dirty_lo, hi = c->dirty_hi;
+    if (c->layers_grew || c->d_layers.cap < n * sizeof(LayerRec)) {
+        CK(c->s.ensure(c->d_layers, n * sizeof(LayerRec)));
+        lo = 0;
+        hi = n;
     }
-    CK(c->s.ensure(c->d_layers, recs.size() * sizeof(LayerRec)));
-    CK(cudaMemcpyAsync(c->d_layers.p, recs.data(), recs.size() * sizeof(LayerRec), cudaMemcpyHostToDevice,
-                       c->stream));
+    if (hi > lo)
+        CK(cudaMemcpyAsync(c->d_layers.as<LayerRec>() + lo, c->layer_recs.data() + lo, (hi - lo) * sizeof(LayerRec),
+                           cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    c->n_layer_recs = n;
-    c->layers_dirty = false;
+    c->n_layer_recs = (uint32_t)c->layer_recs.size();
+    c->dirty_lo = UINT32_MAX;
+    c->dirty_hi = 0;
+    c->layers_grew = false;
     return CGB_OK;
+}
+
+// LayerProps by order (composition.rs:229-237, 247-284): orders_to_layers over
+// the enabled layers, ascending ids, so that the highest id wins a shared order.
+void rebuild_props(cgb_composition* c) {
+    uint32_t n_orders = 1;
+    for (size_t id = 0; id < c->layers.size(); id++) {
+        const HostLayer& l = c->layers[id];
+        if (l.present && l.enabled) n_orders = std::max(n_orders, l.order + 1);
+    }
+    c->order_layer.assign(n_orders, UINT32_MAX);
+    for (size_t id = 0; id < c->layers.size(); id++) {
+        const HostLayer& l = c->layers[id];
+        if (l.present && l.enabled) c->order_layer[l.order] = (uint32_t)id;
+    }
+    c->props_host.assign(n_orders, PaintProps{CGB_FILL_NONZERO, CGB_BLEND_OVER,
+                                              PROPS_SOLID | PROPS_DRAW | PROPS_OPAQUE_OVER, 0, {0, 0, 0, 1}});
+    c->unsupported = 0;
+    for (uint32_t o = 0; o < n_orders; o++) {
+        if (c->order_layer[o] == UINT32_MAX) continue;
+        const cgb_props& p = c->layers[c->order_layer[o]].props.c;
+        if (p.func != CGB_FUNC_DRAW || p.is_clipped || p.fill_kind != CGB_FILL_SOLID) c->unsupported++;
+        PaintProps& pp = c->props_host[o];
+        pp.fill_rule = p.fill_rule;
+        pp.blend_mode = p.blend_mode;
+        pp.flags = PROPS_SOLID | PROPS_DRAW | PROPS_PRESENT;
+        if (p.blend_mode == CGB_BLEND_OVER && p.color[3] == 1.0f) pp.flags |= PROPS_OPAQUE_OVER;
+        std::memcpy(pp.color, p.color, sizeof(pp.color));
+    }
+    c->n_orders = n_orders;
+    c->props_dirty = false;
+    c->props_version++;
 }
 
 // Composition::remove_disabled (mold/src/composition.rs:124-142)
@@ -302,15 +379,15 @@ cgb_status remove_disabled(cgb_composition* c) {
         CK(cudaStreamSynchronize(c->stream));
         c->n_lines = kept;
     }
-    for (auto it = c->layers.begin(); it != c->layers.end();) {
-        if (!it->second.enabled) {
-            c->used_ids.erase(it->first);
-            it = c->layers.erase(it);
-        } else {
-            ++it;
+    for (uint32_t id = 0; id < c->layers.size(); id++) {
+        HostLayer& l = c->layers[id];
+        if (l.present && !l.enabled) {
+            l = HostLayer();
+            release_id(c, id);
+            touch(c, id);
         }
     }
-    c->layers_dirty = true;
+    c->props_dirty = true;
     return CGB_OK;
 }
 
@@ -494,42 +571,28 @@ cgb_status render(cgb_composition* c, const cgb_buffer* buf, const float bg[4], 
     }
     cgb_status s0 = remove_disabled(c);
     if (s0) return s0;
-    for (auto& kv : c->layers)
-        if (kv.second.enabled) c->orders_to_layers[kv.second.order] = kv.first;
-    // LayerProps by order (composition.rs:247-284)
-    uint32_t n_orders = 1;
-    for (auto& kv : c->layers)
-        if (kv.second.enabled) n_orders = std::max(n_orders, kv.second.order + 1);
-    std::vector<PaintProps> props(n_orders);
-    std::vector<uint8_t> unchanged(cache ? n_orders : 0, 0);
-    for (uint32_t o = 0; o < n_orders; o++) {
-        PaintProps& pp = props[o];
-        pp = PaintProps{CGB_FILL_NONZERO, CGB_BLEND_OVER, PROPS_SOLID | PROPS_DRAW | PROPS_OPAQUE_OVER, 0, {0, 0, 0, 1}};
-    }
-    for (auto& kv : c->orders_to_layers) {
-        if (kv.first >= n_orders) continue;
-        HostLayer* l = find_layer(c, kv.second);
-        if (!l || !l->enabled) continue;
-        const cgb_props& p = l->props.c;
-        if (p.func != CGB_FUNC_DRAW || p.is_clipped)
-            return fail(CGB_ERR_INVALID_ARG, "render: clip layers are not supported by the GPU painter");
-        if (p.fill_kind != CGB_FILL_SOLID)
-            return fail(CGB_ERR_INVALID_ARG, "render: gradient fills are not supported by the GPU painter");
-        PaintProps& pp = props[kv.first];
-        pp.fill_rule = p.fill_rule;
-        pp.blend_mode = p.blend_mode;
-        pp.flags = PROPS_SOLID | PROPS_DRAW | PROPS_PRESENT;
-        if (p.blend_mode == CGB_BLEND_OVER && p.color[3] == 1.0f) pp.flags |= PROPS_OPAQUE_OVER;
-        std::memcpy(pp.color, p.color, sizeof(pp.color));
-        if (cache) unchanged[kv.first] = (l->unchanged >> buf->layer_cache) & 1;
+    if (c->props_dirty) rebuild_props(c);
+    if (c->unsupported)
+        return fail(CGB_ERR_INVALID_ARG, "render: clip layers and gradient fills are not supported by the GPU painter");
+    const uint32_t n_orders = c->n_orders;
+    std::vector<uint8_t> unchanged;
+    if (cache) {
+        unchanged.assign(n_orders, 0);
+        for (uint32_t o = 0; o < n_orders; o++)
+            if (c->order_layer[o] != UINT32_MAX)
+                unchanged[o] = (c->layers[c->order_layer[o]].unchanged >> buf->layer_cache) & 1;
     }
     RenderGeom geom{fg.rows, fg.row_len, n_orders, 0};
     geom.key_bits = bits_for((uint64_t)fg.rows * n_orders * (fg.row_len + 1) - 1);
     if (geom.key_bits > 42) return fail(CGB_ERR_LAYER_LIMIT, "render: canvas x orders too large for the segment key");
     cgb_status s1 = upload_layers(c);
     if (s1) return s1;
-    CK(c->s.ensure(c->d_props, props.size() * sizeof(PaintProps)));
-    CK(cudaMemcpyAsync(c->d_props.p, props.data(), props.size() * sizeof(PaintProps), cudaMemcpyHostToDevice, st));
+    if (c->props_uploaded != c->props_version) {
+        CK(c->s.ensure(c->d_props, c->props_host.size() * sizeof(PaintProps)));
+        CK(cudaMemcpyAsync(c->d_props.p, c->props_host.data(), c->props_host.size() * sizeof(PaintProps),
+                           cudaMemcpyHostToDevice, st));
+        c->props_uploaded = c->props_version;
+    }
     if (cache) {
         CK(c->s.ensure(c->d_unchanged, unchanged.size()));
         CK(cudaMemcpyAsync(c->d_unchanged.p, unchanged.data(), unchanged.size(), cudaMemcpyHostToDevice, st));
@@ -597,8 +660,9 @@ cgb_status render(cgb_composition* c, const cgb_buffer* buf, const float bg[4], 
     if (G) CK(scan_u32(cb.item_count, cb.item_off, (uint32_t)G, &c->s, st, &W));
     c->stats.work_items = W;
     const int idx_bits = bits_for(std::max<uint64_t>(G, 1) - 1);
-    const int item_key_bits = bits_for(n_tiles * n_orders * 2 - 1);
-    if (idx_bits + item_key_bits > 64 || W >= (1ull << 30))
+    const int item_key_bits = bits_for(n_tiles * n_orders - 1);
+    const int item_shift = idx_bits + 3;  // TL index, then the full / opaque / carry-only bits
+    if (item_shift + item_key_bits > 64 || W >= (1ull << 30))
         return fail(CGB_ERR_LAYER_LIMIT, "render: too many tile x layer work items");
     CK(c->s.ensure(c->items_a, std::max<uint64_t>(W, 1) * 8));
     CK(c->s.ensure(c->items_b, std::max<uint64_t>(W, 1) * 8));
@@ -609,10 +673,10 @@ cgb_status render(cgb_composition* c, const cgb_buffer* buf, const float bg[4], 
     CK(launch_items_crop(1, sorted, (uint32_t)G, geom, pp, cb, idx_bits, st));
     uint64_t* items_sorted = cb.items;
     int ipasses = 0;
-    CK(radix_sort_u64(cb.items, cb.items_tmp, (uint32_t)W, idx_bits + 1, idx_bits + item_key_bits,
+    CK(radix_sort_u64(cb.items, cb.items_tmp, (uint32_t)W, item_shift, item_shift + item_key_bits,
                       (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &items_sorted, &ipasses));
     c->stats.item_sort_passes = ipasses;
-    CK(launch_tile_ranges(items_sorted, (uint32_t)W, (uint32_t)n_tiles, idx_bits + 1, n_orders, cb.tile_start, st));
+    CK(launch_tile_ranges(items_sorted, (uint32_t)W, (uint32_t)n_tiles, item_shift, n_orders, cb.tile_start, st));
     CK(cudaEventRecord(c->ev[4], st));
 
     // output
@@ -640,9 +704,10 @@ cgb_status render(cgb_composition* c, const cgb_buffer* buf, const float bg[4], 
     c->stats.paint_ms = elapsed(c->ev[4], c->ev[5]);
     c->stats.total_ms = elapsed(c->ev[0], c->ev[5]);
     if (cache)  // composition.rs:322-327
-        for (auto& kv : c->layers) {
-            if (kv.second.enabled) kv.second.unchanged |= 1u << buf->layer_cache;
-            else kv.second.unchanged &= ~(1u << buf->layer_cache);
+        for (HostLayer& l : c->layers) {
+            if (!l.present) continue;
+            if (l.enabled) l.unchanged |= 1u << buf->layer_cache;
+            else l.unchanged &= ~(1u << buf->layer_cache);
         }
     return CGB_OK;
 }
@@ -709,14 +774,18 @@ CGB_EXPORT cgb_status cgb_composition_free(cgb_composition* c) {
 
 CGB_EXPORT cgb_status cgb_create_layer(cgb_composition* c, uint32_t* out_layer_id) {
     if (!c || !out_layer_id) return fail(CGB_ERR_INVALID_ARG, "null argument");
-    uint32_t cand = 0;
-    for (uint32_t u : c->used_ids) {
-        if (u != cand) break;
-        cand++;
+    // IdSet::acquire (mold/src/layer.rs:61-72), lowest free id first
+    uint32_t id;
+    if (!c->released.empty()) {
+        id = *c->released.begin();
+    } else {
+        while (c->next_fresh < c->used.size() && c->used[c->next_fresh]) c->next_fresh++;
+        id = c->next_fresh;
+        if (id >= c->max_ids) return fail(CGB_ERR_LAYER_LIMIT, "create_layer: no free layer id");
+        c->next_fresh++;
     }
-    if (cand >= c->max_ids) return fail(CGB_ERR_LAYER_LIMIT, "create_layer: no free layer id");
-    c->used_ids.insert(cand);
-    *out_layer_id = cand;
+    mark_used(c, id);
+    *out_layer_id = id;
     return CGB_OK;
 }
 
@@ -766,8 +835,14 @@ CGB_EXPORT cgb_status cgb_layer_set_enabled(cgb_composition* c, uint32_t layer_i
     if (!c) return fail(CGB_ERR_INVALID_ARG, "null composition handle");
     HostLayer* l = find_layer(c, layer_id);
     if (!l) return fail(CGB_ERR_NOT_FOUND, "set_enabled: unknown layer");
-    if (l->enabled != (enabled != 0)) c->layers_dirty = true;
-    l->enabled = enabled != 0;
+    const bool e = enabled != 0;
+    if (l->enabled != e) {
+        if (e) c->enabled_len += l->len;
+        else c->enabled_len -= l->len;
+        l->enabled = e;
+        touch(c, layer_id);
+        c->props_dirty = true;
+    }
     return CGB_OK;
 }
 
@@ -789,7 +864,7 @@ static cgb_status set_transform(cgb_composition* c, uint32_t layer_id, const flo
         l->unchanged = 0;
         l->has_transform = has;
         if (has) std::memcpy(l->t, t, sizeof(l->t));
-        c->layers_dirty = true;
+        touch(c, layer_id);
     }
     return CGB_OK;
 }
@@ -819,7 +894,8 @@ CGB_EXPORT cgb_status cgb_layer_set_order(cgb_composition* c, uint32_t layer_id,
         l->unchanged = 0;
         l->has_order = true;
         l->order = order;
-        c->layers_dirty = true;
+        touch(c, layer_id);
+        c->props_dirty = true;
     }
     return CGB_OK;
 }
@@ -840,6 +916,7 @@ CGB_EXPORT cgb_status cgb_layer_set_props(cgb_composition* c, uint32_t layer_id,
     if (!(l->props == hp)) {
         l->unchanged = 0;
         l->props = hp;
+        c->props_dirty = true;
     }
     return CGB_OK;
 }
@@ -971,9 +1048,15 @@ CGB_EXPORT cgb_status cgb_composition_clear(cgb_composition* c) {
     if (!c) return fail(CGB_ERR_INVALID_ARG, "null composition handle");
     c->n_lines = 0;
     c->layers.clear();
-    c->used_ids.clear();
-    c->orders_to_layers.clear();
-    c->layers_dirty = true;
+    c->used.clear();
+    c->released.clear();
+    c->next_fresh = 0;
+    c->enabled_len = 0;
+    c->layer_recs.clear();
+    c->layers_grew = true;
+    c->dirty_lo = UINT32_MAX;
+    c->dirty_hi = 0;
+    c->props_dirty = true;
     for (auto& kv : c->caches) kv.second.tiles = 0;
     return CGB_OK;
 }

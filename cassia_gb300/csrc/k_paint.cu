@@ -117,6 +117,14 @@ __global__ void k_tl_carry(uint32_t G, const uint64_t* __restrict__ tl_cover, co
     } while (h < G && !tl_flags[h]);
 }
 
+// Work-item payload bits above the TL index: the item holds only a cover carry;
+// its layer is full in the tile; and it is also an opaque Solid Over layer.
+constexpr uint32_t ITEM_OWN = 0u;
+constexpr uint32_t ITEM_OPAQUE = 1u;
+constexpr uint32_t ITEM_FULL = 2u;
+constexpr uint32_t ITEM_CARRY = 4u;
+constexpr int ITEM_FLAG_BITS = 3;
+
 struct ItemGeom {
     RenderGeom geom;
     uint32_t h0, h1, v0, v1;  // crop in tiles
@@ -145,24 +153,29 @@ __device__ __forceinline__ uint32_t tl_items(uint32_t g, uint32_t G, const uint6
     if (next > h1) next = h1;
     uint32_t cnt = 0;
     if (i >= h0 && i < h1) {
-        emit(i, 0u);
+        emit(i, ITEM_OWN);  // a layer with segments is never "full" (layer_workbench.rs:164-175)
         cnt++;
     }
     if (next <= i + 1) return cnt;
     const uint64_t carry_out = cover_add(tl_carry[g], tl_cover[g]);
-    const bool nonempty = !cover_is_empty(carry_out, props[L].fill_rule);
+    const PaintProps pp = props[L];
+    const bool nonempty = !cover_is_empty(carry_out, pp.fill_rule);
+    // payload of a cover-carry-only item: its layer_is_full and the opaque
+    // Solid Over test of skip_fully_covered_layers (:335-356)
+    const bool full = cover_is_full(carry_out, pp.fill_rule);
+    const uint32_t flags = ITEM_CARRY | (full ? ITEM_FULL : 0u) | (full && (pp.flags & PROPS_OPAQUE_OVER) ? ITEM_OPAQUE : 0u);
     int32_t t = i + 1;
     if (i < h0) {
         // the first painted tile of the row holds every layer with segments
         // to its left, empty or not
         if (next <= h0) return cnt;
-        emit(h0, 1u);
+        emit(h0, flags);
         cnt++;
         t = h0 + 1;
     }
     if (nonempty)
         for (; t < next; t++) {
-            emit(t, 1u);
+            emit(t, flags);
             cnt++;
         }
     return cnt;
@@ -189,9 +202,9 @@ __global__ void k_items_write(const uint64_t* __restrict__ segs, uint32_t G, con
     const uint64_t L = run % ig.geom.n_orders;
     const uint64_t j = run / ig.geom.n_orders;
     uint32_t o = off[g];
-    tl_items(g, G, segs, tl_start, tl_flags, tl_cover, tl_carry, ig, props, [&](int32_t t, uint32_t carry_only) {
+    tl_items(g, G, segs, tl_start, tl_flags, tl_cover, tl_carry, ig, props, [&](int32_t t, uint32_t flags) {
         uint64_t tile = j * ig.geom.row_len + (uint64_t)t;
-        uint64_t k = ((tile * ig.geom.n_orders + L) << 1) | carry_only;
+        uint64_t k = ((tile * ig.geom.n_orders + L) << ITEM_FLAG_BITS) | flags;
         items[o++] = (k << idx_bits) | g;
     });
 }
@@ -295,11 +308,11 @@ __device__ __forceinline__ uint32_t solid_bytes(const float c[4]) {
 }
 
 __device__ __forceinline__ void item_decode(uint64_t item, int idx_bits, uint32_t n_orders, uint32_t& L,
-                                            uint32_t& carry_only, uint32_t& g) {
+                                            uint32_t& flags, uint32_t& g) {
     g = (uint32_t)(item & ((1ull << idx_bits) - 1));
     uint64_t k = item >> idx_bits;
-    carry_only = (uint32_t)(k & 1);
-    L = (uint32_t)((k >> 1) % n_orders);
+    flags = (uint32_t)(k & 7u);
+    L = (uint32_t)((k >> ITEM_FLAG_BITS) % n_orders);
 }
 
 struct PaintArgs {
@@ -313,11 +326,94 @@ struct PaintArgs {
     const uint64_t* tl_carry;
 };
 
-__global__ void __launch_bounds__(256) k_paint(PaintArgs a) {
+constexpr int PAINT_WARPS = 4;  // tiles per CTA
+constexpr int SEGCAP = 256;     // staged segments per warp and chunk of 32 items
+
+// Per-warp staging of 32 work items.
+struct WarpStage {
+    float4 color[32];
+    uint64_t carry[32];  // cover entering the tile (TL items) or carried through it
+    uint32_t meta[32];   // blend_mode | fill_rule << 4 | carry-only << 5
+    uint32_t sb[32];     // first segment (global index)
+    uint32_t cnt[32];    // segments of the item
+    uint32_t soff[32];   // staging offset of its segments
+    uint32_t seg[SEGCAP];
+    int32_t area[64];    // per-pixel area sums (x * 8 + y)
+    int32_t cov[64];     // per-pixel cover sums, added to the columns right of x
+};
+
+// Loads items [c0, c0 + n) into the stage; all loads of the chunk are in flight together.
+__device__ __forceinline__ void stage_items(const PaintArgs& a, WarpStage& S, uint32_t c0, uint32_t n, int lane,
+                                            bool with_segments) {
+    uint32_t meta = 0, sb = 0, cnt = 0;
+    uint64_t carry = 0;
+    float4 col = make_float4(0.f, 0.f, 0.f, 0.f);
+    if ((uint32_t)lane < n) {
+        uint32_t L, fl, g;
+        item_decode(a.items[c0 + lane], a.idx_bits, a.p.geom.n_orders, L, fl, g);
+        const float4* pp = reinterpret_cast<const float4*>(a.p.props + L);
+        const uint4 hdr = *reinterpret_cast<const uint4*>(pp);
+        col = pp[1];
+        carry = a.tl_carry[g];
+        const uint32_t co = (fl & ITEM_CARRY) ? 1u : 0u;
+        if (co) {
+            carry = cover_add(carry, a.tl_cover[g]);
+        } else if (with_segments) {
+            sb = a.tl_start[g];
+            cnt = a.tl_start[g + 1] - sb;
+        }
+        meta = (hdr.y & 15u) | ((hdr.x & 1u) << 4) | (co << 5);
+    }
+    // exclusive scan of the segment counts -> staging offsets
+    uint32_t inc = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += v;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+    S.color[lane] = col;
+    S.carry[lane] = carry;
+    S.meta[lane] = meta;
+    S.sb[lane] = sb;
+    S.cnt[lane] = cnt;
+    S.soff[lane] = inc - cnt;
+    __syncwarp();
+    if (!with_segments) return;
+    const uint32_t staged = min(total, (uint32_t)SEGCAP);
+    uint32_t src[SEGCAP / 32];
+#pragma unroll
+    for (int r = 0; r < SEGCAP / 32; r++) {
+        const uint32_t s = lane + 32 * r;
+        src[r] = 0xFFFFFFFFu;
+        if (s < staged) {
+            // the item q with soff[q] <= s < soff[q] + cnt[q]
+            uint32_t lo = 0, hi = n;
+            while (hi - lo > 1) {
+                uint32_t mid = (lo + hi) >> 1;
+                if (S.soff[mid] <= s) lo = mid;
+                else hi = mid;
+            }
+            while (lo + 1 < n && (S.cnt[lo] == 0 || s >= S.soff[lo] + S.cnt[lo])) lo++;  // skip empty items sharing the offset
+            src[r] = S.sb[lo] + (s - S.soff[lo]);
+        }
+    }
+    uint32_t v[SEGCAP / 32];
+#pragma unroll
+    for (int r = 0; r < SEGCAP / 32; r++) v[r] = src[r] != 0xFFFFFFFFu ? (uint32_t)a.segs[src[r]] : 0u;
+#pragma unroll
+    for (int r = 0; r < SEGCAP / 32; r++)
+        if (lane + 32 * r < staged) S.seg[lane + 32 * r] = v[r];
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
+    __shared__ WarpStage stages[PAINT_WARPS];
     const PaintParams& p = a.p;
     const int lane = threadIdx.x & 31;
+    WarpStage& S = stages[threadIdx.x >> 5];
     const uint32_t n_tiles = p.geom.rows * p.geom.row_len;
-    const uint32_t t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const uint32_t t = blockIdx.x * PAINT_WARPS + (threadIdx.x >> 5);
     if (t >= n_tiles) return;
     const uint32_t j = t / p.geom.row_len, i = t % p.geom.row_len;
     if (i < p.crop_h0 || i >= p.crop_h1 || j < p.crop_v0 || j >= p.crop_v1) return;
@@ -333,30 +429,29 @@ __global__ void __launch_bounds__(256) k_paint(PaintArgs a) {
         if (old >= 0 && old == layers) {
             bool all = true;
             for (uint32_t k = b + lane; k < e; k += 32) {
-                uint32_t L, co, g;
-                item_decode(a.items[k], a.idx_bits, n_orders, L, co, g);
+                uint32_t L, fl, g;
+                item_decode(a.items[k], a.idx_bits, n_orders, L, fl, g);
                 all &= p.unchanged[L] != 0;
             }
             if (__all_sync(0xffffffffu, all)) return;  // TileWriteOp::None
         }
     }
 
-    // skip_fully_covered_layers (layer_workbench.rs:310-388), top-down.
+    // skip_fully_covered_layers (layer_workbench.rs:310-388), top-down over
+    // the items' precomputed full / opaque bits.
     int64_t k_op = -1;
     int first = 0;  // 0 none, 1 opaque, 2 incomplete
     for (int64_t c0 = (int64_t)e - 1; c0 >= (int64_t)b; c0 -= 32) {
         const int64_t idx = c0 - lane;
         bool inc = false, op = false;
         if (idx >= (int64_t)b) {
-            uint32_t L, co, g;
-            item_decode(a.items[idx], a.idx_bits, n_orders, L, co, g);
-            const PaintProps pp = a.p.props[L];
-            bool full = co && cover_is_full(cover_add(a.tl_carry[g], a.tl_cover[g]), pp.fill_rule);
-            inc = !full;
-            op = full && (pp.flags & PROPS_OPAQUE_OVER);
+            const uint32_t fl = (uint32_t)(a.items[idx] >> a.idx_bits) & 7u;
+            inc = !(fl & ITEM_FULL);
+            op = (fl & ITEM_OPAQUE) != 0;
         }
         const uint32_t bi = __ballot_sync(0xffffffffu, inc), bo = __ballot_sync(0xffffffffu, op);
-        if (first == 0 && (bi | bo)) first = ((bo & -(int32_t)(bi | bo)) != 0) ? 1 : 2;  // lowest lane = topmost item
+        const uint32_t any = bi | bo;
+        if (first == 0 && any) first = (bo & (any & (0u - any))) ? 1 : 2;  // lowest lane = topmost item
         if (bo) {
             k_op = c0 - (__ffs(bo) - 1);
             break;
@@ -365,46 +460,40 @@ __global__ void __launch_bounds__(256) k_paint(PaintArgs a) {
 
     const uint32_t y = lane & 7, xg = lane >> 3;
     const uint32_t x0 = 2 * xg;
-    uint32_t px0, px1;
+    uint32_t px0 = 0, px1 = 0;
     bool painted = true;
     if (first != 2) {
-        // Solid: fold the scalar blend over the (full) layers above the opaque one.
+        // Solid: fold BlendMode::blend (scalar, style.rs:269-285) over the
+        // full layers above the opaque one (or above the clear color).
         float dst[4];
         uint32_t from;
         if (first == 1) {
-            uint32_t L, co, g;
-            item_decode(a.items[k_op], a.idx_bits, n_orders, L, co, g);
-            const PaintProps pp = a.p.props[L];
-            for (int q = 0; q < 4; q++) dst[q] = pp.color[q];
+            uint32_t L, fl, g;
+            item_decode(a.items[k_op], a.idx_bits, n_orders, L, fl, g);
+            const float4 c = reinterpret_cast<const float4*>(p.props + L)[1];
+            dst[0] = c.x, dst[1] = c.y, dst[2] = c.z, dst[3] = c.w;
             from = (uint32_t)k_op + 1;
         } else {
             for (int q = 0; q < 4; q++) dst[q] = p.clear[q];
             from = b;
         }
-        bool ok = true;
-        for (uint32_t k = from; k < e; k++) {
-            uint32_t L, co, g;
-            item_decode(a.items[k], a.idx_bits, n_orders, L, co, g);
-            const PaintProps pp = a.p.props[L];
-            if (!(pp.flags & PROPS_SOLID)) {
-                ok = false;
-                break;
+        for (uint32_t c0 = from; c0 < e; c0 += 32) {
+            const uint32_t n = min(32u, e - c0);
+            stage_items(a, S, c0, n, lane, false);
+            for (uint32_t q = 0; q < n; q++) {
+                const float4 col = S.color[q];
+                const uint32_t mode = S.meta[q] & 15u;
+                const float al = col.w, inv = 1.0f - al;
+                const float o0 = __fmaf_rn(dst[0], inv, blend_fn(mode, dst[0], col.x) * al);
+                const float o1 = __fmaf_rn(dst[1], inv, blend_fn(mode, dst[1], col.y) * al);
+                const float o2 = __fmaf_rn(dst[2], inv, blend_fn(mode, dst[2], col.z) * al);
+                const float o3 = __fmaf_rn(dst[3], inv, al);
+                dst[0] = o0, dst[1] = o1, dst[2] = o2, dst[3] = o3;
             }
-            // BlendMode::blend (style.rs:269-285)
-            const float al = pp.color[3], inv = 1.0f - al;
-            float o0 = __fmaf_rn(dst[0], inv, blend_fn(pp.blend_mode, dst[0], pp.color[0]) * al);
-            float o1 = __fmaf_rn(dst[1], inv, blend_fn(pp.blend_mode, dst[1], pp.color[1]) * al);
-            float o2 = __fmaf_rn(dst[2], inv, blend_fn(pp.blend_mode, dst[2], pp.color[2]) * al);
-            float o3 = __fmaf_rn(dst[3], inv, al);
-            dst[0] = o0;
-            dst[1] = o1;
-            dst[2] = o2;
-            dst[3] = o3;
+            __syncwarp();
         }
-        if (ok) {
-            px0 = px1 = solid_bytes(dst);
-            painted = false;
-        }
+        px0 = px1 = solid_bytes(dst);
+        painted = false;
     }
     if (painted) {
         // ColorBuffer: paint the unculled layers bottom-up (drive_tile_painting, :449-481).
@@ -414,62 +503,69 @@ __global__ void __launch_bounds__(256) k_paint(PaintArgs a) {
 #pragma unroll
             for (int q = 0; q < 4; q++) c[h][q] = p.clear[q];
         const uint32_t start = k_op >= 0 ? (uint32_t)k_op : b;
-        for (uint32_t k = start; k < e; k++) {
-            uint32_t L, co, g;
-            item_decode(a.items[k], a.idx_bits, n_orders, L, co, g);
-            const PaintProps pp = a.p.props[L];
-            float cov[2];
-            if (co) {
-                const uint64_t carry = cover_add(a.tl_carry[g], a.tl_cover[g]);
-                cov[0] = cov[1] = from_area(PIXEL_WIDTH * cover_lane(carry, y), pp.fill_rule);
-            } else {
-                const int32_t cy = cover_lane(a.tl_carry[g], y);
-                int32_t ar0 = 0, ar1 = 0, cv0 = 0, cv1 = 0;
-                const uint32_t sb = a.tl_start[g], se = a.tl_start[g + 1];
-                for (uint32_t base = sb; base < se; base += 32) {
-                    const uint32_t mine = base + lane < se ? (uint32_t)a.segs[base + lane] : 0u;
-                    const uint32_t m = min(32u, se - base);
-                    for (uint32_t q = 0; q < m; q++) {
-                        const uint32_t low = __shfl_sync(0xffffffffu, mine, q);
-                        if (low_tile_y(low) == y) {
-                            const uint32_t tx = low_tile_x(low);
-                            const int32_t ar = low_area(low), cv = low_cover(low);
-                            if (tx == x0) ar0 += ar;
-                            if (tx == x0 + 1) ar1 += ar;
-                            if (tx < x0) cv0 += cv;
-                            if (tx < x0 + 1) cv1 += cv;
-                        }
+        for (uint32_t c0 = start; c0 < e; c0 += 32) {
+            const uint32_t n = min(32u, e - c0);
+            stage_items(a, S, c0, n, lane, true);
+            for (uint32_t q = 0; q < n; q++) {
+                const uint32_t meta = S.meta[q];
+                const uint32_t mode = meta & 15u, fr = (meta >> 4) & 1u;
+                const uint64_t carry = S.carry[q];
+                const int32_t cy = cover_lane(carry, y);
+                float cov[2];
+                if (meta & 32u) {
+                    cov[0] = cov[1] = from_area(PIXEL_WIDTH * cy, fr);
+                } else {
+                    // acc_segment / acc_cover / compute_areas (painter/mod.rs:229-243, 347-362)
+                    S.area[lane] = 0;
+                    S.area[lane + 32] = 0;
+                    S.cov[lane] = 0;
+                    S.cov[lane + 32] = 0;
+                    __syncwarp();
+                    const uint32_t cnt = S.cnt[q], so = S.soff[q], sb = S.sb[q];
+                    for (uint32_t s = lane; s < cnt; s += 32) {
+                        const uint32_t low = so + s < SEGCAP ? S.seg[so + s] : (uint32_t)a.segs[sb + s];
+                        const uint32_t cell = low_tile_x(low) * 8 + low_tile_y(low);
+                        atomicAdd(&S.area[cell], low_area(low));
+                        atomicAdd(&S.cov[cell], low_cover(low));
                     }
+                    __syncwarp();
+                    int32_t cv = cy;
+                    for (uint32_t x = 0; x < x0; x++) cv += S.cov[x * 8 + y];
+                    const int32_t cv1 = cv + S.cov[x0 * 8 + y];
+                    cov[0] = from_area(PIXEL_WIDTH * (int32_t)(int8_t)cv + (int32_t)(int16_t)S.area[x0 * 8 + y], fr);
+                    cov[1] = from_area(PIXEL_WIDTH * (int32_t)(int8_t)cv1 + (int32_t)(int16_t)S.area[x0 * 8 + 8 + y],
+                                       fr);
+                    __syncwarp();
                 }
-                // compute_areas (painter/mod.rs:347-362): 16 * i8 cover + i16 area
-                cov[0] = from_area(PIXEL_WIDTH * (int32_t)(int8_t)(cy + cv0) + (int32_t)(int16_t)ar0, pp.fill_rule);
-                cov[1] = from_area(PIXEL_WIDTH * (int32_t)(int8_t)(cy + cv1) + (int32_t)(int16_t)ar1, pp.fill_rule);
-            }
-            // A column is blended when any of its 8 coverages is non-zero
-            // (painter/mod.rs:287-289).
-            const uint32_t b0 = __ballot_sync(0xffffffffu, cov[0] != 0.0f);
-            const uint32_t b1 = __ballot_sync(0xffffffffu, cov[1] != 0.0f);
-            const bool col[2] = {((b0 >> (8 * xg)) & 0xFFu) != 0, ((b1 >> (8 * xg)) & 0xFFu) != 0};
+                // A column is blended when any of its 8 coverages is non-zero
+                // (painter/mod.rs:287-289).
+                const uint32_t b0 = __ballot_sync(0xffffffffu, cov[0] != 0.0f);
+                const uint32_t b1 = __ballot_sync(0xffffffffu, cov[1] != 0.0f);
+                const bool col[2] = {((b0 >> (8 * xg)) & 0xFFu) != 0, ((b1 >> (8 * xg)) & 0xFFu) != 0};
+                if (!(col[0] | col[1])) continue;
+                const float4 src = S.color[q];
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                if (!col[h]) continue;
-                // blend_at (painter/mod.rs:364-400)
-                const float al = pp.color[3] * cov[h];
-                const float inv = 1.0f - al;
-                const float f0 = blend_vec(pp.blend_mode, c[h][0], pp.color[0]) * al;
-                const float f1 = blend_vec(pp.blend_mode, c[h][1], pp.color[1]) * al;
-                const float f2 = blend_vec(pp.blend_mode, c[h][2], pp.color[2]) * al;
-                c[h][0] = __fmaf_rn(c[h][0], inv, f0);
-                c[h][1] = __fmaf_rn(c[h][1], inv, f1);
-                c[h][2] = __fmaf_rn(c[h][2], inv, f2);
-                c[h][3] = __fmaf_rn(c[h][3], inv, al);
+                for (int h = 0; h < 2; h++) {
+                    if (!col[h]) continue;
+                    // blend_at (painter/mod.rs:364-400)
+                    const float al = src.w * cov[h];
+                    const float inv = 1.0f - al;
+                    const float f0 = blend_vec(mode, c[h][0], src.x) * al;
+                    const float f1 = blend_vec(mode, c[h][1], src.y) * al;
+                    const float f2 = blend_vec(mode, c[h][2], src.z) * al;
+                    c[h][0] = __fmaf_rn(c[h][0], inv, f0);
+                    c[h][1] = __fmaf_rn(c[h][1], inv, f1);
+                    c[h][2] = __fmaf_rn(c[h][2], inv, f2);
+                    c[h][3] = __fmaf_rn(c[h][3], inv, al);
+                }
             }
+            __syncwarp();
         }
         px0 = pixel_bytes(c[0][0], c[0][1], c[0][2], c[0][3]);
         px1 = pixel_bytes(c[1][0], c[1][1], c[1][2], c[1][3]);
     }
 
-    // RGBA8 store: a full tile goes out as 16 x 16-byte rows halves.
+    // RGBA8 store: a full tile goes out as 16 x 16-byte half rows.
     const uint32_t gx = i * 8 + x0, gy = j * 8 + y;
     const bool full_tile = (i * 8 + 8 <= p.width) && (j * 8 + 8 <= p.height) && ((p.stride & 3) == 0) &&
                            ((((uintptr_t)p.out) & 15) == 0);
@@ -556,10 +652,10 @@ cudaError_t launch_paint(const PaintParams& p, const uint64_t* segs, const uint6
                          cudaStream_t st) {
     uint32_t n_tiles = p.geom.rows * p.geom.row_len;
     if (n_tiles == 0) return cudaSuccess;
-    warps_per_block = warps_per_block ? warps_per_block : 4;
+    (void)warps_per_block;
     PaintArgs a{p, segs, items, idx_bits, tile_start, cb.tl_start, cb.tl_cover, cb.tl_carry};
     count_launches(1);
-    k_paint<<<(n_tiles + warps_per_block - 1) / warps_per_block, 32 * warps_per_block, 0, st>>>(a);
+    k_paint<<<(n_tiles + PAINT_WARPS - 1) / PAINT_WARPS, 32 * PAINT_WARPS, 0, st>>>(a);
     return cudaGetLastError();
 }
 

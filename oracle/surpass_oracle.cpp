@@ -1450,16 +1450,24 @@ struct Composition {
             if (kv.second.inner.is_enabled) s += kv.second.len;
         return s;
     }
+    // IdSet::acquire (mold/src/layer.rs:61-72), lowest free id first.
+    uint32_t next_fresh = 0;
+    std::set<uint32_t> released;  // freed ids below next_fresh
     bool acquire(uint32_t& id) {
-        uint32_t cand = 0;
-        for (uint32_t u : used_ids) {
-            if (u != cand) break;
-            cand++;
+        if (!released.empty()) {
+            id = *released.begin();
+            released.erase(released.begin());
+        } else {
+            while (used_ids.count(next_fresh)) next_fresh++;
+            if (next_fresh >= max_ids) return false;
+            id = next_fresh++;
         }
-        if (cand >= max_ids) return false;
-        used_ids.insert(cand);
-        id = cand;
+        used_ids.insert(id);
         return true;
+    }
+    void release(uint32_t id) {  // IdSet::release (mold/src/layer.rs:74-98)
+        used_ids.erase(id);
+        if (id < next_fresh) released.insert(id);
     }
     MLayer& insert_bookkeeping(uint32_t id, size_t n) {  // insert_segments (composition.rs:58-79)
         MLayer& l = layers[id];
@@ -1468,6 +1476,7 @@ struct Composition {
         l.inner.is_enabled = true;
         l.len += n;
         used_ids.insert(id);
+        released.erase(id);
         return l;
     }
     void push(uint32_t id, const Seg4& s) {
@@ -1498,7 +1507,7 @@ struct Composition {
             lids.resize(w);
             for (auto it = layers.begin(); it != layers.end();) {
                 if (!it->second.inner.is_enabled) {
-                    used_ids.erase(it->first);
+                    release(it->first);
                     it = layers.erase(it);
                 } else {
                     ++it;
