@@ -340,7 +340,8 @@ def main():
             "vs_baseline": None, "dtype": "f32+int (fixed point)", "data": "synthetic (seeded)",
             "config": {"workload": args.workload, "canvas": [W, H], "layers": scene.n_layers,
                        "lines": st["lines"], "segments_per_frame": segs,
-                       "painted_segments": st["painted_segments"], "work_items": st["work_items"],
+                       "painted_segments": st["painted_segments"], "tile_layers": st["tile_layers"],
+                       "work_items": st["work_items"],
                        "segment_format": "wide (17-bit layer)" if scene.wide else "reference u16",
                        "l2": "inputs larger than L2 (lines %d MB, segments %d MB)" % (
                            st["lines"] * 20 // 2**20, segs * 8 // 2**20),

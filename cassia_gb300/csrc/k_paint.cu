@@ -251,6 +251,49 @@ __device__ __forceinline__ float blend_vec(uint32_t mode, float d, float s) {
     }
 }
 
+template <int MODE>
+__device__ __forceinline__ float blend_vec_t(float d, float s) {
+    return blend_vec(MODE, d, s);  // MODE is a compile-time constant: the switch folds away
+}
+
+// blend_at for one lane's two pixels of a column pair (painter/mod.rs:364-400),
+// specialised per blend mode so that the mode is dispatched once per layer.
+template <int MODE>
+__device__ __forceinline__ void blend_pixels(float (&c)[2][4], const float4& src, const float (&cov)[2],
+                                             const bool (&col)[2]) {
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        if (!col[h]) continue;
+        const float al = src.w * cov[h];
+        const float inv = 1.0f - al;
+        const float f0 = blend_vec_t<MODE>(c[h][0], src.x) * al;
+        const float f1 = blend_vec_t<MODE>(c[h][1], src.y) * al;
+        const float f2 = blend_vec_t<MODE>(c[h][2], src.z) * al;
+        c[h][0] = __fmaf_rn(c[h][0], inv, f0);
+        c[h][1] = __fmaf_rn(c[h][1], inv, f1);
+        c[h][2] = __fmaf_rn(c[h][2], inv, f2);
+        c[h][3] = __fmaf_rn(c[h][3], inv, al);
+    }
+}
+
+__device__ __forceinline__ void blend_dispatch(uint32_t mode, float (&c)[2][4], const float4& src,
+                                               const float (&cov)[2], const bool (&col)[2]) {
+    switch (mode) {
+        case CGB_BLEND_OVER: blend_pixels<CGB_BLEND_OVER>(c, src, cov, col); break;
+        case CGB_BLEND_MULTIPLY: blend_pixels<CGB_BLEND_MULTIPLY>(c, src, cov, col); break;
+        case CGB_BLEND_SCREEN: blend_pixels<CGB_BLEND_SCREEN>(c, src, cov, col); break;
+        case CGB_BLEND_OVERLAY: blend_pixels<CGB_BLEND_OVERLAY>(c, src, cov, col); break;
+        case CGB_BLEND_DARKEN: blend_pixels<CGB_BLEND_DARKEN>(c, src, cov, col); break;
+        case CGB_BLEND_LIGHTEN: blend_pixels<CGB_BLEND_LIGHTEN>(c, src, cov, col); break;
+        case CGB_BLEND_COLOR_DODGE: blend_pixels<CGB_BLEND_COLOR_DODGE>(c, src, cov, col); break;
+        case CGB_BLEND_COLOR_BURN: blend_pixels<CGB_BLEND_COLOR_BURN>(c, src, cov, col); break;
+        case CGB_BLEND_HARD_LIGHT: blend_pixels<CGB_BLEND_HARD_LIGHT>(c, src, cov, col); break;
+        case CGB_BLEND_SOFT_LIGHT: blend_pixels<CGB_BLEND_SOFT_LIGHT>(c, src, cov, col); break;
+        case CGB_BLEND_DIFFERENCE: blend_pixels<CGB_BLEND_DIFFERENCE>(c, src, cov, col); break;
+        default: blend_pixels<CGB_BLEND_EXCLUSION>(c, src, cov, col); break;
+    }
+}
+
 // BlendMode::blend_fn (style.rs:206-267)
 __device__ float blend_fn(uint32_t mode, float dst, float src) {
     switch (mode) {
@@ -543,21 +586,7 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
                 const uint32_t b1 = __ballot_sync(0xffffffffu, cov[1] != 0.0f);
                 const bool col[2] = {((b0 >> (8 * xg)) & 0xFFu) != 0, ((b1 >> (8 * xg)) & 0xFFu) != 0};
                 if (!(col[0] | col[1])) continue;
-                const float4 src = S.color[q];
-#pragma unroll
-                for (int h = 0; h < 2; h++) {
-                    if (!col[h]) continue;
-                    // blend_at (painter/mod.rs:364-400)
-                    const float al = src.w * cov[h];
-                    const float inv = 1.0f - al;
-                    const float f0 = blend_vec(mode, c[h][0], src.x) * al;
-                    const float f1 = blend_vec(mode, c[h][1], src.y) * al;
-                    const float f2 = blend_vec(mode, c[h][2], src.z) * al;
-                    c[h][0] = __fmaf_rn(c[h][0], inv, f0);
-                    c[h][1] = __fmaf_rn(c[h][1], inv, f1);
-                    c[h][2] = __fmaf_rn(c[h][2], inv, f2);
-                    c[h][3] = __fmaf_rn(c[h][3], inv, al);
-                }
+                blend_dispatch(mode, c, S.color[q], cov, col);
             }
             __syncwarp();
         }

@@ -247,7 +247,10 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(const uint64_t* __res
         s_count[d] = sum;
     }
     __syncthreads();
-    // Decoupled look-back for the tile's global digit offsets.
+    // Decoupled look-back for the tile's global digit offsets: one thread per
+    // digit publishes the tile's count (aggregate status), then walks back
+    // over its predecessors four entries per load round, summing until an
+    // inclusive prefix, and publishes its own inclusive prefix at once.
     if (tid < RADIX) {
         const int d = tid;
         const uint32_t cnt = s_count[d];
@@ -260,20 +263,31 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(const uint64_t* __res
             int64_t t = (int64_t)tile - 1;
             uint32_t spins = 0;
             while (t >= 0) {
-                uint32_t v = ld_relaxed(lookback + (uint64_t)t * RADIX + d);
-                uint32_t stt = v & ~ST_VAL;
-                if (stt == 0) {
-                    if (++spins > SPIN_LIMIT) {
+                uint32_t v[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    v[k] = t - k >= 0 ? ld_relaxed(lookback + (uint64_t)(t - k) * RADIX + d) : (ST_INC | 0u);
+                int used = 0;
+                bool inc = false;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    if (inc || used < k) break;  // stop at the first inclusive or unpublished entry
+                    const uint32_t stt = v[k] & ~ST_VAL;
+                    if (stt == 0) break;
+                    excl += v[k] & ST_VAL;
+                    used++;
+                    if (stt == ST_INC) inc = true;
+                }
+                if (inc) break;
+                if (used == 0) {
+                    if (++spins > SPIN_LIMIT) {  // a predecessor never published
                         atomicExch(err, 1u);
                         s_abort = 1;
                         break;
                     }
-                    __nanosleep(64);
-                    continue;
+                    __nanosleep(32);
                 }
-                excl += v & ST_VAL;
-                if (stt == ST_INC) break;
-                t--;
+                t -= used;
             }
             st_relaxed(mine, ST_INC | ((excl + cnt) & ST_VAL));
         }
