@@ -155,6 +155,7 @@ def _declare(lib):
         "cgb_create_buffer_layer_cache": ([handle, P(i32)], i32),
         "cgb_release_buffer_layer_cache": ([handle, i32], i32),
         "cgb_render": ([handle, P(CgbBuffer), fp, P(CgbRect)], i32),
+        "cgb_render_batch": ([handle, sz, P(vp), P(CgbBuffer), fp, P(CgbRect)], i32),
         "cgb_pixel_segments": ([handle, P(u64), sz, P(u64), P(u64), u32], i32),
         "cgb_get_stats": ([handle, P(CgbStats)], i32),
         "cgb_set_tuning": ([handle, P(CgbTuning)], i32),

@@ -32,6 +32,43 @@ def _fp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
 
 
+def _buffer(pixels, width, layer_cache=-1, width_stride=None, height=None):
+    stride = width_stride or width
+    b = abi.CgbBuffer()
+    if isinstance(pixels, np.ndarray):
+        assert pixels.dtype == np.uint8 and pixels.flags.c_contiguous
+        b.pixels = pixels.ctypes.data
+        b.height = pixels.size // (4 * stride)
+        b.memory = abi.MEMORY_HOST
+    else:
+        b.pixels = int(pixels)
+        b.height = int(height)
+        b.memory = abi.MEMORY_DEVICE
+    b.width = width
+    b.width_stride = stride
+    b.layer_cache = -1 if layer_cache is None else layer_cache
+    return b
+
+
+def render_batch(ctx, scenes, pixels, widths, backgrounds, crops=None, heights=None, layer_caches=None):
+    """Renders several Compositions in one pipeline (cgb_render_batch) on
+    `ctx`'s stream.  pixels[k] is a host numpy RGBA8 array or a device
+    pointer (then heights[k] is required)."""
+    lib = abi.load_library()
+    n = len(scenes)
+    bufs = (abi.CgbBuffer * max(n, 1))()
+    for k in range(n):
+        bufs[k] = _buffer(pixels[k], widths[k], layer_cache=-1 if layer_caches is None else layer_caches[k],
+                          height=None if heights is None else heights[k])
+    handles = (ctypes.c_void_p * max(n, 1))(*[s._h.value for s in scenes])
+    bg = (ctypes.c_float * (4 * max(n, 1)))(*[float(v) for b in backgrounds for v in b])
+    cr = None
+    if crops is not None:
+        cr = (abi.CgbRect * max(n, 1))(*[abi.CgbRect(*c) for c in crops])
+    _check(lib, lib.cgb_render_batch(ctx._h, n, handles, bufs, bg, cr), "render_batch")
+    return pixels
+
+
 def kernel_launches() -> int:
     """Kernels launched by the native library in this process."""
     return int(abi.load_library().cgb_kernel_launches())
@@ -152,20 +189,7 @@ class Composition:
     def render(self, pixels, width, background, crop=None, layer_cache=-1, width_stride=None, height=None):
         """Composition::render.  `pixels` is a host uint8 numpy array of shape
         (height, width_stride, 4), or a device pointer (int) with `height` given."""
-        stride = width_stride or width
-        b = abi.CgbBuffer()
-        if isinstance(pixels, np.ndarray):
-            assert pixels.dtype == np.uint8 and pixels.flags.c_contiguous
-            b.pixels = pixels.ctypes.data
-            b.height = pixels.size // (4 * stride)
-            b.memory = abi.MEMORY_HOST
-        else:
-            b.pixels = int(pixels)
-            b.height = int(height)
-            b.memory = abi.MEMORY_DEVICE
-        b.width = width
-        b.width_stride = stride
-        b.layer_cache = -1 if layer_cache is None else layer_cache
+        b = _buffer(pixels, width, layer_cache, width_stride, height)
         bg = (ctypes.c_float * 4)(*background)
         cr = None
         if crop is not None:

@@ -59,17 +59,44 @@ constexpr uint32_t PROPS_OPAQUE_OVER = 2u;  // Fill::Solid, BlendMode::Over, alp
 constexpr uint32_t PROPS_DRAW = 4u;         // Func::Draw
 constexpr uint32_t PROPS_PRESENT = 8u;      // an enabled layer holds this order
 
-// Segment formats.
-struct SegFormat {
-    uint32_t wide;  // 0: reference CompactSegment; 1: D5 widened layer field
+// One canvas of a frame: a composition's lines, layer table and props, its
+// output buffer, and where its tile rows / tiles sit in the frame's global
+// row and tile numbering.  A frame renders one or many scenes in one pipeline.
+struct SceneDesc {
+    const float* p0x;
+    const float* p0y;
+    const float* p1x;
+    const float* p1y;
+    const uint32_t* lids;
+    const LayerRec* layers;
+    const PaintProps* props;    // by order
+    const uint8_t* unchanged;   // by order, or null (no layer cache)
+    int32_t* prev_layers;       // by tile, or null
+    uint8_t* out;               // device RGBA8
+    const float* default_t;     // LinesBuilder default transform, or null
+    uint64_t line_base;         // first global line index
+    uint32_t n_lines, n_layer_recs, n_orders, wide;
+    uint32_t width, height, stride, rows, row_len;
+    uint32_t row_base, tile_base;
+    uint32_t crop_h0, crop_h1, crop_v0, crop_v1;  // in tiles
+    float clear[4];
 };
 
-// Render-mode key geometry: key = ((j * n_orders + order) * (row_len + 1) + (i + 1)).
-struct RenderGeom {
-    uint32_t rows, row_len;  // tile rows / tiles per row of the canvas
-    uint32_t n_orders;       // max order + 1
-    uint32_t key_bits;       // bits of the largest key
+// Frame-wide geometry of the render-mode segment key
+//   key = ((global row * n_orders + order) * (row_len + 1) + (tile column + 1)),
+// with n_orders and row_len the maxima over the frame's scenes.
+struct BatchGeom {
+    const SceneDesc* scenes;     // device array
+    const uint32_t* row_scene;   // device: scene of each global tile row
+    uint32_t n_scenes;
+    uint32_t total_rows, total_tiles;
+    uint32_t n_orders, row_len;
+    uint32_t key_bits;
+    uint64_t total_lines;
 };
+
+// LineRec.order_octant packing: scene << 20 | order << 3 | octant
+constexpr int LINE_SCENE_SHIFT = 20;
 
 // ---------------------------------------------------------------------------
 // Rust-semantics numerics
@@ -188,15 +215,13 @@ cudaError_t launch_flatten(int write, const uint32_t* kinds, const float* points
                            const uint64_t* pt_off, const float* transforms9, const uint8_t* has_t,
                            const uint32_t* path_layer, uint32_t n_paths, uint32_t* counts, const uint32_t* out_off,
                            float* p0x, float* p0y, float* p1x, float* p1y, uint32_t* lids, cudaStream_t st);
-cudaError_t launch_build_lines(const float* p0x, const float* p0y, const float* p1x, const float* p1y,
-                               const uint32_t* lids, uint32_t n, const LayerRec* layers, uint32_t n_layer_recs,
-                               const float* default_t, LineRec* recs, uint32_t* lengths, cudaStream_t st);
-// mode: 0 = count, 1 = write.  render != 0 selects the culled, re-keyed
-// render format; else the reference format (SegFormat).
-cudaError_t launch_rasterize(int mode, const LineRec* recs, const uint32_t* step_off, uint32_t n_lines,
-                             uint64_t n_steps, uint32_t steps_per_block, uint32_t block, SegFormat fmt, int render,
-                             RenderGeom geom, uint32_t* block_counts, uint32_t* block_totals,
-                             const uint32_t* block_off, uint64_t* out, cudaStream_t st);
+cudaError_t launch_build_lines(const BatchGeom& bg, LineRec* recs, uint32_t* lengths, cudaStream_t st);
+// mode: 0 = count, 1 = write.  render != 0: culled, re-keyed render format;
+// else the reference segment format of the (single) scene.
+cudaError_t launch_rasterize(int mode, int render, const BatchGeom& bg, const LineRec* recs, const uint32_t* step_off,
+                             uint32_t n_lines, uint64_t n_steps, uint32_t block, uint32_t* block_counts,
+                             uint32_t* block_totals, const uint32_t* block_off, uint64_t* out, cudaStream_t st);
+uint32_t raster_grid(uint64_t n_steps, uint32_t block);
 cudaError_t launch_compact_lines(const float* in4[4], const uint32_t* lid_in, uint32_t n, const LayerRec* layers,
                                  uint32_t n_layer_recs, float* out4[4], uint32_t* lid_out, uint32_t* flags,
                                  uint32_t* offsets, Scratch* s, cudaStream_t st, uint32_t* n_out_host);
@@ -210,25 +235,13 @@ cudaError_t scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, Scratch* s, 
 // on return *result points at the sorted array (keys or tmp).
 cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo, int bit_hi, int digit_bits,
                            Scratch* s, uint32_t* err_flag, cudaStream_t st, uint64_t** result, int* passes);
-size_t radix_sort_scratch_bytes(uint32_t n, int bit_lo, int bit_hi, int digit_bits);
-size_t scan_scratch_bytes(uint32_t n);
 
 // k_paint.cu
-struct PaintParams {
-    RenderGeom geom;
-    uint32_t width, height, stride;  // pixels
-    float clear[4];
-    uint8_t* out;  // device RGBA8
-    const PaintProps* props;
-    const uint8_t* unchanged;  // per order, or null (no layer cache)
-    int32_t* prev_layers;      // per tile, or null
-    uint32_t crop_h0, crop_h1, crop_v0, crop_v1;  // in tiles
-};
 struct CarryBuffers {
     uint32_t* tl_start;   // [G + 1]
     uint64_t* tl_cover;   // [G]
     uint64_t* tl_carry;   // [G]
-    uint32_t* tl_flags;   // per-segment / per-TL scratch
+    uint32_t* tl_flags;   // [G]
     uint32_t* item_count; // [G]
     uint32_t* item_off;   // [G + 1]
     uint64_t* items;      // [W]
@@ -237,18 +250,15 @@ struct CarryBuffers {
 };
 cudaError_t launch_tl_heads(int mode, const uint64_t* segs, uint32_t n, uint32_t* block_counts, const uint32_t* block_off,
                             uint32_t* tl_start, cudaStream_t st);
-cudaError_t launch_tl_reduce_scan(const uint64_t* segs, uint32_t n_segs, uint32_t G, const RenderGeom& geom,
-                                  CarryBuffers& cb, Scratch* s, cudaStream_t st);
-cudaError_t launch_items(int mode, const uint64_t* segs, uint32_t G, const RenderGeom& geom, const PaintProps* props,
-                         CarryBuffers& cb, int idx_bits, cudaStream_t st);
+uint32_t tl_heads_grid(uint32_t n);
+cudaError_t launch_tl_reduce_scan(const uint64_t* segs, uint32_t G, const BatchGeom& bg, CarryBuffers& cb,
+                                  cudaStream_t st);
+cudaError_t launch_items(int mode, const uint64_t* segs, uint32_t G, const BatchGeom& bg, CarryBuffers& cb,
+                         int idx_bits, cudaStream_t st);
 cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_tiles, int shift, uint32_t n_orders,
                                uint32_t* tile_start, cudaStream_t st);
-cudaError_t launch_paint(const PaintParams& p, const uint64_t* segs, const uint64_t* items, int idx_bits,
-                         const uint32_t* tile_start, const CarryBuffers& cb, uint32_t warps_per_block,
-                         cudaStream_t st);
+cudaError_t launch_paint(const BatchGeom& bg, const uint64_t* segs, const uint64_t* items, int idx_bits,
+                         const uint32_t* tile_start, const CarryBuffers& cb, cudaStream_t st);
 
-// Generic block-count compaction helper: scan of per-block counts.
-cudaError_t scan_block_counts(const uint32_t* counts, uint32_t* offsets, uint32_t n_blocks, Scratch* s,
-                              cudaStream_t st, uint64_t* total_host);
 
 }  // namespace cgb

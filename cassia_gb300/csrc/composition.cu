@@ -19,13 +19,6 @@
 
 #include "cgb_internal.cuh"
 
-namespace cgb {
-uint32_t raster_grid(uint64_t n_steps, uint32_t block);
-uint32_t tl_heads_grid(uint32_t n);
-cudaError_t launch_items_crop(int mode, const uint64_t* segs, uint32_t G, const RenderGeom& geom,
-                              const PaintParams& pp, CarryBuffers& cb, int idx_bits, cudaStream_t st);
-}  // namespace cgb
-
 using namespace cgb;
 
 namespace {
@@ -138,7 +131,7 @@ struct cgb_composition {
     // frame buffers
     DevBuf recs, lengths, step_off, bcounts, btotals, boff, btoff, segs_a, segs_b;
     DevBuf tl_start, tl_cover, tl_carry, tl_flags, item_count, item_off, items_a, items_b, tile_start;
-    DevBuf d_props, d_unchanged, out_rgba, err, dflt_t;
+    DevBuf d_props, d_unchanged, out_rgba, err, dflt_t, d_scenes, d_row_scene;
     // flatten staging
     DevBuf f_kinds, f_points, f_cmd_off, f_pt_off, f_t9, f_has_t, f_path_layer, f_counts, f_off;
     // GC staging
@@ -475,30 +468,30 @@ cgb_status insert_paths(cgb_composition* c, size_t n_paths, const uint32_t* laye
     return CGB_OK;
 }
 
-struct FrameGeom {
-    uint32_t width, height, stride, rows, row_len;
+// One scene of a frame as the host prepares it.
+struct SceneInput {
+    cgb_composition* comp;
+    const cgb_buffer* buf;
+    const float* bg;
+    const cgb_rect* crop;
+    CacheState* cache;
+    SceneDesc d;
+    size_t staging_off;  // offset in the frame's host-output staging buffer
 };
 
 // LinesBuilder::build + Rasterizer::rasterize (+ re-keying / culling in
-// render mode).  Leaves n_segs keys in segs_a.
-cgb_status build_and_rasterize(cgb_composition* c, int render, const RenderGeom& geom, uint64_t* n_segs,
+// render mode) over every scene of the frame.  Leaves n_segs keys in segs_a.
+cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& bg, uint64_t* n_segs,
                                uint64_t* n_total) {
     cudaStream_t st = c->stream;
-    const uint32_t L = (uint32_t)c->n_lines;
+    if (bg.total_lines >= (1ull << 32)) return fail(CGB_ERR_LAYER_LIMIT, "more than 2^32 lines in a frame");
+    const uint32_t L = (uint32_t)bg.total_lines;
     c->stats.lines = L;
     CK(c->s.ensure(c->recs, std::max<size_t>(L, 1) * sizeof(LineRec)));
     CK(c->s.ensure(c->lengths, std::max<size_t>(L, 1) * 4));
     CK(c->s.ensure(c->step_off, ((size_t)L + 1) * 4));
-    const float* dflt = nullptr;
-    if (c->has_default_transform) {
-        CK(c->s.ensure(c->dflt_t, 6 * 4));
-        CK(cudaMemcpyAsync(c->dflt_t.p, c->default_transform, 24, cudaMemcpyHostToDevice, st));
-        dflt = c->dflt_t.as<float>();
-    }
     CK(cudaEventRecord(c->ev[0], st));
-    CK(launch_build_lines(c->p0x.as<float>(), c->p0y.as<float>(), c->p1x.as<float>(), c->p1y.as<float>(),
-                          c->lids.as<uint32_t>(), L, c->d_layers.as<LayerRec>(), c->n_layer_recs, dflt,
-                          c->recs.as<LineRec>(), c->lengths.as<uint32_t>(), st));
+    CK(launch_build_lines(bg, c->recs.as<LineRec>(), c->lengths.as<uint32_t>(), st));
     uint64_t S = 0;
     CK(scan_u32(c->lengths.as<uint32_t>(), c->step_off.as<uint32_t>(), L, &c->s, st, &S));
     CK(cudaEventRecord(c->ev[1], st));
@@ -510,8 +503,7 @@ cgb_status build_and_rasterize(cgb_composition* c, int render, const RenderGeom&
     CK(c->s.ensure(c->btotals, ((size_t)grid + 1) * 4));
     CK(c->s.ensure(c->boff, ((size_t)grid + 1) * 4));
     CK(c->s.ensure(c->btoff, ((size_t)grid + 1) * 4));
-    SegFormat fmt{c->wide ? 1u : 0u};
-    CK(launch_rasterize(0, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, S, 0, block, fmt, render, geom,
+    CK(launch_rasterize(0, render, bg, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, S, block,
                         c->bcounts.as<uint32_t>(), c->btotals.as<uint32_t>(), nullptr, nullptr, st));
     uint64_t P = 0, PT = 0;
     CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid, &c->s, st, &P));
@@ -519,8 +511,8 @@ cgb_status build_and_rasterize(cgb_composition* c, int render, const RenderGeom&
     if (P >= (1ull << 30)) return fail(CGB_ERR_LAYER_LIMIT, "more than 2^30 pixel segments");
     CK(c->s.ensure(c->segs_a, std::max<size_t>(P, 1) * 8));
     CK(c->s.ensure(c->segs_b, std::max<size_t>(P, 1) * 8));
-    CK(launch_rasterize(1, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, S, 0, block, fmt, render, geom,
-                        nullptr, nullptr, c->boff.as<uint32_t>(), c->segs_a.as<uint64_t>(), st));
+    CK(launch_rasterize(1, render, bg, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, S, block, nullptr,
+                        nullptr, c->boff.as<uint32_t>(), c->segs_a.as<uint64_t>(), st));
     CK(cudaEventRecord(c->ev[2], st));
     *n_segs = P;
     *n_total = PT;
@@ -548,25 +540,27 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
     return ms;
 }
 
-cgb_status render(cgb_composition* c, const cgb_buffer* buf, const float bg[4], const cgb_rect* crop) {
-    if (!buf || !bg || !buf->pixels || buf->width == 0 || buf->height == 0)
+// Host-side preparation of one composition for a frame: mold's
+// remove_disabled, orders_to_layers / props, the layer table and the layer
+// cache (composition.rs:212-241).
+cgb_status prepare_scene(cgb_composition* c, SceneInput& in) {
+    const cgb_buffer* buf = in.buf;
+    if (!buf || !in.bg || !buf->pixels || buf->width == 0 || buf->height == 0)
         return fail(CGB_ERR_INVALID_ARG, "render: empty buffer");
     const uint64_t stride = buf->width_stride ? buf->width_stride : buf->width;
     if (stride < buf->width || buf->width > (1u << 20) || buf->height > (1u << 20))
         return fail(CGB_ERR_INVALID_ARG, "render: bad width/stride/height");
-    cudaStream_t st = c->stream;
-    FrameGeom fg{(uint32_t)buf->width, (uint32_t)buf->height, (uint32_t)stride, (uint32_t)((buf->height + 7) / 8),
-                 (uint32_t)((buf->width + 7) / 8)};
-    const uint64_t n_tiles = (uint64_t)fg.rows * fg.row_len;
-    CacheState* cache = nullptr;
+    const uint32_t rows = (uint32_t)((buf->height + 7) / 8), row_len = (uint32_t)((buf->width + 7) / 8);
+    const uint64_t n_tiles = (uint64_t)rows * row_len;
+    in.cache = nullptr;
     if (buf->layer_cache >= 0) {
         auto it = c->caches.find(buf->layer_cache);
         if (it == c->caches.end()) return fail(CGB_ERR_NOT_FOUND, "render: unknown layer cache");
-        cache = &it->second;
-        if (cache->tiles != n_tiles) {  // composition.rs:218-225
-            CK(c->s.ensure(cache->prev, n_tiles * 4));
-            CK(cudaMemsetAsync(cache->prev.p, 0xFF, n_tiles * 4, st));
-            cache->tiles = n_tiles;
+        in.cache = &it->second;
+        if (in.cache->tiles != n_tiles) {  // composition.rs:218-225
+            CK(c->s.ensure(in.cache->prev, n_tiles * 4));
+            CK(cudaMemsetAsync(in.cache->prev.p, 0xFF, n_tiles * 4, c->stream));
+            in.cache->tiles = n_tiles;
         }
     }
     cgb_status s0 = remove_disabled(c);
@@ -574,38 +568,126 @@ cgb_status render(cgb_composition* c, const cgb_buffer* buf, const float bg[4], 
     if (c->props_dirty) rebuild_props(c);
     if (c->unsupported)
         return fail(CGB_ERR_INVALID_ARG, "render: clip layers and gradient fills are not supported by the GPU painter");
-    const uint32_t n_orders = c->n_orders;
-    std::vector<uint8_t> unchanged;
-    if (cache) {
-        unchanged.assign(n_orders, 0);
-        for (uint32_t o = 0; o < n_orders; o++)
-            if (c->order_layer[o] != UINT32_MAX)
-                unchanged[o] = (c->layers[c->order_layer[o]].unchanged >> buf->layer_cache) & 1;
-    }
-    RenderGeom geom{fg.rows, fg.row_len, n_orders, 0};
-    geom.key_bits = bits_for((uint64_t)fg.rows * n_orders * (fg.row_len + 1) - 1);
-    if (geom.key_bits > 42) return fail(CGB_ERR_LAYER_LIMIT, "render: canvas x orders too large for the segment key");
     cgb_status s1 = upload_layers(c);
     if (s1) return s1;
     if (c->props_uploaded != c->props_version) {
         CK(c->s.ensure(c->d_props, c->props_host.size() * sizeof(PaintProps)));
         CK(cudaMemcpyAsync(c->d_props.p, c->props_host.data(), c->props_host.size() * sizeof(PaintProps),
-                           cudaMemcpyHostToDevice, st));
+                           cudaMemcpyHostToDevice, c->stream));
         c->props_uploaded = c->props_version;
     }
-    if (cache) {
+    if (in.cache) {
+        std::vector<uint8_t> unchanged(c->n_orders, 0);
+        for (uint32_t o = 0; o < c->n_orders; o++)
+            if (c->order_layer[o] != UINT32_MAX)
+                unchanged[o] = (c->layers[c->order_layer[o]].unchanged >> buf->layer_cache) & 1;
         CK(c->s.ensure(c->d_unchanged, unchanged.size()));
-        CK(cudaMemcpyAsync(c->d_unchanged.p, unchanged.data(), unchanged.size(), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(c->d_unchanged.p, unchanged.data(), unchanged.size(), cudaMemcpyHostToDevice, c->stream));
     }
+    if (c->has_default_transform) {
+        CK(c->s.ensure(c->dflt_t, 6 * 4));
+        CK(cudaMemcpyAsync(c->dflt_t.p, c->default_transform, 24, cudaMemcpyHostToDevice, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    SceneDesc& d = in.d;
+    d = SceneDesc{};
+    d.p0x = c->p0x.as<float>();
+    d.p0y = c->p0y.as<float>();
+    d.p1x = c->p1x.as<float>();
+    d.p1y = c->p1y.as<float>();
+    d.lids = c->lids.as<uint32_t>();
+    d.layers = c->d_layers.as<LayerRec>();
+    d.props = c->d_props.as<PaintProps>();
+    d.unchanged = in.cache ? c->d_unchanged.as<uint8_t>() : nullptr;
+    d.prev_layers = in.cache ? in.cache->prev.as<int32_t>() : nullptr;
+    d.default_t = c->has_default_transform ? c->dflt_t.as<float>() : nullptr;
+    d.n_lines = (uint32_t)c->n_lines;
+    d.n_layer_recs = c->n_layer_recs;
+    d.n_orders = c->n_orders;
+    d.wide = c->wide ? 1u : 0u;
+    d.width = (uint32_t)buf->width;
+    d.height = (uint32_t)buf->height;
+    d.stride = (uint32_t)stride;
+    d.rows = rows;
+    d.row_len = row_len;
+    d.crop_h0 = 0;
+    d.crop_h1 = row_len;
+    d.crop_v0 = 0;
+    d.crop_v1 = rows;
+    if (in.crop) {  // Rect::new (buffer_layout.rs:43-50)
+        d.crop_h0 = (uint32_t)std::min<uint64_t>(in.crop->x0 / 8, row_len);
+        d.crop_h1 = (uint32_t)std::min<uint64_t>((in.crop->x1 + 7) / 8, row_len);
+        d.crop_v0 = (uint32_t)std::min<uint64_t>(in.crop->y0 / 8, rows);
+        d.crop_v1 = (uint32_t)std::min<uint64_t>((in.crop->y1 + 7) / 8, rows);
+    }
+    std::memcpy(d.clear, in.bg, sizeof(d.clear));
+    return CGB_OK;
+}
+
+// Renders every scene of `scenes` in one pipeline on `c`'s stream and
+// buffers: build, rasterize, sort, carries / items, paint.
+cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
+    cudaStream_t st = c->stream;
+    for (SceneInput& in : scenes) {
+        cgb_status s0 = prepare_scene(in.comp, in);
+        if (s0) return s0;
+    }
+    // frame geometry: global rows / tiles, key factors, host-output staging
+    uint64_t lines = 0, rows = 0, tiles = 0, staging = 0;
+    uint32_t n_orders = 1, row_len = 1;
+    for (SceneInput& in : scenes) {
+        in.d.line_base = lines;
+        in.d.row_base = (uint32_t)rows;
+        in.d.tile_base = (uint32_t)tiles;
+        lines += in.d.n_lines;
+        rows += in.d.rows;
+        tiles += (uint64_t)in.d.rows * in.d.row_len;
+        n_orders = std::max(n_orders, in.d.n_orders);
+        row_len = std::max(row_len, in.d.row_len);
+        in.staging_off = staging;
+        if (in.buf->memory == CGB_MEMORY_HOST) staging += ((size_t)in.d.height * in.d.stride * 4 + 255) & ~(size_t)255;
+    }
+    if (tiles >= (1ull << 31)) return fail(CGB_ERR_LAYER_LIMIT, "render: too many tiles in a frame");
+    BatchGeom bg{};
+    bg.n_scenes = (uint32_t)scenes.size();
+    bg.total_rows = (uint32_t)rows;
+    bg.total_tiles = (uint32_t)tiles;
+    bg.n_orders = n_orders;
+    bg.row_len = row_len;
+    bg.total_lines = lines;
+    bg.key_bits = bits_for(std::max<uint64_t>(rows * n_orders * (row_len + 1), 1) - 1);
+    if (bg.key_bits > 42) return fail(CGB_ERR_LAYER_LIMIT, "render: rows x orders x tiles too large for the segment key");
+    if (staging) CK(c->s.ensure(c->out_rgba, staging));
+    std::vector<SceneDesc> descs;
+    std::vector<uint32_t> row_scene(std::max<uint64_t>(rows, 1), 0);
+    for (size_t k = 0; k < scenes.size(); k++) {
+        SceneInput& in = scenes[k];
+        if (in.buf->memory == CGB_MEMORY_HOST) {
+            in.d.out = c->out_rgba.as<uint8_t>() + in.staging_off;
+            if (in.cache || in.crop)  // tiles that are not repainted keep the caller's pixels
+                CK(cudaMemcpy2DAsync(in.d.out, (size_t)in.d.stride * 4, in.buf->pixels, (size_t)in.d.stride * 4,
+                                     (size_t)in.d.width * 4, in.d.height, cudaMemcpyHostToDevice, st));
+        } else {
+            in.d.out = in.buf->pixels;
+        }
+        for (uint32_t r = 0; r < in.d.rows; r++) row_scene[in.d.row_base + r] = (uint32_t)k;
+        descs.push_back(in.d);
+    }
+    CK(c->s.ensure(c->d_scenes, descs.size() * sizeof(SceneDesc)));
+    CK(c->s.ensure(c->d_row_scene, row_scene.size() * 4));
+    CK(cudaMemcpyAsync(c->d_scenes.p, descs.data(), descs.size() * sizeof(SceneDesc), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->d_row_scene.p, row_scene.data(), row_scene.size() * 4, cudaMemcpyHostToDevice, st));
+    bg.scenes = c->d_scenes.as<SceneDesc>();
+    bg.row_scene = c->d_row_scene.as<uint32_t>();
 
     uint64_t P = 0, PT = 0;
-    cgb_status s2 = build_and_rasterize(c, 1, geom, &P, &PT);
+    cgb_status s2 = build_and_rasterize(c, 1, bg, &P, &PT);
     if (s2) return s2;
     c->stats.painted_segments = P;
-    // sort by (row, order, tile column)
+    // sort by (global row, order, tile column)
     uint64_t* sorted = c->segs_a.as<uint64_t>();
     int passes = 0;
-    CK(radix_sort_u64(c->segs_a.as<uint64_t>(), c->segs_b.as<uint64_t>(), (uint32_t)P, 22, 22 + (int)geom.key_bits,
+    CK(radix_sort_u64(c->segs_a.as<uint64_t>(), c->segs_b.as<uint64_t>(), (uint32_t)P, 22, 22 + (int)bg.key_bits,
                       (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &sorted, &passes));
     c->stats.sort_passes = passes;
     CK(cudaEventRecord(c->ev[3], st));
@@ -632,69 +714,38 @@ cgb_status render(cgb_composition* c, const cgb_buffer* buf, const float bg[4], 
     cb.item_count = c->item_count.as<uint32_t>();
     cb.item_off = c->item_off.as<uint32_t>();
     CK(launch_tl_heads(1, sorted, (uint32_t)P, nullptr, c->boff.as<uint32_t>(), cb.tl_start, st));
-    uint32_t P32 = (uint32_t)P;
-    CK(cudaMemcpyAsync(cb.tl_start + G, &P32, 4, cudaMemcpyHostToDevice, st));
-    CK(launch_tl_reduce_scan(sorted, (uint32_t)P, (uint32_t)G, geom, cb, &c->s, st));
-
-    PaintParams pp{};
-    pp.geom = geom;
-    pp.width = fg.width;
-    pp.height = fg.height;
-    pp.stride = fg.stride;
-    std::memcpy(pp.clear, bg, sizeof(pp.clear));
-    pp.props = c->d_props.as<PaintProps>();
-    pp.unchanged = cache ? c->d_unchanged.as<uint8_t>() : nullptr;
-    pp.prev_layers = cache ? cache->prev.as<int32_t>() : nullptr;
-    pp.crop_h0 = 0;
-    pp.crop_h1 = fg.row_len;
-    pp.crop_v0 = 0;
-    pp.crop_v1 = fg.rows;
-    if (crop) {  // Rect::new (buffer_layout.rs:43-50)
-        pp.crop_h0 = (uint32_t)std::min<uint64_t>(crop->x0 / 8, fg.row_len);
-        pp.crop_h1 = (uint32_t)std::min<uint64_t>((crop->x1 + 7) / 8, fg.row_len);
-        pp.crop_v0 = (uint32_t)std::min<uint64_t>(crop->y0 / 8, fg.rows);
-        pp.crop_v1 = (uint32_t)std::min<uint64_t>((crop->y1 + 7) / 8, fg.rows);
-    }
-    CK(launch_items_crop(0, sorted, (uint32_t)G, geom, pp, cb, 0, st));
+    c->s.pinned[1] = P;  // tl_start[G] = P
+    CK(cudaMemcpyAsync(cb.tl_start + G, &c->s.pinned[1], 4, cudaMemcpyHostToDevice, st));
+    CK(launch_tl_reduce_scan(sorted, (uint32_t)G, bg, cb, st));
+    CK(launch_items(0, sorted, (uint32_t)G, bg, cb, 0, st));
     uint64_t W = 0;
     if (G) CK(scan_u32(cb.item_count, cb.item_off, (uint32_t)G, &c->s, st, &W));
     c->stats.work_items = W;
     const int idx_bits = bits_for(std::max<uint64_t>(G, 1) - 1);
-    const int item_key_bits = bits_for(n_tiles * n_orders - 1);
+    const int item_key_bits = bits_for(std::max<uint64_t>(tiles * n_orders, 1) - 1);
     const int item_shift = idx_bits + 3;  // TL index, then the full / opaque / carry-only bits
     if (item_shift + item_key_bits > 64 || W >= (1ull << 30))
         return fail(CGB_ERR_LAYER_LIMIT, "render: too many tile x layer work items");
     CK(c->s.ensure(c->items_a, std::max<uint64_t>(W, 1) * 8));
     CK(c->s.ensure(c->items_b, std::max<uint64_t>(W, 1) * 8));
-    CK(c->s.ensure(c->tile_start, (n_tiles + 1) * 4));
+    CK(c->s.ensure(c->tile_start, (tiles + 1) * 4));
     cb.items = c->items_a.as<uint64_t>();
     cb.items_tmp = c->items_b.as<uint64_t>();
     cb.tile_start = c->tile_start.as<uint32_t>();
-    CK(launch_items_crop(1, sorted, (uint32_t)G, geom, pp, cb, idx_bits, st));
+    CK(launch_items(1, sorted, (uint32_t)G, bg, cb, idx_bits, st));
     uint64_t* items_sorted = cb.items;
     int ipasses = 0;
     CK(radix_sort_u64(cb.items, cb.items_tmp, (uint32_t)W, item_shift, item_shift + item_key_bits,
                       (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &items_sorted, &ipasses));
     c->stats.item_sort_passes = ipasses;
-    CK(launch_tile_ranges(items_sorted, (uint32_t)W, (uint32_t)n_tiles, item_shift, n_orders, cb.tile_start, st));
+    CK(launch_tile_ranges(items_sorted, (uint32_t)W, (uint32_t)tiles, item_shift, n_orders, cb.tile_start, st));
     CK(cudaEventRecord(c->ev[4], st));
-
-    // output
-    const bool host = buf->memory == CGB_MEMORY_HOST;
-    uint8_t* out = buf->pixels;
-    if (host) {
-        CK(c->s.ensure(c->out_rgba, (size_t)fg.height * fg.stride * 4));
-        out = c->out_rgba.as<uint8_t>();
-        if (cache || crop)  // tiles that are not repainted keep the caller's pixels
-            CK(cudaMemcpy2DAsync(out, (size_t)fg.stride * 4, buf->pixels, (size_t)fg.stride * 4,
-                                 (size_t)fg.width * 4, fg.height, cudaMemcpyHostToDevice, st));
-    }
-    pp.out = out;
-    CK(launch_paint(pp, sorted, items_sorted, idx_bits, cb.tile_start, cb, c->tuning.paint_warps, st));
+    CK(launch_paint(bg, sorted, items_sorted, idx_bits, cb.tile_start, cb, st));
     CK(cudaEventRecord(c->ev[5], st));
-    if (host)
-        CK(cudaMemcpy2DAsync(buf->pixels, (size_t)fg.stride * 4, out, (size_t)fg.stride * 4, (size_t)fg.width * 4,
-                             fg.height, cudaMemcpyDeviceToHost, st));
+    for (SceneInput& in : scenes)
+        if (in.buf->memory == CGB_MEMORY_HOST)
+            CK(cudaMemcpy2DAsync(in.buf->pixels, (size_t)in.d.stride * 4, in.d.out, (size_t)in.d.stride * 4,
+                                 (size_t)in.d.width * 4, in.d.height, cudaMemcpyDeviceToHost, st));
     cgb_status s3 = check_device_error(c);
     if (s3) return s3;
     c->stats.build_ms = elapsed(c->ev[0], c->ev[1]);
@@ -703,13 +754,23 @@ cgb_status render(cgb_composition* c, const cgb_buffer* buf, const float bg[4], 
     c->stats.carry_ms = elapsed(c->ev[3], c->ev[4]);
     c->stats.paint_ms = elapsed(c->ev[4], c->ev[5]);
     c->stats.total_ms = elapsed(c->ev[0], c->ev[5]);
-    if (cache)  // composition.rs:322-327
-        for (HostLayer& l : c->layers) {
-            if (!l.present) continue;
-            if (l.enabled) l.unchanged |= 1u << buf->layer_cache;
-            else l.unchanged &= ~(1u << buf->layer_cache);
-        }
+    for (SceneInput& in : scenes)
+        if (in.cache)  // composition.rs:322-327
+            for (HostLayer& l : in.comp->layers) {
+                if (!l.present) continue;
+                if (l.enabled) l.unchanged |= 1u << in.buf->layer_cache;
+                else l.unchanged &= ~(1u << in.buf->layer_cache);
+            }
     return CGB_OK;
+}
+
+cgb_status render(cgb_composition* c, const cgb_buffer* buf, const float bg[4], const cgb_rect* crop) {
+    std::vector<SceneInput> scenes(1);
+    scenes[0].comp = c;
+    scenes[0].buf = buf;
+    scenes[0].bg = bg;
+    scenes[0].crop = crop;
+    return render_frame(c, scenes);
 }
 
 }  // namespace
@@ -970,6 +1031,24 @@ CGB_EXPORT cgb_status cgb_render(cgb_composition* c, const cgb_buffer* buffer, c
     return render(c, buffer, background, crop);
 }
 
+CGB_EXPORT cgb_status cgb_render_batch(cgb_composition* ctx, size_t n, cgb_composition* const* comps,
+                                       const cgb_buffer* buffers, const float* backgrounds, const cgb_rect* crops) {
+    if (!ctx || (n && (!comps || !buffers || !backgrounds))) return fail(CGB_ERR_INVALID_ARG, "null argument");
+    if (n > 4096) return fail(CGB_ERR_INVALID_ARG, "render_batch: at most 4096 scenes per frame");
+    DeviceGuard _guard(ctx->device);
+    std::vector<SceneInput> scenes(n);
+    for (size_t k = 0; k < n; k++) {
+        if (!comps[k] || comps[k]->device != ctx->device)
+            return fail(CGB_ERR_INVALID_ARG, "render_batch: scene on another device or null");
+        scenes[k].comp = comps[k];
+        scenes[k].buf = &buffers[k];
+        scenes[k].bg = backgrounds + 4 * k;
+        scenes[k].crop = crops ? &crops[k] : nullptr;
+    }
+    if (n == 0) return CGB_OK;
+    return render_frame(ctx, scenes);
+}
+
 CGB_EXPORT cgb_status cgb_pixel_segments(cgb_composition* c, uint64_t* out, size_t cap, uint64_t* out_len,
                                          uint64_t* out_none, uint32_t order) {
     HANDLE_CHECK();
@@ -979,8 +1058,28 @@ CGB_EXPORT cgb_status cgb_pixel_segments(cgb_composition* c, uint64_t* out, size
     cgb_status s1 = upload_layers(c);
     if (s1) return s1;
     uint64_t P = 0, PT = 0;
-    RenderGeom geom{};
-    cgb_status s2 = build_and_rasterize(c, 0, geom, &P, &PT);
+    if (c->has_default_transform) {
+        CK(c->s.ensure(c->dflt_t, 6 * 4));
+        CK(cudaMemcpyAsync(c->dflt_t.p, c->default_transform, 24, cudaMemcpyHostToDevice, c->stream));
+    }
+    SceneDesc d{};
+    d.p0x = c->p0x.as<float>();
+    d.p0y = c->p0y.as<float>();
+    d.p1x = c->p1x.as<float>();
+    d.p1y = c->p1y.as<float>();
+    d.lids = c->lids.as<uint32_t>();
+    d.layers = c->d_layers.as<LayerRec>();
+    d.default_t = c->has_default_transform ? c->dflt_t.as<float>() : nullptr;
+    d.n_lines = (uint32_t)c->n_lines;
+    d.n_layer_recs = c->n_layer_recs;
+    d.wide = c->wide ? 1u : 0u;
+    CK(c->s.ensure(c->d_scenes, sizeof(SceneDesc)));
+    CK(cudaMemcpyAsync(c->d_scenes.p, &d, sizeof(SceneDesc), cudaMemcpyHostToDevice, c->stream));
+    BatchGeom bg{};
+    bg.scenes = c->d_scenes.as<SceneDesc>();
+    bg.n_scenes = 1;
+    bg.total_lines = c->n_lines;
+    cgb_status s2 = build_and_rasterize(c, 0, bg, &P, &PT);
     if (s2) return s2;
     uint64_t* sorted = c->segs_a.as<uint64_t>();
     int passes = 0;

@@ -295,15 +295,34 @@ __global__ void k_flatten(int write, const uint32_t* __restrict__ kinds, const f
 // LinesBuilder::build
 // ---------------------------------------------------------------------------
 
-__global__ void k_build_lines(const float* __restrict__ p0xs, const float* __restrict__ p0ys,
-                              const float* __restrict__ p1xs, const float* __restrict__ p1ys,
-                              const uint32_t* __restrict__ lids, uint32_t n, const LayerRec* __restrict__ layers,
-                              uint32_t n_layer_recs, const float* __restrict__ default_t, LineRec* __restrict__ recs,
-                              uint32_t* __restrict__ lengths) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float p0x = p0xs[i], p0y = p0ys[i], p1x = p1xs[i], p1y = p1ys[i];
-    uint32_t lid = lids[i];
+constexpr int MAX_SMEM_SCENES = 1024;
+
+// Scene of global line g: the last scene whose line_base <= g.
+__device__ __forceinline__ uint32_t scene_of_line(const uint64_t* base, uint32_t n_scenes, uint64_t g) {
+    uint32_t lo = 0, hi = n_scenes;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (base[mid] <= g) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_build_lines(BatchGeom bg, LineRec* __restrict__ recs, uint32_t* __restrict__ lengths) {
+    __shared__ uint64_t s_base[MAX_SMEM_SCENES];
+    const uint32_t ns = min(bg.n_scenes, (uint32_t)MAX_SMEM_SCENES);
+    for (uint32_t k = threadIdx.x; k < ns; k += blockDim.x) s_base[k] = bg.scenes[k].line_base;
+    __syncthreads();
+    const uint64_t gi = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gi >= bg.total_lines) return;
+    const uint32_t sc = scene_of_line(s_base, ns, gi);
+    const SceneDesc& S = bg.scenes[sc];
+    const uint32_t i = (uint32_t)(gi - S.line_base);
+    float p0x = S.p0x[i], p0y = S.p0y[i], p1x = S.p1x[i], p1y = S.p1y[i];
+    const uint32_t lid = S.lids[i];
+    const LayerRec* __restrict__ layers = S.layers;
+    const uint32_t n_layer_recs = S.n_layer_recs;
+    const float* __restrict__ default_t = S.default_t;
     LineRec r{0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0u};
     uint32_t length = 0;
     uint32_t flags = 0, lorder = 0;
@@ -361,11 +380,11 @@ __global__ void k_build_lines(const float* __restrict__ p0xs, const float* __res
             r.slope_recip = slope_recip;
             r.py_slope_px = __fmaf_rn(slope, -px, py);
             r.px_slope_recip_py = __fmaf_rn(slope_recip, -py, px);
-            r.order_octant = (order << 3) | oct;
+            r.order_octant = (sc << LINE_SCENE_SHIFT) | (order << 3) | oct;
         }
     }
-    recs[i] = r;
-    lengths[i] = length;
+    recs[gi] = r;
+    lengths[gi] = length;
 }
 
 // ---------------------------------------------------------------------------
@@ -409,7 +428,7 @@ __device__ __forceinline__ bool intersects_y_border(int32_t y0, int32_t y1) {
 
 // One pixel step (rasterizer/mod.rs:233-281); returns 1 or 2 segments.
 __device__ __forceinline__ int raster_step(uint32_t wide, const LineRec& l, int32_t pi, uint64_t out[2]) {
-    const uint32_t oct = l.order_octant & 7, layer = l.order_octant >> 3;
+    const uint32_t oct = l.order_octant & 7, layer = (l.order_octant >> 3) & ((1u << (LINE_SCENE_SHIFT - 3)) - 1);
     int32_t x0i = wadd(l.start, pi);
     int32_t x1i = wadd(x0i, 1);
     int32_t border_x = x0i;
@@ -433,12 +452,17 @@ __device__ __forceinline__ int raster_step(uint32_t wide, const LineRec& l, int3
 
 // Render format: culls segments the painter never reads (rows outside the
 // canvas, tiles right of it, 13-bit tile_i wrap) and re-keys the rest by
-// (tile row, order, tile column + 1) above the reference's low 22 bits.
-__device__ __forceinline__ bool render_key(uint32_t wide, const RenderGeom& g, uint64_t seg, uint64_t& out) {
-    int32_t tj = seg_tile_j(wide, seg);
-    int32_t ti = seg_tile_i_stored(wide, seg) - 256;
-    if (tj < 0 || tj >= (int32_t)g.rows || ti < -1 || ti >= (int32_t)g.row_len) return false;
-    uint64_t key = ((uint64_t)tj * g.n_orders + seg_layer(wide, seg)) * (g.row_len + 1) + (uint64_t)(ti + 1);
+// (global tile row, order, tile column + 1) above the reference's low 22 bits.
+struct SceneRaster {
+    uint32_t wide, rows, row_len, row_base;
+};
+
+__device__ __forceinline__ bool render_key(const SceneRaster& sr, const BatchGeom& bg, uint64_t seg, uint64_t& out) {
+    int32_t tj = seg_tile_j(sr.wide, seg);
+    int32_t ti = seg_tile_i_stored(sr.wide, seg) - 256;
+    if (tj < 0 || tj >= (int32_t)sr.rows || ti < -1 || ti >= (int32_t)sr.row_len) return false;
+    uint64_t key = ((uint64_t)(sr.row_base + (uint32_t)tj) * bg.n_orders + seg_layer(sr.wide, seg)) * (bg.row_len + 1) +
+                   (uint64_t)(ti + 1);
     out = (key << 22) | (seg & 0x3FFFFFull);
     return true;
 }
@@ -458,7 +482,7 @@ __device__ __forceinline__ uint32_t find_line(const uint32_t* __restrict__ off, 
 
 template <int MODE, int RENDER>
 __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ recs, const uint32_t* __restrict__ off,
-                                                   uint32_t n_lines, uint64_t n_steps, uint32_t wide, RenderGeom geom,
+                                                   uint32_t n_lines, uint64_t n_steps, BatchGeom bg,
                                                    uint32_t* __restrict__ block_counts,
                                                    uint32_t* __restrict__ block_totals,
                                                    const uint32_t* __restrict__ block_off,
@@ -471,6 +495,8 @@ __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ r
         uint32_t l = find_line(off, n_lines, s0);
         uint32_t next = off[l + 1];
         LineRec rec = recs[l];
+        uint32_t sc = rec.order_octant >> LINE_SCENE_SHIFT;
+        SceneRaster sr{bg.scenes[sc].wide, bg.scenes[sc].rows, bg.scenes[sc].row_len, bg.scenes[sc].row_base};
 #pragma unroll
         for (int k = 0; k < RASTER_ITEMS; k++) {
             uint64_t s = s0 + k;
@@ -479,16 +505,21 @@ __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ r
                     l++;
                     next = off[l + 1];
                     rec = recs[l];
+                    if ((rec.order_octant >> LINE_SCENE_SHIFT) != sc) {
+                        sc = rec.order_octant >> LINE_SCENE_SHIFT;
+                        sr = SceneRaster{bg.scenes[sc].wide, bg.scenes[sc].rows, bg.scenes[sc].row_len,
+                                         bg.scenes[sc].row_base};
+                    }
                 }
                 uint64_t o[2];
-                int m = raster_step(wide, rec, (int32_t)(s - off[l]), o);
+                int m = raster_step(sr.wide, rec, (int32_t)(s - off[l]), o);
                 total += m;
 #pragma unroll
                 for (int q = 0; q < 2; q++) {
                     if (q < m) {
                         uint64_t v = o[q];
                         bool keep = true;
-                        if (RENDER) keep = render_key(wide, geom, o[q], v);
+                        if (RENDER) keep = render_key(sr, bg, o[q], v);
                         if (keep) segs[n++] = v;
                     }
                 }
@@ -584,21 +615,17 @@ cudaError_t launch_flatten(int write, const uint32_t* kinds, const float* points
     return cudaGetLastError();
 }
 
-cudaError_t launch_build_lines(const float* p0x, const float* p0y, const float* p1x, const float* p1y,
-                               const uint32_t* lids, uint32_t n, const LayerRec* layers, uint32_t n_layer_recs,
-                               const float* default_t, LineRec* recs, uint32_t* lengths, cudaStream_t st) {
-    if (n == 0) return cudaSuccess;
+cudaError_t launch_build_lines(const BatchGeom& bg, LineRec* recs, uint32_t* lengths, cudaStream_t st) {
+    if (bg.total_lines == 0) return cudaSuccess;
+    if (bg.n_scenes > MAX_SMEM_SCENES) return cudaErrorInvalidValue;
     count_launches(1);
-    k_build_lines<<<(n + 255) / 256, 256, 0, st>>>(p0x, p0y, p1x, p1y, lids, n, layers, n_layer_recs, default_t,
-                                                   recs, lengths);
+    k_build_lines<<<(uint32_t)((bg.total_lines + 255) / 256), 256, 0, st>>>(bg, recs, lengths);
     return cudaGetLastError();
 }
 
-cudaError_t launch_rasterize(int mode, const LineRec* recs, const uint32_t* step_off, uint32_t n_lines,
-                             uint64_t n_steps, uint32_t steps_per_block, uint32_t block, SegFormat fmt, int render,
-                             RenderGeom geom, uint32_t* block_counts, uint32_t* block_totals,
-                             const uint32_t* block_off, uint64_t* out, cudaStream_t st) {
-    (void)steps_per_block;
+cudaError_t launch_rasterize(int mode, int render, const BatchGeom& bg, const LineRec* recs, const uint32_t* step_off,
+                             uint32_t n_lines, uint64_t n_steps, uint32_t block, uint32_t* block_counts,
+                             uint32_t* block_totals, const uint32_t* block_off, uint64_t* out, cudaStream_t st) {
     if (n_steps == 0) return cudaSuccess;
     block = block ? block : 256;
     uint64_t per_block = (uint64_t)block * RASTER_ITEMS;
@@ -607,18 +634,18 @@ cudaError_t launch_rasterize(int mode, const LineRec* recs, const uint32_t* step
     count_launches(1);
     if (mode == 0) {
         if (render)
-            k_rasterize<0, 1><<<grid, block, 0, st>>>(recs, step_off, n_lines, n_steps, fmt.wide, geom, block_counts,
+            k_rasterize<0, 1><<<grid, block, 0, st>>>(recs, step_off, n_lines, n_steps, bg, block_counts,
                                                       block_totals, block_off, out);
         else
-            k_rasterize<0, 0><<<grid, block, 0, st>>>(recs, step_off, n_lines, n_steps, fmt.wide, geom, block_counts,
+            k_rasterize<0, 0><<<grid, block, 0, st>>>(recs, step_off, n_lines, n_steps, bg, block_counts,
                                                       block_totals, block_off, out);
     } else {
         if (render)
-            k_rasterize<1, 1><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, fmt.wide, geom,
-                                                         block_counts, block_totals, block_off, out);
+            k_rasterize<1, 1><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, block_counts,
+                                                         block_totals, block_off, out);
         else
-            k_rasterize<1, 0><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, fmt.wide, geom,
-                                                         block_counts, block_totals, block_off, out);
+            k_rasterize<1, 0><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, block_counts,
+                                                         block_totals, block_off, out);
     }
     return cudaGetLastError();
 }

@@ -125,40 +125,35 @@ constexpr uint32_t ITEM_FULL = 2u;
 constexpr uint32_t ITEM_CARRY = 4u;
 constexpr int ITEM_FLAG_BITS = 3;
 
-struct ItemGeom {
-    RenderGeom geom;
-    uint32_t h0, h1, v0, v1;  // crop in tiles
-};
-
-// Items of TL g: its own (tile, L) pair and the cover-carry-only tiles up to
-// the next TL of the run.  Returns the count; `emit(tile, carry_only)` is
-// called for each when non-null.
+// Items of TL g: its own (tile, order) pair and the cover-carry-only tiles up
+// to the next TL of its (row, order) run.  Returns the count; `emit(tile,
+// flags)` is called for each.
 template <class Emit>
 __device__ __forceinline__ uint32_t tl_items(uint32_t g, uint32_t G, const uint64_t* __restrict__ segs,
                                              const uint32_t* __restrict__ tl_start, const uint32_t* __restrict__ tl_flags,
                                              const uint64_t* __restrict__ tl_cover,
-                                             const uint64_t* __restrict__ tl_carry, const ItemGeom& ig,
-                                             const PaintProps* __restrict__ props, Emit emit) {
-    const RenderGeom& geo = ig.geom;
+                                             const uint64_t* __restrict__ tl_carry, const BatchGeom& bg, Emit emit) {
     const uint64_t key = segs[tl_start[g]] >> 22;
-    const uint32_t rl1 = geo.row_len + 1;
+    const uint32_t rl1 = bg.row_len + 1;
     const int32_t i = (int32_t)(key % rl1) - 1;
     const uint64_t run = key / rl1;
-    const uint32_t L = (uint32_t)(run % geo.n_orders);
-    const uint32_t j = (uint32_t)(run / geo.n_orders);
-    if (j < ig.v0 || j >= ig.v1) return 0;
-    int32_t next = (int32_t)geo.row_len;
+    const uint32_t L = (uint32_t)(run % bg.n_orders);
+    const uint32_t grow = (uint32_t)(run / bg.n_orders);
+    const SceneDesc& S = bg.scenes[bg.row_scene[grow]];
+    const uint32_t j = grow - S.row_base;
+    if (j < S.crop_v0 || j >= S.crop_v1) return 0;
+    int32_t next = (int32_t)S.row_len;
     if (g + 1 < G && !tl_flags[g + 1]) next = (int32_t)((segs[tl_start[g + 1]] >> 22) % rl1) - 1;
-    const int32_t h0 = (int32_t)ig.h0, h1 = (int32_t)ig.h1;
+    const int32_t h0 = (int32_t)S.crop_h0, h1 = (int32_t)S.crop_h1;
     if (next > h1) next = h1;
     uint32_t cnt = 0;
     if (i >= h0 && i < h1) {
-        emit(i, ITEM_OWN);  // a layer with segments is never "full" (layer_workbench.rs:164-175)
+        emit(S, j, i, ITEM_OWN);  // a layer with segments is never "full" (layer_workbench.rs:164-175)
         cnt++;
     }
     if (next <= i + 1) return cnt;
     const uint64_t carry_out = cover_add(tl_carry[g], tl_cover[g]);
-    const PaintProps pp = props[L];
+    const PaintProps pp = S.props[L];
     const bool nonempty = !cover_is_empty(carry_out, pp.fill_rule);
     // payload of a cover-carry-only item: its layer_is_full and the opaque
     // Solid Over test of skip_fully_covered_layers (:335-356)
@@ -169,13 +164,13 @@ __device__ __forceinline__ uint32_t tl_items(uint32_t g, uint32_t G, const uint6
         // the first painted tile of the row holds every layer with segments
         // to its left, empty or not
         if (next <= h0) return cnt;
-        emit(h0, flags);
+        emit(S, j, h0, flags);
         cnt++;
         t = h0 + 1;
     }
     if (nonempty)
         for (; t < next; t++) {
-            emit(t, flags);
+            emit(S, j, t, flags);
             cnt++;
         }
     return cnt;
@@ -183,30 +178,27 @@ __device__ __forceinline__ uint32_t tl_items(uint32_t g, uint32_t G, const uint6
 
 __global__ void k_items_count(const uint64_t* __restrict__ segs, uint32_t G, const uint32_t* __restrict__ tl_start,
                               const uint32_t* __restrict__ tl_flags, const uint64_t* __restrict__ tl_cover,
-                              const uint64_t* __restrict__ tl_carry, ItemGeom ig, const PaintProps* __restrict__ props,
-                              uint32_t* __restrict__ counts) {
+                              const uint64_t* __restrict__ tl_carry, BatchGeom bg, uint32_t* __restrict__ counts) {
     uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= G) return;
-    counts[g] = tl_items(g, G, segs, tl_start, tl_flags, tl_cover, tl_carry, ig, props, [](int32_t, uint32_t) {});
+    counts[g] = tl_items(g, G, segs, tl_start, tl_flags, tl_cover, tl_carry, bg,
+                         [](const SceneDesc&, uint32_t, int32_t, uint32_t) {});
 }
 
 __global__ void k_items_write(const uint64_t* __restrict__ segs, uint32_t G, const uint32_t* __restrict__ tl_start,
                               const uint32_t* __restrict__ tl_flags, const uint64_t* __restrict__ tl_cover,
-                              const uint64_t* __restrict__ tl_carry, ItemGeom ig, const PaintProps* __restrict__ props,
-                              const uint32_t* __restrict__ off, int idx_bits, uint64_t* __restrict__ items) {
+                              const uint64_t* __restrict__ tl_carry, BatchGeom bg, const uint32_t* __restrict__ off,
+                              int idx_bits, uint64_t* __restrict__ items) {
     uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= G) return;
-    const uint64_t key = segs[tl_start[g]] >> 22;
-    const uint32_t rl1 = ig.geom.row_len + 1;
-    const uint64_t run = key / rl1;
-    const uint64_t L = run % ig.geom.n_orders;
-    const uint64_t j = run / ig.geom.n_orders;
+    const uint64_t L = ((segs[tl_start[g]] >> 22) / (bg.row_len + 1)) % bg.n_orders;
     uint32_t o = off[g];
-    tl_items(g, G, segs, tl_start, tl_flags, tl_cover, tl_carry, ig, props, [&](int32_t t, uint32_t flags) {
-        uint64_t tile = j * ig.geom.row_len + (uint64_t)t;
-        uint64_t k = ((tile * ig.geom.n_orders + L) << ITEM_FLAG_BITS) | flags;
-        items[o++] = (k << idx_bits) | g;
-    });
+    tl_items(g, G, segs, tl_start, tl_flags, tl_cover, tl_carry, bg,
+             [&](const SceneDesc& S, uint32_t j, int32_t t, uint32_t flags) {
+                 const uint64_t tile = (uint64_t)S.tile_base + (uint64_t)j * S.row_len + (uint64_t)t;
+                 const uint64_t k = ((tile * bg.n_orders + L) << ITEM_FLAG_BITS) | flags;
+                 items[o++] = (k << idx_bits) | g;
+             });
 }
 
 __global__ void k_tile_ranges(const uint64_t* __restrict__ items, uint32_t W, uint32_t n_tiles, int shift,
@@ -359,7 +351,7 @@ __device__ __forceinline__ void item_decode(uint64_t item, int idx_bits, uint32_
 }
 
 struct PaintArgs {
-    PaintParams p;
+    BatchGeom bg;
     const uint64_t* segs;
     const uint64_t* items;
     int idx_bits;
@@ -386,15 +378,15 @@ struct WarpStage {
 };
 
 // Loads items [c0, c0 + n) into the stage; all loads of the chunk are in flight together.
-__device__ __forceinline__ void stage_items(const PaintArgs& a, WarpStage& S, uint32_t c0, uint32_t n, int lane,
-                                            bool with_segments) {
+__device__ __forceinline__ void stage_items(const PaintArgs& a, const PaintProps* __restrict__ props, WarpStage& S,
+                                            uint32_t c0, uint32_t n, int lane, bool with_segments) {
     uint32_t meta = 0, sb = 0, cnt = 0;
     uint64_t carry = 0;
     float4 col = make_float4(0.f, 0.f, 0.f, 0.f);
     if ((uint32_t)lane < n) {
         uint32_t L, fl, g;
-        item_decode(a.items[c0 + lane], a.idx_bits, a.p.geom.n_orders, L, fl, g);
-        const float4* pp = reinterpret_cast<const float4*>(a.p.props + L);
+        item_decode(a.items[c0 + lane], a.idx_bits, a.bg.n_orders, L, fl, g);
+        const float4* pp = reinterpret_cast<const float4*>(props + L);
         const uint4 hdr = *reinterpret_cast<const uint4*>(pp);
         col = pp[1];
         carry = a.tl_carry[g];
@@ -452,23 +444,30 @@ __device__ __forceinline__ void stage_items(const PaintArgs& a, WarpStage& S, ui
 
 __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
     __shared__ WarpStage stages[PAINT_WARPS];
-    const PaintParams& p = a.p;
     const int lane = threadIdx.x & 31;
     WarpStage& S = stages[threadIdx.x >> 5];
-    const uint32_t n_tiles = p.geom.rows * p.geom.row_len;
     const uint32_t t = blockIdx.x * PAINT_WARPS + (threadIdx.x >> 5);
-    if (t >= n_tiles) return;
-    const uint32_t j = t / p.geom.row_len, i = t % p.geom.row_len;
+    if (t >= a.bg.total_tiles) return;
+    // the scene holding global tile t
+    uint32_t lo = 0, hi = a.bg.n_scenes;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a.bg.scenes[mid].tile_base <= t) lo = mid;
+        else hi = mid;
+    }
+    const SceneDesc& p = a.bg.scenes[lo];
+    const uint32_t lt = t - p.tile_base;
+    const uint32_t j = lt / p.row_len, i = lt % p.row_len;
     if (i < p.crop_h0 || i >= p.crop_h1 || j < p.crop_v0 || j >= p.crop_v1) return;
     const uint32_t b = a.tile_start[t], e = a.tile_start[t + 1];
-    const uint32_t n_orders = p.geom.n_orders;
+    const uint32_t n_orders = a.bg.n_orders;
 
     // tile_unchanged_pass (layer_workbench.rs:200-222)
     if (p.prev_layers) {
         const int32_t layers = (int32_t)((e - b) & 0xFFFF);
-        const int32_t old = p.prev_layers[t];
+        const int32_t old = p.prev_layers[lt];
         __syncwarp();
-        if (lane == 0) p.prev_layers[t] = layers;
+        if (lane == 0) p.prev_layers[lt] = layers;
         if (old >= 0 && old == layers) {
             bool all = true;
             for (uint32_t k = b + lane; k < e; k += 32) {
@@ -522,7 +521,7 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
         }
         for (uint32_t c0 = from; c0 < e; c0 += 32) {
             const uint32_t n = min(32u, e - c0);
-            stage_items(a, S, c0, n, lane, false);
+            stage_items(a, p.props, S, c0, n, lane, false);
             for (uint32_t q = 0; q < n; q++) {
                 const float4 col = S.color[q];
                 const uint32_t mode = S.meta[q] & 15u;
@@ -548,7 +547,7 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
         const uint32_t start = k_op >= 0 ? (uint32_t)k_op : b;
         for (uint32_t c0 = start; c0 < e; c0 += 32) {
             const uint32_t n = min(32u, e - c0);
-            stage_items(a, S, c0, n, lane, true);
+            stage_items(a, p.props, S, c0, n, lane, true);
             for (uint32_t q = 0; q < n; q++) {
                 const uint32_t meta = S.meta[q];
                 const uint32_t mode = meta & 15u, fr = (meta >> 4) & 1u;
@@ -625,48 +624,26 @@ cudaError_t launch_tl_heads(int mode, const uint64_t* segs, uint32_t n, uint32_t
 
 uint32_t tl_heads_grid(uint32_t n) { return (n + HEAD_THREADS * HEAD_ITEMS - 1) / (HEAD_THREADS * HEAD_ITEMS); }
 
-cudaError_t launch_tl_reduce_scan(const uint64_t* segs, uint32_t n_segs, uint32_t G, const RenderGeom& geom,
-                                  CarryBuffers& cb, Scratch* s, cudaStream_t st) {
-    (void)n_segs;
-    (void)s;
+cudaError_t launch_tl_reduce_scan(const uint64_t* segs, uint32_t G, const BatchGeom& bg, CarryBuffers& cb,
+                                  cudaStream_t st) {
     if (G == 0) return cudaSuccess;
     count_launches(2);
-    k_tl_reduce<<<(G + 255) / 256, 256, 0, st>>>(segs, G, cb.tl_start, geom.row_len, cb.tl_cover, cb.tl_flags);
+    k_tl_reduce<<<(G + 255) / 256, 256, 0, st>>>(segs, G, cb.tl_start, bg.row_len, cb.tl_cover, cb.tl_flags);
     k_tl_carry<<<(G + 255) / 256, 256, 0, st>>>(G, cb.tl_cover, cb.tl_flags, cb.tl_carry);
     return cudaGetLastError();
 }
 
-static ItemGeom item_geom(const RenderGeom& geom, const PaintParams* pp) {
-    ItemGeom ig;
-    ig.geom = geom;
-    ig.h0 = pp ? pp->crop_h0 : 0;
-    ig.h1 = pp ? pp->crop_h1 : geom.row_len;
-    ig.v0 = pp ? pp->crop_v0 : 0;
-    ig.v1 = pp ? pp->crop_v1 : geom.rows;
-    return ig;
-}
-
-cudaError_t launch_items_crop(int mode, const uint64_t* segs, uint32_t G, const RenderGeom& geom,
-                              const PaintParams& pp, CarryBuffers& cb, int idx_bits, cudaStream_t st) {
+cudaError_t launch_items(int mode, const uint64_t* segs, uint32_t G, const BatchGeom& bg, CarryBuffers& cb,
+                         int idx_bits, cudaStream_t st) {
     if (G == 0) return cudaSuccess;
-    ItemGeom ig = item_geom(geom, &pp);
     count_launches(1);
     if (mode == 0)
-        k_items_count<<<(G + 255) / 256, 256, 0, st>>>(segs, G, cb.tl_start, cb.tl_flags, cb.tl_cover, cb.tl_carry, ig,
-                                                       pp.props, cb.item_count);
+        k_items_count<<<(G + 255) / 256, 256, 0, st>>>(segs, G, cb.tl_start, cb.tl_flags, cb.tl_cover, cb.tl_carry, bg,
+                                                       cb.item_count);
     else
-        k_items_write<<<(G + 255) / 256, 256, 0, st>>>(segs, G, cb.tl_start, cb.tl_flags, cb.tl_cover, cb.tl_carry, ig,
-                                                       pp.props, cb.item_off, idx_bits, cb.items);
+        k_items_write<<<(G + 255) / 256, 256, 0, st>>>(segs, G, cb.tl_start, cb.tl_flags, cb.tl_cover, cb.tl_carry, bg,
+                                                       cb.item_off, idx_bits, cb.items);
     return cudaGetLastError();
-}
-
-cudaError_t launch_items(int mode, const uint64_t* segs, uint32_t G, const RenderGeom& geom, const PaintProps* props,
-                         CarryBuffers& cb, int idx_bits, cudaStream_t st) {
-    PaintParams pp{};
-    pp.props = props;
-    pp.crop_h1 = geom.row_len;
-    pp.crop_v1 = geom.rows;
-    return launch_items_crop(mode, segs, G, geom, pp, cb, idx_bits, st);
 }
 
 cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_tiles, int shift, uint32_t n_orders,
@@ -676,15 +653,12 @@ cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_til
     return cudaGetLastError();
 }
 
-cudaError_t launch_paint(const PaintParams& p, const uint64_t* segs, const uint64_t* items, int idx_bits,
-                         const uint32_t* tile_start, const CarryBuffers& cb, uint32_t warps_per_block,
-                         cudaStream_t st) {
-    uint32_t n_tiles = p.geom.rows * p.geom.row_len;
-    if (n_tiles == 0) return cudaSuccess;
-    (void)warps_per_block;
-    PaintArgs a{p, segs, items, idx_bits, tile_start, cb.tl_start, cb.tl_cover, cb.tl_carry};
+cudaError_t launch_paint(const BatchGeom& bg, const uint64_t* segs, const uint64_t* items, int idx_bits,
+                         const uint32_t* tile_start, const CarryBuffers& cb, cudaStream_t st) {
+    if (bg.total_tiles == 0) return cudaSuccess;
+    PaintArgs a{bg, segs, items, idx_bits, tile_start, cb.tl_start, cb.tl_cover, cb.tl_carry};
     count_launches(1);
-    k_paint<<<(n_tiles + PAINT_WARPS - 1) / PAINT_WARPS, 32 * PAINT_WARPS, 0, st>>>(a);
+    k_paint<<<(bg.total_tiles + PAINT_WARPS - 1) / PAINT_WARPS, 32 * PAINT_WARPS, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -243,6 +243,17 @@ CGB_EXPORT cgb_status cgb_release_buffer_layer_cache(cgb_composition* c, int32_t
 CGB_EXPORT cgb_status cgb_render(cgb_composition* c, const cgb_buffer* buffer,
                                  const float background[4], const cgb_rect* crop);
 
+/* Composition::render for n compositions at once: every scene is built,
+ * rasterized, sorted and painted in one pipeline (one set of launches) on
+ * `ctx`'s stream and scratch buffers; `ctx` may be one of the scenes or an
+ * empty composition.  scenes[k] renders into buffers[k] with background
+ * backgrounds[4k..4k+3] and crop crops[k] (crops may be NULL).  The
+ * reference renders one Composition per call (mold/src/composition.rs:212-329);
+ * each scene's pixels equal its own cgb_render. */
+CGB_EXPORT cgb_status cgb_render_batch(cgb_composition* ctx, size_t n, cgb_composition* const* scenes,
+                                       const cgb_buffer* buffers, const float* backgrounds,
+                                       const cgb_rect* crops);
+
 /* Composition::pixel_segments (mold/src/composition.rs:153-188): the real
  * pixel segments after build + rasterize + sort, copied to the host array
  * `out` (capacity `cap` u64).  `*out_len` receives P even when cap < P (then
