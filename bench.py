@@ -34,12 +34,15 @@ WORKLOADS = {
     "mixed20k": dict(kind="mixed", n_layers=20_000, width=2560, height=1600, seed=2),
     "circles": dict(kind="circles", n_layers=1000, width=1024, height=1024, seed=1),
     "glyphs": dict(kind="glyphs", n_layers=50_000, width=3840, height=2160, seed=3),
+    "batch256": dict(kind="batch", n_scenes=256, seed=4),
 }
 
 
 def make_scene(name):
     from cassia_gb300 import scenes
     w = WORKLOADS[name]
+    if w["kind"] == "batch":
+        raise ValueError("the batch workload has no single scene")
     if w["kind"] == "mixed":
         return scenes.mixed(seed=w["seed"], n_layers=w["n_layers"], width=w["width"], height=w["height"])
     if w["kind"] == "circles":
@@ -115,7 +118,7 @@ class ClockSampler:
 def stage_bytes(st, scene):
     """Algorithmic bytes per stage: each stage reads its input once and
     writes its output once; one sort pass is one read + one write."""
-    L, P, N = st["lines"], st["segments"], scene.n_layers
+    L, P, N = st["lines"], st["segments"], scene.n_layers  # rasterized segments
     return {
         "rasterize": 18 * L + 8 * P,
         "sort": 16 * st["painted_segments"],
@@ -183,6 +186,98 @@ def cpu_reference(scene, steps, warmup, budget_s=150.0):
             "ms_per_step": t * 1e3, "frames_per_s": 1.0 / t}
 
 
+def group_scenes(comps, line_budget=16_000_000):
+    """Consecutive scenes whose lines fit one frame's budget."""
+    groups, cur, lines = [], [], 0
+    for k, c in enumerate(comps):
+        n = c.lens()[0]
+        if cur and lines + n > line_budget:
+            groups.append(cur)
+            cur, lines = [], 0
+        cur.append(k)
+        lines += n
+    if cur:
+        groups.append(cur)
+    return groups
+
+
+def run_batch(args, rank, world, local):
+    """Batched workload: 256 independent scenes (layer count log-U[10, 50,000],
+    canvas side in {256, 512, 1024, 2048}).  Batched = the scenes rendered
+    together, a few pipelines per pass (grouped by a line budget); plain = one
+    render call per scene.  Outputs are compared bit for bit."""
+    import torch
+    from cassia_gb300 import Composition, scenes
+    from cassia_gb300.composition import kernel_launches, render_batch
+    w = WORKLOADS[args.workload]
+    t0 = time.time()
+    sset = scenes.batch(seed=w["seed"] + rank, n_scenes=w["n_scenes"])
+    gen_s = time.time() - t0
+    comps = []
+    for sc in sset:
+        c = Composition(wide=sc.wide)
+        scenes.load(sc, c)
+        comps.append(c)
+    outs_b = [torch.zeros((sc.height, sc.width, 4), dtype=torch.uint8, device="cuda") for sc in sset]
+    outs_p = [torch.zeros_like(o) for o in outs_b]
+    ctx = Composition()
+    groups = group_scenes(comps)
+
+    def batched():
+        for g in groups:
+            render_batch(ctx, [comps[k] for k in g], [outs_b[k].data_ptr() for k in g], [sset[k].width for k in g],
+                         [sset[k].background for k in g], heights=[sset[k].height for k in g])
+
+    def plain():
+        for k, sc in enumerate(sset):
+            comps[k].render(outs_p[k].data_ptr(), sc.width, sc.background, height=sc.height)
+
+    def timed(fn, reps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) / reps
+
+    for _ in range(args.warmup):
+        batched()
+        plain()
+    exact = all(torch.equal(a, b) for a, b in zip(outs_b, outs_p))
+    launches0 = kernel_launches()
+    with ClockSampler(local) as clk:
+        tb = timed(batched, args.steps)
+    launches = kernel_launches() - launches0
+    tp = timed(plain, max(1, args.steps // 2))
+    segs = sum(c.count_segments()[0] for c in comps)
+    # e2e: the same batched pass into pinned host buffers (RGBA8 read back each pass)
+    host = [torch.zeros((sc.height, sc.width, 4), dtype=torch.uint8).pin_memory().numpy() for sc in sset]
+
+    def batched_host():
+        for g in groups:
+            render_batch(ctx, [comps[k] for k in g], [host[k] for k in g], [sset[k].width for k in g],
+                         [sset[k].background for k in g])
+
+    batched_host()
+    te = timed(batched_host, max(1, args.steps // 2))
+    if rank == 0:
+        line = {
+            "metric": "scenes/s", "value": world * len(sset) / tb, "unit": "scenes/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": tb * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+int (fixed point)", "data": "synthetic (seeded)",
+            "config": {"workload": args.workload, "scenes": len(sset), "layers": int(sum(s.n_layers for s in sset)),
+                       "frames_per_pass": len(groups), "segments_per_pass": int(segs),
+                       "l2": "inputs larger than L2"},
+            "plain_scenes_per_s": world * len(sset) / tp, "plain_ms_per_pass": tp * 1e3,
+            "speedup_vs_plain": tp / tb, "bit_exact_batched_vs_plain": bool(exact),
+            "e2e": {"value": world * len(sset) / te, "unit": "scenes/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": int(sum(s.width * s.height * 4 for s in sset)), "ms_per_step": te * 1e3},
+            "gpu_launches": launches, "clocks": clk.summary(), "setup_s": {"scene_gen": gen_s},
+        }
+        print(json.dumps(line))
+    return 0
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -231,6 +326,11 @@ def main():
         return rc
 
     torch.cuda.set_device(local)
+    if WORKLOADS[args.workload]["kind"] == "batch":
+        rc = run_batch(args, rank, world, local)
+        if dist:
+            dist.destroy_process_group()
+        return rc
     from cassia_gb300 import Composition, scenes
     from cassia_gb300.composition import kernel_launches
 
@@ -242,6 +342,10 @@ def main():
     scenes.load(scene, comp)
     load_s = time.time() - t0
     H, W = scene.height, scene.width
+    # The reference rasterizes every line of the frame; render mode skips lines
+    # whose segments cannot reach the canvas.  The metric counts the
+    # reference's segments, counted once here.
+    ref_segments, _ = comp.count_segments()
     out = torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda")
     stream = torch.cuda.ExternalStream(comp.stream())
 
@@ -274,7 +378,7 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms_step = float(t.item())
     st = stats[-1]
-    segs = st["segments"]
+    segs = ref_segments
     value = world * segs / (ms_step / 1e3) / 1e6
 
     # stage times (device events on the launching stream), averaged over the timed steps
@@ -322,7 +426,7 @@ def main():
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             e2e_s = float(t.item())
         h2d = scene.n_layers * (6 * 4)
-        e2e = {"value": world * comp.stats()["segments"] / e2e_s / 1e6, "unit": "Msegments/s",
+        e2e = {"value": world * segs / e2e_s / 1e6, "unit": "Msegments/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": W * H * 4, "ms_per_step": e2e_s * 1e3}
 
     cpu = None
@@ -340,6 +444,7 @@ def main():
             "vs_baseline": None, "dtype": "f32+int (fixed point)", "data": "synthetic (seeded)",
             "config": {"workload": args.workload, "canvas": [W, H], "layers": scene.n_layers,
                        "lines": st["lines"], "segments_per_frame": segs,
+                       "segments_rasterized": st["segments"],
                        "painted_segments": st["painted_segments"], "tile_layers": st["tile_layers"],
                        "work_items": st["work_items"],
                        "segment_format": "wide (17-bit layer)" if scene.wide else "reference u16",

@@ -198,6 +198,15 @@ class Composition:
         _check(self._lib, st, "render")
         return pixels
 
+    def count_segments(self):
+        """Real pixel segments the reference's rasterizer emits for the current
+        scene (Composition::pixel_segments without the copy), and its NONE count."""
+        n, none = ctypes.c_uint64(), ctypes.c_uint64()
+        st = self._lib.cgb_pixel_segments(self._h, None, 0, ctypes.byref(n), ctypes.byref(none), abi.SORT_KEY)
+        if st not in (abi.OK, abi.ERR_CAPACITY):
+            _check(self._lib, st, "pixel_segments")
+        return n.value, none.value
+
     def pixel_segments(self, canonical: bool = True):
         """Composition::pixel_segments: (sorted real segments, NONE count)."""
         n, none = ctypes.c_uint64(), ctypes.c_uint64()

@@ -215,7 +215,8 @@ cudaError_t launch_flatten(int write, const uint32_t* kinds, const float* points
                            const uint64_t* pt_off, const float* transforms9, const uint8_t* has_t,
                            const uint32_t* path_layer, uint32_t n_paths, uint32_t* counts, const uint32_t* out_off,
                            float* p0x, float* p0y, float* p1x, float* p1y, uint32_t* lids, cudaStream_t st);
-cudaError_t launch_build_lines(const BatchGeom& bg, LineRec* recs, uint32_t* lengths, cudaStream_t st);
+// cull != 0 (render mode) drops lines whose segments the painter never reads.
+cudaError_t launch_build_lines(const BatchGeom& bg, int cull, LineRec* recs, uint32_t* lengths, cudaStream_t st);
 // mode: 0 = count, 1 = write.  render != 0: culled, re-keyed render format;
 // else the reference segment format of the (single) scene.
 cudaError_t launch_rasterize(int mode, int render, const BatchGeom& bg, const LineRec* recs, const uint32_t* step_off,

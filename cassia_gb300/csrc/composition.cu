@@ -491,7 +491,7 @@ cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& 
     CK(c->s.ensure(c->lengths, std::max<size_t>(L, 1) * 4));
     CK(c->s.ensure(c->step_off, ((size_t)L + 1) * 4));
     CK(cudaEventRecord(c->ev[0], st));
-    CK(launch_build_lines(bg, c->recs.as<LineRec>(), c->lengths.as<uint32_t>(), st));
+    CK(launch_build_lines(bg, render, c->recs.as<LineRec>(), c->lengths.as<uint32_t>(), st));
     uint64_t S = 0;
     CK(scan_u32(c->lengths.as<uint32_t>(), c->step_off.as<uint32_t>(), L, &c->s, st, &S));
     CK(cudaEventRecord(c->ev[1], st));

@@ -308,7 +308,7 @@ __device__ __forceinline__ uint32_t scene_of_line(const uint64_t* base, uint32_t
     return lo;
 }
 
-__global__ void k_build_lines(BatchGeom bg, LineRec* __restrict__ recs, uint32_t* __restrict__ lengths) {
+__global__ void k_build_lines(BatchGeom bg, int cull, LineRec* __restrict__ recs, uint32_t* __restrict__ lengths) {
     __shared__ uint64_t s_base[MAX_SMEM_SCENES];
     const uint32_t ns = min(bg.n_scenes, (uint32_t)MAX_SMEM_SCENES);
     for (uint32_t k = threadIdx.x; k < ns; k += blockDim.x) s_base[k] = bg.scenes[k].line_base;
@@ -357,7 +357,20 @@ __global__ void k_build_lines(BatchGeom bg, LineRec* __restrict__ recs, uint32_t
         }
         int32_t p0x_sub = to_sub_pixel(p0x), p0y_sub = to_sub_pixel(p0y);
         int32_t p1x_sub = to_sub_pixel(p1x), p1y_sub = to_sub_pixel(p1y);
-        if (p0y_sub != p1y_sub) {
+        // Render mode: a line wholly above, below or right of the canvas (with
+        // a pixel of margin for rounding) yields only segments the painter
+        // never reads, unless the 12-bit tile_j / 13-bit tile_i fields could
+        // wrap back into the canvas (|y| >= 16,384 px, x >= 30,720 px).
+        bool off_canvas = false;
+        if (cull) {
+            const int32_t ymin = min(p0y_sub, p1y_sub), ymax = max(p0y_sub, p1y_sub);
+            const int32_t xmin = min(p0x_sub, p1x_sub), xmax = max(p0x_sub, p1x_sub);
+            const int32_t lim_y = 16384 * PIXEL_WIDTH, lim_x = 30720 * PIXEL_WIDTH;
+            off_canvas = (ymax < -PIXEL_WIDTH && ymin > -lim_y) ||
+                         (ymin >= (int32_t)(S.rows * 8 + 1) * PIXEL_WIDTH && ymax < lim_y) ||
+                         (xmin >= (int32_t)(S.row_len * 8 + 1) * PIXEL_WIDTH && xmax < lim_x);
+        }
+        if (p0y_sub != p1y_sub && !off_canvas) {
             int32_t dx = wsub(p1x_sub, p0x_sub), dy = wsub(p1y_sub, p0y_sub);
             bool dx_dy = wabs(dx) > wabs(dy);
             bool sum_0 = wadd(dx, dy) > 0 || (dx == wsub(0, dy) && dx < dy);
@@ -615,11 +628,11 @@ cudaError_t launch_flatten(int write, const uint32_t* kinds, const float* points
     return cudaGetLastError();
 }
 
-cudaError_t launch_build_lines(const BatchGeom& bg, LineRec* recs, uint32_t* lengths, cudaStream_t st) {
+cudaError_t launch_build_lines(const BatchGeom& bg, int cull, LineRec* recs, uint32_t* lengths, cudaStream_t st) {
     if (bg.total_lines == 0) return cudaSuccess;
     if (bg.n_scenes > MAX_SMEM_SCENES) return cudaErrorInvalidValue;
     count_launches(1);
-    k_build_lines<<<(uint32_t)((bg.total_lines + 255) / 256), 256, 0, st>>>(bg, recs, lengths);
+    k_build_lines<<<(uint32_t)((bg.total_lines + 255) / 256), 256, 0, st>>>(bg, cull, recs, lengths);
     return cudaGetLastError();
 }
 

@@ -101,6 +101,14 @@ def _assemble(name, width, height, background, wide, n_layers, per_path_kinds, p
                  np.asarray(blend_mode, np.uint32), np.asarray(color, np.float32), meta or {})
 
 
+def _flat_scene(name, width, height, wide, n_layers, geo, transforms, fill_rule, blend_mode, color):
+    """A scene with one path per layer from already-flattened command arrays."""
+    kinds, points, cmd_off, pt_off = geo
+    return Scene(name, width, height, (1.0, 1.0, 1.0, 1.0), wide, n_layers, np.arange(n_layers, dtype=np.uint32),
+                 cmd_off, kinds, pt_off, points, transforms, np.asarray(fill_rule, np.uint32),
+                 np.asarray(blend_mode, np.uint32), np.asarray(color, np.float32))
+
+
 def _polygon_path(xs, ys):
     """Closed polygon as LINE commands plus CLOSE."""
     n = len(xs)
@@ -160,34 +168,52 @@ def _mixed_geometry(rng_tag_seed, n_layers, width, height):
     nc = 4 + np.minimum((C[:, 0] * 9).astype(np.int64), 8)
     box = np.exp(np.log(4.0) + C[:, 1] * (np.log(300.0) - np.log(4.0)))
 
-    kinds, points = [], []
-    for i in range(n_layers):
-        if is_poly[i]:
-            n = int(nv[i])
-            jit = V[i, 4:4 + n]
-            ang = (np.arange(n) + 0.8 * jit) * (2.0 * np.pi / n)
-            rr = np.full(n, radius[i])
-            if star[i]:
-                rr[1::2] *= inner[i]
-            k, p = _polygon_path((rr * np.cos(ang)).astype(np.float32), (rr * np.sin(ang)).astype(np.float32))
-        else:
-            n = int(nc[i])
-            half = box[i] / 2.0
-            # anchors on a loop around the origin, controls anywhere in the box
-            a_ang = (np.arange(n) + 0.5 * C[i, 2:2 + n]) * (2.0 * np.pi / n)
-            a_r = half * (0.5 + 0.5 * C[i, 14:14 + n])
-            ax, ay = a_r * np.cos(a_ang), a_r * np.sin(a_ang)
-            ctl = (C[i, 26:26 + 4 * n].reshape(n, 4) * 2.0 - 1.0) * half
-            pts = np.empty((n, 8), np.float64)
-            pts[:, 0], pts[:, 1] = ax, ay
-            pts[:, 2:6] = ctl
-            pts[:, 6], pts[:, 7] = np.roll(ax, -1), np.roll(ay, -1)
-            k = np.full(n + 1, abi.CMD_CUBIC, np.uint32)
-            k[-1] = abi.CMD_CLOSE
-            p = pts.astype(np.float32).reshape(-1)
-        kinds.append(k)
-        points.append(p)
-    return kinds, points, transforms, fill_rule, blend, color
+    # per-layer command / float counts, then every polygon and every cubic
+    # loop written at its layer's offsets (padded to 32 vertices / 12 cubics)
+    n_cmd = np.where(is_poly, nv + 1, nc + 1).astype(np.int64)
+    n_flt = np.where(is_poly, nv * 4, nc * 8).astype(np.int64)
+    cmd_off = np.concatenate([[0], np.cumsum(n_cmd)])
+    pt_off = np.concatenate([[0], np.cumsum(n_flt)])
+    kinds = np.empty(int(cmd_off[-1]), np.uint32)
+    points = np.empty(int(pt_off[-1]), np.float32)
+
+    P = np.nonzero(is_poly)[0]
+    if len(P):
+        n = nv[P][:, None]
+        k = np.arange(32)[None, :]
+        mask = k < n
+        ang = (k + 0.8 * V[P, 4:36]) * (2.0 * np.pi / n)
+        rr = radius[P][:, None] * np.where(star[P][:, None] & (k % 2 == 1), inner[P][:, None], 1.0)
+        x = (rr * np.cos(ang)).astype(np.float32)
+        y = (rr * np.sin(ang)).astype(np.float32)
+        nxt = (k + 1) % n
+        seg = np.stack([x, y, np.take_along_axis(x, nxt, 1), np.take_along_axis(y, nxt, 1)], -1)
+        dst = (pt_off[P][:, None] + 4 * k)[mask]
+        points[(dst[:, None] + np.arange(4)[None, :]).reshape(-1)] = seg[mask].reshape(-1)
+        kinds[(cmd_off[P][:, None] + k)[mask]] = abi.CMD_LINE
+        kinds[cmd_off[P] + nv[P]] = abi.CMD_CLOSE
+    Q = np.nonzero(~is_poly)[0]
+    if len(Q):
+        n = nc[Q][:, None]
+        k = np.arange(12)[None, :]
+        mask = k < n
+        half = (box[Q] / 2.0)[:, None]
+        a_ang = (k + 0.5 * C[Q, 2:14]) * (2.0 * np.pi / n)
+        a_r = half * (0.5 + 0.5 * C[Q, 14:26])
+        ax, ay = a_r * np.cos(a_ang), a_r * np.sin(a_ang)
+        ctl = (C[Q, 26:74].reshape(-1, 12, 4) * 2.0 - 1.0) * half[:, :, None]
+        nxt = (k + 1) % n
+        pts = np.empty((len(Q), 12, 8), np.float64)
+        pts[..., 0], pts[..., 1] = ax, ay
+        pts[..., 2:6] = ctl
+        pts[..., 6], pts[..., 7] = np.take_along_axis(ax, nxt, 1), np.take_along_axis(ay, nxt, 1)
+        pts = pts.astype(np.float32)
+        dst = (pt_off[Q][:, None] + 8 * k)[mask]
+        points[(dst[:, None] + np.arange(8)[None, :]).reshape(-1)] = pts[mask].reshape(-1)
+        kinds[(cmd_off[Q][:, None] + k)[mask]] = abi.CMD_CUBIC
+        kinds[cmd_off[Q] + nc[Q]] = abi.CMD_CLOSE
+    geo = (kinds, points, cmd_off.astype(np.uint64), pt_off.astype(np.uint64))
+    return geo, transforms, fill_rule, blend, color
 
 
 def mixed(seed: int = 2, n_layers: int = 100_000, width: int = 2560, height: int = 1600) -> Scene:
@@ -195,9 +221,8 @@ def mixed(seed: int = 2, n_layers: int = 100_000, width: int = 2560, height: int
     4-12-cubic paths (40%), random affine, NonZero/EvenOdd 50/50, blend mode
     uniform over the 12 modes, alpha U[0.2,1], white background.  More than
     65,536 layers selects the widened (17-bit layer) segment format."""
-    kinds, points, transforms, fr, bm, color = _mixed_geometry(seed, n_layers, width, height)
-    return _assemble(f"mixed{n_layers}", width, height, (1.0, 1.0, 1.0, 1.0), n_layers > 65536, n_layers, kinds,
-                     points, np.arange(n_layers), transforms, fr, bm, color)
+    geo, transforms, fr, bm, color = _mixed_geometry(seed, n_layers, width, height)
+    return _flat_scene(f"mixed{n_layers}", width, height, n_layers > 65536, n_layers, geo, transforms, fr, bm, color)
 
 
 def glyphs(seed: int = 3, n_layers: int = 50_000, width: int = 3840, height: int = 2160,
@@ -262,9 +287,8 @@ def batch(seed: int = 4, n_scenes: int = 256, max_layers: int = 50_000) -> List[
     for s in range(n_scenes):
         n = int(np.exp(np.log(10.0) + U[s, 0] * (np.log(max_layers) - np.log(10.0))))
         side = (256, 512, 1024, 2048)[min(int(U[s, 1] * 4), 3)]
-        kinds, points, tr, fr, bm, color = _mixed_geometry(seed * 1000003 + s, n, side, side)
-        out.append(_assemble(f"batch{s}", side, side, (1.0, 1.0, 1.0, 1.0), False, n, kinds, points,
-                             np.arange(n), tr, fr, bm, color))
+        geo, tr, fr, bm, color = _mixed_geometry(seed * 1000003 + s, n, side, side)
+        out.append(_flat_scene(f"batch{s}", side, side, False, n, geo, tr, fr, bm, color))
     return out
 
 
