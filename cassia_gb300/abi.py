@@ -141,6 +141,7 @@ def _declare(lib):
         "cgb_composition_new": ([u32, u64, P(vp)], i32),
         "cgb_composition_free": ([handle], i32),
         "cgb_create_layer": ([handle, P(u32)], i32),
+        "cgb_create_layers": ([handle, sz, P(u32)], i32),
         "cgb_insert_in_layer": ([handle, u32, P(u32), sz, fp, sz, fp], i32),
         "cgb_insert_paths": ([handle, sz, P(u32), P(u64), P(u32), P(u64), fp, fp, P(ctypes.c_uint8)], i32),
         "cgb_insert_lines": ([handle, u32, fp, sz], i32),
@@ -150,6 +151,7 @@ def _declare(lib):
         "cgb_layer_set_props": ([handle, u32, P(CgbProps)], i32),
         "cgb_layers_set_transforms": ([handle, sz, P(u32), fp, u32], i32),
         "cgb_layers_set_props": ([handle, sz, P(u32), P(CgbProps)], i32),
+        "cgb_layers_set_enabled": ([handle, sz, P(u32), P(ctypes.c_uint8)], i32),
         "cgb_remove_disabled": ([handle], i32),
         "cgb_lines_len": ([handle, P(u64), P(u64)], i32),
         "cgb_create_buffer_layer_cache": ([handle, P(i32)], i32),

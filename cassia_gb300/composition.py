@@ -107,6 +107,11 @@ class Composition:
         st = self._lib.cgb_create_layer(self._h, ctypes.byref(out))
         return None if st else out.value
 
+    def create_layers(self, n: int) -> np.ndarray:
+        out = np.zeros(max(n, 1), np.uint32)
+        _check(self._lib, self._lib.cgb_create_layers(self._h, n, _u32p(out)), "create_layers")
+        return out[:n]
+
     def insert_in_layer(self, layer_id: int, path: Path, transform9=None):
         k, p = path.c_arrays()
         st = self._lib.cgb_insert_in_layer(self._h, layer_id, k, len(path.kinds), p, len(path.points),
@@ -131,6 +136,13 @@ class Composition:
 
     def set_enabled(self, layer_id: int, enabled: bool):
         _check(self._lib, self._lib.cgb_layer_set_enabled(self._h, layer_id, int(bool(enabled))), "set_enabled")
+
+    def set_enabled_many(self, ids, enabled):
+        ids = np.ascontiguousarray(ids, np.uint32)
+        en = np.ascontiguousarray(enabled, np.uint8)
+        st = self._lib.cgb_layers_set_enabled(self._h, len(ids), _u32p(ids),
+                                              en.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+        _check(self._lib, st, "set_enabled_many")
 
     def set_transform(self, layer_id: int, affine6, unchecked: bool = False):
         st = self._lib.cgb_layer_set_transform(self._h, layer_id, transform_array(affine6, 6),

@@ -99,7 +99,7 @@ struct cgb_composition {
     bool wide = false;
     uint32_t max_ids = 1u << 16;
     Scratch s;
-    cgb_tuning tuning{8, 256, 2048, 4};
+    cgb_tuning tuning{9, 256, 2048, 4};
     cgb_stats stats{};
 
     // LinesBuilder (device SoA)
@@ -850,6 +850,15 @@ CGB_EXPORT cgb_status cgb_create_layer(cgb_composition* c, uint32_t* out_layer_i
     return CGB_OK;
 }
 
+CGB_EXPORT cgb_status cgb_create_layers(cgb_composition* c, size_t n, uint32_t* out_layer_ids) {
+    if (!c || (n && !out_layer_ids)) return fail(CGB_ERR_INVALID_ARG, "null argument");
+    for (size_t i = 0; i < n; i++) {
+        cgb_status st = cgb_create_layer(c, out_layer_ids + i);
+        if (st) return st;
+    }
+    return CGB_OK;
+}
+
 CGB_EXPORT cgb_status cgb_insert_in_layer(cgb_composition* c, uint32_t layer_id, const uint32_t* kinds,
                                           size_t n_cmds, const float* points, size_t n_point_floats,
                                           const float* transform9) {
@@ -978,6 +987,16 @@ CGB_EXPORT cgb_status cgb_layer_set_props(cgb_composition* c, uint32_t layer_id,
         l->unchanged = 0;
         l->props = hp;
         c->props_dirty = true;
+    }
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_layers_set_enabled(cgb_composition* c, size_t n, const uint32_t* layer_ids,
+                                             const uint8_t* enabled) {
+    if (!c || (n && (!layer_ids || !enabled))) return fail(CGB_ERR_INVALID_ARG, "null argument");
+    for (size_t i = 0; i < n; i++) {
+        cgb_status st = cgb_layer_set_enabled(c, layer_ids[i], enabled[i]);
+        if (st) return st;
     }
     return CGB_OK;
 }
@@ -1113,7 +1132,7 @@ CGB_EXPORT cgb_status cgb_get_stats(cgb_composition* c, cgb_stats* out) {
 CGB_EXPORT cgb_status cgb_set_tuning(cgb_composition* c, const cgb_tuning* t) {
     if (!c || !t) return fail(CGB_ERR_INVALID_ARG, "null argument");
     if (t->radix_bits) {
-        if (t->radix_bits < 4 || t->radix_bits > 8) return fail(CGB_ERR_INVALID_ARG, "radix_bits must be 4..8");
+        if (t->radix_bits < 4 || t->radix_bits > 9) return fail(CGB_ERR_INVALID_ARG, "radix_bits must be 4..9");
         c->tuning.radix_bits = t->radix_bits;
     }
     if (t->raster_block) {

@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const uint32_t* __r
 // radix sort
 // ---------------------------------------------------------------------------
 
-constexpr int RADIX = 256;
+constexpr int RADIX = 512;  // up to 9-bit digits: one digit per thread of a sort CTA
 constexpr int MAX_PASSES = 11;
 constexpr int SORT_THREADS = 512;
 constexpr int SORT_WARPS = SORT_THREADS / 32;
@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(512) k_radix_hist(const uint64_t* __restrict__
     }
 }
 
-// Exclusive scan of each pass's 256 bins (one CTA of 256 threads per pass).
+// Exclusive scan of each pass's RADIX bins (one CTA of RADIX threads per pass).
 __global__ void __launch_bounds__(RADIX) k_radix_hist_scan(uint32_t* hist) {
     uint32_t* h = hist + blockIdx.x * RADIX;
     uint32_t v = h[threadIdx.x];
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(const uint64_t* __res
     __shared__ uint32_t s_count[RADIX];
     __shared__ uint32_t s_start[RADIX];
     __shared__ uint32_t s_base[RADIX];
-    __shared__ uint64_t s_keys[SORT_TILE];
+    extern __shared__ uint64_t s_keys[];  // SORT_TILE keys (dynamic: the CTA needs > 48 KB)
     __shared__ uint32_t s_tile;
     __shared__ uint32_t s_abort;
 
@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(const uint64_t* __res
         }
         s_base[d] = global_off[d] + excl;
     }
-    // Tile-local digit starts: exclusive scan of s_count over the 256 digits.
+    // Tile-local digit starts: exclusive scan of s_count over the RADIX digits.
     {
         uint32_t v = tid < RADIX ? s_count[tid] : 0;
         uint32_t ex = block_exclusive_scan<uint32_t>(v, nullptr);
@@ -314,6 +314,24 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(const uint64_t* __res
         uint32_t pos = s_base[d] + (i - s_start[d]);
         if (pos < n) out[pos] = k;
     }
+}
+
+constexpr size_t ONESWEEP_DYN_SMEM = SORT_TILE * sizeof(uint64_t);
+
+// Opts the onesweep kernel into its dynamic shared memory (once per device).
+cudaError_t onesweep_setup() {
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= 64) return e != cudaSuccess ? e : cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!done[dev]) {
+        e = cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ONESWEEP_DYN_SMEM);
+        if (e != cudaSuccess) return e;
+        done[dev] = true;
+    }
+    return cudaSuccess;
 }
 
 }  // namespace
@@ -350,7 +368,7 @@ cudaError_t scan_block_counts(const uint32_t* counts, uint32_t* offsets, uint32_
 static PassPlan make_plan(int bit_lo, int bit_hi, int digit_bits) {
     PassPlan p{};
     int bits = std::max(0, bit_hi - bit_lo);
-    digit_bits = std::min(8, std::max(1, digit_bits));
+    digit_bits = std::min(9, std::max(1, digit_bits));
     p.n = (bits + digit_bits - 1) / digit_bits;
     if (p.n > MAX_PASSES) p.n = MAX_PASSES;
     int sh = bit_lo;
@@ -377,7 +395,8 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo
     if (n <= 1 || plan.n == 0) return cudaSuccess;
     if (n >= ST_VAL) return cudaErrorInvalidValue;
     uint32_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
-    cudaError_t e;
+    cudaError_t e = onesweep_setup();
+    if (e != cudaSuccess) return e;
     if ((e = s->ensure(s->sort_hist, (size_t)MAX_PASSES * RADIX * 4)) != cudaSuccess) return e;
     if ((e = s->ensure(s->sort_lookback, (size_t)tiles * RADIX * 4)) != cudaSuccess) return e;
     if ((e = s->ensure(s->sort_counter, MAX_PASSES * 4)) != cudaSuccess) return e;
@@ -397,8 +416,8 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo
     uint64_t* dst = tmp;
     for (int p = 0; p < plan.n; p++) {
         if ((e = cudaMemsetAsync(lb, 0, (size_t)tiles * RADIX * 4, st)) != cudaSuccess) return e;
-        k_onesweep<<<tiles, SORT_THREADS, 0, st>>>(src, dst, n, plan.shift[p], plan.bits[p], hist + p * RADIX, lb,
-                                                   ctr + p, err_flag);
+        k_onesweep<<<tiles, SORT_THREADS, ONESWEEP_DYN_SMEM, st>>>(src, dst, n, plan.shift[p], plan.bits[p],
+                                                                   hist + p * RADIX, lb, ctr + p, err_flag);
         std::swap(src, dst);
     }
     *result = src;
@@ -476,11 +495,12 @@ extern "C" CGB_EXPORT cgb_status cgb_sort_keys_noalloc(uint64_t* keys, uint64_t*
     }
     uint32_t* scratch = nullptr;
     if (noalloc_scratch(&scratch) != cudaSuccess) return CGB_ERR_DEVICE;
+    if (onesweep_setup() != cudaSuccess) return CGB_ERR_DEVICE;
     uint32_t* hist = scratch;
     uint32_t* ctr = scratch + NOALLOC_CTR_OFF;
     uint32_t* err = scratch + NOALLOC_ERR_OFF;
     uint32_t* lb = scratch + NOALLOC_LB_OFF;
-    const PassPlan plan = make_plan((int)bit_lo, (int)bit_hi, 8);
+    const PassPlan plan = make_plan((int)bit_lo, (int)bit_hi, 9);
     const uint32_t nn = (uint32_t)n;
     const uint32_t tiles = (nn + SORT_TILE - 1) / SORT_TILE;
     cudaError_t e = cudaMemsetAsync(scratch, 0, (size_t)NOALLOC_LB_OFF * 4, st);  // hist, counters, error flag
@@ -499,8 +519,8 @@ extern "C" CGB_EXPORT cgb_status cgb_sort_keys_noalloc(uint64_t* keys, uint64_t*
     for (int p = 0; p < plan.n && e == cudaSuccess; p++) {
         e = cudaMemsetAsync(lb, 0, (size_t)tiles * RADIX * 4, st);
         if (e != cudaSuccess) break;
-        k_onesweep<<<tiles, SORT_THREADS, 0, st>>>(src, dst, nn, plan.shift[p], plan.bits[p], hist + p * RADIX, lb,
-                                                   ctr + p, err);
+        k_onesweep<<<tiles, SORT_THREADS, ONESWEEP_DYN_SMEM, st>>>(src, dst, nn, plan.shift[p], plan.bits[p],
+                                                                   hist + p * RADIX, lb, ctr + p, err);
         e = cudaGetLastError();
         std::swap(src, dst);
     }

@@ -1,0 +1,286 @@
+"""A render server with continuous batching over resident compositions.
+
+Each client owns a Composition whose lines, layer table and styles stay
+resident on the GPU between frames.  A request asks for a client's next
+frame after a seeded update of its scene (new affine transforms for a share
+of its layers, a few layers added or removed).  Worker threads form batches
+of ready requests -- at most one per client, oldest first, admitted while the
+estimated device memory of the batch fits the HBM budget -- and render each
+batch in one pipeline (cgb_render_batch) on the worker's own stream, so a
+batch that arrives while another is on the GPU overlaps it on the device.
+
+The reference renders one Composition per call and has no server
+(mold/src/composition.rs:212-329); this module is the serving pattern built
+on the batched pipeline.  `mode="plain"` serves the same requests one render
+call at a time for comparison.
+"""
+import collections
+import threading
+import time
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional
+
+import numpy as np
+
+from . import scenes
+from .composition import Composition, render_batch
+
+
+@dataclass
+class Request:
+    client: int
+    seq: int
+    arrival: float  # seconds after the start of the run
+    t_start: float = 0.0
+    t_render: float = 0.0  # render call start (after the scene update)
+    t_done: float = 0.0
+    batch_size: int = 0
+
+
+@dataclass
+class Client:
+    comp: Composition
+    scene: scenes.Scene
+    out: object                 # device RGBA8 tensor (torch) or host numpy array
+    enabled: np.ndarray         # bool per layer id
+    transforms: np.ndarray      # float32 [n, 6]
+    est_bytes: int = 0          # estimated frame scratch of the last frame
+    done_seq: int = -1
+    pool: Optional[scenes.Scene] = None  # shapes new layers are drawn from
+    pool_next: int = 0
+
+
+def poisson_arrivals(rate: float, n_clients: int, duration: float, seed: int = 0) -> List[Request]:
+    """Poisson arrivals at `rate` requests/s over `duration` seconds, each for a
+    uniformly chosen client; per-client sequence numbers in arrival order."""
+    rng = np.random.default_rng(seed)
+    t, out, seq = 0.0, [], collections.Counter()
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration:
+            break
+        c = int(rng.integers(n_clients))
+        out.append(Request(c, seq[c], t))
+        seq[c] += 1
+    return out
+
+
+def make_clients(n_clients: int, seed: int, device_out: bool = True, max_layers: int = 50_000):
+    """Clients with compositions drawn from the batched-workload distribution."""
+    import torch
+    sset = scenes.batch(seed=seed, n_scenes=n_clients, max_layers=max_layers)
+    clients = []
+    for k, sc in enumerate(sset):
+        c = Composition(wide=sc.wide)
+        scenes.load(sc, c)
+        if device_out:
+            out = torch.zeros((sc.height, sc.width, 4), dtype=torch.uint8, device="cuda")
+        else:
+            out = np.zeros((sc.height, sc.width, 4), np.uint8)
+        pool = scenes.mixed(seed=seed * 7919 + k, n_layers=256, width=sc.width, height=sc.height)
+        clients.append(Client(c, sc, out, np.ones(sc.n_layers, bool), sc.transforms.copy(), pool=pool))
+    return clients
+
+
+def apply_update(cl: Client, client_id: int, seq: int, changed: float = 0.2, churn: float = 0.01):
+    """The scene update of frame `seq`: `changed` of the enabled layers get a
+    new affine (seeded), `churn` of them are removed and as many added."""
+    rng = np.random.default_rng((client_id << 32) ^ (seq * 2654435761 % (1 << 32)))
+    live = np.nonzero(cl.enabled)[0]
+    if len(live) == 0:
+        return
+    n_chg = max(1, int(round(changed * len(live))))
+    ids = rng.choice(live, size=min(n_chg, len(live)), replace=False).astype(np.uint32)
+    t = cl.transforms[ids]
+    th = rng.uniform(-0.05, 0.05, size=len(ids)).astype(np.float32)
+    c, s = np.cos(th), np.sin(th)
+    a, b, cc, d = t[:, 0].copy(), t[:, 1].copy(), t[:, 2].copy(), t[:, 3].copy()
+    t[:, 0], t[:, 1] = c * a - s * cc, c * b - s * d
+    t[:, 2], t[:, 3] = s * a + c * cc, s * b + c * d
+    t[:, 4] += rng.uniform(-3, 3, size=len(ids)).astype(np.float32)
+    t[:, 5] += rng.uniform(-3, 3, size=len(ids)).astype(np.float32)
+    cl.transforms[ids] = t
+    cl.comp.set_transforms(ids, t)
+    n_churn = int(churn * len(live))
+    if n_churn:
+        gone = rng.choice(live, size=n_churn, replace=False).astype(np.uint32)
+        cl.comp.set_enabled_many(gone, np.zeros(len(gone), np.uint8))
+        cl.enabled[gone] = False
+        add_layers(cl, n_churn)
+
+
+def add_layers(cl: Client, n: int):
+    """Adds n layers drawn from the client's shape pool (one insert call)."""
+    p = cl.pool
+    ids = cl.comp.create_layers(n)
+    picks = (cl.pool_next + np.arange(n)) % p.n_layers
+    cl.pool_next += n
+    kinds = [p.path(k)[0] for k in picks]
+    pts = [p.path(k)[1] for k in picks]
+    co = np.concatenate([[0], np.cumsum([len(k) for k in kinds])]).astype(np.uint64)
+    po = np.concatenate([[0], np.cumsum([len(x) for x in pts])]).astype(np.uint64)
+    sub = scenes.Scene("add", p.width, p.height, p.background, p.wide, len(ids), ids, co,
+                       np.concatenate(kinds).astype(np.uint32), po, np.concatenate(pts).astype(np.float32))
+    cl.comp.insert_paths(sub)
+    cl.comp.set_layers_solid(ids, p.fill_rule[picks], p.blend_mode[picks], p.color[picks])
+    cl.comp.set_transforms(ids, p.transforms[picks])
+    top = int(ids.max()) + 1
+    if top > len(cl.enabled):
+        grow = top - len(cl.enabled)
+        cl.enabled = np.concatenate([cl.enabled, np.zeros(grow, bool)])
+        cl.transforms = np.concatenate([cl.transforms, np.zeros((grow, 6), np.float32)])
+    cl.enabled[ids] = True
+    cl.transforms[ids] = p.transforms[picks]
+
+
+def frame_bytes(st: dict) -> int:
+    """Device scratch a frame of this size holds (segments, groups, items)."""
+    return int(16 * st.get("segments", 0) + 36 * st.get("tile_layers", 0) + 16 * st.get("work_items", 0) +
+               40 * st.get("lines", 0))
+
+
+class Server:
+    def __init__(self, clients: List[Client], mode: str = "batched", workers: int = 2, max_batch: int = 16,
+                 hbm_budget: float = 40e9):
+        assert mode in ("batched", "plain")
+        self.clients = clients
+        self.mode = mode
+        self.workers = 1 if mode == "plain" else workers
+        self.max_batch = 1 if mode == "plain" else max_batch
+        self.budget = hbm_budget
+        self.ctx = [Composition() for _ in range(self.workers)] if mode == "batched" else []
+        self.cv = threading.Condition()
+        self.pending: Dict[int, collections.deque] = collections.defaultdict(collections.deque)
+        self.busy = set()
+        self.inflight_bytes = 0
+        self.errors: List[BaseException] = []
+
+    def _ready_batch(self, now):
+        """Oldest-first ready requests, one per idle client, within the budget."""
+        heads = [(q[0].arrival, c) for c, q in self.pending.items() if q and c not in self.busy and q[0].arrival <= now]
+        heads.sort()
+        batch, mem = [], 0
+        for _, c in heads:
+            est = max(self.clients[c].est_bytes, 1 << 20)
+            # admit while the batch fits beside the batches in flight; a
+            # request that fits nowhere runs alone once nothing is in flight
+            if self.inflight_bytes + mem + est > self.budget and (batch or self.inflight_bytes > 0):
+                continue
+            batch.append(self.pending[c].popleft())
+            mem += est
+            if len(batch) >= self.max_batch:
+                break
+        return batch, mem
+
+    def _worker(self, wid, t0, total):
+        while True:
+            with self.cv:
+                while True:
+                    if self.completed >= total or self.errors:
+                        return
+                    now = time.perf_counter() - t0
+                    batch, mem = self._ready_batch(now)
+                    if batch:
+                        for r in batch:
+                            self.busy.add(r.client)
+                        self.inflight_bytes += mem
+                        break
+                    nxt = self._next_arrival()
+                    self.cv.wait(timeout=0.002 if nxt is None else max(0.0, min(0.002, nxt - now)))
+            try:
+                ts = time.perf_counter() - t0
+                for r in batch:
+                    r.t_start = ts
+                    apply_update(self.clients[r.client], r.client, r.seq)
+                tr = time.perf_counter() - t0
+                for r in batch:
+                    r.t_render = tr
+                if self.mode == "plain":
+                    r = batch[0]
+                    cl = self.clients[r.client]
+                    _render_one(cl)
+                else:
+                    cls = [self.clients[r.client] for r in batch]
+                    _render_many(self.ctx[wid], cls)
+                td = time.perf_counter() - t0
+                for r in batch:
+                    r.t_done = td
+                    r.batch_size = len(batch)
+                    cl = self.clients[r.client]
+                    cl.done_seq = r.seq
+                    cl.est_bytes = frame_bytes(cl.comp.stats()) if self.mode == "plain" else cl.est_bytes
+            except BaseException as e:  # surface to the caller
+                with self.cv:
+                    self.errors.append(e)
+                    self.cv.notify_all()
+                return
+            with self.cv:
+                for r in batch:
+                    self.busy.discard(r.client)
+                self.inflight_bytes -= mem
+                self.completed += len(batch)
+                self.cv.notify_all()
+
+    def _next_arrival(self):
+        if self._cursor < len(self._requests):
+            return self._requests[self._cursor].arrival
+        return None
+
+    def run(self, requests: List[Request]) -> List[Request]:
+        """Serves `requests` (sorted by arrival) in real time; returns them
+        with start / completion times filled in."""
+        self._requests = requests
+        self._cursor = 0
+        self.completed = 0
+        for cl in self.clients:  # size estimates from one frame each
+            if cl.est_bytes == 0:
+                _render_one(cl)
+                cl.est_bytes = frame_bytes(cl.comp.stats())
+        t0 = time.perf_counter()
+        threads = [threading.Thread(target=self._worker, args=(w, t0, len(requests)), daemon=True)
+                   for w in range(self.workers)]
+        for th in threads:
+            th.start()
+        # feed arrivals in real time
+        while self._cursor < len(requests):
+            now = time.perf_counter() - t0
+            with self.cv:
+                while self._cursor < len(requests) and requests[self._cursor].arrival <= now:
+                    r = requests[self._cursor]
+                    self.pending[r.client].append(r)
+                    self._cursor += 1
+                self.cv.notify_all()
+                if self.errors:
+                    break
+            if self._cursor < len(requests):
+                time.sleep(max(0.0, min(0.001, requests[self._cursor].arrival - now)))
+        for th in threads:
+            th.join()
+        if self.errors:
+            raise self.errors[0]
+        return requests
+
+
+def _render_one(cl: Client):
+    sc = cl.scene
+    if isinstance(cl.out, np.ndarray):
+        cl.comp.render(cl.out, sc.width, sc.background)
+    else:
+        cl.comp.render(cl.out.data_ptr(), sc.width, sc.background, height=sc.height)
+
+
+def _render_many(ctx: Composition, cls: List[Client]):
+    outs = [cl.out if isinstance(cl.out, np.ndarray) else cl.out.data_ptr() for cl in cls]
+    render_batch(ctx, [cl.comp for cl in cls], outs, [cl.scene.width for cl in cls],
+                 [cl.scene.background for cl in cls], heights=[cl.scene.height for cl in cls])
+
+
+def latency_summary(reqs: List[Request], duration: float) -> dict:
+    lat = np.array([r.t_done - r.arrival for r in reqs]) * 1e3
+    span = max(r.t_done for r in reqs) - min(r.arrival for r in reqs)
+    render = np.array([r.t_done - r.t_render for r in reqs]) * 1e3
+    update = np.array([r.t_render - r.t_start for r in reqs]) * 1e3
+    return {"requests": len(reqs), "frames_per_s": len(reqs) / span, "p50_ms": float(np.percentile(lat, 50)),
+            "render_call_ms_mean": float(render.mean()), "update_ms_mean": float(update.mean()),
+            "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
+            "mean_batch": float(np.mean([r.batch_size for r in reqs])), "offered_s": duration}

@@ -161,7 +161,7 @@ typedef struct cgb_stats {
 
 /* Autotuned knobs (0 keeps the current value). */
 typedef struct cgb_tuning {
-    uint32_t radix_bits;     /* digit width of the segment sort: 6, 7 or 8 */
+    uint32_t radix_bits;     /* widest digit of the radix sorts: 4..9 (passes split the key evenly) */
     uint32_t raster_block;   /* threads per rasterizer block: 128..1024 */
     uint32_t steps_per_block;/* pixel steps per rasterizer block */
     uint32_t paint_warps;    /* warps (tiles) per painter block */
@@ -186,6 +186,8 @@ CGB_EXPORT cgb_status cgb_composition_free(cgb_composition* c);
 /* Composition::create_layer (mold/src/composition.rs:54-56), IdSet::acquire
  * (mold/src/layer.rs:61-72).  Ids are handed out lowest-free-first. */
 CGB_EXPORT cgb_status cgb_create_layer(cgb_composition* c, uint32_t* out_layer_id);
+/* n create_layer calls; out_layer_ids receives n ids (stops at the first failure). */
+CGB_EXPORT cgb_status cgb_create_layers(cgb_composition* c, size_t n, uint32_t* out_layer_ids);
 
 /* Composition::insert_in_layer / insert_in_layer_transformed
  * (mold/src/composition.rs:58-94): flattens the path on the GPU
@@ -218,6 +220,9 @@ CGB_EXPORT cgb_status cgb_layer_set_transform(cgb_composition* c, uint32_t layer
 CGB_EXPORT cgb_status cgb_layer_set_order(cgb_composition* c, uint32_t layer_id, uint32_t order);
 CGB_EXPORT cgb_status cgb_layer_set_props(cgb_composition* c, uint32_t layer_id,
                                           const cgb_props* props);
+/* Batched Layer::set_is_enabled: enabled[k] (0/1) applies to layer_ids[k]. */
+CGB_EXPORT cgb_status cgb_layers_set_enabled(cgb_composition* c, size_t n, const uint32_t* layer_ids,
+                                             const uint8_t* enabled);
 /* Batched set_props: props[k] applies to layer_ids[k]. */
 CGB_EXPORT cgb_status cgb_layers_set_props(cgb_composition* c, size_t n, const uint32_t* layer_ids,
                                            const cgb_props* props);
@@ -286,7 +291,7 @@ CGB_EXPORT uint64_t cgb_kernel_launches(void);
  * the sort ping-pongs between it and `out` (n u64), which receives the sorted
  * keys; both are on the current device and must not overlap.  At most
  * 16,777,216 keys (larger n returns CGB_ERR_CAPACITY before any work).  The
- * scratch is one static device array of about 4 MB held by every GPU that
+ * scratch is one static device array of about 8 MB held by every GPU that
  * loads the library; the first call on a device looks up its address, so make
  * that first call before any stream capture.  Calls share the array: calls
  * whose work overlaps on the GPU race, so serialize them.  Runs on `stream`

@@ -193,6 +193,9 @@ class Composition:
         st = self._L.orc_comp_create_layer(self._h, ctypes.byref(out))
         return None if st else out.value
 
+    def create_layers(self, n):
+        return np.array([self.create_layer() for _ in range(n)], np.uint32)
+
     def insert_in_layer(self, layer_id, path: Path, transform9=None):
         k, p = path.c_arrays()
         _check(self._L.orc_comp_insert_path(self._h, layer_id, k, len(path.kinds), p,
@@ -230,6 +233,10 @@ class Composition:
         st = self._L.orc_layers_set_transforms(self._h, len(ids), ids.ctypes.data_as(P(ctypes.c_uint32)), _fptr(t),
                                                abi.TRANSFORM_UNCHECKED if unchecked else 0)
         _check(st, "set_transforms")
+
+    def set_enabled_many(self, ids, enabled):
+        for lid, e in zip(ids, enabled):
+            self.set_enabled(int(lid), bool(e))
 
     def set_enabled(self, layer_id, enabled):
         _check(self._L.orc_layer_set_enabled(self._h, layer_id, int(bool(enabled))), "set_enabled")
