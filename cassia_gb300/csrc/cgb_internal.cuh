@@ -239,24 +239,27 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo
 
 // k_paint.cu
 struct CarryBuffers {
-    uint32_t* tl_start;   // [G + 1]
-    uint64_t* tl_cover;   // [G]
-    uint64_t* tl_carry;   // [G]
-    uint32_t* tl_flags;   // [G]
+    uint32_t* tl_start;   // [G + 1] first segment of each tile-layer group (TL)
+    uint64_t* tl_key;     // [G] its segment key (bits 22..63)
+    uint64_t* tl_cover;   // [G] lane-wise cover sum of its segments
+    uint64_t* tl_carry;   // [G] cover entering it along its (row, order) run
+    uint32_t* tl_flags;   // [G] 1 = first TL of its run
     uint32_t* item_count; // [G]
     uint32_t* item_off;   // [G + 1]
     uint64_t* items;      // [W]
     uint64_t* items_tmp;  // [W]
     uint32_t* tile_start; // [tiles + 1]
+    uint64_t* blk_cover;  // [tl_scan_grid] per block: cover sum before its first TL head
+    uint32_t* blk_head;   // [tl_scan_grid] per block: holds a TL head
+    int order_bits;       // width of the order field of an item
 };
-cudaError_t launch_tl_heads(int mode, const uint64_t* segs, uint32_t n, uint32_t* block_counts, const uint32_t* block_off,
-                            uint32_t* tl_start, cudaStream_t st);
-uint32_t tl_heads_grid(uint32_t n);
-cudaError_t launch_tl_reduce_scan(const uint64_t* segs, uint32_t G, const BatchGeom& bg, CarryBuffers& cb,
-                                  cudaStream_t st);
-cudaError_t launch_items(int mode, const uint64_t* segs, uint32_t G, const BatchGeom& bg, CarryBuffers& cb,
-                         int idx_bits, cudaStream_t st);
-cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_tiles, int shift, uint32_t n_orders,
+cudaError_t launch_tl_scan(int mode, const uint64_t* segs, uint32_t n, uint32_t row_len, uint32_t* block_counts,
+                           const uint32_t* block_off, const CarryBuffers& cb, cudaStream_t st);
+uint32_t tl_scan_grid(uint32_t n);
+cudaError_t launch_tl_carry(uint32_t G, const CarryBuffers& cb, cudaStream_t st);
+cudaError_t launch_items(int mode, uint32_t G, const BatchGeom& bg, const CarryBuffers& cb, int idx_bits,
+                         cudaStream_t st);
+cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_tiles, int tile_shift,
                                uint32_t* tile_start, cudaStream_t st);
 cudaError_t launch_paint(const BatchGeom& bg, const uint64_t* segs, const uint64_t* items, int idx_bits,
                          const uint32_t* tile_start, const CarryBuffers& cb, cudaStream_t st);

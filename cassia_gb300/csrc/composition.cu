@@ -130,7 +130,8 @@ struct cgb_composition {
 
     // frame buffers
     DevBuf recs, lengths, step_off, bcounts, btotals, boff, btoff, segs_a, segs_b;
-    DevBuf tl_start, tl_cover, tl_carry, tl_flags, item_count, item_off, items_a, items_b, tile_start;
+    DevBuf tl_start, tl_key, tl_cover, tl_carry, tl_flags, item_count, item_off, items_a, items_b, tile_start;
+    DevBuf blk_cover, blk_head;
     DevBuf d_props, d_unchanged, out_rgba, err, dflt_t, d_scenes, d_row_scene;
     // flatten staging
     DevBuf f_kinds, f_points, f_cmd_off, f_pt_off, f_t9, f_has_t, f_path_layer, f_counts, f_off;
@@ -694,37 +695,44 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
 
     // tile-layer groups, carries, work items
     CarryBuffers cb{};
-    const uint32_t hg = tl_heads_grid((uint32_t)P);
+    const uint32_t hg = tl_scan_grid((uint32_t)P);
     CK(c->s.ensure(c->bcounts, ((size_t)hg + 1) * 4));
     CK(c->s.ensure(c->boff, ((size_t)hg + 1) * 4));
-    CK(launch_tl_heads(0, sorted, (uint32_t)P, c->bcounts.as<uint32_t>(), nullptr, nullptr, st));
+    CK(c->s.ensure(c->blk_cover, ((size_t)hg + 1) * 8));
+    CK(c->s.ensure(c->blk_head, ((size_t)hg + 1) * 4));
+    cb.blk_cover = c->blk_cover.as<uint64_t>();
+    cb.blk_head = c->blk_head.as<uint32_t>();
+    CK(launch_tl_scan(0, sorted, (uint32_t)P, bg.row_len, c->bcounts.as<uint32_t>(), nullptr, cb, st));
     uint64_t G = 0;
     if (P) CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), hg, &c->s, st, &G));
     c->stats.tile_layers = G;
     CK(c->s.ensure(c->tl_start, (G + 1) * 4));
+    CK(c->s.ensure(c->tl_key, std::max<uint64_t>(G, 1) * 8));
     CK(c->s.ensure(c->tl_cover, std::max<uint64_t>(G, 1) * 8));
     CK(c->s.ensure(c->tl_carry, std::max<uint64_t>(G, 1) * 8));
     CK(c->s.ensure(c->tl_flags, std::max<uint64_t>(G, 1) * 4));
     CK(c->s.ensure(c->item_count, std::max<uint64_t>(G, 1) * 4));
     CK(c->s.ensure(c->item_off, (G + 1) * 4));
     cb.tl_start = c->tl_start.as<uint32_t>();
+    cb.tl_key = c->tl_key.as<uint64_t>();
     cb.tl_cover = c->tl_cover.as<uint64_t>();
     cb.tl_carry = c->tl_carry.as<uint64_t>();
     cb.tl_flags = c->tl_flags.as<uint32_t>();
     cb.item_count = c->item_count.as<uint32_t>();
     cb.item_off = c->item_off.as<uint32_t>();
-    CK(launch_tl_heads(1, sorted, (uint32_t)P, nullptr, c->boff.as<uint32_t>(), cb.tl_start, st));
+    cb.order_bits = bits_for(std::max<uint32_t>(n_orders, 1) - 1);
+    CK(launch_tl_scan(1, sorted, (uint32_t)P, bg.row_len, nullptr, c->boff.as<uint32_t>(), cb, st));
     c->s.pinned[1] = P;  // tl_start[G] = P
     CK(cudaMemcpyAsync(cb.tl_start + G, &c->s.pinned[1], 4, cudaMemcpyHostToDevice, st));
-    CK(launch_tl_reduce_scan(sorted, (uint32_t)G, bg, cb, st));
-    CK(launch_items(0, sorted, (uint32_t)G, bg, cb, 0, st));
+    CK(launch_tl_carry((uint32_t)G, cb, st));
+    CK(launch_items(0, (uint32_t)G, bg, cb, 0, st));
     uint64_t W = 0;
     if (G) CK(scan_u32(cb.item_count, cb.item_off, (uint32_t)G, &c->s, st, &W));
     c->stats.work_items = W;
     const int idx_bits = bits_for(std::max<uint64_t>(G, 1) - 1);
-    const int item_key_bits = bits_for(std::max<uint64_t>(tiles * n_orders, 1) - 1);
-    const int item_shift = idx_bits + 3;  // TL index, then the full / opaque / carry-only bits
-    if (item_shift + item_key_bits > 64 || W >= (1ull << 30))
+    const int tile_bits = bits_for(std::max<uint64_t>(tiles, 1) - 1);
+    const int tile_shift = idx_bits + 3 + cb.order_bits;  // TL index, item flags, order, then the tile
+    if (tile_shift + tile_bits > 64 || W >= (1ull << 30))
         return fail(CGB_ERR_LAYER_LIMIT, "render: too many tile x layer work items");
     CK(c->s.ensure(c->items_a, std::max<uint64_t>(W, 1) * 8));
     CK(c->s.ensure(c->items_b, std::max<uint64_t>(W, 1) * 8));
@@ -732,13 +740,14 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
     cb.items = c->items_a.as<uint64_t>();
     cb.items_tmp = c->items_b.as<uint64_t>();
     cb.tile_start = c->tile_start.as<uint32_t>();
-    CK(launch_items(1, sorted, (uint32_t)G, bg, cb, idx_bits, st));
+    CK(launch_items(1, (uint32_t)G, bg, cb, idx_bits, st));
     uint64_t* items_sorted = cb.items;
     int ipasses = 0;
-    CK(radix_sort_u64(cb.items, cb.items_tmp, (uint32_t)W, item_shift, item_shift + item_key_bits,
+    // stable sort on the tile field: each tile's items stay in order
+    CK(radix_sort_u64(cb.items, cb.items_tmp, (uint32_t)W, tile_shift, tile_shift + tile_bits,
                       (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &items_sorted, &ipasses));
     c->stats.item_sort_passes = ipasses;
-    CK(launch_tile_ranges(items_sorted, (uint32_t)W, (uint32_t)tiles, item_shift, n_orders, cb.tile_start, st));
+    CK(launch_tile_ranges(items_sorted, (uint32_t)W, (uint32_t)tiles, tile_shift, cb.tile_start, st));
     CK(cudaEventRecord(c->ev[4], st));
     CK(launch_paint(bg, sorted, items_sorted, idx_bits, cb.tile_start, cb, st));
     CK(cudaEventRecord(c->ev[5], st));
@@ -817,7 +826,7 @@ CGB_EXPORT cgb_status cgb_composition_free(cgb_composition* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     DevBuf* bufs[] = {&c->p0x, &c->p0y, &c->p1x, &c->p1y, &c->lids, &c->d_layers, &c->recs, &c->lengths,
                       &c->step_off, &c->bcounts, &c->btotals, &c->boff, &c->btoff, &c->segs_a, &c->segs_b,
-                      &c->tl_start, &c->tl_cover, &c->tl_carry, &c->tl_flags, &c->item_count, &c->item_off,
+                      &c->tl_start, &c->tl_key, &c->blk_cover, &c->blk_head, &c->tl_cover, &c->tl_carry, &c->tl_flags, &c->item_count, &c->item_off,
                       &c->items_a, &c->items_b, &c->tile_start, &c->d_props, &c->d_unchanged, &c->out_rgba, &c->err,
                       &c->dflt_t, &c->f_kinds, &c->f_points, &c->f_cmd_off, &c->f_pt_off, &c->f_t9, &c->f_has_t,
                       &c->f_path_layer, &c->f_counts, &c->f_off, &c->g_flags, &c->g_off, &c->s.scan_sums,

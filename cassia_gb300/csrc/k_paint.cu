@@ -19,8 +19,9 @@
 // multiples of 32 for EvenOdd (whose tests are mod 32) and exactly for NonZero,
 // so every decision and coverage below is bit-identical.
 //
-// Work items are (tile, order) pairs, sorted by (tile, order) with the radix
-// sort.  The painter gives each tile one warp (2 pixels per lane), replicates
+// Work items are (tile, order) pairs, written in (row, order, column) order
+// and sorted by tile with the (stable) radix sort, which leaves each tile's
+// items in order.  The painter gives each tile one warp (2 pixels per lane), replicates
 // tile_unchanged_pass and skip_fully_covered_layers (:200-222, :310-388),
 // paints the surviving layers bottom-up in f32 with the reference's vector
 // blend formulas, and writes RGBA8 with 128-bit stores.
@@ -32,74 +33,144 @@ namespace {
 
 constexpr int HEAD_THREADS = 256;
 constexpr int HEAD_ITEMS = 8;
+constexpr int HEAD_WARPS = HEAD_THREADS / 32;
 
-__global__ void __launch_bounds__(HEAD_THREADS) k_tl_heads(int mode, const uint64_t* __restrict__ segs, uint32_t n,
-                                                           uint32_t* __restrict__ block_counts,
-                                                           const uint32_t* __restrict__ block_off,
-                                                           uint32_t* __restrict__ tl_start) {
+// The cover of one segment as a packed 8 x i8 value (its row's lane).
+__device__ __forceinline__ uint64_t seg_cover(uint32_t low) {
+    return (uint64_t)(uint8_t)(int8_t)low_cover(low) << (8 * low_tile_y(low));
+}
+
+// TL heads and their cover sums in one pass over the sorted segments.
+//
+// Each thread owns HEAD_ITEMS consecutive segments; a segment starts a TL when
+// its key (bits 22..63) differs from its predecessor's.  A TL's cover sum is
+// the lane-wise sum of its segments' covers; the part of it that lies beyond
+// the owning thread is R(t + 1), where R(t) = pre(t) + (t has a head ? 0 :
+// R(t + 1)) and pre(t) is the sum of thread t's segments before its first
+// head.  R is a reverse segmented scan: within a warp by shuffles, across
+// warps in shared memory, and across blocks through each block's R(0)
+// (blk_cover, written by the counting pass) and whether the block holds a head.
+//
+// mode 0: per block, the TL count, blk_cover and blk_head.
+// mode 1: per TL g, its first segment, key, cover sum and run-start flag.
+__global__ void __launch_bounds__(HEAD_THREADS) k_tl_scan(int mode, const uint64_t* __restrict__ segs, uint32_t n,
+                                                          uint32_t row_len, uint32_t* __restrict__ block_counts,
+                                                          const uint32_t* __restrict__ block_off, CarryBuffers cb) {
     const uint64_t s0 = ((uint64_t)blockIdx.x * HEAD_THREADS + threadIdx.x) * HEAD_ITEMS;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t key[HEAD_ITEMS];
+    uint32_t low[HEAD_ITEMS];
     uint32_t flags = 0, cnt = 0;
-    if (s0 < n) {
-        uint64_t prev = s0 == 0 ? ~0ull : (segs[s0 - 1] >> 22);
+    uint64_t prev = ~0ull;
+    if (s0 < n && s0 > 0) prev = segs[s0 - 1] >> 22;
+    const uint64_t first_prev = prev;
 #pragma unroll
-        for (int k = 0; k < HEAD_ITEMS; k++) {
-            uint64_t s = s0 + k;
-            if (s < n) {
-                uint64_t key = segs[s] >> 22;
-                if (key != prev) {
-                    flags |= 1u << k;
-                    cnt++;
-                }
-                prev = key;
+    for (int k = 0; k < HEAD_ITEMS; k++) {
+        const uint64_t s = s0 + k;
+        key[k] = ~0ull;
+        low[k] = 0;
+        if (s < n) {
+            const uint64_t v = segs[s];
+            key[k] = v >> 22;
+            low[k] = (uint32_t)v;
+            if (key[k] != prev) {
+                flags |= 1u << k;
+                cnt++;
             }
+            prev = key[k];
         }
     }
-    __shared__ uint32_t warp_sums[HEAD_THREADS / 32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // pre(t): covers before the thread's first head (all of them without one)
+    uint64_t pre = 0;
+#pragma unroll
+    for (int k = 0; k < HEAD_ITEMS; k++)
+        if ((flags & ((2u << k) - 1)) == 0) pre = cover_add(pre, seg_cover(low[k]));
+
+    // reverse segmented scan of (pre, has head) within the warp
+    uint64_t r = pre;
+    bool stop = flags != 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t nr = __shfl_down_sync(0xffffffffu, r, o);
+        const bool ns = __shfl_down_sync(0xffffffffu, stop ? 1 : 0, o) != 0;
+        if (!stop && lane + o < 32) {
+            r = cover_add(r, nr);
+            stop = ns;
+        }
+    }
+    // TL counts: inclusive scan within the warp
     uint32_t inc = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        uint32_t a = __shfl_up_sync(0xffffffffu, inc, o);
+        const uint32_t a = __shfl_up_sync(0xffffffffu, inc, o);
         if (lane >= o) inc += a;
     }
-    if (lane == 31) warp_sums[warp] = inc;
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t w = lane < HEAD_THREADS / 32 ? warp_sums[lane] : 0, wi = w;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t a = __shfl_up_sync(0xffffffffu, wi, o);
-            if (lane >= o) wi += a;
+    __shared__ uint64_t w_r[HEAD_WARPS], w_carry[HEAD_WARPS];
+    __shared__ uint32_t w_stop[HEAD_WARPS], w_sums[HEAD_WARPS];
+    __shared__ uint64_t s_next;  // R of the first thread of the next block
+    if (lane == 0) {
+        w_r[warp] = r;
+        w_stop[warp] = stop ? 1u : 0u;
+    }
+    if (lane == 31) w_sums[warp] = inc;
+    if (mode == 1 && threadIdx.x == 0) {
+        uint64_t x = 0;
+        for (uint32_t b = blockIdx.x + 1; b < gridDim.x; b++) {
+            x = cover_add(x, cb.blk_cover[b]);
+            if (cb.blk_head[b]) break;
         }
-        if (lane < HEAD_THREADS / 32) warp_sums[lane] = wi - w;
-        if (lane == 31 && mode == 0) block_counts[blockIdx.x] = wi;
+        s_next = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // carry into each warp from the warps after it (and the next block)
+        uint64_t c = mode == 1 ? s_next : 0;
+        for (int w = HEAD_WARPS - 1; w >= 0; w--) {
+            w_carry[w] = c;
+            c = w_stop[w] ? w_r[w] : cover_add(w_r[w], c);
+        }
+        uint32_t run = 0;
+        for (int w = 0; w < HEAD_WARPS; w++) {
+            const uint32_t v = w_sums[w];
+            w_sums[w] = run;
+            run += v;
+        }
+        if (mode == 0) {
+            block_counts[blockIdx.x] = run;
+            cb.blk_cover[blockIdx.x] = c;  // R(0) up to the block end
+            cb.blk_head[blockIdx.x] = run != 0 ? 1u : 0u;
+        }
     }
     __syncthreads();
     if (mode == 0) return;
-    uint32_t o = block_off[blockIdx.x] + warp_sums[warp] + inc - cnt;
+    const uint64_t R = stop ? r : cover_add(r, w_carry[warp]);
+    const uint64_t r_next_lane = __shfl_down_sync(0xffffffffu, R, 1);
+    const uint64_t cont = lane == 31 ? w_carry[warp] : r_next_lane;  // R(t + 1)
+    if (!flags) return;
+    uint32_t o = block_off[blockIdx.x] + w_sums[warp] + inc - cnt;
+    const uint32_t rl1 = row_len + 1;
+    uint64_t pk = first_prev;
+    uint64_t acc = 0;
+    int open = -1;
 #pragma unroll
-    for (int k = 0; k < HEAD_ITEMS; k++)
-        if (flags & (1u << k)) tl_start[o++] = (uint32_t)(s0 + k);
-}
-
-// Per TL: cover sums per tile row (8 x i8 lanes) and the run-start flag.
-__global__ void k_tl_reduce(const uint64_t* __restrict__ segs, uint32_t G, const uint32_t* __restrict__ tl_start,
-                            uint32_t row_len, uint64_t* __restrict__ tl_cover, uint32_t* __restrict__ tl_flags) {
-    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= G) return;
-    const uint32_t b = tl_start[g], e = tl_start[g + 1];
-    int32_t c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (uint32_t s = b; s < e; s++) {
-        uint32_t low = (uint32_t)segs[s];
-        c[low_tile_y(low)] += low_cover(low);
+    for (int k = 0; k < HEAD_ITEMS; k++) {
+        if (flags & (1u << k)) {
+            if (open >= 0) {
+                cb.tl_cover[o] = acc;
+                o++;
+            }
+            open = k;
+            acc = 0;
+            cb.tl_start[o] = (uint32_t)(s0 + k);
+            cb.tl_key[o] = key[k];
+            // a run is one (row, order) pair: a new run starts unless the
+            // previous segment is in the same row and order
+            cb.tl_flags[o] = (pk == ~0ull || pk / rl1 != key[k] / rl1) ? 1u : 0u;
+        }
+        if (s0 + k < n) acc = cover_add(acc, seg_cover(low[k]));
+        pk = key[k];
     }
-    uint64_t packed = 0;
-#pragma unroll
-    for (int y = 0; y < 8; y++) packed |= (uint64_t)(uint8_t)c[y] << (8 * y);
-    tl_cover[g] = packed;
-    const uint64_t run = (segs[b] >> 22) / (row_len + 1);
-    const bool start = g == 0 || ((segs[tl_start[g - 1]] >> 22) / (row_len + 1)) != run;
-    tl_flags[g] = start ? 1u : 0u;
+    cb.tl_cover[o] = cover_add(acc, cont);
 }
 
 // Exclusive prefix of the cover sums along each (j, L) run: one thread walks
@@ -129,11 +200,9 @@ constexpr int ITEM_FLAG_BITS = 3;
 // to the next TL of its (row, order) run.  Returns the count; `emit(tile,
 // flags)` is called for each.
 template <class Emit>
-__device__ __forceinline__ uint32_t tl_items(uint32_t g, uint32_t G, const uint64_t* __restrict__ segs,
-                                             const uint32_t* __restrict__ tl_start, const uint32_t* __restrict__ tl_flags,
-                                             const uint64_t* __restrict__ tl_cover,
-                                             const uint64_t* __restrict__ tl_carry, const BatchGeom& bg, Emit emit) {
-    const uint64_t key = segs[tl_start[g]] >> 22;
+__device__ __forceinline__ uint32_t tl_items(uint32_t g, uint32_t G,
+                                             const CarryBuffers& cb, const BatchGeom& bg, Emit emit) {
+    const uint64_t key = cb.tl_key[g];
     const uint32_t rl1 = bg.row_len + 1;
     const int32_t i = (int32_t)(key % rl1) - 1;
     const uint64_t run = key / rl1;
@@ -143,7 +212,7 @@ __device__ __forceinline__ uint32_t tl_items(uint32_t g, uint32_t G, const uint6
     const uint32_t j = grow - S.row_base;
     if (j < S.crop_v0 || j >= S.crop_v1) return 0;
     int32_t next = (int32_t)S.row_len;
-    if (g + 1 < G && !tl_flags[g + 1]) next = (int32_t)((segs[tl_start[g + 1]] >> 22) % rl1) - 1;
+    if (g + 1 < G && !cb.tl_flags[g + 1]) next = (int32_t)(cb.tl_key[g + 1] % rl1) - 1;
     const int32_t h0 = (int32_t)S.crop_h0, h1 = (int32_t)S.crop_h1;
     if (next > h1) next = h1;
     uint32_t cnt = 0;
@@ -152,7 +221,7 @@ __device__ __forceinline__ uint32_t tl_items(uint32_t g, uint32_t G, const uint6
         cnt++;
     }
     if (next <= i + 1) return cnt;
-    const uint64_t carry_out = cover_add(tl_carry[g], tl_cover[g]);
+    const uint64_t carry_out = cover_add(cb.tl_carry[g], cb.tl_cover[g]);
     const PaintProps pp = S.props[L];
     const bool nonempty = !cover_is_empty(carry_out, pp.fill_rule);
     // payload of a cover-carry-only item: its layer_is_full and the opaque
@@ -176,37 +245,35 @@ __device__ __forceinline__ uint32_t tl_items(uint32_t g, uint32_t G, const uint6
     return cnt;
 }
 
-__global__ void k_items_count(const uint64_t* __restrict__ segs, uint32_t G, const uint32_t* __restrict__ tl_start,
-                              const uint32_t* __restrict__ tl_flags, const uint64_t* __restrict__ tl_cover,
-                              const uint64_t* __restrict__ tl_carry, BatchGeom bg, uint32_t* __restrict__ counts) {
+__global__ void k_items_count(uint32_t G, CarryBuffers cb, BatchGeom bg) {
     uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= G) return;
-    counts[g] = tl_items(g, G, segs, tl_start, tl_flags, tl_cover, tl_carry, bg,
-                         [](const SceneDesc&, uint32_t, int32_t, uint32_t) {});
+    cb.item_count[g] = tl_items(g, G, cb, bg, [](const SceneDesc&, uint32_t, int32_t, uint32_t) {});
 }
 
-__global__ void k_items_write(const uint64_t* __restrict__ segs, uint32_t G, const uint32_t* __restrict__ tl_start,
-                              const uint32_t* __restrict__ tl_flags, const uint64_t* __restrict__ tl_cover,
-                              const uint64_t* __restrict__ tl_carry, BatchGeom bg, const uint32_t* __restrict__ off,
-                              int idx_bits, uint64_t* __restrict__ items) {
+// Item = tile | order | flags | TL index, high to low; the tile field is the
+// sort key.  The items of a tile are written in ascending order (the TLs
+// are sorted by row, then order), so a stable sort on the tile alone leaves
+// each tile's items in paint order.
+__global__ void k_items_write(uint32_t G, CarryBuffers cb, BatchGeom bg, int idx_bits) {
     uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= G) return;
-    const uint64_t L = ((segs[tl_start[g]] >> 22) / (bg.row_len + 1)) % bg.n_orders;
-    uint32_t o = off[g];
-    tl_items(g, G, segs, tl_start, tl_flags, tl_cover, tl_carry, bg,
-             [&](const SceneDesc& S, uint32_t j, int32_t t, uint32_t flags) {
-                 const uint64_t tile = (uint64_t)S.tile_base + (uint64_t)j * S.row_len + (uint64_t)t;
-                 const uint64_t k = ((tile * bg.n_orders + L) << ITEM_FLAG_BITS) | flags;
-                 items[o++] = (k << idx_bits) | g;
-             });
+    const uint64_t L = (cb.tl_key[g] / (bg.row_len + 1)) % bg.n_orders;
+    const int ob = cb.order_bits;
+    uint32_t o = cb.item_off[g];
+    tl_items(g, G, cb, bg, [&](const SceneDesc& S, uint32_t j, int32_t t, uint32_t flags) {
+        const uint64_t tile = (uint64_t)S.tile_base + (uint64_t)j * S.row_len + (uint64_t)t;
+        const uint64_t k = ((((tile << ob) | L) << ITEM_FLAG_BITS) | flags);
+        cb.items[o++] = (k << idx_bits) | g;
+    });
 }
 
-__global__ void k_tile_ranges(const uint64_t* __restrict__ items, uint32_t W, uint32_t n_tiles, int shift,
-                              uint32_t n_orders, uint32_t* __restrict__ tile_start) {
+__global__ void k_tile_ranges(const uint64_t* __restrict__ items, uint32_t W, uint32_t n_tiles, int tile_shift,
+                              uint32_t* __restrict__ tile_start) {
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k > W) return;
-    int64_t cur = k < W ? (int64_t)((items[k] >> shift) / n_orders) : (int64_t)n_tiles;
-    int64_t prev = k > 0 ? (int64_t)((items[k - 1] >> shift) / n_orders) : -1;
+    int64_t cur = k < W ? (int64_t)(items[k] >> tile_shift) : (int64_t)n_tiles;
+    int64_t prev = k > 0 ? (int64_t)(items[k - 1] >> tile_shift) : -1;
     for (int64_t t = prev + 1; t <= cur; t++) tile_start[t] = k;
 }
 
@@ -342,12 +409,12 @@ __device__ __forceinline__ uint32_t solid_bytes(const float c[4]) {
            (to_byte(linear_to_srgb(c[2] * ar)) << 16) | (to_byte(c[3]) << 24);
 }
 
-__device__ __forceinline__ void item_decode(uint64_t item, int idx_bits, uint32_t n_orders, uint32_t& L,
+__device__ __forceinline__ void item_decode(uint64_t item, int idx_bits, int order_bits, uint32_t& L,
                                             uint32_t& flags, uint32_t& g) {
     g = (uint32_t)(item & ((1ull << idx_bits) - 1));
     uint64_t k = item >> idx_bits;
     flags = (uint32_t)(k & 7u);
-    L = (uint32_t)((k >> ITEM_FLAG_BITS) % n_orders);
+    L = (uint32_t)((k >> ITEM_FLAG_BITS) & ((1ull << order_bits) - 1));
 }
 
 struct PaintArgs {
@@ -355,6 +422,7 @@ struct PaintArgs {
     const uint64_t* segs;
     const uint64_t* items;
     int idx_bits;
+    int order_bits;
     const uint32_t* tile_start;
     const uint32_t* tl_start;
     const uint64_t* tl_cover;
@@ -385,7 +453,7 @@ __device__ __forceinline__ void stage_items(const PaintArgs& a, const PaintProps
     float4 col = make_float4(0.f, 0.f, 0.f, 0.f);
     if ((uint32_t)lane < n) {
         uint32_t L, fl, g;
-        item_decode(a.items[c0 + lane], a.idx_bits, a.bg.n_orders, L, fl, g);
+        item_decode(a.items[c0 + lane], a.idx_bits, a.order_bits, L, fl, g);
         const float4* pp = reinterpret_cast<const float4*>(props + L);
         const uint4 hdr = *reinterpret_cast<const uint4*>(pp);
         col = pp[1];
@@ -472,7 +540,7 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
             bool all = true;
             for (uint32_t k = b + lane; k < e; k += 32) {
                 uint32_t L, fl, g;
-                item_decode(a.items[k], a.idx_bits, n_orders, L, fl, g);
+                item_decode(a.items[k], a.idx_bits, a.order_bits, L, fl, g);
                 all &= p.unchanged[L] != 0;
             }
             if (__all_sync(0xffffffffu, all)) return;  // TileWriteOp::None
@@ -511,7 +579,7 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
         uint32_t from;
         if (first == 1) {
             uint32_t L, fl, g;
-            item_decode(a.items[k_op], a.idx_bits, n_orders, L, fl, g);
+            item_decode(a.items[k_op], a.idx_bits, a.order_bits, L, fl, g);
             const float4 c = reinterpret_cast<const float4*>(p.props + L)[1];
             dst[0] = c.x, dst[1] = c.y, dst[2] = c.z, dst[3] = c.w;
             from = (uint32_t)k_op + 1;
@@ -613,50 +681,45 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
 
 }  // namespace
 
-cudaError_t launch_tl_heads(int mode, const uint64_t* segs, uint32_t n, uint32_t* block_counts,
-                            const uint32_t* block_off, uint32_t* tl_start, cudaStream_t st) {
+cudaError_t launch_tl_scan(int mode, const uint64_t* segs, uint32_t n, uint32_t row_len, uint32_t* block_counts,
+                           const uint32_t* block_off, const CarryBuffers& cb, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    uint32_t per = HEAD_THREADS * HEAD_ITEMS;
     count_launches(1);
-    k_tl_heads<<<(n + per - 1) / per, HEAD_THREADS, 0, st>>>(mode, segs, n, block_counts, block_off, tl_start);
+    k_tl_scan<<<tl_scan_grid(n), HEAD_THREADS, 0, st>>>(mode, segs, n, row_len, block_counts, block_off, cb);
     return cudaGetLastError();
 }
 
-uint32_t tl_heads_grid(uint32_t n) { return (n + HEAD_THREADS * HEAD_ITEMS - 1) / (HEAD_THREADS * HEAD_ITEMS); }
+uint32_t tl_scan_grid(uint32_t n) { return (n + HEAD_THREADS * HEAD_ITEMS - 1) / (HEAD_THREADS * HEAD_ITEMS); }
 
-cudaError_t launch_tl_reduce_scan(const uint64_t* segs, uint32_t G, const BatchGeom& bg, CarryBuffers& cb,
-                                  cudaStream_t st) {
+cudaError_t launch_tl_carry(uint32_t G, const CarryBuffers& cb, cudaStream_t st) {
     if (G == 0) return cudaSuccess;
-    count_launches(2);
-    k_tl_reduce<<<(G + 255) / 256, 256, 0, st>>>(segs, G, cb.tl_start, bg.row_len, cb.tl_cover, cb.tl_flags);
+    count_launches(1);
     k_tl_carry<<<(G + 255) / 256, 256, 0, st>>>(G, cb.tl_cover, cb.tl_flags, cb.tl_carry);
     return cudaGetLastError();
 }
 
-cudaError_t launch_items(int mode, const uint64_t* segs, uint32_t G, const BatchGeom& bg, CarryBuffers& cb,
-                         int idx_bits, cudaStream_t st) {
+cudaError_t launch_items(int mode, uint32_t G, const BatchGeom& bg, const CarryBuffers& cb, int idx_bits,
+                         cudaStream_t st) {
     if (G == 0) return cudaSuccess;
     count_launches(1);
     if (mode == 0)
-        k_items_count<<<(G + 255) / 256, 256, 0, st>>>(segs, G, cb.tl_start, cb.tl_flags, cb.tl_cover, cb.tl_carry, bg,
-                                                       cb.item_count);
+        k_items_count<<<(G + 255) / 256, 256, 0, st>>>(G, cb, bg);
     else
-        k_items_write<<<(G + 255) / 256, 256, 0, st>>>(segs, G, cb.tl_start, cb.tl_flags, cb.tl_cover, cb.tl_carry, bg,
-                                                       cb.item_off, idx_bits, cb.items);
+        k_items_write<<<(G + 255) / 256, 256, 0, st>>>(G, cb, bg, idx_bits);
     return cudaGetLastError();
 }
 
-cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_tiles, int shift, uint32_t n_orders,
+cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_tiles, int tile_shift,
                                uint32_t* tile_start, cudaStream_t st) {
     count_launches(1);
-    k_tile_ranges<<<(W + 1 + 255) / 256, 256, 0, st>>>(items, W, n_tiles, shift, n_orders, tile_start);
+    k_tile_ranges<<<(W + 1 + 255) / 256, 256, 0, st>>>(items, W, n_tiles, tile_shift, tile_start);
     return cudaGetLastError();
 }
 
 cudaError_t launch_paint(const BatchGeom& bg, const uint64_t* segs, const uint64_t* items, int idx_bits,
                          const uint32_t* tile_start, const CarryBuffers& cb, cudaStream_t st) {
     if (bg.total_tiles == 0) return cudaSuccess;
-    PaintArgs a{bg, segs, items, idx_bits, tile_start, cb.tl_start, cb.tl_cover, cb.tl_carry};
+    PaintArgs a{bg, segs, items, idx_bits, cb.order_bits, tile_start, cb.tl_start, cb.tl_cover, cb.tl_carry};
     count_launches(1);
     k_paint<<<(bg.total_tiles + PAINT_WARPS - 1) / PAINT_WARPS, 32 * PAINT_WARPS, 0, st>>>(a);
     return cudaGetLastError();

@@ -229,3 +229,30 @@ def test_disable_and_gc_matches_oracle():
     a, b = _render_both(sc, g, o)
     _assert_same_image(a, b)
     assert g.lens() == o.lens()
+
+
+def test_render_tile_layer_longer_than_scan_blocks():
+    # one layer zigzags inside a single tile: its tile-layer group holds
+    # thousands of segments, so whole blocks of the group scan hold no group
+    # head and the group's cover sum crosses several blocks
+    from cassia_gb300 import Composition
+    g, o = Composition(), oracle.Composition()
+    for c in (g, o):
+        for k, (fr, x0) in enumerate([(FillRule.NonZero, 8.0), (FillRule.EvenOdd, 24.0)]):
+            lid = c.create_layer()
+            p = Path()
+            pts = [(x0 + 0.2 + 0.0047 * i, 8.2 if i % 2 == 0 else 15.8) for i in range(1300)]
+            for a, b in zip(pts, pts[1:] + pts[:1]):
+                p.line(a, b)
+            c.insert_in_layer(lid, p.close())
+            c.set_props(lid, Props(fill_rule=fr, func=Style(fill=(0.9, 0.3 * k, 0.1, 0.7))))
+        lid = c.create_layer()  # a plain shape across the same rows
+        c.insert_in_layer(lid, Path().line((1.5, 3.0), (38.0, 12.5)).line((38.0, 12.5), (5.0, 22.0)).close())
+        c.set_props(lid, solid((0.1, 0.2, 0.9, 0.6)))
+    a = np.zeros((32, 40, 4), np.uint8)
+    b = np.zeros_like(a)
+    g.render(a, 40, (1.0, 1.0, 1.0, 1.0))
+    o.render(b, 40, (1.0, 1.0, 1.0, 1.0))
+    stats_segments = g.stats()["segments"]
+    assert stats_segments > 3 * 2048
+    _assert_same_image(a, b)
