@@ -219,9 +219,13 @@ cudaError_t launch_flatten(int write, const uint32_t* kinds, const float* points
 cudaError_t launch_build_lines(const BatchGeom& bg, int cull, LineRec* recs, uint32_t* lengths, cudaStream_t st);
 // mode: 0 = count, 1 = write.  render != 0: culled, re-keyed render format;
 // else the reference segment format of the (single) scene.
-cudaError_t launch_rasterize(int mode, int render, const BatchGeom& bg, const LineRec* recs, const uint32_t* step_off,
-                             uint32_t n_lines, uint64_t n_steps, uint32_t block, uint32_t* block_counts,
-                             uint32_t* block_totals, const uint32_t* block_off, uint64_t* out, cudaStream_t st);
+// Rasterizes every pixel step; block b stores its kept segments at
+// runs[b * raster_run_slots(block)...] and their count at run_count[b];
+// *produced (zeroed by the caller) accumulates all segments, kept or not.
+cudaError_t launch_rasterize(int render, const BatchGeom& bg, const LineRec* recs, const uint32_t* step_off,
+                             uint32_t n_lines, uint64_t n_steps, uint32_t block, uint64_t* runs, uint32_t* run_count,
+                             unsigned long long* produced, cudaStream_t st);
+uint32_t raster_run_slots(uint32_t block);
 uint32_t raster_grid(uint64_t n_steps, uint32_t block);
 cudaError_t launch_compact_lines(const float* in4[4], const uint32_t* lid_in, uint32_t n, const LayerRec* layers,
                                  uint32_t n_layer_recs, float* out4[4], uint32_t* lid_out, uint32_t* flags,
@@ -233,9 +237,18 @@ cudaError_t launch_compact_lines(const float* in4[4], const uint32_t* lid_in, ui
 cudaError_t scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, Scratch* s, cudaStream_t st,
                      uint64_t* total_host);
 // Sort n u64 keys by bits [bit_lo, bit_hi).  `keys` and `tmp` hold n keys;
-// on return *result points at the sorted array (keys or tmp).
+// on return *result points at the sorted array (keys or tmp).  With
+// hist_ready the digit counts of every pass are already in s->sort_hist
+// (from radix_gather_hist).
 cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo, int bit_hi, int digit_bits,
-                           Scratch* s, uint32_t* err_flag, cudaStream_t st, uint64_t** result, int* passes);
+                           Scratch* s, uint32_t* err_flag, cudaStream_t st, uint64_t** result, int* passes,
+                           bool hist_ready = false);
+// Packs runs of keys (run r: run_count[r] keys at runs[r * run_slots...],
+// placed at run_off[r] of out) and counts the digits of every pass of the sort
+// by bits [bit_lo, bit_hi) into s->sort_hist, for radix_sort_u64(hist_ready).
+cudaError_t radix_gather_hist(const uint64_t* runs, uint32_t run_slots, const uint32_t* run_count,
+                              const uint32_t* run_off, uint32_t n_runs, uint64_t* out, int bit_lo, int bit_hi,
+                              int digit_bits, Scratch* s, cudaStream_t st);
 
 // k_paint.cu
 struct CarryBuffers {

@@ -129,9 +129,9 @@ struct cgb_composition {
     uint64_t props_version = 1, props_uploaded = 0;
 
     // frame buffers
-    DevBuf recs, lengths, step_off, bcounts, btotals, boff, btoff, segs_a, segs_b;
+    DevBuf recs, lengths, step_off, bcounts, boff, segs_a, segs_b;
     DevBuf tl_start, tl_key, tl_cover, tl_carry, tl_flags, item_count, item_off, items_a, items_b, tile_start;
-    DevBuf blk_cover, blk_head;
+    DevBuf blk_cover, blk_head, rlb;
     DevBuf d_props, d_unchanged, out_rgba, err, dflt_t, d_scenes, d_row_scene;
     // flatten staging
     DevBuf f_kinds, f_points, f_cmd_off, f_pt_off, f_t9, f_has_t, f_path_layer, f_counts, f_off;
@@ -482,8 +482,12 @@ struct SceneInput {
 
 // LinesBuilder::build + Rasterizer::rasterize (+ re-keying / culling in
 // render mode) over every scene of the frame.  Leaves n_segs keys in segs_a.
-cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& bg, uint64_t* n_segs,
-                               uint64_t* n_total) {
+// LinesBuilder::build + Rasterizer::rasterize (+ re-keying / culling in
+// render mode) over every scene of the frame.  Leaves n_segs keys packed at
+// *keys (segs_b; segs_a is free for the sort) with the digit histogram of the
+// sort by bits [sort_lo, sort_hi) counted.
+cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& bg, int sort_lo, int sort_hi,
+                               uint64_t* n_segs, uint64_t* n_total, uint64_t** keys) {
     cudaStream_t st = c->stream;
     if (bg.total_lines >= (1ull << 32)) return fail(CGB_ERR_LAYER_LIMIT, "more than 2^32 lines in a frame");
     const uint32_t L = (uint32_t)bg.total_lines;
@@ -500,23 +504,27 @@ cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& 
     c->stats.steps = S;
     const uint32_t block = c->tuning.raster_block;
     const uint32_t grid = raster_grid(S, block);
+    const uint32_t slots = raster_run_slots(block);
+    CK(c->s.ensure(c->segs_a, std::max<size_t>((size_t)grid * slots, 1) * 8));
     CK(c->s.ensure(c->bcounts, ((size_t)grid + 1) * 4));
-    CK(c->s.ensure(c->btotals, ((size_t)grid + 1) * 4));
     CK(c->s.ensure(c->boff, ((size_t)grid + 1) * 4));
-    CK(c->s.ensure(c->btoff, ((size_t)grid + 1) * 4));
-    CK(launch_rasterize(0, render, bg, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, S, block,
-                        c->bcounts.as<uint32_t>(), c->btotals.as<uint32_t>(), nullptr, nullptr, st));
-    uint64_t P = 0, PT = 0;
-    CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid, &c->s, st, &P));
-    CK(scan_u32(c->btotals.as<uint32_t>(), c->btoff.as<uint32_t>(), grid, &c->s, st, &PT));
-    if (P >= (1ull << 30)) return fail(CGB_ERR_LAYER_LIMIT, "more than 2^30 pixel segments");
-    CK(c->s.ensure(c->segs_a, std::max<size_t>(P, 1) * 8));
+    CK(c->s.ensure(c->rlb, 8));
+    CK(cudaMemsetAsync(c->rlb.p, 0, 8, st));
+    unsigned long long* produced = c->rlb.as<unsigned long long>();
+    CK(launch_rasterize(render, bg, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, S, block,
+                        c->segs_a.as<uint64_t>(), c->bcounts.as<uint32_t>(), produced, st));
+    CK(cudaMemcpyAsync(&c->s.pinned[3], produced, 8, cudaMemcpyDeviceToHost, st));
+    uint64_t P = 0;
+    if (grid) CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid, &c->s, st, &P));
+    const uint64_t PT = S ? c->s.pinned[3] : 0;
+    if (P >= (1ull << 30) - 1) return fail(CGB_ERR_LAYER_LIMIT, "more than 2^30 pixel segments");
     CK(c->s.ensure(c->segs_b, std::max<size_t>(P, 1) * 8));
-    CK(launch_rasterize(1, render, bg, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, S, block, nullptr,
-                        nullptr, c->boff.as<uint32_t>(), c->segs_a.as<uint64_t>(), st));
+    CK(radix_gather_hist(c->segs_a.as<uint64_t>(), slots, c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid,
+                         c->segs_b.as<uint64_t>(), sort_lo, sort_hi, (int)c->tuning.radix_bits, &c->s, st));
     CK(cudaEventRecord(c->ev[2], st));
     *n_segs = P;
     *n_total = PT;
+    *keys = c->segs_b.as<uint64_t>();
     c->stats.segments = PT;
     return CGB_OK;
 }
@@ -682,14 +690,15 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
     bg.row_scene = c->d_row_scene.as<uint32_t>();
 
     uint64_t P = 0, PT = 0;
-    cgb_status s2 = build_and_rasterize(c, 1, bg, &P, &PT);
+    uint64_t* keys = nullptr;
+    cgb_status s2 = build_and_rasterize(c, 1, bg, 22, 22 + (int)bg.key_bits, &P, &PT, &keys);
     if (s2) return s2;
     c->stats.painted_segments = P;
     // sort by (global row, order, tile column)
-    uint64_t* sorted = c->segs_a.as<uint64_t>();
+    uint64_t* sorted = keys;
     int passes = 0;
-    CK(radix_sort_u64(c->segs_a.as<uint64_t>(), c->segs_b.as<uint64_t>(), (uint32_t)P, 22, 22 + (int)bg.key_bits,
-                      (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &sorted, &passes));
+    CK(radix_sort_u64(keys, c->segs_a.as<uint64_t>(), (uint32_t)P, 22, 22 + (int)bg.key_bits,
+                      (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &sorted, &passes, true));
     c->stats.sort_passes = passes;
     CK(cudaEventRecord(c->ev[3], st));
 
@@ -825,8 +834,8 @@ CGB_EXPORT cgb_status cgb_composition_free(cgb_composition* c) {
     DeviceGuard g(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     DevBuf* bufs[] = {&c->p0x, &c->p0y, &c->p1x, &c->p1y, &c->lids, &c->d_layers, &c->recs, &c->lengths,
-                      &c->step_off, &c->bcounts, &c->btotals, &c->boff, &c->btoff, &c->segs_a, &c->segs_b,
-                      &c->tl_start, &c->tl_key, &c->blk_cover, &c->blk_head, &c->tl_cover, &c->tl_carry, &c->tl_flags, &c->item_count, &c->item_off,
+                      &c->step_off, &c->bcounts, &c->boff, &c->segs_a, &c->segs_b,
+                      &c->tl_start, &c->tl_key, &c->blk_cover, &c->blk_head, &c->rlb, &c->tl_cover, &c->tl_carry, &c->tl_flags, &c->item_count, &c->item_off,
                       &c->items_a, &c->items_b, &c->tile_start, &c->d_props, &c->d_unchanged, &c->out_rgba, &c->err,
                       &c->dflt_t, &c->f_kinds, &c->f_points, &c->f_cmd_off, &c->f_pt_off, &c->f_t9, &c->f_has_t,
                       &c->f_path_layer, &c->f_counts, &c->f_off, &c->g_flags, &c->g_off, &c->s.scan_sums,
@@ -1107,13 +1116,14 @@ CGB_EXPORT cgb_status cgb_pixel_segments(cgb_composition* c, uint64_t* out, size
     bg.scenes = c->d_scenes.as<SceneDesc>();
     bg.n_scenes = 1;
     bg.total_lines = c->n_lines;
-    cgb_status s2 = build_and_rasterize(c, 0, bg, &P, &PT);
-    if (s2) return s2;
-    uint64_t* sorted = c->segs_a.as<uint64_t>();
-    int passes = 0;
     const int lo = order == CGB_SORT_CANONICAL ? 0 : 22;
-    CK(radix_sort_u64(c->segs_a.as<uint64_t>(), c->segs_b.as<uint64_t>(), (uint32_t)P, lo, 64,
-                      (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), c->stream, &sorted, &passes));
+    uint64_t* keys = nullptr;
+    cgb_status s2 = build_and_rasterize(c, 0, bg, lo, 64, &P, &PT, &keys);
+    if (s2) return s2;
+    uint64_t* sorted = keys;
+    int passes = 0;
+    CK(radix_sort_u64(keys, c->segs_a.as<uint64_t>(), (uint32_t)P, lo, 64, (int)c->tuning.radix_bits, &c->s,
+                      c->err.as<uint32_t>(), c->stream, &sorted, &passes, true));
     c->stats.sort_passes = passes;
     CK(cudaEventRecord(c->ev[3], c->stream));
     *out_len = P;

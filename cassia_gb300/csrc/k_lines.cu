@@ -6,10 +6,10 @@
 //   k_build_lines  LinesBuilder::build (surpass/src/segment.rs:91-237): one
 //                  thread per line; writes a packed 32-byte LineRec + length.
 //   k_rasterize    Rasterizer::rasterize (surpass/src/rasterizer/mod.rs:214-285):
-//                  each thread walks 8 consecutive pixel steps; a count pass
-//                  sizes every block's output, a write pass block-scans the
-//                  per-thread counts, stages the segments in shared memory and
-//                  stores each block's run with coalesced 128-bit stores.  No
+//                  each thread walks 8 consecutive pixel steps; each block
+//                  block-scans the per-thread counts, stages its segments in
+//                  shared memory and stores them coalesced into its own run
+//                  of slots; k_gather_hist (k_sort.cu) packs the runs.  No
 //                  NONE slots are materialized.
 #include "cgb_internal.cuh"
 
@@ -493,14 +493,17 @@ __device__ __forceinline__ uint32_t find_line(const uint32_t* __restrict__ off, 
     return lo;
 }
 
-template <int MODE, int RENDER>
+// Every block rasterizes RASTER_ITEMS pixel steps per thread and stores its
+// kept segments, in step order, at the start of its own run of
+// 2 * RASTER_ITEMS * blockDim.x slots (a step yields at most two segments);
+// run_count[block] receives how many.  No block waits on another: a later
+// gather (fused with the sort's digit histogram) packs the runs.
+template <int RENDER>
 __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ recs, const uint32_t* __restrict__ off,
                                                    uint32_t n_lines, uint64_t n_steps, BatchGeom bg,
-                                                   uint32_t* __restrict__ block_counts,
-                                                   uint32_t* __restrict__ block_totals,
-                                                   const uint32_t* __restrict__ block_off,
-                                                   uint64_t* __restrict__ out) {
-    extern __shared__ uint64_t s_out[];  // 2 * RASTER_ITEMS * blockDim.x (write mode)
+                                                   uint64_t* __restrict__ runs, uint32_t* __restrict__ run_count,
+                                                   unsigned long long* __restrict__ produced) {
+    extern __shared__ uint64_t s_out[];  // 2 * RASTER_ITEMS * blockDim.x
     const uint64_t s0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * RASTER_ITEMS;
     uint64_t segs[2 * RASTER_ITEMS];
     int n = 0, total = 0;
@@ -573,21 +576,17 @@ __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ r
         }
         if (lane < nw) warp_sums[lane] = wi - w;
         if (lane == 31) {
-            if (MODE == 0) {
-                block_counts[blockIdx.x] = wi;
-                block_totals[blockIdx.x] = wti;
-            } else {
-                warp_tot[0] = wi;  // block total
-            }
+            warp_tot[0] = wi;
+            run_count[blockIdx.x] = wi;
+            if (wti) atomicAdd(produced, (unsigned long long)wti);
         }
     }
     __syncthreads();
-    if (MODE == 0) return;
     const uint32_t local = warp_sums[warp] + inc - n;
     const uint32_t btotal = warp_tot[0];
     for (int q = 0; q < n; q++) s_out[local + q] = segs[q];
     __syncthreads();
-    uint64_t* dst = out + block_off[blockIdx.x];
+    uint64_t* dst = runs + (uint64_t)blockIdx.x * (2 * RASTER_ITEMS * blockDim.x);
     for (uint32_t i = threadIdx.x; i < btotal; i += blockDim.x) dst[i] = s_out[i];
 }
 
@@ -636,32 +635,23 @@ cudaError_t launch_build_lines(const BatchGeom& bg, int cull, LineRec* recs, uin
     return cudaGetLastError();
 }
 
-cudaError_t launch_rasterize(int mode, int render, const BatchGeom& bg, const LineRec* recs, const uint32_t* step_off,
-                             uint32_t n_lines, uint64_t n_steps, uint32_t block, uint32_t* block_counts,
-                             uint32_t* block_totals, const uint32_t* block_off, uint64_t* out, cudaStream_t st) {
+cudaError_t launch_rasterize(int render, const BatchGeom& bg, const LineRec* recs, const uint32_t* step_off,
+                             uint32_t n_lines, uint64_t n_steps, uint32_t block, uint64_t* runs, uint32_t* run_count,
+                             unsigned long long* produced, cudaStream_t st) {
     if (n_steps == 0) return cudaSuccess;
     block = block ? block : 256;
     uint64_t per_block = (uint64_t)block * RASTER_ITEMS;
     uint32_t grid = (uint32_t)((n_steps + per_block - 1) / per_block);
-    size_t smem = mode ? (size_t)2 * per_block * sizeof(uint64_t) : 0;
+    size_t smem = (size_t)2 * per_block * sizeof(uint64_t);
     count_launches(1);
-    if (mode == 0) {
-        if (render)
-            k_rasterize<0, 1><<<grid, block, 0, st>>>(recs, step_off, n_lines, n_steps, bg, block_counts,
-                                                      block_totals, block_off, out);
-        else
-            k_rasterize<0, 0><<<grid, block, 0, st>>>(recs, step_off, n_lines, n_steps, bg, block_counts,
-                                                      block_totals, block_off, out);
-    } else {
-        if (render)
-            k_rasterize<1, 1><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, block_counts,
-                                                         block_totals, block_off, out);
-        else
-            k_rasterize<1, 0><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, block_counts,
-                                                         block_totals, block_off, out);
-    }
+    if (render)
+        k_rasterize<1><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced);
+    else
+        k_rasterize<0><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced);
     return cudaGetLastError();
 }
+
+uint32_t raster_run_slots(uint32_t block) { return 2 * RASTER_ITEMS * (block ? block : 256); }
 
 uint32_t raster_grid(uint64_t n_steps, uint32_t block) {
     block = block ? block : 256;

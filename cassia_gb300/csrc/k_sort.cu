@@ -179,6 +179,36 @@ __global__ void __launch_bounds__(512) k_radix_hist(const uint64_t* __restrict__
     }
 }
 
+// Packs the rasterizer's runs into one array and histograms every pass's
+// digits on the way (the counting pass of the sort, fused with the copy).
+__global__ void __launch_bounds__(512) k_gather_hist(const uint64_t* __restrict__ runs, uint32_t run_slots,
+                                                     const uint32_t* __restrict__ run_count,
+                                                     const uint32_t* __restrict__ run_off, uint32_t n_runs,
+                                                     uint64_t* __restrict__ out, PassPlan plan,
+                                                     uint32_t* __restrict__ hist) {
+    __shared__ uint32_t sh[MAX_PASSES][RADIX];
+    for (int i = threadIdx.x; i < plan.n * RADIX; i += blockDim.x) (&sh[0][0])[i] = 0;
+    __syncthreads();
+    for (uint32_t r = blockIdx.x; r < n_runs; r += gridDim.x) {
+        const uint32_t cnt = run_count[r];
+        const uint64_t* src = runs + (uint64_t)r * run_slots;
+        uint64_t* dst = out + run_off[r];
+        for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) {
+            const uint64_t k = src[i];
+            dst[i] = k;
+            for (int p = 0; p < plan.n; p++) {
+                const uint32_t d = (uint32_t)(k >> plan.shift[p]) & ((1u << plan.bits[p]) - 1);
+                atomicAdd(&sh[p][d], 1u);
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < plan.n * RADIX; i += blockDim.x) {
+        const uint32_t v = (&sh[0][0])[i];
+        if (v) atomicAdd(&hist[i], v);
+    }
+}
+
 // Exclusive scan of each pass's RADIX bins (one CTA of RADIX threads per pass).
 __global__ void __launch_bounds__(RADIX) k_radix_hist_scan(uint32_t* hist) {
     uint32_t* h = hist + blockIdx.x * RADIX;
@@ -387,8 +417,31 @@ size_t radix_sort_scratch_bytes(uint32_t n, int bit_lo, int bit_hi, int digit_bi
     return (size_t)p.n * RADIX * 4 + tiles * RADIX * 4 + 64;
 }
 
+static int sm_count() {
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+}
+
+cudaError_t radix_gather_hist(const uint64_t* runs, uint32_t run_slots, const uint32_t* run_count,
+                              const uint32_t* run_off, uint32_t n_runs, uint64_t* out, int bit_lo, int bit_hi,
+                              int digit_bits, Scratch* s, cudaStream_t st) {
+    const PassPlan plan = make_plan(bit_lo, bit_hi, digit_bits);
+    cudaError_t e = s->ensure(s->sort_hist, (size_t)MAX_PASSES * RADIX * 4);
+    if (e != cudaSuccess) return e;
+    uint32_t* hist = s->sort_hist.as<uint32_t>();
+    if ((e = cudaMemsetAsync(hist, 0, (size_t)MAX_PASSES * RADIX * 4, st)) != cudaSuccess) return e;
+    if (n_runs == 0) return cudaSuccess;
+    const uint32_t blocks = std::min<uint32_t>(n_runs, (uint32_t)sm_count() * 4);
+    count_launches(1);
+    k_gather_hist<<<blocks, 512, 0, st>>>(runs, run_slots, run_count, run_off, n_runs, out, plan, hist);
+    return cudaGetLastError();
+}
+
 cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo, int bit_hi, int digit_bits,
-                           Scratch* s, uint32_t* err_flag, cudaStream_t st, uint64_t** result, int* passes) {
+                           Scratch* s, uint32_t* err_flag, cudaStream_t st, uint64_t** result, int* passes,
+                           bool hist_ready) {
     PassPlan plan = make_plan(bit_lo, bit_hi, digit_bits);
     *result = keys;
     if (passes) *passes = plan.n;
@@ -403,14 +456,14 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo
     uint32_t* hist = s->sort_hist.as<uint32_t>();
     uint32_t* lb = s->sort_lookback.as<uint32_t>();
     uint32_t* ctr = s->sort_counter.as<uint32_t>();
-    if ((e = cudaMemsetAsync(hist, 0, (size_t)plan.n * RADIX * 4, st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(ctr, 0, MAX_PASSES * 4, st)) != cudaSuccess) return e;
-    int dev = 0, sms = 148;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    uint32_t hist_blocks = std::min<uint32_t>((n + 511) / 512, (uint32_t)sms * 4);
-    count_launches(2 + plan.n);
-    k_radix_hist<<<hist_blocks, 512, 0, st>>>(keys, n, plan, hist);
+    if (!hist_ready) {
+        if ((e = cudaMemsetAsync(hist, 0, (size_t)plan.n * RADIX * 4, st)) != cudaSuccess) return e;
+        uint32_t hist_blocks = std::min<uint32_t>((n + 511) / 512, (uint32_t)sm_count() * 4);
+        count_launches(1);
+        k_radix_hist<<<hist_blocks, 512, 0, st>>>(keys, n, plan, hist);
+    }
+    count_launches(1 + plan.n);
     k_radix_hist_scan<<<plan.n, RADIX, 0, st>>>(hist);
     uint64_t* src = keys;
     uint64_t* dst = tmp;
