@@ -322,16 +322,20 @@ __device__ __forceinline__ void blend_pixels(float (&c)[2][4], const float4& src
                                              const bool (&col)[2]) {
 #pragma unroll
     for (int h = 0; h < 2; h++) {
-        if (!col[h]) continue;
+        // computed for every pixel, kept where the column is blended
         const float al = src.w * cov[h];
         const float inv = 1.0f - al;
         const float f0 = blend_vec_t<MODE>(c[h][0], src.x) * al;
         const float f1 = blend_vec_t<MODE>(c[h][1], src.y) * al;
         const float f2 = blend_vec_t<MODE>(c[h][2], src.z) * al;
-        c[h][0] = __fmaf_rn(c[h][0], inv, f0);
-        c[h][1] = __fmaf_rn(c[h][1], inv, f1);
-        c[h][2] = __fmaf_rn(c[h][2], inv, f2);
-        c[h][3] = __fmaf_rn(c[h][3], inv, al);
+        const float n0 = __fmaf_rn(c[h][0], inv, f0);
+        const float n1 = __fmaf_rn(c[h][1], inv, f1);
+        const float n2 = __fmaf_rn(c[h][2], inv, f2);
+        const float n3 = __fmaf_rn(c[h][3], inv, al);
+        c[h][0] = col[h] ? n0 : c[h][0];
+        c[h][1] = col[h] ? n1 : c[h][1];
+        c[h][2] = col[h] ? n2 : c[h][2];
+        c[h][3] = col[h] ? n3 : c[h][3];
     }
 }
 
@@ -432,11 +436,15 @@ struct PaintArgs {
 constexpr int PAINT_WARPS = 4;  // tiles per CTA
 constexpr int SEGCAP = 256;     // staged segments per warp and chunk of 32 items
 
+constexpr uint32_t META_CARRY_ONLY = 32u;  // the item only carries cover through the tile
+constexpr uint32_t META_ACTIVE = 64u;      // carry-only: some tile row has non-zero coverage
+
 // Per-warp staging of 32 work items.
 struct WarpStage {
     float4 color[32];
-    uint64_t carry[32];  // cover entering the tile (TL items) or carried through it
-    uint32_t meta[32];   // blend_mode | fill_rule << 4 | carry-only << 5
+    float4 rowcov[32][2];  // carry-only items: coverage of each tile row
+    uint64_t carry[32];    // cover entering the tile (TL items)
+    uint32_t meta[32];     // blend_mode | fill_rule << 4 | META_CARRY_ONLY | META_ACTIVE
     uint32_t sb[32];     // first segment (global index)
     uint32_t cnt[32];    // segments of the item
     uint32_t soff[32];   // staging offset of its segments
@@ -459,13 +467,29 @@ __device__ __forceinline__ void stage_items(const PaintArgs& a, const PaintProps
         col = pp[1];
         carry = a.tl_carry[g];
         const uint32_t co = (fl & ITEM_CARRY) ? 1u : 0u;
+        const uint32_t fr = hdr.x & 1u;
+        meta = (hdr.y & 15u) | (fr << 4);
         if (co) {
             carry = cover_add(carry, a.tl_cover[g]);
+            meta |= META_CARRY_ONLY;
+            if (with_segments) {
+                // every pixel of a tile row has the row's coverage; the
+                // layer's columns are blended iff some row is covered
+                float rc[8];
+                bool any = false;
+#pragma unroll
+                for (int yy = 0; yy < 8; yy++) {
+                    rc[yy] = from_area(PIXEL_WIDTH * cover_lane(carry, yy), fr);
+                    any |= rc[yy] != 0.0f;
+                }
+                S.rowcov[lane][0] = make_float4(rc[0], rc[1], rc[2], rc[3]);
+                S.rowcov[lane][1] = make_float4(rc[4], rc[5], rc[6], rc[7]);
+                if (any) meta |= META_ACTIVE;
+            }
         } else if (with_segments) {
             sb = a.tl_start[g];
             cnt = a.tl_start[g + 1] - sb;
         }
-        meta = (hdr.y & 15u) | ((hdr.x & 1u) << 4) | (co << 5);
     }
     // exclusive scan of the segment counts -> staging offsets
     uint32_t inc = cnt;
@@ -613,24 +637,27 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
 #pragma unroll
             for (int q = 0; q < 4; q++) c[h][q] = p.clear[q];
         const uint32_t start = k_op >= 0 ? (uint32_t)k_op : b;
+        S.area[lane] = 0;
+        S.area[lane + 32] = 0;
+        S.cov[lane] = 0;
+        S.cov[lane + 32] = 0;
         for (uint32_t c0 = start; c0 < e; c0 += 32) {
             const uint32_t n = min(32u, e - c0);
             stage_items(a, p.props, S, c0, n, lane, true);
             for (uint32_t q = 0; q < n; q++) {
                 const uint32_t meta = S.meta[q];
                 const uint32_t mode = meta & 15u, fr = (meta >> 4) & 1u;
-                const uint64_t carry = S.carry[q];
-                const int32_t cy = cover_lane(carry, y);
                 float cov[2];
-                if (meta & 32u) {
-                    cov[0] = cov[1] = from_area(PIXEL_WIDTH * cy, fr);
+                bool col[2];
+                if (meta & META_CARRY_ONLY) {
+                    if (!(meta & META_ACTIVE)) continue;
+                    cov[0] = cov[1] = reinterpret_cast<const float*>(&S.rowcov[q][0])[y];
+                    col[0] = col[1] = true;
                 } else {
-                    // acc_segment / acc_cover / compute_areas (painter/mod.rs:229-243, 347-362)
-                    S.area[lane] = 0;
-                    S.area[lane + 32] = 0;
-                    S.cov[lane] = 0;
-                    S.cov[lane + 32] = 0;
-                    __syncwarp();
+                    // acc_segment / acc_cover / compute_areas (painter/mod.rs:229-243, 347-362):
+                    // per-cell sums in shared memory, then each lane reads
+                    // (and clears) the cells of its two pixels
+                    const int32_t cy = cover_lane(S.carry[q], y);
                     const uint32_t cnt = S.cnt[q], so = S.soff[q], sb = S.sb[q];
                     for (uint32_t s = lane; s < cnt; s += 32) {
                         const uint32_t low = so + s < SEGCAP ? S.seg[so + s] : (uint32_t)a.segs[sb + s];
@@ -639,20 +666,32 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
                         atomicAdd(&S.cov[cell], low_cover(low));
                     }
                     __syncwarp();
-                    int32_t cv = cy;
-                    for (uint32_t x = 0; x < x0; x++) cv += S.cov[x * 8 + y];
-                    const int32_t cv1 = cv + S.cov[x0 * 8 + y];
-                    cov[0] = from_area(PIXEL_WIDTH * (int32_t)(int8_t)cv + (int32_t)(int16_t)S.area[x0 * 8 + y], fr);
-                    cov[1] = from_area(PIXEL_WIDTH * (int32_t)(int8_t)cv1 + (int32_t)(int16_t)S.area[x0 * 8 + 8 + y],
-                                       fr);
+                    const uint32_t c0i = x0 * 8 + y, c1i = c0i + 8;
+                    const int32_t a0 = S.area[c0i], a1 = S.area[c1i];
+                    const int32_t v0 = S.cov[c0i], v1 = S.cov[c1i];
+                    S.area[c0i] = 0;
+                    S.area[c1i] = 0;
+                    S.cov[c0i] = 0;
+                    S.cov[c1i] = 0;
+                    // covers of the columns left of x0: prefix over the lane's column pairs
+                    int32_t pre = v0 + v1;
+                    int32_t t = __shfl_up_sync(0xffffffffu, pre, 8);
+                    if (xg >= 1) pre += t;
+                    t = __shfl_up_sync(0xffffffffu, pre, 16);
+                    if (xg >= 2) pre += t;
+                    const int32_t cv = cy + pre - (v0 + v1);
+                    const int32_t cv1 = cv + v0;
+                    cov[0] = from_area(PIXEL_WIDTH * (int32_t)(int8_t)cv + (int32_t)(int16_t)a0, fr);
+                    cov[1] = from_area(PIXEL_WIDTH * (int32_t)(int8_t)cv1 + (int32_t)(int16_t)a1, fr);
                     __syncwarp();
+                    // A column is blended when any of its 8 coverages is non-zero
+                    // (painter/mod.rs:287-289).
+                    const uint32_t b0 = __ballot_sync(0xffffffffu, cov[0] != 0.0f);
+                    const uint32_t b1 = __ballot_sync(0xffffffffu, cov[1] != 0.0f);
+                    if (!(b0 | b1)) continue;
+                    col[0] = ((b0 >> (8 * xg)) & 0xFFu) != 0;
+                    col[1] = ((b1 >> (8 * xg)) & 0xFFu) != 0;
                 }
-                // A column is blended when any of its 8 coverages is non-zero
-                // (painter/mod.rs:287-289).
-                const uint32_t b0 = __ballot_sync(0xffffffffu, cov[0] != 0.0f);
-                const uint32_t b1 = __ballot_sync(0xffffffffu, cov[1] != 0.0f);
-                const bool col[2] = {((b0 >> (8 * xg)) & 0xFFu) != 0, ((b1 >> (8 * xg)) & 0xFFu) != 0};
-                if (!(col[0] | col[1])) continue;
                 blend_dispatch(mode, c, S.color[q], cov, col);
             }
             __syncwarp();
