@@ -82,18 +82,37 @@ struct SceneDesc {
     float clear[4];
 };
 
-// Frame-wide geometry of the render-mode segment key
-//   key = ((global row * n_orders + order) * (row_len + 1) + (tile column + 1)),
-// with n_orders and row_len the maxima over the frame's scenes.
+// Frame-wide geometry of the render-mode segment key, bit fields from high
+// to low:
+//   key = global tile row | order | tile column + 1
+// (order_bits and col_bits wide), with n_orders and row_len the maxima over
+// the frame's scenes.
 struct BatchGeom {
     const SceneDesc* scenes;     // device array
     const uint32_t* row_scene;   // device: scene of each global tile row
     uint32_t n_scenes;
     uint32_t total_rows, total_tiles;
     uint32_t n_orders, row_len;
+    uint32_t order_bits, col_bits;
     uint32_t key_bits;
     uint64_t total_lines;
 };
+
+__host__ __device__ __forceinline__ uint64_t make_render_key(const BatchGeom& bg, uint32_t grow, uint32_t order,
+                                                             uint32_t col1) {
+    return ((((uint64_t)grow << bg.order_bits) | order) << bg.col_bits) | col1;
+}
+// (row, order) run of a key, its tile column + 1, its order and row
+__host__ __device__ __forceinline__ uint64_t key_run(uint64_t key, uint32_t col_bits) { return key >> col_bits; }
+__host__ __device__ __forceinline__ uint32_t key_col1(uint64_t key, uint32_t col_bits) {
+    return (uint32_t)(key & ((1ull << col_bits) - 1));
+}
+__host__ __device__ __forceinline__ uint32_t run_order(uint64_t run, uint32_t order_bits) {
+    return (uint32_t)(run & ((1ull << order_bits) - 1));
+}
+__host__ __device__ __forceinline__ uint32_t run_row(uint64_t run, uint32_t order_bits) {
+    return (uint32_t)(run >> order_bits);
+}
 
 // LineRec.order_octant packing: scene << 20 | order << 3 | octant
 constexpr int LINE_SCENE_SHIFT = 20;
@@ -266,7 +285,7 @@ struct CarryBuffers {
     uint32_t* blk_head;   // [tl_scan_grid] per block: holds a TL head
     int order_bits;       // width of the order field of an item
 };
-cudaError_t launch_tl_scan(int mode, const uint64_t* segs, uint32_t n, uint32_t row_len, uint32_t* block_counts,
+cudaError_t launch_tl_scan(int mode, const uint64_t* segs, uint32_t n, uint32_t col_bits, uint32_t* block_counts,
                            const uint32_t* block_off, const CarryBuffers& cb, cudaStream_t st);
 uint32_t tl_scan_grid(uint32_t n);
 cudaError_t launch_tl_carry(uint32_t G, const CarryBuffers& cb, cudaStream_t st);

@@ -664,7 +664,9 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
     bg.n_orders = n_orders;
     bg.row_len = row_len;
     bg.total_lines = lines;
-    bg.key_bits = bits_for(std::max<uint64_t>(rows * n_orders * (row_len + 1), 1) - 1);
+    bg.order_bits = bits_for(std::max<uint32_t>(n_orders, 1) - 1);
+    bg.col_bits = bits_for(row_len);
+    bg.key_bits = bits_for(std::max<uint64_t>(rows, 1) - 1) + bg.order_bits + bg.col_bits;
     if (bg.key_bits > 42) return fail(CGB_ERR_LAYER_LIMIT, "render: rows x orders x tiles too large for the segment key");
     if (staging) CK(c->s.ensure(c->out_rgba, staging));
     std::vector<SceneDesc> descs;
@@ -711,7 +713,7 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
     CK(c->s.ensure(c->blk_head, ((size_t)hg + 1) * 4));
     cb.blk_cover = c->blk_cover.as<uint64_t>();
     cb.blk_head = c->blk_head.as<uint32_t>();
-    CK(launch_tl_scan(0, sorted, (uint32_t)P, bg.row_len, c->bcounts.as<uint32_t>(), nullptr, cb, st));
+    CK(launch_tl_scan(0, sorted, (uint32_t)P, bg.col_bits, c->bcounts.as<uint32_t>(), nullptr, cb, st));
     uint64_t G = 0;
     if (P) CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), hg, &c->s, st, &G));
     c->stats.tile_layers = G;
@@ -729,8 +731,8 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
     cb.tl_flags = c->tl_flags.as<uint32_t>();
     cb.item_count = c->item_count.as<uint32_t>();
     cb.item_off = c->item_off.as<uint32_t>();
-    cb.order_bits = bits_for(std::max<uint32_t>(n_orders, 1) - 1);
-    CK(launch_tl_scan(1, sorted, (uint32_t)P, bg.row_len, nullptr, c->boff.as<uint32_t>(), cb, st));
+    cb.order_bits = (int)bg.order_bits;
+    CK(launch_tl_scan(1, sorted, (uint32_t)P, bg.col_bits, nullptr, c->boff.as<uint32_t>(), cb, st));
     c->s.pinned[1] = P;  // tl_start[G] = P
     CK(cudaMemcpyAsync(cb.tl_start + G, &c->s.pinned[1], 4, cudaMemcpyHostToDevice, st));
     CK(launch_tl_carry((uint32_t)G, cb, st));

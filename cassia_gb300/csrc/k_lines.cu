@@ -474,8 +474,7 @@ __device__ __forceinline__ bool render_key(const SceneRaster& sr, const BatchGeo
     int32_t tj = seg_tile_j(sr.wide, seg);
     int32_t ti = seg_tile_i_stored(sr.wide, seg) - 256;
     if (tj < 0 || tj >= (int32_t)sr.rows || ti < -1 || ti >= (int32_t)sr.row_len) return false;
-    uint64_t key = ((uint64_t)(sr.row_base + (uint32_t)tj) * bg.n_orders + seg_layer(sr.wide, seg)) * (bg.row_len + 1) +
-                   (uint64_t)(ti + 1);
+    const uint64_t key = make_render_key(bg, sr.row_base + (uint32_t)tj, seg_layer(sr.wide, seg), (uint32_t)(ti + 1));
     out = (key << 22) | (seg & 0x3FFFFFull);
     return true;
 }

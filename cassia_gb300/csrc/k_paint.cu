@@ -53,9 +53,11 @@ __device__ __forceinline__ uint64_t seg_cover(uint32_t low) {
 //
 // mode 0: per block, the TL count, blk_cover and blk_head.
 // mode 1: per TL g, its first segment, key, cover sum and run-start flag.
-__global__ void __launch_bounds__(HEAD_THREADS) k_tl_scan(int mode, const uint64_t* __restrict__ segs, uint32_t n,
-                                                          uint32_t row_len, uint32_t* __restrict__ block_counts,
+template <int MODE>
+__global__ void __launch_bounds__(HEAD_THREADS) k_tl_scan(const uint64_t* __restrict__ segs, uint32_t n,
+                                                          uint32_t col_bits, uint32_t* __restrict__ block_counts,
                                                           const uint32_t* __restrict__ block_off, CarryBuffers cb) {
+    constexpr int mode = MODE;
     const uint64_t s0 = ((uint64_t)blockIdx.x * HEAD_THREADS + threadIdx.x) * HEAD_ITEMS;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint64_t key[HEAD_ITEMS];
@@ -148,7 +150,6 @@ __global__ void __launch_bounds__(HEAD_THREADS) k_tl_scan(int mode, const uint64
     const uint64_t cont = lane == 31 ? w_carry[warp] : r_next_lane;  // R(t + 1)
     if (!flags) return;
     uint32_t o = block_off[blockIdx.x] + w_sums[warp] + inc - cnt;
-    const uint32_t rl1 = row_len + 1;
     uint64_t pk = first_prev;
     uint64_t acc = 0;
     int open = -1;
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(HEAD_THREADS) k_tl_scan(int mode, const uint64
             cb.tl_key[o] = key[k];
             // a run is one (row, order) pair: a new run starts unless the
             // previous segment is in the same row and order
-            cb.tl_flags[o] = (pk == ~0ull || pk / rl1 != key[k] / rl1) ? 1u : 0u;
+            cb.tl_flags[o] = (pk == ~0ull || key_run(pk, col_bits) != key_run(key[k], col_bits)) ? 1u : 0u;
         }
         if (s0 + k < n) acc = cover_add(acc, seg_cover(low[k]));
         pk = key[k];
@@ -203,16 +204,15 @@ template <class Emit>
 __device__ __forceinline__ uint32_t tl_items(uint32_t g, uint32_t G,
                                              const CarryBuffers& cb, const BatchGeom& bg, Emit emit) {
     const uint64_t key = cb.tl_key[g];
-    const uint32_t rl1 = bg.row_len + 1;
-    const int32_t i = (int32_t)(key % rl1) - 1;
-    const uint64_t run = key / rl1;
-    const uint32_t L = (uint32_t)(run % bg.n_orders);
-    const uint32_t grow = (uint32_t)(run / bg.n_orders);
+    const int32_t i = (int32_t)key_col1(key, bg.col_bits) - 1;
+    const uint64_t run = key_run(key, bg.col_bits);
+    const uint32_t L = run_order(run, bg.order_bits);
+    const uint32_t grow = run_row(run, bg.order_bits);
     const SceneDesc& S = bg.scenes[bg.row_scene[grow]];
     const uint32_t j = grow - S.row_base;
     if (j < S.crop_v0 || j >= S.crop_v1) return 0;
     int32_t next = (int32_t)S.row_len;
-    if (g + 1 < G && !cb.tl_flags[g + 1]) next = (int32_t)(cb.tl_key[g + 1] % rl1) - 1;
+    if (g + 1 < G && !cb.tl_flags[g + 1]) next = (int32_t)key_col1(cb.tl_key[g + 1], bg.col_bits) - 1;
     const int32_t h0 = (int32_t)S.crop_h0, h1 = (int32_t)S.crop_h1;
     if (next > h1) next = h1;
     uint32_t cnt = 0;
@@ -258,7 +258,7 @@ __global__ void k_items_count(uint32_t G, CarryBuffers cb, BatchGeom bg) {
 __global__ void k_items_write(uint32_t G, CarryBuffers cb, BatchGeom bg, int idx_bits) {
     uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= G) return;
-    const uint64_t L = (cb.tl_key[g] / (bg.row_len + 1)) % bg.n_orders;
+    const uint64_t L = run_order(key_run(cb.tl_key[g], bg.col_bits), bg.order_bits);
     const int ob = cb.order_bits;
     uint32_t o = cb.item_off[g];
     tl_items(g, G, cb, bg, [&](const SceneDesc& S, uint32_t j, int32_t t, uint32_t flags) {
@@ -288,72 +288,119 @@ __device__ __forceinline__ float from_area(int32_t area, uint32_t fill_rule) {
     return ((area >> 8) & 1) == 0 ? capped : 1.0f - capped;
 }
 
-// blend_function! per lane (style.rs:288-418)
-__device__ __forceinline__ float blend_vec(uint32_t mode, float d, float s) {
-    switch (mode) {
-        case CGB_BLEND_OVER: return s;
-        case CGB_BLEND_MULTIPLY: return d * s;
-        case CGB_BLEND_SCREEN: return __fmaf_rn(d, -s, d) + s;
-        case CGB_BLEND_OVERLAY: return s <= 0.5f ? (d * s * 2.0f) : 2.0f * (s + d - __fmaf_rn(s, d, 0.5f));
-        case CGB_BLEND_DARKEN: return fminf(d, s);
-        case CGB_BLEND_LIGHTEN: return fmaxf(d, s);
-        case CGB_BLEND_COLOR_DODGE: return s == 0.0f ? 0.0f : fminf(1.0f, s / (1.0f - d));
-        case CGB_BLEND_COLOR_BURN: return s == 1.0f ? 1.0f : 1.0f - fminf(1.0f, (1.0f - s) / d);
-        case CGB_BLEND_HARD_LIGHT: return d <= 0.5f ? (d * s * 2.0f) : 2.0f * (s + d - __fmaf_rn(s, d, 0.5f));
-        case CGB_BLEND_SOFT_LIGHT: {
-            float dd = s <= 0.25f ? __fmaf_rn(__fmaf_rn(16.0f, s, -12.0f), s, 4.0f) * s : sqrtf(s);
-            float k = __fmaf_rn(2.0f, d, -1.0f);
-            return d <= 0.5f ? __fmaf_rn(s * (1.0f - s), k, s) : __fmaf_rn(dd - s, k, s);
-        }
-        case CGB_BLEND_DIFFERENCE: return fabsf(d - s);
-        default: return __fmaf_rn(-2.0f * d, s, d) + s;  // EXCLUSION
-    }
+// Packed pixel pairs.  Each lane holds two pixels of a tile row, so every
+// per-pixel operation of the blend is issued as one f32x2 instruction; each
+// element is rounded exactly as the scalar f32 operation (.rn, no flush).
+__device__ __forceinline__ unsigned long long f2u(float2 v) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(v.x), "f"(v.y));
+    return r;
+}
+__device__ __forceinline__ float2 u2f(unsigned long long r) {
+    float2 v;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
+    return v;
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(f2u(a)), "l"(f2u(b)), "l"(f2u(c)));
+    return u2f(d);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2u(a)), "l"(f2u(b)));
+    return u2f(d);
+}
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2u(a)), "l"(f2u(b)));
+    return u2f(d);
+}
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2u(a)), "l"(f2u(b)));
+    return u2f(d);
+}
+__device__ __forceinline__ float2 splat(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 sel2(bool a, bool b, float2 x, float2 y) {
+    return make_float2(a ? x.x : y.x, b ? x.y : y.y);
 }
 
+// blend_function! (style.rs:288-418) for a pixel pair
 template <int MODE>
-__device__ __forceinline__ float blend_vec_t(float d, float s) {
-    return blend_vec(MODE, d, s);  // MODE is a compile-time constant: the switch folds away
+__device__ __forceinline__ float2 blend_vec2(float2 d, float s) {
+    const float2 S = splat(s);
+    if (MODE == CGB_BLEND_OVER) return S;
+    if (MODE == CGB_BLEND_MULTIPLY) return mul2(d, S);
+    if (MODE == CGB_BLEND_SCREEN) return add2(fma2(d, splat(-s), d), S);
+    if (MODE == CGB_BLEND_OVERLAY) {
+        if (s <= 0.5f) return mul2(mul2(d, S), splat(2.0f));
+        return mul2(splat(2.0f), sub2(add2(S, d), fma2(S, d, splat(0.5f))));
+    }
+    if (MODE == CGB_BLEND_DARKEN) return make_float2(fminf(d.x, s), fminf(d.y, s));
+    if (MODE == CGB_BLEND_LIGHTEN) return make_float2(fmaxf(d.x, s), fmaxf(d.y, s));
+    if (MODE == CGB_BLEND_COLOR_DODGE) {
+        if (s == 0.0f) return splat(0.0f);
+        const float2 om = sub2(splat(1.0f), d);
+        return make_float2(fminf(1.0f, s / om.x), fminf(1.0f, s / om.y));
+    }
+    if (MODE == CGB_BLEND_COLOR_BURN) {
+        if (s == 1.0f) return splat(1.0f);
+        const float t = 1.0f - s;
+        return sub2(splat(1.0f), make_float2(fminf(1.0f, t / d.x), fminf(1.0f, t / d.y)));
+    }
+    if (MODE == CGB_BLEND_HARD_LIGHT) {
+        const float2 lo = mul2(mul2(d, S), splat(2.0f));
+        const float2 hi = mul2(splat(2.0f), sub2(add2(S, d), fma2(S, d, splat(0.5f))));
+        return sel2(d.x <= 0.5f, d.y <= 0.5f, lo, hi);
+    }
+    if (MODE == CGB_BLEND_SOFT_LIGHT) {
+        const float dd = s <= 0.25f ? __fmaf_rn(__fmaf_rn(16.0f, s, -12.0f), s, 4.0f) * s : sqrtf(s);
+        const float2 k = fma2(splat(2.0f), d, splat(-1.0f));
+        const float2 lo = fma2(splat(s * (1.0f - s)), k, S);
+        const float2 hi = fma2(splat(dd - s), k, S);
+        return sel2(d.x <= 0.5f, d.y <= 0.5f, lo, hi);
+    }
+    if (MODE == CGB_BLEND_DIFFERENCE) {
+        const float2 t = sub2(d, S);
+        return make_float2(fabsf(t.x), fabsf(t.y));
+    }
+    return add2(fma2(mul2(splat(-2.0f), d), S, d), S);  // EXCLUSION
 }
 
-// blend_at for one lane's two pixels of a column pair (painter/mod.rs:364-400),
+// blend_at for one lane's pixel pair of a tile row (painter/mod.rs:364-400),
 // specialised per blend mode so that the mode is dispatched once per layer.
+// C[q] holds channel q of the two pixels; a pixel whose column is not blended
+// keeps its color.
 template <int MODE>
-__device__ __forceinline__ void blend_pixels(float (&c)[2][4], const float4& src, const float (&cov)[2],
-                                             const bool (&col)[2]) {
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-        // computed for every pixel, kept where the column is blended
-        const float al = src.w * cov[h];
-        const float inv = 1.0f - al;
-        const float f0 = blend_vec_t<MODE>(c[h][0], src.x) * al;
-        const float f1 = blend_vec_t<MODE>(c[h][1], src.y) * al;
-        const float f2 = blend_vec_t<MODE>(c[h][2], src.z) * al;
-        const float n0 = __fmaf_rn(c[h][0], inv, f0);
-        const float n1 = __fmaf_rn(c[h][1], inv, f1);
-        const float n2 = __fmaf_rn(c[h][2], inv, f2);
-        const float n3 = __fmaf_rn(c[h][3], inv, al);
-        c[h][0] = col[h] ? n0 : c[h][0];
-        c[h][1] = col[h] ? n1 : c[h][1];
-        c[h][2] = col[h] ? n2 : c[h][2];
-        c[h][3] = col[h] ? n3 : c[h][3];
-    }
+__device__ __forceinline__ void blend_pixels(float2 (&C)[4], const float4& src, float2 cov, bool col0, bool col1) {
+    const float2 al = mul2(splat(src.w), cov);
+    const float2 inv = sub2(splat(1.0f), al);
+    const float2 n0 = fma2(C[0], inv, mul2(blend_vec2<MODE>(C[0], src.x), al));
+    const float2 n1 = fma2(C[1], inv, mul2(blend_vec2<MODE>(C[1], src.y), al));
+    const float2 n2 = fma2(C[2], inv, mul2(blend_vec2<MODE>(C[2], src.z), al));
+    const float2 n3 = fma2(C[3], inv, al);
+    C[0] = sel2(col0, col1, n0, C[0]);
+    C[1] = sel2(col0, col1, n1, C[1]);
+    C[2] = sel2(col0, col1, n2, C[2]);
+    C[3] = sel2(col0, col1, n3, C[3]);
 }
 
-__device__ __forceinline__ void blend_dispatch(uint32_t mode, float (&c)[2][4], const float4& src,
-                                               const float (&cov)[2], const bool (&col)[2]) {
+__device__ __forceinline__ void blend_dispatch(uint32_t mode, float2 (&C)[4], const float4& src, float2 cov,
+                                               bool col0, bool col1) {
     switch (mode) {
-        case CGB_BLEND_OVER: blend_pixels<CGB_BLEND_OVER>(c, src, cov, col); break;
-        case CGB_BLEND_MULTIPLY: blend_pixels<CGB_BLEND_MULTIPLY>(c, src, cov, col); break;
-        case CGB_BLEND_SCREEN: blend_pixels<CGB_BLEND_SCREEN>(c, src, cov, col); break;
-        case CGB_BLEND_OVERLAY: blend_pixels<CGB_BLEND_OVERLAY>(c, src, cov, col); break;
-        case CGB_BLEND_DARKEN: blend_pixels<CGB_BLEND_DARKEN>(c, src, cov, col); break;
-        case CGB_BLEND_LIGHTEN: blend_pixels<CGB_BLEND_LIGHTEN>(c, src, cov, col); break;
-        case CGB_BLEND_COLOR_DODGE: blend_pixels<CGB_BLEND_COLOR_DODGE>(c, src, cov, col); break;
-        case CGB_BLEND_COLOR_BURN: blend_pixels<CGB_BLEND_COLOR_BURN>(c, src, cov, col); break;
-        case CGB_BLEND_HARD_LIGHT: blend_pixels<CGB_BLEND_HARD_LIGHT>(c, src, cov, col); break;
-        case CGB_BLEND_SOFT_LIGHT: blend_pixels<CGB_BLEND_SOFT_LIGHT>(c, src, cov, col); break;
-        case CGB_BLEND_DIFFERENCE: blend_pixels<CGB_BLEND_DIFFERENCE>(c, src, cov, col); break;
-        default: blend_pixels<CGB_BLEND_EXCLUSION>(c, src, cov, col); break;
+        case CGB_BLEND_OVER: blend_pixels<CGB_BLEND_OVER>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_MULTIPLY: blend_pixels<CGB_BLEND_MULTIPLY>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_SCREEN: blend_pixels<CGB_BLEND_SCREEN>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_OVERLAY: blend_pixels<CGB_BLEND_OVERLAY>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_DARKEN: blend_pixels<CGB_BLEND_DARKEN>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_LIGHTEN: blend_pixels<CGB_BLEND_LIGHTEN>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_COLOR_DODGE: blend_pixels<CGB_BLEND_COLOR_DODGE>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_COLOR_BURN: blend_pixels<CGB_BLEND_COLOR_BURN>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_HARD_LIGHT: blend_pixels<CGB_BLEND_HARD_LIGHT>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_SOFT_LIGHT: blend_pixels<CGB_BLEND_SOFT_LIGHT>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_DIFFERENCE: blend_pixels<CGB_BLEND_DIFFERENCE>(C, src, cov, col0, col1); break;
+        default: blend_pixels<CGB_BLEND_EXCLUSION>(C, src, cov, col0, col1); break;
     }
 }
 
@@ -552,7 +599,6 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
     const uint32_t j = lt / p.row_len, i = lt % p.row_len;
     if (i < p.crop_h0 || i >= p.crop_h1 || j < p.crop_v0 || j >= p.crop_v1) return;
     const uint32_t b = a.tile_start[t], e = a.tile_start[t + 1];
-    const uint32_t n_orders = a.bg.n_orders;
 
     // tile_unchanged_pass (layer_workbench.rs:200-222)
     if (p.prev_layers) {
@@ -631,11 +677,9 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
     }
     if (painted) {
         // ColorBuffer: paint the unculled layers bottom-up (drive_tile_painting, :449-481).
-        float c[2][4];
+        float2 C[4];
 #pragma unroll
-        for (int h = 0; h < 2; h++)
-#pragma unroll
-            for (int q = 0; q < 4; q++) c[h][q] = p.clear[q];
+        for (int q = 0; q < 4; q++) C[q] = splat(p.clear[q]);
         const uint32_t start = k_op >= 0 ? (uint32_t)k_op : b;
         S.area[lane] = 0;
         S.area[lane + 32] = 0;
@@ -647,12 +691,12 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
             for (uint32_t q = 0; q < n; q++) {
                 const uint32_t meta = S.meta[q];
                 const uint32_t mode = meta & 15u, fr = (meta >> 4) & 1u;
-                float cov[2];
-                bool col[2];
+                float2 cov;
+                bool col0, col1;
                 if (meta & META_CARRY_ONLY) {
                     if (!(meta & META_ACTIVE)) continue;
-                    cov[0] = cov[1] = reinterpret_cast<const float*>(&S.rowcov[q][0])[y];
-                    col[0] = col[1] = true;
+                    cov = splat(reinterpret_cast<const float*>(&S.rowcov[q][0])[y]);
+                    col0 = col1 = true;
                 } else {
                     // acc_segment / acc_cover / compute_areas (painter/mod.rs:229-243, 347-362):
                     // per-cell sums in shared memory, then each lane reads
@@ -681,23 +725,23 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
                     if (xg >= 2) pre += t;
                     const int32_t cv = cy + pre - (v0 + v1);
                     const int32_t cv1 = cv + v0;
-                    cov[0] = from_area(PIXEL_WIDTH * (int32_t)(int8_t)cv + (int32_t)(int16_t)a0, fr);
-                    cov[1] = from_area(PIXEL_WIDTH * (int32_t)(int8_t)cv1 + (int32_t)(int16_t)a1, fr);
+                    cov.x = from_area(PIXEL_WIDTH * (int32_t)(int8_t)cv + (int32_t)(int16_t)a0, fr);
+                    cov.y = from_area(PIXEL_WIDTH * (int32_t)(int8_t)cv1 + (int32_t)(int16_t)a1, fr);
                     __syncwarp();
                     // A column is blended when any of its 8 coverages is non-zero
                     // (painter/mod.rs:287-289).
-                    const uint32_t b0 = __ballot_sync(0xffffffffu, cov[0] != 0.0f);
-                    const uint32_t b1 = __ballot_sync(0xffffffffu, cov[1] != 0.0f);
+                    const uint32_t b0 = __ballot_sync(0xffffffffu, cov.x != 0.0f);
+                    const uint32_t b1 = __ballot_sync(0xffffffffu, cov.y != 0.0f);
                     if (!(b0 | b1)) continue;
-                    col[0] = ((b0 >> (8 * xg)) & 0xFFu) != 0;
-                    col[1] = ((b1 >> (8 * xg)) & 0xFFu) != 0;
+                    col0 = ((b0 >> (8 * xg)) & 0xFFu) != 0;
+                    col1 = ((b1 >> (8 * xg)) & 0xFFu) != 0;
                 }
-                blend_dispatch(mode, c, S.color[q], cov, col);
+                blend_dispatch(mode, C, S.color[q], cov, col0, col1);
             }
             __syncwarp();
         }
-        px0 = pixel_bytes(c[0][0], c[0][1], c[0][2], c[0][3]);
-        px1 = pixel_bytes(c[1][0], c[1][1], c[1][2], c[1][3]);
+        px0 = pixel_bytes(C[0].x, C[1].x, C[2].x, C[3].x);
+        px1 = pixel_bytes(C[0].y, C[1].y, C[2].y, C[3].y);
     }
 
     // RGBA8 store: a full tile goes out as 16 x 16-byte half rows.
@@ -720,11 +764,14 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
 
 }  // namespace
 
-cudaError_t launch_tl_scan(int mode, const uint64_t* segs, uint32_t n, uint32_t row_len, uint32_t* block_counts,
+cudaError_t launch_tl_scan(int mode, const uint64_t* segs, uint32_t n, uint32_t col_bits, uint32_t* block_counts,
                            const uint32_t* block_off, const CarryBuffers& cb, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     count_launches(1);
-    k_tl_scan<<<tl_scan_grid(n), HEAD_THREADS, 0, st>>>(mode, segs, n, row_len, block_counts, block_off, cb);
+    if (mode == 0)
+        k_tl_scan<0><<<tl_scan_grid(n), HEAD_THREADS, 0, st>>>(segs, n, col_bits, block_counts, block_off, cb);
+    else
+        k_tl_scan<1><<<tl_scan_grid(n), HEAD_THREADS, 0, st>>>(segs, n, col_bits, block_counts, block_off, cb);
     return cudaGetLastError();
 }
 
