@@ -277,19 +277,30 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(const uint64_t* __res
         s_count[d] = sum;
     }
     __syncthreads();
+    // The tile's digit counts are published at once (aggregate status; the
+    // first tile's are already inclusive), so that later tiles can sum them
+    // while this one places its keys in shared memory.
+    const uint32_t my_cnt = tid < RADIX ? s_count[tid] : 0;
+    uint32_t* mine = lookback + (uint64_t)tile * RADIX + tid;
+    if (tid < RADIX) st_relaxed(mine, (tile == 0 ? ST_INC : ST_AGG) | my_cnt);
+    // Tile-local digit starts: exclusive scan of s_count over the RADIX digits.
+    {
+        uint32_t ex = block_exclusive_scan<uint32_t>(my_cnt, nullptr);
+        if (tid < RADIX) s_start[tid] = ex;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < SORT_ITEMS; k++) {
+        uint32_t d = dig[k];
+        if (d < RADIX) s_keys[s_start[d] + s_hist[warp][d] + rank[k]] = key[k];
+    }
     // Decoupled look-back for the tile's global digit offsets: one thread per
-    // digit publishes the tile's count (aggregate status), then walks back
-    // over its predecessors four entries per load round, summing until an
-    // inclusive prefix, and publishes its own inclusive prefix at once.
+    // digit walks back over its predecessors four entries per load round,
+    // summing until an inclusive prefix, and publishes its own.
     if (tid < RADIX) {
         const int d = tid;
-        const uint32_t cnt = s_count[d];
         uint32_t excl = 0;
-        uint32_t* mine = lookback + (uint64_t)tile * RADIX + d;
-        if (tile == 0) {
-            st_relaxed(mine, ST_INC | cnt);
-        } else {
-            st_relaxed(mine, ST_AGG | cnt);
+        if (tile > 0) {
             int64_t t = (int64_t)tile - 1;
             uint32_t spins = 0;
             while (t >= 0) {
@@ -319,21 +330,9 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(const uint64_t* __res
                 }
                 t -= used;
             }
-            st_relaxed(mine, ST_INC | ((excl + cnt) & ST_VAL));
+            st_relaxed(mine, ST_INC | ((excl + my_cnt) & ST_VAL));
         }
         s_base[d] = global_off[d] + excl;
-    }
-    // Tile-local digit starts: exclusive scan of s_count over the RADIX digits.
-    {
-        uint32_t v = tid < RADIX ? s_count[tid] : 0;
-        uint32_t ex = block_exclusive_scan<uint32_t>(v, nullptr);
-        if (tid < RADIX) s_start[tid] = ex;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < SORT_ITEMS; k++) {
-        uint32_t d = dig[k];
-        if (d < RADIX) s_keys[s_start[d] + s_hist[warp][d] + rank[k]] = key[k];
     }
     __syncthreads();
     if (s_abort) return;  // a predecessor never published: leave the output, the host reports the timeout
