@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(RADIX) k_radix_hist_scan(uint32_t* hist) {
     h[threadIdx.x] = ex;
 }
 
-__global__ void __launch_bounds__(SORT_THREADS) k_onesweep(const uint64_t* __restrict__ in, uint64_t* __restrict__ out,
+__global__ void __launch_bounds__(SORT_THREADS, 3) k_onesweep(const uint64_t* __restrict__ in, uint64_t* __restrict__ out,
                                                            uint32_t n, int shift, int bits,
                                                            const uint32_t* __restrict__ global_off,
                                                            uint32_t* lookback, uint32_t* tile_counter,
@@ -242,27 +242,26 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(const uint64_t* __res
     const uint64_t base = (uint64_t)tile * SORT_TILE;
 
     uint64_t key[SORT_ITEMS];
-    uint32_t dig[SORT_ITEMS];
-    uint32_t rank[SORT_ITEMS];
+    uint32_t dr[SORT_ITEMS];  // digit (RADIX = none) | rank within the warp << 16
 #pragma unroll
     for (int k = 0; k < SORT_ITEMS; k++) {
         uint64_t idx = base + (uint64_t)warp * 32 * SORT_ITEMS + k * 32 + lane;
         bool valid = idx < n;
         key[k] = valid ? in[idx] : 0;
-        dig[k] = valid ? ((uint32_t)(key[k] >> shift) & mask) : RADIX;
+        dr[k] = valid ? ((uint32_t)(key[k] >> shift) & mask) : RADIX;
     }
     // Warp-level multi-split ranking, in key order within the warp (stable).
     const uint32_t lt = lanemask_lt();
 #pragma unroll
     for (int k = 0; k < SORT_ITEMS; k++) {
-        uint32_t d = dig[k];
+        uint32_t d = dr[k];
         uint32_t peers = __match_any_sync(0xffffffffu, d);
         uint32_t r = __popc(peers & lt);
         uint32_t cnt = d < RADIX ? s_hist[warp][d] : 0;
         __syncwarp();
         if (d < RADIX && r == 0) s_hist[warp][d] = (uint16_t)(cnt + __popc(peers));
         __syncwarp();
-        rank[k] = cnt + r;
+        dr[k] = d | ((cnt + r) << 16);
     }
     __syncthreads();
     // Per digit: exclusive offsets across warps and the tile's count.
@@ -291,8 +290,8 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(const uint64_t* __res
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < SORT_ITEMS; k++) {
-        uint32_t d = dig[k];
-        if (d < RADIX) s_keys[s_start[d] + s_hist[warp][d] + rank[k]] = key[k];
+        const uint32_t d = dr[k] & 0xFFFFu;
+        if (d < RADIX) s_keys[s_start[d] + s_hist[warp][d] + (dr[k] >> 16)] = key[k];
     }
     // Decoupled look-back for the tile's global digit offsets: one thread per
     // digit walks back over its predecessors four entries per load round,
