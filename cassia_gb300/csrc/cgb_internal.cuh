@@ -145,30 +145,7 @@ __device__ __forceinline__ int32_t sext(uint64_t v, int bits) {
     return (int32_t)(int64_t)((v ^ m) - m);
 }
 
-// CompactSegment packing (raster_segment.rs:142-154) and the D5 layout.
-__device__ __forceinline__ uint64_t pack_segment(uint32_t wide, int32_t tile_j, int32_t tile_i_stored, uint32_t layer,
-                                                 uint32_t ty, uint32_t tx, int32_t area, int32_t cover) {
-    uint64_t v;
-    if (!wide) {
-        v = ((uint64_t)(uint32_t)tile_j & 0xFFF);
-        v = (v << 13) | ((uint64_t)(uint32_t)tile_i_stored & 0x1FFF);
-        v = (v << 16) | ((uint64_t)layer & 0xFFFF);
-    } else {
-        v = ((uint64_t)(uint32_t)tile_j & 0xFFF);
-        v = (v << 13) | ((uint64_t)(uint32_t)tile_i_stored & 0x1FFF);
-        v = (v << 17) | ((uint64_t)layer & 0x1FFFF);
-    }
-    v = (v << 3) | (ty & 7);
-    v = (v << 3) | (tx & 7);
-    v = (v << 10) | ((uint64_t)(uint32_t)area & 0x3FF);
-    v = (v << 6) | ((uint64_t)(uint32_t)cover & 0x3F);
-    return v;
-}
-__device__ __forceinline__ int32_t seg_tile_j(uint32_t wide, uint64_t s) { return sext(s >> (wide ? 52 : 51), 12); }
-__device__ __forceinline__ int32_t seg_tile_i_stored(uint32_t wide, uint64_t s) { return sext(s >> (wide ? 39 : 38), 13); }
-__device__ __forceinline__ uint32_t seg_layer(uint32_t wide, uint64_t s) {
-    return wide ? (uint32_t)((s >> 22) & 0x1FFFF) : (uint32_t)((s >> 22) & 0xFFFF);
-}
+// Low 22 bits of a CompactSegment (raster_segment.rs:142-154): tile_y | tile_x | area | cover.
 __device__ __forceinline__ uint32_t low_tile_y(uint32_t low) { return (low >> 19) & 7; }
 __device__ __forceinline__ uint32_t low_tile_x(uint32_t low) { return (low >> 16) & 7; }
 __device__ __forceinline__ int32_t low_area(uint32_t low) { return sext(low >> 6, 10); }

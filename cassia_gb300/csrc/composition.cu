@@ -10,7 +10,9 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <new>
 #include <map>
 #include <mutex>
 #include <set>
@@ -91,6 +93,44 @@ struct CacheState {
     uint64_t tiles = 0;
 };
 
+// Page-locked host storage for the layer table mirror, so that its upload is
+// one asynchronous DMA instead of a staged pageable copy.  Falls back to
+// pageable memory if pinning fails.
+template <class T>
+struct PinnedAllocator {
+    using value_type = T;
+    PinnedAllocator() = default;
+    template <class U>
+    PinnedAllocator(const PinnedAllocator<U>&) {}
+    T* allocate(size_t n) {
+        void* p = nullptr;
+        if (cudaMallocHost(&p, n * sizeof(T)) != cudaSuccess) {
+            cudaGetLastError();
+            p = std::malloc(n * sizeof(T));
+            if (!p) throw std::bad_alloc();
+            pageable().insert(p);
+        }
+        return static_cast<T*>(p);
+    }
+    void deallocate(T* p, size_t) {
+        auto it = pageable().find(p);
+        if (it != pageable().end()) {
+            pageable().erase(it);
+            std::free(p);
+        } else {
+            cudaFreeHost(p);
+        }
+    }
+    static std::set<void*>& pageable() {
+        static std::set<void*> s;
+        return s;
+    }
+    template <class U>
+    bool operator==(const PinnedAllocator<U>&) const { return true; }
+    template <class U>
+    bool operator!=(const PinnedAllocator<U>&) const { return false; }
+};
+
 }  // namespace
 
 struct cgb_composition {
@@ -115,7 +155,7 @@ struct cgb_composition {
     std::set<uint32_t> released;
     uint32_t next_fresh = 0;
     uint64_t enabled_len = 0;            // Composition::actual_len, kept incrementally
-    std::vector<LayerRec> layer_recs;    // host mirror of the device layer table
+    std::vector<LayerRec, PinnedAllocator<LayerRec>> layer_recs;  // host mirror of the device layer table
     uint32_t dirty_lo = UINT32_MAX, dirty_hi = 0;
     bool layers_grew = true;
     DevBuf d_layers;
@@ -968,9 +1008,29 @@ CGB_EXPORT cgb_status cgb_layer_set_transform(cgb_composition* c, uint32_t layer
 CGB_EXPORT cgb_status cgb_layers_set_transforms(cgb_composition* c, size_t n, const uint32_t* layer_ids,
                                                 const float* affine6, uint32_t flags) {
     if (!c || (n && (!layer_ids || !affine6))) return fail(CGB_ERR_INVALID_ARG, "null argument");
+    const bool check = !(flags & CGB_TRANSFORM_UNCHECKED);
     for (size_t i = 0; i < n; i++) {
-        cgb_status st = set_transform(c, layer_ids[i], affine6 + 6 * i, flags);
-        if (st) return st;
+        const uint32_t id = layer_ids[i];
+        const float* t = affine6 + 6 * i;
+        // the common case inline: an existing layer whose transform stays a
+        // non-identity one; everything else through set_transform
+        HostLayer* l = find_layer(c, id);
+        const bool identity = t[0] == 1 && t[1] == 0 && t[2] == 0 && t[3] == 1 && t[4] == 0 && t[5] == 0;
+        if (!l || identity || !l->has_transform || id >= c->layer_recs.size()) {
+            cgb_status st = set_transform(c, id, t, flags);
+            if (st) return st;
+            continue;
+        }
+        if (check && (t[0] * t[0] + t[2] * t[2] > 1.001f || t[1] * t[1] + t[3] * t[3] > 1.001f))
+            return fail(CGB_ERR_SCALE, "set_transform: Layer's scaling on each axis must be between -1.0 and 1.0");
+        if (l->t[0] == t[0] && l->t[1] == t[1] && l->t[2] == t[2] && l->t[3] == t[3] && l->t[4] == t[4] &&
+            l->t[5] == t[5])
+            continue;  // equal as f32 (Layer::set_transform compares with ==)
+        l->unchanged = 0;
+        std::memcpy(l->t, t, sizeof(l->t));
+        std::memcpy(c->layer_recs[id].t, t, sizeof(l->t));
+        c->dirty_lo = std::min(c->dirty_lo, id);
+        c->dirty_hi = std::max(c->dirty_hi, id + 1);
     }
     return CGB_OK;
 }

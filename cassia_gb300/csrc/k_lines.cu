@@ -404,79 +404,110 @@ __global__ void k_build_lines(BatchGeom bg, int cull, LineRec* __restrict__ recs
 // rasterization
 // ---------------------------------------------------------------------------
 
-// tiles + area_cover + CompactSegment::new (rasterizer/mod.rs:134-189)
-__device__ __forceinline__ uint64_t make_segment(uint32_t wide, uint32_t layer, int32_t x0, int32_t x1, int32_t y0,
-                                                 int32_t y1, int32_t bx, int32_t by, uint32_t oct) {
-    if (oct == 1 || oct == 2 || oct == 5 || oct == 6) {
-        int32_t t = bx;
-        bx = by;
-        by = t;
-    }
-    int32_t ti = (int16_t)(bx >> TILE_SHIFT);
-    int32_t tj = (int16_t)(by >> TILE_SHIFT);
-    uint32_t tx = (uint32_t)(bx & TILE_MASK), ty = (uint32_t)(by & TILE_MASK);
-    int32_t a0 = x0, a1 = x1, b0 = y0, b1 = y1;
-    switch (oct) {
-        case 1: a0 = y0; a1 = y1; b0 = x0; b1 = x1; break;
-        case 2: a0 = y1; a1 = y0; b0 = x0; b1 = x1; break;
-        case 3:
-        case 4: b0 = y1; b1 = y0; break;
-        case 5: a0 = y0; a1 = y1; b0 = x1; b1 = x0; break;
-        case 6: a0 = y1; a1 = y0; b0 = x1; b1 = x0; break;
-        default: break;
-    }
-    int32_t border = wadd(a0 & ~PIXEL_MASK, PIXEL_WIDTH);
-    int32_t height = wsub(b1, b0);
-    int32_t triangle = (int16_t)(wmul(height, wsub(a1, a0)) / 2);
-    int32_t rectangle = (int16_t)wmul(height, wsub(border, a1));
-    int32_t area = (int16_t)(uint16_t)((uint32_t)triangle + (uint32_t)rectangle);
-    int32_t cover = (int8_t)height;
-    int32_t tis = (int16_t)(uint16_t)((uint32_t)(ti > -1 ? ti : -1) + 256u);
-    return pack_segment(wide, tj, tis, layer, ty, tx, area, cover);
+// The fields of one CompactSegment: tile_j, the stored tile_i (+256) and the
+// low 22 bits (tile_y | tile_x | area | cover).
+struct SegFields {
+    int32_t tj, tis;
+    uint32_t low;
+};
+
+// tiles + area_cover + CompactSegment::new (rasterizer/mod.rs:134-189).  The
+// octant's coordinate swaps are selects, so lanes on lines of different
+// octants do not diverge.
+__device__ __forceinline__ SegFields seg_fields(int32_t x0, int32_t x1, int32_t y0, int32_t y1, int32_t bx,
+                                                int32_t by, uint32_t oct) {
+    const bool swap = (0x66u >> oct) & 1u;    // octants 1, 2, 5, 6: x and y exchanged
+    const bool flip_a = (0x44u >> oct) & 1u;  // 2, 6: the first coordinate's ends exchanged
+    const bool flip_b = (0x78u >> oct) & 1u;  // 3, 4, 5, 6: the second coordinate's ends exchanged
+    const int32_t cx = swap ? by : bx, cy = swap ? bx : by;
+    const int32_t p0 = swap ? y0 : x0, p1 = swap ? y1 : x1;
+    const int32_t q0 = swap ? x0 : y0, q1 = swap ? x1 : y1;
+    const int32_t a0 = flip_a ? p1 : p0, a1 = flip_a ? p0 : p1;
+    const int32_t b0 = flip_b ? q1 : q0, b1 = flip_b ? q0 : q1;
+    const int32_t ti = (int16_t)(cx >> TILE_SHIFT);
+    const int32_t tj = (int16_t)(cy >> TILE_SHIFT);
+    const uint32_t tx = (uint32_t)(cx & TILE_MASK), ty = (uint32_t)(cy & TILE_MASK);
+    const int32_t border = wadd(a0 & ~PIXEL_MASK, PIXEL_WIDTH);
+    const int32_t height = wsub(b1, b0);
+    const int32_t triangle = (int16_t)(wmul(height, wsub(a1, a0)) / 2);
+    const int32_t rectangle = (int16_t)wmul(height, wsub(border, a1));
+    const int32_t area = (int16_t)(uint16_t)((uint32_t)triangle + (uint32_t)rectangle);
+    const int32_t cover = (int8_t)height;
+    const int32_t tis = (int16_t)(uint16_t)((uint32_t)(ti > -1 ? ti : -1) + 256u);
+    return SegFields{tj, tis, (ty << 19) | (tx << 16) | (((uint32_t)area & 0x3FFu) << 6) | ((uint32_t)cover & 0x3Fu)};
+}
+
+// The packed CompactSegment (raster_segment.rs:142-154; with `wide`, the
+// 17-bit layer field of the widened format in place of is_none).
+__device__ __forceinline__ uint64_t pack_fields(uint32_t wide, uint32_t layer, const SegFields& f) {
+    const uint64_t hi = ((uint64_t)((uint32_t)f.tj & 0xFFFu) << 13) | ((uint32_t)f.tis & 0x1FFFu);
+    const uint64_t mid = wide ? ((hi << 17) | (layer & 0x1FFFFu)) : ((hi << 16) | (layer & 0xFFFFu));
+    return (mid << 22) | f.low;
 }
 
 __device__ __forceinline__ bool intersects_y_border(int32_t y0, int32_t y1) {
     return (y0 & PIXEL_MASK) != 0 && (y1 & PIXEL_MASK) != 0 && (y0 >> PIXEL_SHIFT) != (y1 >> PIXEL_SHIFT);
 }
 
-// One pixel step (rasterizer/mod.rs:233-281); returns 1 or 2 segments.
-__device__ __forceinline__ int raster_step(uint32_t wide, const LineRec& l, int32_t pi, uint64_t out[2]) {
-    const uint32_t oct = l.order_octant & 7, layer = (l.order_octant >> 3) & ((1u << (LINE_SCENE_SHIFT - 3)) - 1);
-    int32_t x0i = wadd(l.start, pi);
-    int32_t x1i = wadd(x0i, 1);
-    int32_t border_x = x0i;
-    float x0 = fmaxf((float)x0i, l.start_f32);
-    float x1 = fminf((float)x1i, l.end_f32);
-    float y0 = __fmaf_rn(l.slope, x0, l.py_slope_px);
-    float y1 = __fmaf_rn(l.slope, x1, l.py_slope_px);
-    int32_t x0s = to_sub_pixel(x0), x1s = to_sub_pixel(x1), y0s = to_sub_pixel(y0), y1s = to_sub_pixel(y1);
-    if (intersects_y_border(y0s, y1s)) {
-        int32_t y = max(y0s, y1s) >> PIXEL_SHIFT;
-        int32_t ys = (int32_t)((uint32_t)y << PIXEL_SHIFT);
-        float x = __fmaf_rn(l.slope_recip, (float)y, l.px_slope_recip_py);
-        int32_t xs = to_sub_pixel(x);
-        out[0] = make_segment(wide, layer, x0s, xs, y0s, ys, border_x, min(ys, y0s) >> PIXEL_SHIFT, oct);
-        out[1] = make_segment(wide, layer, xs, x1s, ys, y1s, border_x, min(ys, y1s) >> PIXEL_SHIFT, oct);
-        return 2;
-    }
-    out[0] = make_segment(wide, layer, x0s, x1s, y0s, y1s, border_x, min(y0s, y1s) >> PIXEL_SHIFT, oct);
-    return 1;
-}
-
 // Render format: culls segments the painter never reads (rows outside the
 // canvas, tiles right of it, 13-bit tile_i wrap) and re-keys the rest by
 // (global tile row, order, tile column + 1) above the reference's low 22 bits.
+// The tile fields are read as the packed segment stores them (12-bit
+// tile_j, 13-bit tile_i), so wrapped values land where the reference's do.
 struct SceneRaster {
     uint32_t wide, rows, row_len, row_base;
 };
 
-__device__ __forceinline__ bool render_key(const SceneRaster& sr, const BatchGeom& bg, uint64_t seg, uint64_t& out) {
-    int32_t tj = seg_tile_j(sr.wide, seg);
-    int32_t ti = seg_tile_i_stored(sr.wide, seg) - 256;
+__device__ __forceinline__ bool render_key(const SceneRaster& sr, const BatchGeom& bg, uint32_t layer,
+                                           const SegFields& f, uint64_t& out) {
+    const int32_t tj = (int32_t)((uint32_t)f.tj << 20) >> 20;
+    const int32_t ti = ((int32_t)((uint32_t)f.tis << 19) >> 19) - 256;
     if (tj < 0 || tj >= (int32_t)sr.rows || ti < -1 || ti >= (int32_t)sr.row_len) return false;
-    const uint64_t key = make_render_key(bg, sr.row_base + (uint32_t)tj, seg_layer(sr.wide, seg), (uint32_t)(ti + 1));
-    out = (key << 22) | (seg & 0x3FFFFFull);
+    const uint32_t lmask = sr.wide ? 0x1FFFFu : 0xFFFFu;
+    out = (make_render_key(bg, sr.row_base + (uint32_t)tj, layer & lmask, (uint32_t)(ti + 1)) << 22) | f.low;
     return true;
+}
+
+// One pixel step (rasterizer/mod.rs:233-281): one or two segments, of which
+// the kept ones (all of them outside render mode) go to out; `produced`
+// counts both.
+template <int RENDER>
+__device__ __forceinline__ int raster_step(const SceneRaster& sr, const BatchGeom& bg, const LineRec& l, int32_t pi,
+                                           uint64_t out[2], int& produced) {
+    const uint32_t oct = l.order_octant & 7, layer = (l.order_octant >> 3) & ((1u << (LINE_SCENE_SHIFT - 3)) - 1);
+    const int32_t x0i = wadd(l.start, pi);
+    const int32_t x1i = wadd(x0i, 1);
+    const int32_t border_x = x0i;
+    const float x0 = fmaxf((float)x0i, l.start_f32);
+    const float x1 = fminf((float)x1i, l.end_f32);
+    const float y0 = __fmaf_rn(l.slope, x0, l.py_slope_px);
+    const float y1 = __fmaf_rn(l.slope, x1, l.py_slope_px);
+    const int32_t x0s = to_sub_pixel(x0), x1s = to_sub_pixel(x1), y0s = to_sub_pixel(y0), y1s = to_sub_pixel(y1);
+    const bool inter = intersects_y_border(y0s, y1s);
+    // the crossing of the pixel row border (used only when the step crosses it)
+    const int32_t ys = (int32_t)((uint32_t)(max(y0s, y1s) >> PIXEL_SHIFT) << PIXEL_SHIFT);
+    const int32_t xs = to_sub_pixel(__fmaf_rn(l.slope_recip, (float)(max(y0s, y1s) >> PIXEL_SHIFT), l.px_slope_recip_py));
+    const int32_t ex = inter ? xs : x1s, ey = inter ? ys : y1s;
+    int m = 0;
+    {
+        const SegFields f = seg_fields(x0s, ex, y0s, ey, border_x, min(ey, y0s) >> PIXEL_SHIFT, oct);
+        if (RENDER) {
+            if (render_key(sr, bg, layer, f, out[m])) m++;
+        } else {
+            out[m++] = pack_fields(sr.wide, layer, f);
+        }
+    }
+    produced += 1;
+    if (inter) {
+        const SegFields f = seg_fields(xs, x1s, ys, y1s, border_x, min(ys, y1s) >> PIXEL_SHIFT, oct);
+        if (RENDER) {
+            if (render_key(sr, bg, layer, f, out[m])) m++;
+        } else {
+            out[m++] = pack_fields(sr.wide, layer, f);
+        }
+        produced += 1;
+    }
+    return m;
 }
 
 constexpr int RASTER_ITEMS = 8;  // consecutive pixel steps per thread
@@ -527,17 +558,10 @@ __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ r
                     }
                 }
                 uint64_t o[2];
-                int m = raster_step(sr.wide, rec, (int32_t)(s - off[l]), o);
-                total += m;
+                const int m = raster_step<RENDER>(sr, bg, rec, (int32_t)(s - off[l]), o, total);
 #pragma unroll
-                for (int q = 0; q < 2; q++) {
-                    if (q < m) {
-                        uint64_t v = o[q];
-                        bool keep = true;
-                        if (RENDER) keep = render_key(sr, bg, o[q], v);
-                        if (keep) segs[n++] = v;
-                    }
-                }
+                for (int q = 0; q < 2; q++)
+                    if (q < m) segs[n++] = o[q];
             }
         }
     }
