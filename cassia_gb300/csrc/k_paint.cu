@@ -197,12 +197,22 @@ constexpr uint32_t ITEM_FULL = 2u;
 constexpr uint32_t ITEM_CARRY = 4u;
 constexpr int ITEM_FLAG_BITS = 3;
 
-// Items of TL g: its own (tile, order) pair and the cover-carry-only tiles up
-// to the next TL of its (row, order) run.  Returns the count; `emit(tile,
-// flags)` is called for each.
-template <class Emit>
-__device__ __forceinline__ uint32_t tl_items(uint32_t g, uint32_t G,
-                                             const CarryBuffers& cb, const BatchGeom& bg, Emit emit) {
+// The work items of TL g: its own (tile, order) pair, when its tile is
+// painted, and cover-carry-only items for the tiles [ta, tb) of its row, up
+// to the next TL of its (row, order) run.
+struct TlItems {
+    uint64_t row_tile;  // global index of the first tile of the TL's row
+    int32_t own;        // tile column of the own item, or -1
+    int32_t ta, tb;     // the carry-only items' tile columns (none if ta >= tb)
+    uint32_t flags;     // the carry-only items' flags
+    uint32_t L;
+    __device__ __forceinline__ uint32_t count() const {
+        return (own >= 0 ? 1u : 0u) + (tb > ta ? (uint32_t)(tb - ta) : 0u);
+    }
+};
+
+__device__ __forceinline__ TlItems tl_items(uint32_t g, uint32_t G, const CarryBuffers& cb, const BatchGeom& bg) {
+    TlItems r{0, -1, 0, 0, 0, 0};
     const uint64_t key = cb.tl_key[g];
     const int32_t i = (int32_t)key_col1(key, bg.col_bits) - 1;
     const uint64_t run = key_run(key, bg.col_bits);
@@ -210,62 +220,94 @@ __device__ __forceinline__ uint32_t tl_items(uint32_t g, uint32_t G,
     const uint32_t grow = run_row(run, bg.order_bits);
     const SceneDesc& S = bg.scenes[bg.row_scene[grow]];
     const uint32_t j = grow - S.row_base;
-    if (j < S.crop_v0 || j >= S.crop_v1) return 0;
+    if (j < S.crop_v0 || j >= S.crop_v1) return r;
+    r.L = L;
+    r.row_tile = (uint64_t)S.tile_base + (uint64_t)j * S.row_len;
     int32_t next = (int32_t)S.row_len;
     if (g + 1 < G && !cb.tl_flags[g + 1]) next = (int32_t)key_col1(cb.tl_key[g + 1], bg.col_bits) - 1;
     const int32_t h0 = (int32_t)S.crop_h0, h1 = (int32_t)S.crop_h1;
     if (next > h1) next = h1;
-    uint32_t cnt = 0;
-    if (i >= h0 && i < h1) {
-        emit(S, j, i, ITEM_OWN);  // a layer with segments is never "full" (layer_workbench.rs:164-175)
-        cnt++;
-    }
-    if (next <= i + 1) return cnt;
+    if (i >= h0 && i < h1) r.own = i;  // a layer with segments is never "full" (layer_workbench.rs:164-175)
+    if (next <= i + 1) return r;
     const uint64_t carry_out = cover_add(cb.tl_carry[g], cb.tl_cover[g]);
     const PaintProps pp = S.props[L];
     const bool nonempty = !cover_is_empty(carry_out, pp.fill_rule);
     // payload of a cover-carry-only item: its layer_is_full and the opaque
     // Solid Over test of skip_fully_covered_layers (:335-356)
     const bool full = cover_is_full(carry_out, pp.fill_rule);
-    const uint32_t flags = ITEM_CARRY | (full ? ITEM_FULL : 0u) | (full && (pp.flags & PROPS_OPAQUE_OVER) ? ITEM_OPAQUE : 0u);
-    int32_t t = i + 1;
+    r.flags = ITEM_CARRY | (full ? ITEM_FULL : 0u) | (full && (pp.flags & PROPS_OPAQUE_OVER) ? ITEM_OPAQUE : 0u);
     if (i < h0) {
         // the first painted tile of the row holds every layer with segments
         // to its left, empty or not
-        if (next <= h0) return cnt;
-        emit(S, j, h0, flags);
-        cnt++;
-        t = h0 + 1;
+        if (next <= h0) return r;
+        r.ta = h0;
+        r.tb = nonempty ? next : h0 + 1;
+        return r;
     }
-    if (nonempty)
-        for (; t < next; t++) {
-            emit(S, j, t, flags);
-            cnt++;
-        }
-    return cnt;
+    if (nonempty) {
+        r.ta = i + 1;
+        r.tb = next;
+    }
+    return r;
 }
 
 __global__ void k_items_count(uint32_t G, CarryBuffers cb, BatchGeom bg) {
     uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= G) return;
-    cb.item_count[g] = tl_items(g, G, cb, bg, [](const SceneDesc&, uint32_t, int32_t, uint32_t) {});
+    cb.item_count[g] = tl_items(g, G, cb, bg).count();
 }
 
 // Item = tile | order | flags | TL index, high to low; the tile field is the
 // sort key.  The items of a tile are written in ascending order (the TLs
 // are sorted by row, then order), so a stable sort on the tile alone leaves
-// each tile's items in paint order.
-__global__ void k_items_write(uint32_t G, CarryBuffers cb, BatchGeom bg, int idx_bits) {
-    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= G) return;
-    const uint64_t L = run_order(key_run(cb.tl_key[g], bg.col_bits), bg.order_bits);
+// each tile's items in paint order.  Each block expands the items of its 256
+// TLs together: thread t writes items t, t + 256, ... of the block's range.
+constexpr int IW_THREADS = 256;
+
+__global__ void __launch_bounds__(IW_THREADS) k_items_write(uint32_t G, CarryBuffers cb, BatchGeom bg, int idx_bits) {
+    __shared__ uint32_t s_off[IW_THREADS + 1];  // item offsets of the block's TLs, from its first item
+    __shared__ uint64_t s_row[IW_THREADS];
+    __shared__ int32_t s_own[IW_THREADS], s_ta[IW_THREADS];
+    __shared__ uint32_t s_lf[IW_THREADS];  // order << 3 | carry-only flags
+    const uint32_t g0 = blockIdx.x * IW_THREADS, g = g0 + threadIdx.x;
+    const uint32_t nt = min(G - g0, (uint32_t)IW_THREADS);
+    const uint32_t base = cb.item_off[g0];
+    if (g < G) {
+        const TlItems r = tl_items(g, G, cb, bg);
+        s_off[threadIdx.x] = cb.item_off[g] - base;
+        s_row[threadIdx.x] = r.row_tile;
+        s_own[threadIdx.x] = r.own;
+        s_ta[threadIdx.x] = r.ta;
+        s_lf[threadIdx.x] = (r.L << ITEM_FLAG_BITS) | r.flags;
+    }
+    if (threadIdx.x == 0) s_off[nt] = cb.item_off[g0 + nt] - base;
+    __syncthreads();
+    const uint32_t total = s_off[nt];
     const int ob = cb.order_bits;
-    uint32_t o = cb.item_off[g];
-    tl_items(g, G, cb, bg, [&](const SceneDesc& S, uint32_t j, int32_t t, uint32_t flags) {
-        const uint64_t tile = (uint64_t)S.tile_base + (uint64_t)j * S.row_len + (uint64_t)t;
-        const uint64_t k = ((((tile << ob) | L) << ITEM_FLAG_BITS) | flags);
-        cb.items[o++] = (k << idx_bits) | g;
-    });
+    for (uint32_t idx = threadIdx.x; idx < total; idx += IW_THREADS) {
+        // the TL q with s_off[q] <= idx < s_off[q + 1] (the last one with s_off[q] <= idx)
+        uint32_t lo = 0, hi = nt;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (s_off[mid] <= idx) lo = mid;
+            else hi = mid;
+        }
+        const uint32_t k = idx - s_off[lo];
+        const int32_t own = s_own[lo];
+        const uint32_t lf = s_lf[lo];
+        int32_t col;
+        uint32_t fl;
+        if (own >= 0 && k == 0) {
+            col = own;
+            fl = ITEM_OWN;
+        } else {
+            col = s_ta[lo] + (int32_t)(k - (own >= 0 ? 1u : 0u));
+            fl = lf & 7u;
+        }
+        const uint64_t tile = s_row[lo] + (uint64_t)col;
+        const uint64_t key = (((tile << ob) | (lf >> ITEM_FLAG_BITS)) << ITEM_FLAG_BITS) | fl;
+        cb.items[base + idx] = (key << idx_bits) | (g0 + lo);
+    }
 }
 
 __global__ void k_tile_ranges(const uint64_t* __restrict__ items, uint32_t W, uint32_t n_tiles, int tile_shift,
@@ -791,7 +833,7 @@ cudaError_t launch_items(int mode, uint32_t G, const BatchGeom& bg, const CarryB
     if (mode == 0)
         k_items_count<<<(G + 255) / 256, 256, 0, st>>>(G, cb, bg);
     else
-        k_items_write<<<(G + 255) / 256, 256, 0, st>>>(G, cb, bg, idx_bits);
+        k_items_write<<<(G + IW_THREADS - 1) / IW_THREADS, IW_THREADS, 0, st>>>(G, cb, bg, idx_bits);
     return cudaGetLastError();
 }
 
