@@ -71,7 +71,10 @@ def make_clients(n_clients: int, seed: int, device_out: bool = True, max_layers:
     sset = scenes.batch(seed=seed, n_scenes=n_clients, max_layers=max_layers)
     clients = []
     for k, sc in enumerate(sset):
-        c = Composition(wide=sc.wide)
+        # churn needs fresh layer ids until the lines garbage collection of
+        # remove_disabled frees the removed ones (at 50% garbage): large
+        # clients use the widened 17-bit layer format
+        c = Composition(wide=sc.wide or sc.n_layers > 30_000)
         scenes.load(sc, c)
         if device_out:
             out = torch.zeros((sc.height, sc.width, 4), dtype=torch.uint8, device="cuda")
@@ -82,15 +85,31 @@ def make_clients(n_clients: int, seed: int, device_out: bool = True, max_layers:
     return clients
 
 
+def _u01(ids: np.ndarray, salt: int) -> np.ndarray:
+    """Seeded uniform [0, 1) per id (splitmix64 of id and salt), vectorized."""
+    with np.errstate(over="ignore"):
+        z = ids.astype(np.uint64) * np.uint64(0x9E3779B97F4A7C15) + np.uint64(salt & 0xFFFFFFFFFFFFFFFF)
+        z ^= z >> np.uint64(30)
+        z *= np.uint64(0xBF58476D1CE4E5B9)
+        z ^= z >> np.uint64(27)
+        z *= np.uint64(0x94D049BB133111EB)
+        z ^= z >> np.uint64(31)
+    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / (1 << 53))
+
+
 def apply_update(cl: Client, client_id: int, seq: int, changed: float = 0.2, churn: float = 0.01):
-    """The scene update of frame `seq`: `changed` of the enabled layers get a
-    new affine (seeded), `churn` of them are removed and as many added."""
-    rng = np.random.default_rng((client_id << 32) ^ (seq * 2654435761 % (1 << 32)))
-    live = np.nonzero(cl.enabled)[0]
+    """The scene update of frame `seq`: each enabled layer gets a new affine
+    with probability `changed` and is removed with probability `churn`
+    (seeded per client and frame); as many layers as were removed are added."""
+    live = np.flatnonzero(cl.enabled).astype(np.uint32)
     if len(live) == 0:
         return
-    n_chg = max(1, int(round(changed * len(live))))
-    ids = rng.choice(live, size=min(n_chg, len(live)), replace=False).astype(np.uint32)
+    salt = (client_id << 40) ^ (seq * 0x9E3779B1)
+    u = _u01(live, salt)
+    ids = live[u < changed]
+    if len(ids) == 0:
+        ids = live[:1]
+    rng = np.random.default_rng((client_id << 32) ^ (seq * 2654435761 % (1 << 32)))
     t = cl.transforms[ids]
     th = rng.uniform(-0.05, 0.05, size=len(ids)).astype(np.float32)
     c, s = np.cos(th), np.sin(th)
@@ -101,24 +120,45 @@ def apply_update(cl: Client, client_id: int, seq: int, changed: float = 0.2, chu
     t[:, 5] += rng.uniform(-3, 3, size=len(ids)).astype(np.float32)
     cl.transforms[ids] = t
     cl.comp.set_transforms(ids, t)
-    n_churn = int(churn * len(live))
-    if n_churn:
-        gone = rng.choice(live, size=n_churn, replace=False).astype(np.uint32)
+    gone = live[_u01(live, salt ^ 0x5DEECE66D) < churn]
+    if len(gone):
         cl.comp.set_enabled_many(gone, np.zeros(len(gone), np.uint8))
         cl.enabled[gone] = False
-        add_layers(cl, n_churn)
+        cl.comp.remove_disabled()  # mold's GC: drops the disabled layers at 50% garbage
+        add_layers(cl, len(gone))
+
+
+def _pool_runs(start: int, n: int, size: int):
+    """[a, b) runs of pool indices start, start + 1, ... (n of them, mod size)."""
+    runs, a = [], start % size
+    while n > 0:
+        b = min(size, a + n)
+        runs.append((a, b))
+        n -= b - a
+        a = 0
+    return runs
 
 
 def add_layers(cl: Client, n: int):
-    """Adds n layers drawn from the client's shape pool (one insert call)."""
+    """Adds n layers drawn in turn from the client's shape pool (one path
+    per pool layer), with one insert call."""
     p = cl.pool
     ids = cl.comp.create_layers(n)
-    picks = (cl.pool_next + np.arange(n)) % p.n_layers
+    runs = _pool_runs(cl.pool_next, n, p.n_layers)
+    picks = np.concatenate([np.arange(a, b) for a, b in runs])
     cl.pool_next += n
-    kinds = [p.path(k)[0] for k in picks]
-    pts = [p.path(k)[1] for k in picks]
-    co = np.concatenate([[0], np.cumsum([len(k) for k in kinds])]).astype(np.uint64)
-    po = np.concatenate([[0], np.cumsum([len(x) for x in pts])]).astype(np.uint64)
+    co = [np.zeros(1, np.uint64)]
+    po = [np.zeros(1, np.uint64)]
+    kinds, pts = [], []
+    for a, b in runs:
+        c0, c1 = int(p.cmd_offsets[a]), int(p.cmd_offsets[b])
+        q0, q1 = int(p.point_offsets[a]), int(p.point_offsets[b])
+        kinds.append(p.kinds[c0:c1])
+        pts.append(p.points[q0:q1])
+        co.append(np.diff(p.cmd_offsets[a:b + 1]))
+        po.append(np.diff(p.point_offsets[a:b + 1]))
+    co = np.cumsum(np.concatenate(co)).astype(np.uint64)
+    po = np.cumsum(np.concatenate(po)).astype(np.uint64)
     sub = scenes.Scene("add", p.width, p.height, p.background, p.wide, len(ids), ids, co,
                        np.concatenate(kinds).astype(np.uint32), po, np.concatenate(pts).astype(np.float32))
     cl.comp.insert_paths(sub)

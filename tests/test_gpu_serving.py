@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 def _oracle_replay(cl, client_id, last_seq):
     from cassia_gb300 import scenes, serving
     sc = cl.scene
-    o = oracle.Composition(wide=sc.wide)
+    o = oracle.Composition(wide=cl.comp.wide)
     scenes.load(sc, o)
     shadow = serving.Client(o, sc, None, np.ones(sc.n_layers, bool), sc.transforms.copy(), pool=cl.pool)
     for seq in range(last_seq + 1):
