@@ -118,21 +118,49 @@ class ClockSampler:
 
 def stage_bytes(st, scene):
     """Algorithmic bytes per stage: each stage reads its input once and
-    writes its output once; one sort pass is one read + one write."""
+    writes its output once; one sort pass is one read + one write; the
+    painter reads each segment, work item and tile-layer record (first
+    segment, cover, carry) once, each layer style once and writes the frame."""
     L, P, N = st["lines"], st["segments"], scene.n_layers  # rasterized segments
     return {
         "rasterize": 18 * L + 8 * P,
         "sort": 16 * st["painted_segments"],
-        "paint": 8 * st["painted_segments"] + 32 * N + 4 * scene.width * scene.height,
+        "paint": (8 * st["painted_segments"] + 8 * st["work_items"] + 20 * st["tile_layers"] + 32 * N +
+                  4 * scene.width * scene.height),
     }
+
+
+def read_traffic(workload, stage):
+    """DRAM bytes per launch of the stage's dominant kernel from the table in
+    profiles/traffic.md (one ncu capture), or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            cells = [c.strip() for c in line.strip().strip("|").split("|")]
+            if len(cells) == 5 and cells[0] == workload and cells[1] == stage:
+                try:
+                    return int(cells[3])
+                except ValueError:
+                    return None
+    return None
 
 
 STAGE_KERNELS = {
     "build": "k_build_lines + scan",
-    "rasterize": "k_rasterize (count + write)",
-    "sort": "k_radix_hist + k_onesweep",
-    "carry": "k_tl_* + k_items_* + item sort",
+    "rasterize": "k_rasterize + k_gather_hist",
+    "sort": "k_onesweep (one launch per digit pass)",
+    "carry": "k_tl_scan + k_tl_carry + k_items_* + item sort",
     "paint": "k_paint",
+}
+
+# What bounds each stage's dominant kernel, from the ncu captures summarised
+# in profiles/kernels_mixed20k.md.
+STAGE_LIMITERS = {
+    "rasterize": "SM issue and line-record load latency (52% issue active, long-scoreboard stalls)",
+    "sort": "latency of the onesweep tile (65% issue active, 2.2 TB/s)",
+    "paint": "SM issue (78% of issue slots); its DRAM traffic equals its algorithmic input",
 }
 
 
@@ -441,15 +469,7 @@ def main():
     sb = stage_bytes(st, scene)
     dom = max(("rasterize", "sort", "paint"), key=lambda k: stage_ms[k])
     achieved = sb[dom] / (stage_ms[dom] / 1e3) / 1e9
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tfile):
-        try:
-            with open(tfile) as f:
-                tr = json.load(f).get(args.workload, {}).get(dom)
-            traffic = tr
-        except Exception:
-            traffic = None
+    traffic = read_traffic(args.workload, dom)
     frame_bytes = 18 * st["lines"] + 32 * segs + 32 * scene.n_layers + 4 * W * H
 
     # e2e through the public API with host buffers: every step uploads all
@@ -508,7 +528,8 @@ def main():
             "stage_ms": stage_ms,
             "roofline": {"bound": "hbm", "kernel": STAGE_KERNELS[dom], "stage": dom, "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                         "traffic": traffic, "algorithmic_bytes": sb[dom]},
+                         "traffic": traffic, "algorithmic_bytes": sb[dom],
+                         "limiter": STAGE_LIMITERS.get(dom)},
             "frame_roofline": {"algorithmic_bytes": frame_bytes,
                                "achieved": frame_bytes / (ms_step / 1e3) / 1e9,
                                "frac": frame_bytes / (ms_step / 1e3) / 1e9 / peak},
