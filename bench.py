@@ -269,6 +269,16 @@ def run_batch(args, rank, world, local):
         torch.cuda.synchronize()
         return (time.perf_counter() - t) / reps
 
+    # the autotuner picks the digit width, rasterizer block and painter block
+    # for the batched pipeline; the same setting is applied to every
+    # per-scene composition so that the comparison isolates batching
+    from cassia_gb300 import autotune
+    t_tune = time.time()
+    tuning, trials = autotune.tune(ctx, batched, snapshot=lambda: [o.clone() for o in outs_b],
+                                   same=lambda a, b: all(torch.equal(x, y) for x, y in zip(a, b)), reps=2)
+    tune_s = time.time() - t_tune
+    for c in comps:
+        c.set_tuning(**tuning)
     for _ in range(args.warmup):
         batched()
         plain()
@@ -299,6 +309,8 @@ def run_batch(args, rank, world, local):
                        "l2": "inputs larger than L2"},
             "plain_scenes_per_s": world * len(sset) / tp, "plain_ms_per_pass": tp * 1e3,
             "speedup_vs_plain": tp / tb, "bit_exact_batched_vs_plain": bool(exact),
+            "tuning": tuning, "autotune": {"trials": len(trials), "seconds": tune_s,
+                                           "ms_per_pass": {str(i): t["ms"] for i, t in enumerate(trials)}},
             "e2e": {"value": world * len(sset) / te, "unit": "scenes/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": int(sum(s.width * s.height * 4 for s in sset)), "ms_per_step": te * 1e3},
             "gpu_launches": launches, "clocks": clk.summary(), "setup_s": {"scene_gen": gen_s},

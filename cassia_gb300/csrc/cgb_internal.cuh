@@ -215,14 +215,15 @@ cudaError_t launch_flatten(int write, const uint32_t* kinds, const float* points
 cudaError_t launch_build_lines(const BatchGeom& bg, int cull, LineRec* recs, uint32_t* lengths, cudaStream_t st);
 // mode: 0 = count, 1 = write.  render != 0: culled, re-keyed render format;
 // else the reference segment format of the (single) scene.
-// Rasterizes every pixel step; block b stores its kept segments at
-// runs[b * raster_run_slots(block)...] and their count at run_count[b];
-// *produced (zeroed by the caller) accumulates all segments, kept or not.
+// Rasterizes every pixel step (`items` consecutive steps per thread, 4 or 8);
+// block b stores its kept segments at runs[b * raster_run_slots(block, items)...]
+// and their count at run_count[b]; *produced (zeroed by the caller)
+// accumulates all segments, kept or not.
 cudaError_t launch_rasterize(int render, const BatchGeom& bg, const LineRec* recs, const uint32_t* step_off,
-                             uint32_t n_lines, uint64_t n_steps, uint32_t block, uint64_t* runs, uint32_t* run_count,
-                             unsigned long long* produced, cudaStream_t st);
-uint32_t raster_run_slots(uint32_t block);
-uint32_t raster_grid(uint64_t n_steps, uint32_t block);
+                             uint32_t n_lines, uint64_t n_steps, uint32_t block, uint32_t items, uint64_t* runs,
+                             uint32_t* run_count, unsigned long long* produced, cudaStream_t st);
+uint32_t raster_run_slots(uint32_t block, uint32_t items);
+uint32_t raster_grid(uint64_t n_steps, uint32_t block, uint32_t items);
 cudaError_t launch_compact_lines(const float* in4[4], const uint32_t* lid_in, uint32_t n, const LayerRec* layers,
                                  uint32_t n_layer_recs, float* out4[4], uint32_t* lid_out, uint32_t* flags,
                                  uint32_t* offsets, Scratch* s, cudaStream_t st, uint32_t* n_out_host);
@@ -271,7 +272,7 @@ cudaError_t launch_items(int mode, uint32_t G, const BatchGeom& bg, const CarryB
 cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_tiles, int tile_shift,
                                uint32_t* tile_start, cudaStream_t st);
 cudaError_t launch_paint(const BatchGeom& bg, const uint64_t* segs, const uint64_t* items, int idx_bits,
-                         const uint32_t* tile_start, const CarryBuffers& cb, cudaStream_t st);
+                         const uint32_t* tile_start, const CarryBuffers& cb, uint32_t warps, cudaStream_t st);
 
 
 }  // namespace cgb

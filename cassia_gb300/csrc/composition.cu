@@ -139,7 +139,7 @@ struct cgb_composition {
     bool wide = false;
     uint32_t max_ids = 1u << 16;
     Scratch s;
-    cgb_tuning tuning{9, 256, 2048, 4};
+    cgb_tuning tuning{9, 256, 2048, 4};  // radix bits, raster block, steps per block, painter warps
     cgb_stats stats{};
 
     // LinesBuilder (device SoA)
@@ -543,15 +543,16 @@ cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& 
     if (S >= (1ull << 32)) return fail(CGB_ERR_LAYER_LIMIT, "more than 2^32 pixel steps");
     c->stats.steps = S;
     const uint32_t block = c->tuning.raster_block;
-    const uint32_t grid = raster_grid(S, block);
-    const uint32_t slots = raster_run_slots(block);
+    const uint32_t items = c->tuning.steps_per_block / block;
+    const uint32_t grid = raster_grid(S, block, items);
+    const uint32_t slots = raster_run_slots(block, items);
     CK(c->s.ensure(c->segs_a, std::max<size_t>((size_t)grid * slots, 1) * 8));
     CK(c->s.ensure(c->bcounts, ((size_t)grid + 1) * 4));
     CK(c->s.ensure(c->boff, ((size_t)grid + 1) * 4));
     CK(c->s.ensure(c->rlb, 8));
     CK(cudaMemsetAsync(c->rlb.p, 0, 8, st));
     unsigned long long* produced = c->rlb.as<unsigned long long>();
-    CK(launch_rasterize(render, bg, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, S, block,
+    CK(launch_rasterize(render, bg, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, S, block, items,
                         c->segs_a.as<uint64_t>(), c->bcounts.as<uint32_t>(), produced, st));
     CK(cudaMemcpyAsync(&c->s.pinned[3], produced, 8, cudaMemcpyDeviceToHost, st));
     uint64_t P = 0;
@@ -800,7 +801,7 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
     c->stats.item_sort_passes = ipasses;
     CK(launch_tile_ranges(items_sorted, (uint32_t)W, (uint32_t)tiles, tile_shift, cb.tile_start, st));
     CK(cudaEventRecord(c->ev[4], st));
-    CK(launch_paint(bg, sorted, items_sorted, idx_bits, cb.tile_start, cb, st));
+    CK(launch_paint(bg, sorted, items_sorted, idx_bits, cb.tile_start, cb, c->tuning.paint_warps, st));
     CK(cudaEventRecord(c->ev[5], st));
     for (SceneInput& in : scenes)
         if (in.buf->memory == CGB_MEMORY_HOST)
@@ -1216,16 +1217,19 @@ CGB_EXPORT cgb_status cgb_set_tuning(cgb_composition* c, const cgb_tuning* t) {
         if (t->radix_bits < 4 || t->radix_bits > 9) return fail(CGB_ERR_INVALID_ARG, "radix_bits must be 4..9");
         c->tuning.radix_bits = t->radix_bits;
     }
-    if (t->raster_block) {
-        if (t->raster_block % 32 || t->raster_block > 256)
-            return fail(CGB_ERR_INVALID_ARG, "raster_block must be a multiple of 32, <= 256");
-        c->tuning.raster_block = t->raster_block;
-    }
-    if (t->steps_per_block) c->tuning.steps_per_block = t->steps_per_block;
-    if (t->paint_warps) {
-        if (t->paint_warps > 8) return fail(CGB_ERR_INVALID_ARG, "paint_warps must be <= 8");
-        c->tuning.paint_warps = t->paint_warps;
-    }
+    const uint32_t block = t->raster_block ? t->raster_block : c->tuning.raster_block;
+    if (block % 32 || block < 32 || block > 256)
+        return fail(CGB_ERR_INVALID_ARG, "raster_block must be a multiple of 32 in 32..256");
+    // steps per block: 4 or 8 steps per thread (the current count per thread when not given)
+    const uint32_t steps = t->steps_per_block ? t->steps_per_block
+                                              : block * (c->tuning.steps_per_block / c->tuning.raster_block);
+    if (steps != 4 * block && steps != 8 * block)
+        return fail(CGB_ERR_INVALID_ARG, "steps_per_block must be 4 or 8 x raster_block");
+    if (t->paint_warps && t->paint_warps != 2 && t->paint_warps != 4 && t->paint_warps != 8)
+        return fail(CGB_ERR_INVALID_ARG, "paint_warps must be 2, 4 or 8");
+    c->tuning.raster_block = block;
+    c->tuning.steps_per_block = steps;
+    if (t->paint_warps) c->tuning.paint_warps = t->paint_warps;
     return CGB_OK;
 }
 

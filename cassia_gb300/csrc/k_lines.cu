@@ -6,7 +6,7 @@
 //   k_build_lines  LinesBuilder::build (surpass/src/segment.rs:91-237): one
 //                  thread per line; writes a packed 32-byte LineRec + length.
 //   k_rasterize    Rasterizer::rasterize (surpass/src/rasterizer/mod.rs:214-285):
-//                  each thread walks 8 consecutive pixel steps; each block
+//                  each thread walks 4 or 8 consecutive pixel steps; each block
 //                  block-scans the per-thread counts, stages its segments in
 //                  shared memory and stores them coalesced into its own run
 //                  of slots; k_gather_hist (k_sort.cu) packs the runs.  No
@@ -510,7 +510,6 @@ __device__ __forceinline__ int raster_step(const SceneRaster& sr, const BatchGeo
     return m;
 }
 
-constexpr int RASTER_ITEMS = 8;  // consecutive pixel steps per thread
 
 __device__ __forceinline__ uint32_t find_line(const uint32_t* __restrict__ off, uint32_t n_lines, uint64_t s) {
     // largest l with off[l] <= s (off has n_lines + 1 entries, off[0] = 0)
@@ -528,7 +527,7 @@ __device__ __forceinline__ uint32_t find_line(const uint32_t* __restrict__ off, 
 // 2 * RASTER_ITEMS * blockDim.x slots (a step yields at most two segments);
 // run_count[block] receives how many.  No block waits on another: a later
 // gather (fused with the sort's digit histogram) packs the runs.
-template <int RENDER>
+template <int RENDER, int RASTER_ITEMS>
 __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ recs, const uint32_t* __restrict__ off,
                                                    uint32_t n_lines, uint64_t n_steps, BatchGeom bg,
                                                    uint64_t* __restrict__ runs, uint32_t* __restrict__ run_count,
@@ -659,26 +658,31 @@ cudaError_t launch_build_lines(const BatchGeom& bg, int cull, LineRec* recs, uin
 }
 
 cudaError_t launch_rasterize(int render, const BatchGeom& bg, const LineRec* recs, const uint32_t* step_off,
-                             uint32_t n_lines, uint64_t n_steps, uint32_t block, uint64_t* runs, uint32_t* run_count,
-                             unsigned long long* produced, cudaStream_t st) {
+                             uint32_t n_lines, uint64_t n_steps, uint32_t block, uint32_t items, uint64_t* runs,
+                             uint32_t* run_count, unsigned long long* produced, cudaStream_t st) {
     if (n_steps == 0) return cudaSuccess;
-    block = block ? block : 256;
-    uint64_t per_block = (uint64_t)block * RASTER_ITEMS;
-    uint32_t grid = (uint32_t)((n_steps + per_block - 1) / per_block);
-    size_t smem = (size_t)2 * per_block * sizeof(uint64_t);
+    if (block == 0 || block % 32 || block > 256 || (items != 4 && items != 8)) return cudaErrorInvalidValue;
+    const uint32_t grid = raster_grid(n_steps, block, items);
+    const size_t smem = (size_t)raster_run_slots(block, items) * sizeof(uint64_t);
     count_launches(1);
-    if (render)
-        k_rasterize<1><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced);
-    else
-        k_rasterize<0><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced);
+    if (render) {
+        if (items == 4)
+            k_rasterize<1, 4><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced);
+        else
+            k_rasterize<1, 8><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced);
+    } else {
+        if (items == 4)
+            k_rasterize<0, 4><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced);
+        else
+            k_rasterize<0, 8><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced);
+    }
     return cudaGetLastError();
 }
 
-uint32_t raster_run_slots(uint32_t block) { return 2 * RASTER_ITEMS * (block ? block : 256); }
+uint32_t raster_run_slots(uint32_t block, uint32_t items) { return 2 * items * block; }
 
-uint32_t raster_grid(uint64_t n_steps, uint32_t block) {
-    block = block ? block : 256;
-    uint64_t per_block = (uint64_t)block * RASTER_ITEMS;
+uint32_t raster_grid(uint64_t n_steps, uint32_t block, uint32_t items) {
+    const uint64_t per_block = (uint64_t)block * items;
     return (uint32_t)((n_steps + per_block - 1) / per_block);
 }
 

@@ -522,7 +522,6 @@ struct PaintArgs {
     const uint64_t* tl_carry;
 };
 
-constexpr int PAINT_WARPS = 4;  // tiles per CTA
 constexpr int SEGCAP = 256;     // staged segments per warp and chunk of 32 items
 
 constexpr uint32_t META_CARRY_ONLY = 32u;  // the item only carries cover through the tile
@@ -623,6 +622,7 @@ __device__ __forceinline__ void stage_items(const PaintArgs& a, const PaintProps
     __syncwarp();
 }
 
+template <int PAINT_WARPS>  // tiles per CTA
 __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
     __shared__ WarpStage stages[PAINT_WARPS];
     const int lane = threadIdx.x & 31;
@@ -845,11 +845,17 @@ cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_til
 }
 
 cudaError_t launch_paint(const BatchGeom& bg, const uint64_t* segs, const uint64_t* items, int idx_bits,
-                         const uint32_t* tile_start, const CarryBuffers& cb, cudaStream_t st) {
+                         const uint32_t* tile_start, const CarryBuffers& cb, uint32_t warps, cudaStream_t st) {
     if (bg.total_tiles == 0) return cudaSuccess;
     PaintArgs a{bg, segs, items, idx_bits, cb.order_bits, tile_start, cb.tl_start, cb.tl_cover, cb.tl_carry};
     count_launches(1);
-    k_paint<<<(bg.total_tiles + PAINT_WARPS - 1) / PAINT_WARPS, 32 * PAINT_WARPS, 0, st>>>(a);
+    const uint32_t T = bg.total_tiles;
+    switch (warps) {
+        case 2: k_paint<2><<<(T + 1) / 2, 64, 0, st>>>(a); break;
+        case 4: k_paint<4><<<(T + 3) / 4, 128, 0, st>>>(a); break;
+        case 8: k_paint<8><<<(T + 7) / 8, 256, 0, st>>>(a); break;
+        default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 

@@ -159,12 +159,13 @@ typedef struct cgb_stats {
     float build_ms, rasterize_ms, sort_ms, carry_ms, paint_ms, total_ms;
 } cgb_stats;
 
-/* Autotuned knobs (0 keeps the current value). */
+/* Autotuned knobs (0 keeps the current value).  Every setting renders the
+ * same pixels; only the parallel decomposition changes. */
 typedef struct cgb_tuning {
     uint32_t radix_bits;     /* widest digit of the radix sorts: 4..9 (passes split the key evenly) */
-    uint32_t raster_block;   /* threads per rasterizer block: 128..1024 */
-    uint32_t steps_per_block;/* pixel steps per rasterizer block */
-    uint32_t paint_warps;    /* warps (tiles) per painter block */
+    uint32_t raster_block;   /* threads per rasterizer block: a multiple of 32 in 32..256 */
+    uint32_t steps_per_block;/* pixel steps per rasterizer block: 4 or 8 x raster_block */
+    uint32_t paint_warps;    /* warps (8x8 tiles) per painter block: 2, 4 or 8 */
 } cgb_tuning;
 
 typedef struct cgb_composition cgb_composition;
