@@ -31,6 +31,8 @@ GRADIENT_LINEAR, GRADIENT_RADIAL = 0, 1
 CMD_LINE, CMD_QUAD, CMD_RAT_QUAD, CMD_CUBIC, CMD_RAT_CUBIC, CMD_CLOSE = range(6)
 CMD_FLOATS = {CMD_LINE: 4, CMD_QUAD: 6, CMD_RAT_QUAD: 9, CMD_CUBIC: 8, CMD_RAT_CUBIC: 12, CMD_CLOSE: 0}
 COMPOSITION_WIDE_LAYERS = 1
+COMPOSITION_PRIORITY_HIGH = 2
+COMPOSITION_PRIORITY_LOW = 4
 TRANSFORM_UNCHECKED = 1
 SORT_CANONICAL, SORT_KEY = 0, 1
 MEMORY_HOST, MEMORY_DEVICE = 0, 1

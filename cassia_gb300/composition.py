@@ -77,12 +77,14 @@ def kernel_launches() -> int:
 class Composition:
     """mold::Composition on the GPU.  `wide=True` selects the 17-bit layer
     segment format for more than 65,536 layer orders; `hbm_budget` caps the
-    device memory the handle may hold (bytes, 0 = unlimited)."""
+    device memory the handle may hold (bytes, 0 = unlimited); `priority`
+    ("normal", "high", "low") sets the priority of the handle's stream."""
 
-    def __init__(self, wide: bool = False, hbm_budget: int = 0):
+    def __init__(self, wide: bool = False, hbm_budget: int = 0, priority: str = "normal"):
         self._lib = abi.load_library()
         h = ctypes.c_void_p()
         flags = abi.COMPOSITION_WIDE_LAYERS if wide else 0
+        flags |= {"normal": 0, "high": abi.COMPOSITION_PRIORITY_HIGH, "low": abi.COMPOSITION_PRIORITY_LOW}[priority]
         _check(self._lib, self._lib.cgb_composition_new(flags, hbm_budget, ctypes.byref(h)), "Composition::new")
         self._h = h
         self.wide = wide

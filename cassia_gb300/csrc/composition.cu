@@ -857,7 +857,12 @@ CGB_EXPORT cgb_status cgb_composition_new(uint32_t flags, uint64_t hbm_budget_by
     c->wide = (flags & CGB_COMPOSITION_WIDE_LAYERS) != 0;
     c->max_ids = c->wide ? (1u << 17) : (1u << 16);
     c->s.budget = hbm_budget_bytes;
-    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    int prio_least = 0, prio_greatest = 0;  // numerically: least = lowest priority
+    cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+    const int prio = (flags & CGB_COMPOSITION_PRIORITY_HIGH)  ? prio_greatest
+                     : (flags & CGB_COMPOSITION_PRIORITY_LOW) ? prio_least
+                                                              : 0;
+    cudaError_t e = cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio);
     if (e == cudaSuccess) e = cudaMallocHost(&c->s.pinned, 64);
     for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
     if (e == cudaSuccess) e = c->s.ensure(c->err, 256);

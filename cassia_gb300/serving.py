@@ -74,7 +74,7 @@ def make_clients(n_clients: int, seed: int, device_out: bool = True, max_layers:
         # churn needs fresh layer ids until the lines garbage collection of
         # remove_disabled frees the removed ones (at 50% garbage): large
         # clients use the widened 17-bit layer format
-        c = Composition(wide=sc.wide or sc.n_layers > 30_000)
+        c = Composition(wide=sc.wide or sc.n_layers > 30_000, priority="high")
         scenes.load(sc, c)
         if device_out:
             out = torch.zeros((sc.height, sc.width, 4), dtype=torch.uint8, device="cuda")
@@ -188,7 +188,9 @@ class Server:
         self.workers = 1 if mode == "plain" else workers
         self.max_batch = 1 if mode == "plain" else max_batch
         self.budget = hbm_budget
-        self.ctx = [Composition() for _ in range(self.workers)] if mode == "batched" else []
+        # batch renders run at low priority so that the clients' small update
+        # kernels (path flattening) are not queued behind them
+        self.ctx = [Composition(priority="low") for _ in range(self.workers)] if mode == "batched" else []
         self.cv = threading.Condition()
         self.pending: Dict[int, collections.deque] = collections.defaultdict(collections.deque)
         self.busy = set()

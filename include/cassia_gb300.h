@@ -93,6 +93,11 @@ typedef int32_t cgb_status;
  * for scenes with more than 65,536 layer orders (the reference's u16 limit,
  * mold/src/layer.rs:13, surpass/src/rasterizer/raster_segment.rs:148). */
 #define CGB_COMPOSITION_WIDE_LAYERS 1u
+/* Stream priority of the handle's stream: work of a high-priority handle
+ * (e.g. a client's scene updates) is scheduled before waiting blocks of
+ * low-priority handles (e.g. a server's batch renders) on a busy GPU. */
+#define CGB_COMPOSITION_PRIORITY_HIGH 2u
+#define CGB_COMPOSITION_PRIORITY_LOW 4u
 
 /* layer transform flags */
 /* Skip mold's per-axis scale <= ~1 check (mold/src/layer.rs:186-190) and store
