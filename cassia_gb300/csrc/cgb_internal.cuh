@@ -138,18 +138,13 @@ __device__ __forceinline__ int32_t to_sub_pixel(float v) {
     return f2i32(__fmaf_rn(v, (float)PIXEL_WIDTH, copysignf(0.5f, v)));
 }
 
-// Sign-extend the low `bits` of v.
-__device__ __forceinline__ int32_t sext(uint64_t v, int bits) {
-    uint64_t m = 1ull << (bits - 1);
-    v &= (1ull << bits) - 1;
-    return (int32_t)(int64_t)((v ^ m) - m);
-}
-
 // Low 22 bits of a CompactSegment (raster_segment.rs:142-154): tile_y | tile_x | area | cover.
 __device__ __forceinline__ uint32_t low_tile_y(uint32_t low) { return (low >> 19) & 7; }
 __device__ __forceinline__ uint32_t low_tile_x(uint32_t low) { return (low >> 16) & 7; }
-__device__ __forceinline__ int32_t low_area(uint32_t low) { return sext(low >> 6, 10); }
-__device__ __forceinline__ int32_t low_cover(uint32_t low) { return sext(low, 6); }
+// pixel index y * 8 + x within the tile (the two 3-bit fields side by side)
+__device__ __forceinline__ uint32_t low_cell(uint32_t low) { return (low >> 16) & 63; }
+__device__ __forceinline__ int32_t low_area(uint32_t low) { return (int32_t)(low << 16) >> 22; }  // bits 6..15
+__device__ __forceinline__ int32_t low_cover(uint32_t low) { return (int32_t)(low << 26) >> 26; }  // bits 0..5
 
 // 8 x i8 cover lanes packed in a u64 (lane y = byte y); lane-wise wrapping add.
 __device__ __forceinline__ uint64_t cover_add(uint64_t a, uint64_t b) {

@@ -414,7 +414,7 @@ __device__ __forceinline__ float2 blend_vec2(float2 d, float s) {
 // specialised per blend mode so that the mode is dispatched once per layer.
 // C[q] holds channel q of the two pixels; a pixel whose column is not blended
 // keeps its color.
-template <int MODE>
+template <int MODE, bool MASKED>
 __device__ __forceinline__ void blend_pixels(float2 (&C)[4], const float4& src, float2 cov, bool col0, bool col1) {
     const float2 al = mul2(splat(src.w), cov);
     const float2 inv = sub2(splat(1.0f), al);
@@ -422,27 +422,37 @@ __device__ __forceinline__ void blend_pixels(float2 (&C)[4], const float4& src, 
     const float2 n1 = fma2(C[1], inv, mul2(blend_vec2<MODE>(C[1], src.y), al));
     const float2 n2 = fma2(C[2], inv, mul2(blend_vec2<MODE>(C[2], src.z), al));
     const float2 n3 = fma2(C[3], inv, al);
-    C[0] = sel2(col0, col1, n0, C[0]);
-    C[1] = sel2(col0, col1, n1, C[1]);
-    C[2] = sel2(col0, col1, n2, C[2]);
-    C[3] = sel2(col0, col1, n3, C[3]);
+    if (MASKED) {
+        C[0] = sel2(col0, col1, n0, C[0]);
+        C[1] = sel2(col0, col1, n1, C[1]);
+        C[2] = sel2(col0, col1, n2, C[2]);
+        C[3] = sel2(col0, col1, n3, C[3]);
+    } else {
+        C[0] = n0;
+        C[1] = n1;
+        C[2] = n2;
+        C[3] = n3;
+    }
 }
 
+// MASKED = false when both columns of every lane are blended (cover-carry-only
+// items: every column has the same per-row coverage).
+template <bool MASKED>
 __device__ __forceinline__ void blend_dispatch(uint32_t mode, float2 (&C)[4], const float4& src, float2 cov,
                                                bool col0, bool col1) {
     switch (mode) {
-        case CGB_BLEND_OVER: blend_pixels<CGB_BLEND_OVER>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_MULTIPLY: blend_pixels<CGB_BLEND_MULTIPLY>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_SCREEN: blend_pixels<CGB_BLEND_SCREEN>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_OVERLAY: blend_pixels<CGB_BLEND_OVERLAY>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_DARKEN: blend_pixels<CGB_BLEND_DARKEN>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_LIGHTEN: blend_pixels<CGB_BLEND_LIGHTEN>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_COLOR_DODGE: blend_pixels<CGB_BLEND_COLOR_DODGE>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_COLOR_BURN: blend_pixels<CGB_BLEND_COLOR_BURN>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_HARD_LIGHT: blend_pixels<CGB_BLEND_HARD_LIGHT>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_SOFT_LIGHT: blend_pixels<CGB_BLEND_SOFT_LIGHT>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_DIFFERENCE: blend_pixels<CGB_BLEND_DIFFERENCE>(C, src, cov, col0, col1); break;
-        default: blend_pixels<CGB_BLEND_EXCLUSION>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_OVER: blend_pixels<CGB_BLEND_OVER, MASKED>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_MULTIPLY: blend_pixels<CGB_BLEND_MULTIPLY, MASKED>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_SCREEN: blend_pixels<CGB_BLEND_SCREEN, MASKED>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_OVERLAY: blend_pixels<CGB_BLEND_OVERLAY, MASKED>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_DARKEN: blend_pixels<CGB_BLEND_DARKEN, MASKED>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_LIGHTEN: blend_pixels<CGB_BLEND_LIGHTEN, MASKED>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_COLOR_DODGE: blend_pixels<CGB_BLEND_COLOR_DODGE, MASKED>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_COLOR_BURN: blend_pixels<CGB_BLEND_COLOR_BURN, MASKED>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_HARD_LIGHT: blend_pixels<CGB_BLEND_HARD_LIGHT, MASKED>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_SOFT_LIGHT: blend_pixels<CGB_BLEND_SOFT_LIGHT, MASKED>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_DIFFERENCE: blend_pixels<CGB_BLEND_DIFFERENCE, MASKED>(C, src, cov, col0, col1); break;
+        default: blend_pixels<CGB_BLEND_EXCLUSION, MASKED>(C, src, cov, col0, col1); break;
     }
 }
 
@@ -523,6 +533,7 @@ struct PaintArgs {
 };
 
 constexpr int SEGCAP = 256;     // staged segments per warp and chunk of 32 items
+static_assert(SEGCAP == 8 * 32, "the staging owner map gives each lane 8 positions");
 
 constexpr uint32_t META_CARRY_ONLY = 32u;  // the item only carries cover through the tile
 constexpr uint32_t META_ACTIVE = 64u;      // carry-only: some tile row has non-zero coverage
@@ -537,7 +548,8 @@ struct WarpStage {
     uint32_t cnt[32];    // segments of the item
     uint32_t soff[32];   // staging offset of its segments
     uint32_t seg[SEGCAP];
-    int32_t area[64];    // per-pixel area sums (x * 8 + y)
+    alignas(8) uint8_t owner[SEGCAP];  // item of each staged segment
+    alignas(8) int32_t area[64];    // per-pixel area sums (y * 8 + x)
     int32_t cov[64];     // per-pixel cover sums, added to the columns right of x
 };
 
@@ -595,30 +607,50 @@ __device__ __forceinline__ void stage_items(const PaintArgs& a, const PaintProps
     S.soff[lane] = inc - cnt;
     __syncwarp();
     if (!with_segments) return;
+    // Staged segment s belongs to the last item q with soff[q] <= s among the
+    // items with segments: mark each such item at its offset, take a running
+    // maximum over the offsets, then copy 32 segments per round.
     const uint32_t staged = min(total, (uint32_t)SEGCAP);
-    uint32_t src[SEGCAP / 32];
+    const uint32_t soff = inc - cnt;
+    *reinterpret_cast<uint2*>(&S.owner[8 * lane]) = make_uint2(0u, 0u);
+    __syncwarp();
+    if (cnt > 0 && soff < (uint32_t)SEGCAP) S.owner[soff] = (uint8_t)lane;
+    __syncwarp();
+    {
+        uint2 w = *reinterpret_cast<const uint2*>(&S.owner[8 * lane]);
+        uint32_t run = 0, b[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const uint32_t v = ((k < 4 ? w.x : w.y) >> (8 * (k & 3))) & 0xFFu;
+            run = max(run, v);
+            b[k] = run;
+        }
+        uint32_t scan = run;  // inclusive max over lanes <= this one
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, scan, o);
+            if (lane >= o) scan = max(scan, t);
+        }
+        uint32_t carry = __shfl_up_sync(0xffffffffu, scan, 1);
+        if (lane == 0) carry = 0;
+        uint32_t lo = 0, hi = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const uint32_t v = max(carry, b[k]);
+            if (k < 4) lo |= v << (8 * k);
+            else hi |= v << (8 * (k - 4));
+        }
+        *reinterpret_cast<uint2*>(&S.owner[8 * lane]) = make_uint2(lo, hi);
+    }
+    __syncwarp();
 #pragma unroll
     for (int r = 0; r < SEGCAP / 32; r++) {
-        const uint32_t s = lane + 32 * r;
-        src[r] = 0xFFFFFFFFu;
-        if (s < staged) {
-            // the item q with soff[q] <= s < soff[q] + cnt[q]
-            uint32_t lo = 0, hi = n;
-            while (hi - lo > 1) {
-                uint32_t mid = (lo + hi) >> 1;
-                if (S.soff[mid] <= s) lo = mid;
-                else hi = mid;
-            }
-            while (lo + 1 < n && (S.cnt[lo] == 0 || s >= S.soff[lo] + S.cnt[lo])) lo++;  // skip empty items sharing the offset
-            src[r] = S.sb[lo] + (s - S.soff[lo]);
-        }
+        const uint32_t pos = lane + 32 * r;
+        const uint32_t q = pos < staged ? S.owner[pos] : 0u;
+        const uint32_t qsb = __shfl_sync(0xffffffffu, sb, q);
+        const uint32_t qoff = __shfl_sync(0xffffffffu, soff, q);
+        if (pos < staged) S.seg[pos] = (uint32_t)a.segs[qsb + (pos - qoff)];
     }
-    uint32_t v[SEGCAP / 32];
-#pragma unroll
-    for (int r = 0; r < SEGCAP / 32; r++) v[r] = src[r] != 0xFFFFFFFFu ? (uint32_t)a.segs[src[r]] : 0u;
-#pragma unroll
-    for (int r = 0; r < SEGCAP / 32; r++)
-        if (lane + 32 * r < staged) S.seg[lane + 32 * r] = v[r];
     __syncwarp();
 }
 
@@ -738,7 +770,8 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
                 if (meta & META_CARRY_ONLY) {
                     if (!(meta & META_ACTIVE)) continue;
                     cov = splat(reinterpret_cast<const float*>(&S.rowcov[q][0])[y]);
-                    col0 = col1 = true;
+                    blend_dispatch<false>(mode, C, S.color[q], cov, true, true);
+                    continue;
                 } else {
                     // acc_segment / acc_cover / compute_areas (painter/mod.rs:229-243, 347-362):
                     // per-cell sums in shared memory, then each lane reads
@@ -747,18 +780,18 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
                     const uint32_t cnt = S.cnt[q], so = S.soff[q], sb = S.sb[q];
                     for (uint32_t s = lane; s < cnt; s += 32) {
                         const uint32_t low = so + s < SEGCAP ? S.seg[so + s] : (uint32_t)a.segs[sb + s];
-                        const uint32_t cell = low_tile_x(low) * 8 + low_tile_y(low);
+                        const uint32_t cell = low_cell(low);
                         atomicAdd(&S.area[cell], low_area(low));
                         atomicAdd(&S.cov[cell], low_cover(low));
                     }
                     __syncwarp();
-                    const uint32_t c0i = x0 * 8 + y, c1i = c0i + 8;
-                    const int32_t a0 = S.area[c0i], a1 = S.area[c1i];
-                    const int32_t v0 = S.cov[c0i], v1 = S.cov[c1i];
-                    S.area[c0i] = 0;
-                    S.area[c1i] = 0;
-                    S.cov[c0i] = 0;
-                    S.cov[c1i] = 0;
+                    // the lane's two pixels are adjacent cells: one 64-bit access each
+                    const uint32_t c0i = y * 8 + x0;
+                    const int2 aa = *reinterpret_cast<const int2*>(&S.area[c0i]);
+                    const int2 vv = *reinterpret_cast<const int2*>(&S.cov[c0i]);
+                    *reinterpret_cast<int2*>(&S.area[c0i]) = make_int2(0, 0);
+                    *reinterpret_cast<int2*>(&S.cov[c0i]) = make_int2(0, 0);
+                    const int32_t a0 = aa.x, a1 = aa.y, v0 = vv.x, v1 = vv.y;
                     // covers of the columns left of x0: prefix over the lane's column pairs
                     int32_t pre = v0 + v1;
                     int32_t t = __shfl_up_sync(0xffffffffu, pre, 8);
@@ -778,7 +811,7 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
                     col0 = ((b0 >> (8 * xg)) & 0xFFu) != 0;
                     col1 = ((b1 >> (8 * xg)) & 0xFFu) != 0;
                 }
-                blend_dispatch(mode, C, S.color[q], cov, col0, col1);
+                blend_dispatch<true>(mode, C, S.color[q], cov, col0, col1);
             }
             __syncwarp();
         }
