@@ -266,7 +266,7 @@ cudaError_t launch_items(int mode, uint32_t G, const BatchGeom& bg, const CarryB
                          cudaStream_t st);
 cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_tiles, int tile_shift,
                                uint32_t* tile_start, cudaStream_t st);
-cudaError_t launch_paint(const BatchGeom& bg, const uint64_t* segs, const uint64_t* items, int idx_bits,
+cudaError_t launch_paint(const BatchGeom& bg, const uint64_t* segs, const uint64_t* items, int idx_bits, uint32_t G,
                          const uint32_t* tile_start, const CarryBuffers& cb, uint32_t warps, cudaStream_t st);
 
 

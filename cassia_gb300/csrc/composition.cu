@@ -801,7 +801,7 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
     c->stats.item_sort_passes = ipasses;
     CK(launch_tile_ranges(items_sorted, (uint32_t)W, (uint32_t)tiles, tile_shift, cb.tile_start, st));
     CK(cudaEventRecord(c->ev[4], st));
-    CK(launch_paint(bg, sorted, items_sorted, idx_bits, cb.tile_start, cb, c->tuning.paint_warps, st));
+    CK(launch_paint(bg, sorted, items_sorted, idx_bits, (uint32_t)G, cb.tile_start, cb, c->tuning.paint_warps, st));
     CK(cudaEventRecord(c->ev[5], st));
     for (SceneInput& in : scenes)
         if (in.buf->memory == CGB_MEMORY_HOST)

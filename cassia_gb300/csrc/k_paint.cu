@@ -218,9 +218,12 @@ __device__ __forceinline__ TlItems tl_items(uint32_t g, uint32_t G, const CarryB
     const uint64_t run = key_run(key, bg.col_bits);
     const uint32_t L = run_order(run, bg.order_bits);
     const uint32_t grow = run_row(run, bg.order_bits);
+    // fields out of range only come from a sort that gave up (its error
+    // flag is reported after the frame): no items rather than a stray access
+    if (grow >= bg.total_rows) return r;
     const SceneDesc& S = bg.scenes[bg.row_scene[grow]];
     const uint32_t j = grow - S.row_base;
-    if (j < S.crop_v0 || j >= S.crop_v1) return r;
+    if (j < S.crop_v0 || j >= S.crop_v1 || L >= S.n_orders) return r;
     r.L = L;
     r.row_tile = (uint64_t)S.tile_base + (uint64_t)j * S.row_len;
     int32_t next = (int32_t)S.row_len;
@@ -314,8 +317,8 @@ __global__ void k_tile_ranges(const uint64_t* __restrict__ items, uint32_t W, ui
                               uint32_t* __restrict__ tile_start) {
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k > W) return;
-    int64_t cur = k < W ? (int64_t)(items[k] >> tile_shift) : (int64_t)n_tiles;
-    int64_t prev = k > 0 ? (int64_t)(items[k - 1] >> tile_shift) : -1;
+    int64_t cur = k < W ? (int64_t)min(items[k] >> tile_shift, (uint64_t)n_tiles) : (int64_t)n_tiles;
+    int64_t prev = k > 0 ? (int64_t)min(items[k - 1] >> tile_shift, (uint64_t)n_tiles) : -1;
     for (int64_t t = prev + 1; t <= cur; t++) tile_start[t] = k;
 }
 
@@ -526,6 +529,7 @@ struct PaintArgs {
     const uint64_t* items;
     int idx_bits;
     int order_bits;
+    uint32_t G;  // TL count (item TL indices are below it)
     const uint32_t* tile_start;
     const uint32_t* tl_start;
     const uint64_t* tl_cover;
@@ -554,14 +558,14 @@ struct WarpStage {
 };
 
 // Loads items [c0, c0 + n) into the stage; all loads of the chunk are in flight together.
-__device__ __forceinline__ void stage_items(const PaintArgs& a, const PaintProps* __restrict__ props, WarpStage& S,
-                                            uint32_t c0, uint32_t n, int lane, bool with_segments) {
+__device__ __forceinline__ void stage_items(const PaintArgs& a, const PaintProps* __restrict__ props, uint32_t n_orders,
+                                            WarpStage& S, uint32_t c0, uint32_t n, int lane, bool with_segments) {
     uint32_t meta = 0, sb = 0, cnt = 0;
     uint64_t carry = 0;
     float4 col = make_float4(0.f, 0.f, 0.f, 0.f);
-    if ((uint32_t)lane < n) {
-        uint32_t L, fl, g;
-        item_decode(a.items[c0 + lane], a.idx_bits, a.order_bits, L, fl, g);
+    uint32_t L = 0, fl = 0, g = 0;
+    if ((uint32_t)lane < n) item_decode(a.items[c0 + lane], a.idx_bits, a.order_bits, L, fl, g);
+    if ((uint32_t)lane < n && L < n_orders && g < a.G) {  // out of range only after a failed sort
         const float4* pp = reinterpret_cast<const float4*>(props + L);
         const uint4 hdr = *reinterpret_cast<const uint4*>(pp);
         col = pp[1];
@@ -685,7 +689,7 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
             for (uint32_t k = b + lane; k < e; k += 32) {
                 uint32_t L, fl, g;
                 item_decode(a.items[k], a.idx_bits, a.order_bits, L, fl, g);
-                all &= p.unchanged[L] != 0;
+                all &= L < p.n_orders && p.unchanged[L] != 0;
             }
             if (__all_sync(0xffffffffu, all)) return;  // TileWriteOp::None
         }
@@ -724,7 +728,7 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
         if (first == 1) {
             uint32_t L, fl, g;
             item_decode(a.items[k_op], a.idx_bits, a.order_bits, L, fl, g);
-            const float4 c = reinterpret_cast<const float4*>(p.props + L)[1];
+            const float4 c = reinterpret_cast<const float4*>(p.props + min(L, p.n_orders - 1))[1];
             dst[0] = c.x, dst[1] = c.y, dst[2] = c.z, dst[3] = c.w;
             from = (uint32_t)k_op + 1;
         } else {
@@ -733,7 +737,7 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
         }
         for (uint32_t c0 = from; c0 < e; c0 += 32) {
             const uint32_t n = min(32u, e - c0);
-            stage_items(a, p.props, S, c0, n, lane, false);
+            stage_items(a, p.props, p.n_orders, S, c0, n, lane, false);
             for (uint32_t q = 0; q < n; q++) {
                 const float4 col = S.color[q];
                 const uint32_t mode = S.meta[q] & 15u;
@@ -761,7 +765,7 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
         S.cov[lane + 32] = 0;
         for (uint32_t c0 = start; c0 < e; c0 += 32) {
             const uint32_t n = min(32u, e - c0);
-            stage_items(a, p.props, S, c0, n, lane, true);
+            stage_items(a, p.props, p.n_orders, S, c0, n, lane, true);
             for (uint32_t q = 0; q < n; q++) {
                 const uint32_t meta = S.meta[q];
                 const uint32_t mode = meta & 15u, fr = (meta >> 4) & 1u;
@@ -877,10 +881,10 @@ cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_til
     return cudaGetLastError();
 }
 
-cudaError_t launch_paint(const BatchGeom& bg, const uint64_t* segs, const uint64_t* items, int idx_bits,
+cudaError_t launch_paint(const BatchGeom& bg, const uint64_t* segs, const uint64_t* items, int idx_bits, uint32_t G,
                          const uint32_t* tile_start, const CarryBuffers& cb, uint32_t warps, cudaStream_t st) {
     if (bg.total_tiles == 0) return cudaSuccess;
-    PaintArgs a{bg, segs, items, idx_bits, cb.order_bits, tile_start, cb.tl_start, cb.tl_cover, cb.tl_carry};
+    PaintArgs a{bg, segs, items, idx_bits, cb.order_bits, G, tile_start, cb.tl_start, cb.tl_cover, cb.tl_carry};
     count_launches(1);
     const uint32_t T = bg.total_tiles;
     switch (warps) {
