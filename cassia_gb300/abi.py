@@ -169,6 +169,7 @@ def _declare(lib):
         "cgb_kernel_launches": ([], u64),
         "cgb_composition_clear": ([handle], i32),
         "cgb_sort_keys_noalloc": ([vp, vp, sz, u32, u32, vp], i32),
+        "cgb_selftest_bounded_wait": ([], i32),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

@@ -235,6 +235,9 @@ cudaError_t scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, Scratch* s, 
 cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo, int bit_hi, int digit_bits,
                            Scratch* s, uint32_t* err_flag, cudaStream_t st, uint64_t** result, int* passes,
                            bool hist_ready = false);
+// Runs one onesweep CTA whose predecessor tile never publishes; *flag_host
+// receives the kernel's error flag (1 = the bounded wait gave up).
+cudaError_t selftest_bounded_wait(cudaStream_t st, uint32_t* flag_host);
 // Packs runs of keys (run r: run_count[r] keys at runs[r * run_slots...],
 // placed at run_off[r] of out) and counts the digits of every pass of the sort
 // by bits [bit_lo, bit_hi) into s->sort_hist, for radix_sort_u64(hist_ready).

@@ -19,6 +19,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "cgb_internal.cuh"
 
 using namespace cgb;
@@ -182,6 +184,8 @@ struct cgb_composition {
     std::map<int32_t, CacheState> caches;
 
     cudaEvent_t ev[8] = {};
+    nvtxRangeId_t nvtx_range = 0;  // the open stage range (visible in Nsight tools)
+    bool nvtx_open = false;
 
     cgb_status cuda_fail(cudaError_t e, const char* where) {
         if (e == cudaErrorMemoryAllocation && s.over_budget) {
@@ -520,6 +524,15 @@ struct SceneInput {
     size_t staging_off;  // offset in the frame's host-output staging buffer
 };
 
+// Stage boundary: records CUDA event k on the stream (the stage times of
+// cgb_stats) and closes the open NVTX range, opening `next` if given.
+cudaError_t stage_mark(cgb_composition* c, int k, cudaStream_t st, const char* next) {
+    if (c->nvtx_open) nvtxRangeEnd(c->nvtx_range);
+    c->nvtx_open = next != nullptr;
+    if (next) c->nvtx_range = nvtxRangeStartA(next);
+    return cudaEventRecord(c->ev[k], st);
+}
+
 // LinesBuilder::build + Rasterizer::rasterize (+ re-keying / culling in
 // render mode) over every scene of the frame.  Leaves n_segs keys in segs_a.
 // LinesBuilder::build + Rasterizer::rasterize (+ re-keying / culling in
@@ -535,11 +548,11 @@ cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& 
     CK(c->s.ensure(c->recs, std::max<size_t>(L, 1) * sizeof(LineRec)));
     CK(c->s.ensure(c->lengths, std::max<size_t>(L, 1) * 4));
     CK(c->s.ensure(c->step_off, ((size_t)L + 1) * 4));
-    CK(cudaEventRecord(c->ev[0], st));
+    CK(stage_mark(c, 0, st, "cgb:build_lines"));
     CK(launch_build_lines(bg, render, c->recs.as<LineRec>(), c->lengths.as<uint32_t>(), st));
     uint64_t S = 0;
     CK(scan_u32(c->lengths.as<uint32_t>(), c->step_off.as<uint32_t>(), L, &c->s, st, &S));
-    CK(cudaEventRecord(c->ev[1], st));
+    CK(stage_mark(c, 1, st, "cgb:rasterize"));
     if (S >= (1ull << 32)) return fail(CGB_ERR_LAYER_LIMIT, "more than 2^32 pixel steps");
     c->stats.steps = S;
     const uint32_t block = c->tuning.raster_block;
@@ -562,7 +575,7 @@ cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& 
     CK(c->s.ensure(c->segs_b, std::max<size_t>(P, 1) * 8));
     CK(radix_gather_hist(c->segs_a.as<uint64_t>(), slots, c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid,
                          c->segs_b.as<uint64_t>(), sort_lo, sort_hi, (int)c->tuning.radix_bits, &c->s, st));
-    CK(cudaEventRecord(c->ev[2], st));
+    CK(stage_mark(c, 2, st, "cgb:sort"));
     *n_segs = P;
     *n_total = PT;
     *keys = c->segs_b.as<uint64_t>();
@@ -743,7 +756,7 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
     CK(radix_sort_u64(keys, c->segs_a.as<uint64_t>(), (uint32_t)P, 22, 22 + (int)bg.key_bits,
                       (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &sorted, &passes, true));
     c->stats.sort_passes = passes;
-    CK(cudaEventRecord(c->ev[3], st));
+    CK(stage_mark(c, 3, st, "cgb:carry"));
 
     // tile-layer groups, carries, work items
     CarryBuffers cb{};
@@ -800,9 +813,9 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
                       (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &items_sorted, &ipasses));
     c->stats.item_sort_passes = ipasses;
     CK(launch_tile_ranges(items_sorted, (uint32_t)W, (uint32_t)tiles, tile_shift, cb.tile_start, st));
-    CK(cudaEventRecord(c->ev[4], st));
+    CK(stage_mark(c, 4, st, "cgb:paint"));
     CK(launch_paint(bg, sorted, items_sorted, idx_bits, (uint32_t)G, cb.tile_start, cb, c->tuning.paint_warps, st));
-    CK(cudaEventRecord(c->ev[5], st));
+    CK(stage_mark(c, 5, st, nullptr));
     for (SceneInput& in : scenes)
         if (in.buf->memory == CGB_MEMORY_HOST)
             CK(cudaMemcpy2DAsync(in.buf->pixels, (size_t)in.d.stride * 4, in.d.out, (size_t)in.d.stride * 4,
@@ -1193,7 +1206,7 @@ CGB_EXPORT cgb_status cgb_pixel_segments(cgb_composition* c, uint64_t* out, size
     CK(radix_sort_u64(keys, c->segs_a.as<uint64_t>(), (uint32_t)P, lo, 64, (int)c->tuning.radix_bits, &c->s,
                       c->err.as<uint32_t>(), c->stream, &sorted, &passes, true));
     c->stats.sort_passes = passes;
-    CK(cudaEventRecord(c->ev[3], c->stream));
+    CK(stage_mark(c, 3, c->stream, nullptr));
     *out_len = P;
     *out_none = 2 * c->stats.steps - P;
     if (cap < P) {
@@ -1251,6 +1264,46 @@ CGB_EXPORT cgb_status cgb_get_stream(cgb_composition* c, void** out_stream) {
 }
 
 CGB_EXPORT uint64_t cgb_kernel_launches(void) { return g_launches.load(); }
+
+CGB_EXPORT cgb_status cgb_selftest_bounded_wait(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(CGB_ERR_NO_DEVICE, "no CUDA device");
+    }
+    cudaStream_t st = nullptr;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(CGB_ERR_DEVICE, "selftest: stream");
+    uint32_t flag = 0;
+    cudaError_t e = selftest_bounded_wait(st, &flag);
+    // the context must still work: sort a few keys the normal way
+    bool sorted_ok = false;
+    if (e == cudaSuccess) {
+        const uint32_t n_keys = 10000;
+        std::vector<uint64_t> host(n_keys);
+        uint64_t x = 88172645463325252ull;
+        for (auto& v : host) {
+            x ^= x << 13, x ^= x >> 7, x ^= x << 17;
+            v = x;
+        }
+        uint64_t* d = nullptr;
+        if (cudaMalloc(&d, 2 * n_keys * 8) == cudaSuccess) {
+            cudaMemcpyAsync(d, host.data(), n_keys * 8, cudaMemcpyHostToDevice, st);
+            cgb_status s = cgb_sort_keys_noalloc(d, d + n_keys, n_keys, 0, 64, st);
+            std::vector<uint64_t> back(n_keys);
+            cudaMemcpyAsync(back.data(), d + n_keys, n_keys * 8, cudaMemcpyDeviceToHost, st);
+            e = cudaStreamSynchronize(st);
+            std::sort(host.begin(), host.end());
+            sorted_ok = s == CGB_OK && e == cudaSuccess && back == host;
+            cudaFree(d);
+        }
+    }
+    cudaStreamDestroy(st);
+    if (e != cudaSuccess) return fail(CGB_ERR_DEVICE, std::string("selftest: ") + cudaGetErrorString(e));
+    if (flag != 1) return fail(CGB_ERR_DEVICE, "selftest: the bounded wait did not report its expiry");
+    if (!sorted_ok) return fail(CGB_ERR_DEVICE, "selftest: the device did not sort correctly afterwards");
+    return fail(CGB_ERR_DEVICE_TIMEOUT, "selftest: the bounded wait expired as designed");
+}
 
 CGB_EXPORT cgb_status cgb_composition_clear(cgb_composition* c) {
     if (!c) return fail(CGB_ERR_INVALID_ARG, "null composition handle");

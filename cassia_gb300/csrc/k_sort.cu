@@ -475,6 +475,38 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo
     return cudaGetLastError();
 }
 
+// Self-test of the bounded wait: one CTA is given tile 1 of a two-tile pass
+// (the tile counter starts at 1), so the predecessor it looks back at never
+// publishes.  Its digit threads give up after SPIN_LIMIT rounds, set the error
+// flag and return without writing; nothing traps or hangs.  Returns the flag.
+cudaError_t selftest_bounded_wait(cudaStream_t st, uint32_t* flag_host) {
+    cudaError_t e = onesweep_setup();
+    if (e != cudaSuccess) return e;
+    const uint32_t n = 2 * SORT_TILE;
+    const size_t keys_b = (size_t)n * 8, hist_b = RADIX * 4, lb_b = 2 * RADIX * 4;
+    void* buf = nullptr;
+    if ((e = cudaMalloc(&buf, 2 * keys_b + hist_b + lb_b + 64)) != cudaSuccess) return e;
+    uint8_t* b = static_cast<uint8_t*>(buf);
+    uint64_t* in = reinterpret_cast<uint64_t*>(b);
+    uint64_t* out = reinterpret_cast<uint64_t*>(b + keys_b);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(b + 2 * keys_b);
+    uint32_t* lb = reinterpret_cast<uint32_t*>(b + 2 * keys_b + hist_b);
+    uint32_t* ctr = reinterpret_cast<uint32_t*>(b + 2 * keys_b + hist_b + lb_b);
+    uint32_t* err = ctr + 1;
+    const uint32_t one = 1;
+    e = cudaMemsetAsync(buf, 0, 2 * keys_b + hist_b + lb_b + 64, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctr, &one, 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        count_launches(1);
+        k_onesweep<<<1, SORT_THREADS, ONESWEEP_DYN_SMEM, st>>>(in, out, n, 0, 8, hist, lb, ctr, err);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(flag_host, err, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaError_t e2 = cudaFree(buf);
+    return e != cudaSuccess ? e : e2;
+}
+
 }  // namespace cgb
 
 // ---------------------------------------------------------------------------

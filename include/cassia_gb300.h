@@ -306,6 +306,15 @@ CGB_EXPORT uint64_t cgb_kernel_launches(void);
 CGB_EXPORT cgb_status cgb_sort_keys_noalloc(uint64_t* keys, uint64_t* out, size_t n, uint32_t bit_lo,
                                             uint32_t bit_hi, void* stream);
 
+/* Diagnostic: exercises the bounded device-side wait of the sort's decoupled
+ * look-back.  One sort CTA waits on a predecessor tile that never publishes;
+ * after its iteration limit (well under a second) it records the expiry in an
+ * error flag and returns, without trapping.  Returns CGB_ERR_DEVICE_TIMEOUT
+ * when the wait expired as designed and the device then still sorts
+ * correctly, CGB_ERR_DEVICE otherwise.  No counterpart in the reference
+ * (whose waits are host-side). */
+CGB_EXPORT cgb_status cgb_selftest_bounded_wait(void);
+
 /* Drops every layer and line, as Lines::cleared does for the builder
  * (surpass/src/segment.rs:282-301); device buffers are kept for reuse. */
 CGB_EXPORT cgb_status cgb_composition_clear(cgb_composition* c);
