@@ -51,8 +51,20 @@ struct PaintProps {
     uint32_t fill_rule;
     uint32_t blend_mode;
     uint32_t flags;  // PROPS_*
-    uint32_t pad;
+    uint32_t grad;   // gradient fills: index of the GradRec
     float color[4];
+};
+// A gradient fill (style.rs:29-175): type, its stops [first, first + n) in
+// the GradStop table (positions already resolved as GradientBuilder::build
+// does), start and end points.
+struct GradRec {
+    uint32_t type, n_stops, first, pad;
+    float start[2], end[2];
+};
+struct GradStop {
+    float color[4];
+    float stop;
+    float pad[3];
 };
 constexpr uint32_t PROPS_SOLID = 1u;        // Fill::Solid
 constexpr uint32_t PROPS_OPAQUE_OVER = 2u;  // Fill::Solid, BlendMode::Over, alpha == 1.0
@@ -70,6 +82,8 @@ struct SceneDesc {
     const uint32_t* lids;
     const LayerRec* layers;
     const PaintProps* props;    // by order
+    const GradRec* grads;       // gradient fills of props (PaintProps::grad)
+    const GradStop* stops;
     const uint8_t* unchanged;   // by order, or null (no layer cache)
     int32_t* prev_layers;       // by tile, or null
     uint8_t* out;               // device RGBA8
@@ -269,8 +283,10 @@ cudaError_t launch_items(int mode, uint32_t G, const BatchGeom& bg, const CarryB
                          cudaStream_t st);
 cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_tiles, int tile_shift,
                                uint32_t* tile_start, cudaStream_t st);
+// grad: some scene of the frame has gradient fills (selects the painter variant that handles them)
 cudaError_t launch_paint(const BatchGeom& bg, const uint64_t* segs, const uint64_t* items, int idx_bits, uint32_t G,
-                         const uint32_t* tile_start, const CarryBuffers& cb, uint32_t warps, cudaStream_t st);
+                         const uint32_t* tile_start, const CarryBuffers& cb, uint32_t warps, bool grad,
+                         cudaStream_t st);
 
 
 }  // namespace cgb

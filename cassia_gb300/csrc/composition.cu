@@ -165,6 +165,8 @@ struct cgb_composition {
     // LayerProps by order (orders_to_layers + Layer::props), rebuilt when dirty
     bool props_dirty = true;
     std::vector<PaintProps> props_host;
+    std::vector<GradRec> grads_host;
+    std::vector<GradStop> stops_host;
     std::vector<uint32_t> order_layer;
     uint32_t n_orders = 1;
     uint32_t unsupported = 0;  // enabled layers whose props the GPU painter does not take
@@ -174,7 +176,7 @@ struct cgb_composition {
     DevBuf recs, lengths, step_off, bcounts, boff, segs_a, segs_b;
     DevBuf tl_start, tl_key, tl_cover, tl_carry, tl_flags, item_count, item_off, items_a, items_b, tile_start;
     DevBuf blk_cover, blk_head, rlb;
-    DevBuf d_props, d_unchanged, out_rgba, err, dflt_t, d_scenes, d_row_scene;
+    DevBuf d_props, d_grads, d_stops, d_unchanged, out_rgba, err, dflt_t, d_scenes, d_row_scene;
     // flatten staging
     DevBuf f_kinds, f_points, f_cmd_off, f_pt_off, f_t9, f_has_t, f_path_layer, f_counts, f_off;
     // GC staging
@@ -378,16 +380,36 @@ void rebuild_props(cgb_composition* c) {
     c->props_host.assign(n_orders, PaintProps{CGB_FILL_NONZERO, CGB_BLEND_OVER,
                                               PROPS_SOLID | PROPS_DRAW | PROPS_OPAQUE_OVER, 0, {0, 0, 0, 1}});
     c->unsupported = 0;
+    c->grads_host.clear();
+    c->stops_host.clear();
     for (uint32_t o = 0; o < n_orders; o++) {
         if (c->order_layer[o] == UINT32_MAX) continue;
-        const cgb_props& p = c->layers[c->order_layer[o]].props.c;
-        if (p.func != CGB_FUNC_DRAW || p.is_clipped || p.fill_kind != CGB_FILL_SOLID) c->unsupported++;
+        const HostProps& hp = c->layers[c->order_layer[o]].props;
+        const cgb_props& p = hp.c;
+        if (p.func != CGB_FUNC_DRAW || p.is_clipped) c->unsupported++;
         PaintProps& pp = c->props_host[o];
         pp.fill_rule = p.fill_rule;
         pp.blend_mode = p.blend_mode;
-        pp.flags = PROPS_SOLID | PROPS_DRAW | PROPS_PRESENT;
-        if (p.blend_mode == CGB_BLEND_OVER && p.color[3] == 1.0f) pp.flags |= PROPS_OPAQUE_OVER;
+        pp.flags = PROPS_DRAW | PROPS_PRESENT;
+        pp.grad = 0;
         std::memcpy(pp.color, p.color, sizeof(pp.color));
+        if (p.fill_kind == CGB_FILL_SOLID) {
+            pp.flags |= PROPS_SOLID;
+            if (p.blend_mode == CGB_BLEND_OVER && p.color[3] == 1.0f) pp.flags |= PROPS_OPAQUE_OVER;
+        } else {
+            // GradientBuilder::build (style.rs:66-84): a stop given as 0 takes
+            // its evenly spaced default position
+            GradRec g{p.gradient_type, p.n_stops, (uint32_t)c->stops_host.size(), 0,
+                      {p.gradient_start[0], p.gradient_start[1]}, {p.gradient_end[0], p.gradient_end[1]}};
+            const float inc = 1.0f / (float)(p.n_stops - 1);
+            for (uint32_t i = 0; i < p.n_stops; i++) {
+                const float* st = hp.stops.data() + 5 * (size_t)i;
+                GradStop gs{{st[0], st[1], st[2], st[3]}, st[4] == -0.0f ? (float)i * inc : st[4], {0, 0, 0}};
+                c->stops_host.push_back(gs);
+            }
+            pp.grad = (uint32_t)c->grads_host.size();
+            c->grads_host.push_back(g);
+        }
     }
     c->n_orders = n_orders;
     c->props_dirty = false;
@@ -630,13 +652,21 @@ cgb_status prepare_scene(cgb_composition* c, SceneInput& in) {
     if (s0) return s0;
     if (c->props_dirty) rebuild_props(c);
     if (c->unsupported)
-        return fail(CGB_ERR_INVALID_ARG, "render: clip layers and gradient fills are not supported by the GPU painter");
+        return fail(CGB_ERR_INVALID_ARG, "render: clip layers are not supported by the GPU painter");
     cgb_status s1 = upload_layers(c);
     if (s1) return s1;
     if (c->props_uploaded != c->props_version) {
         CK(c->s.ensure(c->d_props, c->props_host.size() * sizeof(PaintProps)));
         CK(cudaMemcpyAsync(c->d_props.p, c->props_host.data(), c->props_host.size() * sizeof(PaintProps),
                            cudaMemcpyHostToDevice, c->stream));
+        if (!c->grads_host.empty()) {
+            CK(c->s.ensure(c->d_grads, c->grads_host.size() * sizeof(GradRec)));
+            CK(c->s.ensure(c->d_stops, c->stops_host.size() * sizeof(GradStop)));
+            CK(cudaMemcpyAsync(c->d_grads.p, c->grads_host.data(), c->grads_host.size() * sizeof(GradRec),
+                               cudaMemcpyHostToDevice, c->stream));
+            CK(cudaMemcpyAsync(c->d_stops.p, c->stops_host.data(), c->stops_host.size() * sizeof(GradStop),
+                               cudaMemcpyHostToDevice, c->stream));
+        }
         c->props_uploaded = c->props_version;
     }
     if (in.cache) {
@@ -661,6 +691,8 @@ cgb_status prepare_scene(cgb_composition* c, SceneInput& in) {
     d.lids = c->lids.as<uint32_t>();
     d.layers = c->d_layers.as<LayerRec>();
     d.props = c->d_props.as<PaintProps>();
+    d.grads = c->grads_host.empty() ? nullptr : c->d_grads.as<GradRec>();
+    d.stops = c->grads_host.empty() ? nullptr : c->d_stops.as<GradStop>();
     d.unchanged = in.cache ? c->d_unchanged.as<uint8_t>() : nullptr;
     d.prev_layers = in.cache ? in.cache->prev.as<int32_t>() : nullptr;
     d.default_t = c->has_default_transform ? c->dflt_t.as<float>() : nullptr;
@@ -814,7 +846,10 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
     c->stats.item_sort_passes = ipasses;
     CK(launch_tile_ranges(items_sorted, (uint32_t)W, (uint32_t)tiles, tile_shift, cb.tile_start, st));
     CK(stage_mark(c, 4, st, "cgb:paint"));
-    CK(launch_paint(bg, sorted, items_sorted, idx_bits, (uint32_t)G, cb.tile_start, cb, c->tuning.paint_warps, st));
+    bool grad = false;
+    for (const SceneInput& in : scenes) grad |= in.d.grads != nullptr;
+    CK(launch_paint(bg, sorted, items_sorted, idx_bits, (uint32_t)G, cb.tile_start, cb, c->tuning.paint_warps, grad,
+                    st));
     CK(stage_mark(c, 5, st, nullptr));
     for (SceneInput& in : scenes)
         if (in.buf->memory == CGB_MEMORY_HOST)
@@ -897,7 +932,7 @@ CGB_EXPORT cgb_status cgb_composition_free(cgb_composition* c) {
     DevBuf* bufs[] = {&c->p0x, &c->p0y, &c->p1x, &c->p1y, &c->lids, &c->d_layers, &c->recs, &c->lengths,
                       &c->step_off, &c->bcounts, &c->boff, &c->segs_a, &c->segs_b,
                       &c->tl_start, &c->tl_key, &c->blk_cover, &c->blk_head, &c->rlb, &c->tl_cover, &c->tl_carry, &c->tl_flags, &c->item_count, &c->item_off,
-                      &c->items_a, &c->items_b, &c->tile_start, &c->d_props, &c->d_unchanged, &c->out_rgba, &c->err,
+                      &c->items_a, &c->items_b, &c->tile_start, &c->d_props, &c->d_grads, &c->d_stops, &c->d_unchanged, &c->out_rgba, &c->err,
                       &c->dflt_t, &c->f_kinds, &c->f_points, &c->f_cmd_off, &c->f_pt_off, &c->f_t9, &c->f_has_t,
                       &c->f_path_layer, &c->f_counts, &c->f_off, &c->g_flags, &c->g_off, &c->s.scan_sums,
                       &c->s.sort_hist, &c->s.sort_lookback, &c->s.sort_counter};
@@ -1079,7 +1114,14 @@ CGB_EXPORT cgb_status cgb_layer_set_props(cgb_composition* c, uint32_t layer_id,
     hp.c = *props;
     hp.c.stops = nullptr;
     if (props->fill_kind == CGB_FILL_GRADIENT) {
+        // GradientBuilder::build (style.rs:66-84): at least two stops, each in
+        // [0, 1] (color_with_stop panics otherwise), linear or radial
         if (props->n_stops < 2 || !props->stops) return fail(CGB_ERR_INVALID_ARG, "set_props: gradient needs 2 stops");
+        if (props->gradient_type > CGB_GRADIENT_RADIAL) return fail(CGB_ERR_INVALID_ARG, "set_props: gradient type");
+        for (uint32_t i = 0; i < props->n_stops; i++) {
+            const float st = props->stops[5 * (size_t)i + 4];
+            if (st < 0.0f || st > 1.0f) return fail(CGB_ERR_INVALID_ARG, "set_props: gradient stop outside [0, 1]");
+        }
         hp.stops.assign(props->stops, props->stops + 5 * (size_t)props->n_stops);
     }
     if (!(l->props == hp)) {

@@ -459,6 +459,116 @@ __device__ __forceinline__ void blend_dispatch(uint32_t mode, float2 (&C)[4], co
     }
 }
 
+// blend_function! (style.rs:288-418) for one pixel: blend_vec2's operations
+// on one element.
+template <int MODE>
+__device__ __forceinline__ float blend_vec1(float d, float s) {
+    if (MODE == CGB_BLEND_OVER) return s;
+    if (MODE == CGB_BLEND_MULTIPLY) return d * s;
+    if (MODE == CGB_BLEND_SCREEN) return __fmaf_rn(d, -s, d) + s;
+    if (MODE == CGB_BLEND_OVERLAY) return s <= 0.5f ? (d * s) * 2.0f : 2.0f * ((s + d) - __fmaf_rn(s, d, 0.5f));
+    if (MODE == CGB_BLEND_DARKEN) return fminf(d, s);
+    if (MODE == CGB_BLEND_LIGHTEN) return fmaxf(d, s);
+    if (MODE == CGB_BLEND_COLOR_DODGE) return s == 0.0f ? 0.0f : fminf(1.0f, s / (1.0f - d));
+    if (MODE == CGB_BLEND_COLOR_BURN) return s == 1.0f ? 1.0f : 1.0f - fminf(1.0f, (1.0f - s) / d);
+    if (MODE == CGB_BLEND_HARD_LIGHT) return d <= 0.5f ? (d * s) * 2.0f : 2.0f * ((s + d) - __fmaf_rn(s, d, 0.5f));
+    if (MODE == CGB_BLEND_SOFT_LIGHT) {
+        const float dd = s <= 0.25f ? __fmaf_rn(__fmaf_rn(16.0f, s, -12.0f), s, 4.0f) * s : sqrtf(s);
+        const float k = __fmaf_rn(2.0f, d, -1.0f);
+        return d <= 0.5f ? __fmaf_rn(s * (1.0f - s), k, s) : __fmaf_rn(dd - s, k, s);
+    }
+    if (MODE == CGB_BLEND_DIFFERENCE) return fabsf(d - s);
+    return __fmaf_rn(-2.0f * d, s, d) + s;  // EXCLUSION
+}
+
+// Gradient::get_t + color_at (style.rs:96-174) for one pixel.  x is the
+// column argument the painter passes (the pixel's column + 1, as
+// paint_layer's loop does), y the tile's top row, k the row in the tile.
+// Stop lanes are merged by OR-ing float bits, as the vector code does.
+__device__ float4 gradient_color(const GradRec& g, const GradStop* __restrict__ stops, float x, float y,
+                                             int k) {
+    const float dx = g.end[0] - g.start[0];
+    const float dy = g.end[1] - g.start[1];
+    const float dot = dx * dx + dy * dy;
+    const float dot_recip = 1.0f / dot;
+    float t;
+    if (g.type == CGB_GRADIENT_LINEAR) {
+        const float tx = (x - g.start[0]) * dx * dot_recip;
+        const float ty = y - g.start[1];
+        t = __fmaf_rn(((float)k + ty) * dy, dot_recip, tx);
+    } else {
+        const float px = x - g.start[0];
+        const float px2 = px * px;
+        const float py = (float)k + (y - g.start[1]);
+        t = sqrtf(__fmaf_rn(py, py, px2) * dot_recip);
+    }
+    uint32_t out[4] = {0u, 0u, 0u, 0u};
+    const GradStop* st = stops + g.first;
+    bool acc = t <= st[0].stop;
+    if (acc)
+        for (int c = 0; c < 4; c++) out[c] |= __float_as_uint(st[0].color[c]);
+    float start_stop = 0.0f;
+    float sc[4] = {st[0].color[0], st[0].color[1], st[0].color[2], st[0].color[3]};
+    for (uint32_t si = 1; si < g.n_stops; si++) {
+        const float end_stop = st[si].stop;
+        const bool m = acc ^ (t < end_stop);
+        if (m) {
+            const float d = end_stop - start_stop;
+            const float dr = 1.0f / d;
+            const float lt = (t - start_stop) * dr;
+            for (int c = 0; c < 4; c++)
+                out[c] |= __float_as_uint(__fmaf_rn(lt, st[si].color[c], __fmaf_rn(-lt, sc[c], sc[c])));
+        }
+        acc = acc || m;
+        start_stop = end_stop;
+        for (int c = 0; c < 4; c++) sc[c] = st[si].color[c];
+    }
+    if (!acc)
+        for (int c = 0; c < 4; c++) out[c] |= __float_as_uint(st[g.n_stops - 1].color[c]);
+    return make_float4(__uint_as_float(out[0]), __uint_as_float(out[1]), __uint_as_float(out[2]),
+                       __uint_as_float(out[3]));
+}
+
+// blend_at with a per-pixel source (gradient fills).
+template <int MODE>
+__device__ __forceinline__ void blend_pixels_src(float2 (&C)[4], const float4 (&src)[2], float2 cov, bool col0,
+                                                 bool col1) {
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const float cv = h ? cov.y : cov.x;
+        const bool on = h ? col1 : col0;
+        float c[4] = {h ? C[0].y : C[0].x, h ? C[1].y : C[1].x, h ? C[2].y : C[2].x, h ? C[3].y : C[3].x};
+        const float al = src[h].w * cv;
+        const float inv = 1.0f - al;
+        const float n0 = __fmaf_rn(c[0], inv, blend_vec1<MODE>(c[0], src[h].x) * al);
+        const float n1 = __fmaf_rn(c[1], inv, blend_vec1<MODE>(c[1], src[h].y) * al);
+        const float n2 = __fmaf_rn(c[2], inv, blend_vec1<MODE>(c[2], src[h].z) * al);
+        const float n3 = __fmaf_rn(c[3], inv, al);
+        if (on) {
+            if (h) C[0].y = n0, C[1].y = n1, C[2].y = n2, C[3].y = n3;
+            else C[0].x = n0, C[1].x = n1, C[2].x = n2, C[3].x = n3;
+        }
+    }
+}
+
+__device__ void blend_dispatch_src(uint32_t mode, float2 (&C)[4], const float4 (&src)[2], float2 cov, bool col0,
+                                   bool col1) {
+    switch (mode) {
+        case CGB_BLEND_OVER: blend_pixels_src<CGB_BLEND_OVER>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_MULTIPLY: blend_pixels_src<CGB_BLEND_MULTIPLY>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_SCREEN: blend_pixels_src<CGB_BLEND_SCREEN>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_OVERLAY: blend_pixels_src<CGB_BLEND_OVERLAY>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_DARKEN: blend_pixels_src<CGB_BLEND_DARKEN>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_LIGHTEN: blend_pixels_src<CGB_BLEND_LIGHTEN>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_COLOR_DODGE: blend_pixels_src<CGB_BLEND_COLOR_DODGE>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_COLOR_BURN: blend_pixels_src<CGB_BLEND_COLOR_BURN>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_HARD_LIGHT: blend_pixels_src<CGB_BLEND_HARD_LIGHT>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_SOFT_LIGHT: blend_pixels_src<CGB_BLEND_SOFT_LIGHT>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_DIFFERENCE: blend_pixels_src<CGB_BLEND_DIFFERENCE>(C, src, cov, col0, col1); break;
+        default: blend_pixels_src<CGB_BLEND_EXCLUSION>(C, src, cov, col0, col1); break;
+    }
+}
+
 // BlendMode::blend_fn (style.rs:206-267)
 __device__ float blend_fn(uint32_t mode, float dst, float src) {
     switch (mode) {
@@ -541,6 +651,7 @@ static_assert(SEGCAP == 8 * 32, "the staging owner map gives each lane 8 positio
 
 constexpr uint32_t META_CARRY_ONLY = 32u;  // the item only carries cover through the tile
 constexpr uint32_t META_ACTIVE = 64u;      // carry-only: some tile row has non-zero coverage
+constexpr uint32_t META_GRAD = 128u;       // a gradient fill (its GradRec index in color.x's bits)
 
 // Per-warp staging of 32 work items.
 struct WarpStage {
@@ -573,6 +684,10 @@ __device__ __forceinline__ void stage_items(const PaintArgs& a, const PaintProps
         const uint32_t co = (fl & ITEM_CARRY) ? 1u : 0u;
         const uint32_t fr = hdr.x & 1u;
         meta = (hdr.y & 15u) | (fr << 4);
+        if (!(hdr.z & PROPS_SOLID)) {
+            meta |= META_GRAD;
+            col.x = __uint_as_float(hdr.w);
+        }
         if (co) {
             carry = cover_add(carry, a.tl_cover[g]);
             meta |= META_CARRY_ONLY;
@@ -658,7 +773,8 @@ __device__ __forceinline__ void stage_items(const PaintArgs& a, const PaintProps
     __syncwarp();
 }
 
-template <int PAINT_WARPS>  // tiles per CTA
+// PAINT_WARPS tiles per CTA; GRAD: the frame holds gradient fills
+template <int PAINT_WARPS, bool GRAD>
 __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
     __shared__ WarpStage stages[PAINT_WARPS];
     const int lane = threadIdx.x & 31;
@@ -720,6 +836,21 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
     const uint32_t x0 = 2 * xg;
     uint32_t px0 = 0, px1 = 0;
     bool painted = true;
+    // the gradient column argument of the lane's first pixel, less one, and the tile's top row
+    const float gx0 = (float)(i * 8 + x0), gy0 = (float)(j * 8);
+    if (GRAD && first != 2) {
+        // the fold takes Solid fills only (skip_fully_covered_layers, :376-383)
+        const uint32_t from0 = first == 1 ? (uint32_t)k_op + 1 : b;
+        for (uint32_t c0 = from0; c0 < e && first != 2; c0 += 32) {
+            bool ok = true;
+            if (c0 + lane < e) {
+                uint32_t L, fl, g;
+                item_decode(a.items[c0 + lane], a.idx_bits, a.order_bits, L, fl, g);
+                ok = L < p.n_orders && (p.props[L].flags & PROPS_SOLID);
+            }
+            if (!__all_sync(0xffffffffu, ok)) first = 2;
+        }
+    }
     if (first != 2) {
         // Solid: fold BlendMode::blend (scalar, style.rs:269-285) over the
         // full layers above the opaque one (or above the clear color).
@@ -774,7 +905,14 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
                 if (meta & META_CARRY_ONLY) {
                     if (!(meta & META_ACTIVE)) continue;
                     cov = splat(reinterpret_cast<const float*>(&S.rowcov[q][0])[y]);
-                    blend_dispatch<false>(mode, C, S.color[q], cov, true, true);
+                    if (GRAD && (meta & META_GRAD)) {
+                        const GradRec g = p.grads[__float_as_uint(S.color[q].x)];
+                        const float4 src[2] = {gradient_color(g, p.stops, gx0 + 1.0f, gy0, (int)y),
+                                               gradient_color(g, p.stops, gx0 + 2.0f, gy0, (int)y)};
+                        blend_dispatch_src(mode, C, src, cov, true, true);
+                    } else {
+                        blend_dispatch<false>(mode, C, S.color[q], cov, true, true);
+                    }
                     continue;
                 } else {
                     // acc_segment / acc_cover / compute_areas (painter/mod.rs:229-243, 347-362):
@@ -815,7 +953,14 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
                     col0 = ((b0 >> (8 * xg)) & 0xFFu) != 0;
                     col1 = ((b1 >> (8 * xg)) & 0xFFu) != 0;
                 }
-                blend_dispatch<true>(mode, C, S.color[q], cov, col0, col1);
+                if (GRAD && (meta & META_GRAD)) {
+                    const GradRec g = p.grads[__float_as_uint(S.color[q].x)];
+                    const float4 src[2] = {gradient_color(g, p.stops, gx0 + 1.0f, gy0, (int)y),
+                                           gradient_color(g, p.stops, gx0 + 2.0f, gy0, (int)y)};
+                    blend_dispatch_src(mode, C, src, cov, col0, col1);
+                } else {
+                    blend_dispatch<true>(mode, C, S.color[q], cov, col0, col1);
+                }
             }
             __syncwarp();
         }
@@ -882,16 +1027,26 @@ cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_til
 }
 
 cudaError_t launch_paint(const BatchGeom& bg, const uint64_t* segs, const uint64_t* items, int idx_bits, uint32_t G,
-                         const uint32_t* tile_start, const CarryBuffers& cb, uint32_t warps, cudaStream_t st) {
+                         const uint32_t* tile_start, const CarryBuffers& cb, uint32_t warps, bool grad,
+                         cudaStream_t st) {
     if (bg.total_tiles == 0) return cudaSuccess;
     PaintArgs a{bg, segs, items, idx_bits, cb.order_bits, G, tile_start, cb.tl_start, cb.tl_cover, cb.tl_carry};
     count_launches(1);
     const uint32_t T = bg.total_tiles;
-    switch (warps) {
-        case 2: k_paint<2><<<(T + 1) / 2, 64, 0, st>>>(a); break;
-        case 4: k_paint<4><<<(T + 3) / 4, 128, 0, st>>>(a); break;
-        case 8: k_paint<8><<<(T + 7) / 8, 256, 0, st>>>(a); break;
-        default: return cudaErrorInvalidValue;
+    if (grad) {
+        switch (warps) {
+            case 2: k_paint<2, true><<<(T + 1) / 2, 64, 0, st>>>(a); break;
+            case 4: k_paint<4, true><<<(T + 3) / 4, 128, 0, st>>>(a); break;
+            case 8: k_paint<8, true><<<(T + 7) / 8, 256, 0, st>>>(a); break;
+            default: return cudaErrorInvalidValue;
+        }
+    } else {
+        switch (warps) {
+            case 2: k_paint<2, false><<<(T + 1) / 2, 64, 0, st>>>(a); break;
+            case 4: k_paint<4, false><<<(T + 3) / 4, 128, 0, st>>>(a); break;
+            case 8: k_paint<8, false><<<(T + 7) / 8, 256, 0, st>>>(a); break;
+            default: return cudaErrorInvalidValue;
+        }
     }
     return cudaGetLastError();
 }
