@@ -51,7 +51,7 @@ struct PaintProps {
     uint32_t fill_rule;
     uint32_t blend_mode;
     uint32_t flags;  // PROPS_*
-    uint32_t grad;   // gradient fills: index of the GradRec
+    uint32_t aux;    // gradient fills: index of the GradRec; clip layers: the layers they clip
     float color[4];
 };
 // A gradient fill (style.rs:29-175): type, its stops [first, first + n) in
@@ -70,6 +70,11 @@ constexpr uint32_t PROPS_SOLID = 1u;        // Fill::Solid
 constexpr uint32_t PROPS_OPAQUE_OVER = 2u;  // Fill::Solid, BlendMode::Over, alpha == 1.0
 constexpr uint32_t PROPS_DRAW = 4u;         // Func::Draw
 constexpr uint32_t PROPS_PRESENT = 8u;      // an enabled layer holds this order
+constexpr uint32_t PROPS_CLIP = 16u;        // Func::Clip
+constexpr uint32_t PROPS_CLIPPED = 32u;     // Style::is_clipped (a Draw layer)
+// SceneDesc::features
+constexpr uint32_t FEAT_GRADIENTS = 1u;     // some layer has a gradient fill
+constexpr uint32_t FEAT_CLIPS = 2u;         // some layer clips or is clipped
 
 // One canvas of a frame: a composition's lines, layer table and props, its
 // output buffer, and where its tile rows / tiles sit in the frame's global
@@ -93,6 +98,7 @@ struct SceneDesc {
     uint32_t width, height, stride, rows, row_len;
     uint32_t row_base, tile_base;
     uint32_t crop_h0, crop_h1, crop_v0, crop_v1;  // in tiles
+    uint32_t features;                            // FEAT_*
     float clear[4];
 };
 
@@ -283,10 +289,12 @@ cudaError_t launch_items(int mode, uint32_t G, const BatchGeom& bg, const CarryB
                          cudaStream_t st);
 cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_tiles, int tile_shift,
                                uint32_t* tile_start, cudaStream_t st);
-// grad: some scene of the frame has gradient fills (selects the painter variant that handles them)
+// full: some scene of the frame has gradient fills or clips (selects the
+// painter variant that handles them); item_state: one byte per work item
+// (clip pass results), needed when a scene has clips.
 cudaError_t launch_paint(const BatchGeom& bg, const uint64_t* segs, const uint64_t* items, int idx_bits, uint32_t G,
-                         const uint32_t* tile_start, const CarryBuffers& cb, uint32_t warps, bool grad,
-                         cudaStream_t st);
+                         const uint32_t* tile_start, const CarryBuffers& cb, uint32_t warps, bool full,
+                         uint8_t* item_state, cudaStream_t st);
 
 
 }  // namespace cgb

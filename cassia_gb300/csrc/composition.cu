@@ -169,13 +169,13 @@ struct cgb_composition {
     std::vector<GradStop> stops_host;
     std::vector<uint32_t> order_layer;
     uint32_t n_orders = 1;
-    uint32_t unsupported = 0;  // enabled layers whose props the GPU painter does not take
+    uint32_t features = 0;     // FEAT_* of the enabled layers' props
     uint64_t props_version = 1, props_uploaded = 0;
 
     // frame buffers
     DevBuf recs, lengths, step_off, bcounts, boff, segs_a, segs_b;
     DevBuf tl_start, tl_key, tl_cover, tl_carry, tl_flags, item_count, item_off, items_a, items_b, tile_start;
-    DevBuf blk_cover, blk_head, rlb;
+    DevBuf blk_cover, blk_head, rlb, item_state;
     DevBuf d_props, d_grads, d_stops, d_unchanged, out_rgba, err, dflt_t, d_scenes, d_row_scene;
     // flatten staging
     DevBuf f_kinds, f_points, f_cmd_off, f_pt_off, f_t9, f_has_t, f_path_layer, f_counts, f_off;
@@ -379,20 +379,30 @@ void rebuild_props(cgb_composition* c) {
     }
     c->props_host.assign(n_orders, PaintProps{CGB_FILL_NONZERO, CGB_BLEND_OVER,
                                               PROPS_SOLID | PROPS_DRAW | PROPS_OPAQUE_OVER, 0, {0, 0, 0, 1}});
-    c->unsupported = 0;
+    c->features = 0;
     c->grads_host.clear();
     c->stops_host.clear();
     for (uint32_t o = 0; o < n_orders; o++) {
         if (c->order_layer[o] == UINT32_MAX) continue;
         const HostProps& hp = c->layers[c->order_layer[o]].props;
         const cgb_props& p = hp.c;
-        if (p.func != CGB_FUNC_DRAW || p.is_clipped) c->unsupported++;
         PaintProps& pp = c->props_host[o];
         pp.fill_rule = p.fill_rule;
         pp.blend_mode = p.blend_mode;
-        pp.flags = PROPS_DRAW | PROPS_PRESENT;
-        pp.grad = 0;
+        pp.flags = PROPS_PRESENT;
+        pp.aux = 0;
         std::memcpy(pp.color, p.color, sizeof(pp.color));
+        if (p.func == CGB_FUNC_CLIP) {  // Func::Clip(n): masks the next n layers
+            pp.flags |= PROPS_CLIP;
+            pp.aux = p.clip_layers;
+            c->features |= FEAT_CLIPS;
+            continue;
+        }
+        pp.flags |= PROPS_DRAW;
+        if (p.is_clipped) {
+            pp.flags |= PROPS_CLIPPED;
+            c->features |= FEAT_CLIPS;
+        }
         if (p.fill_kind == CGB_FILL_SOLID) {
             pp.flags |= PROPS_SOLID;
             if (p.blend_mode == CGB_BLEND_OVER && p.color[3] == 1.0f) pp.flags |= PROPS_OPAQUE_OVER;
@@ -407,8 +417,9 @@ void rebuild_props(cgb_composition* c) {
                 GradStop gs{{st[0], st[1], st[2], st[3]}, st[4] == -0.0f ? (float)i * inc : st[4], {0, 0, 0}};
                 c->stops_host.push_back(gs);
             }
-            pp.grad = (uint32_t)c->grads_host.size();
+            pp.aux = (uint32_t)c->grads_host.size();
             c->grads_host.push_back(g);
+            c->features |= FEAT_GRADIENTS;
         }
     }
     c->n_orders = n_orders;
@@ -651,8 +662,6 @@ cgb_status prepare_scene(cgb_composition* c, SceneInput& in) {
     cgb_status s0 = remove_disabled(c);
     if (s0) return s0;
     if (c->props_dirty) rebuild_props(c);
-    if (c->unsupported)
-        return fail(CGB_ERR_INVALID_ARG, "render: clip layers are not supported by the GPU painter");
     cgb_status s1 = upload_layers(c);
     if (s1) return s1;
     if (c->props_uploaded != c->props_version) {
@@ -700,6 +709,7 @@ cgb_status prepare_scene(cgb_composition* c, SceneInput& in) {
     d.n_layer_recs = c->n_layer_recs;
     d.n_orders = c->n_orders;
     d.wide = c->wide ? 1u : 0u;
+    d.features = c->features;
     d.width = (uint32_t)buf->width;
     d.height = (uint32_t)buf->height;
     d.stride = (uint32_t)stride;
@@ -846,10 +856,15 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
     c->stats.item_sort_passes = ipasses;
     CK(launch_tile_ranges(items_sorted, (uint32_t)W, (uint32_t)tiles, tile_shift, cb.tile_start, st));
     CK(stage_mark(c, 4, st, "cgb:paint"));
-    bool grad = false;
-    for (const SceneInput& in : scenes) grad |= in.d.grads != nullptr;
-    CK(launch_paint(bg, sorted, items_sorted, idx_bits, (uint32_t)G, cb.tile_start, cb, c->tuning.paint_warps, grad,
-                    st));
+    uint32_t features = 0;
+    for (const SceneInput& in : scenes) features |= in.d.features;
+    uint8_t* item_state = nullptr;
+    if (features & FEAT_CLIPS) {
+        CK(c->s.ensure(c->item_state, std::max<uint64_t>(W, 1)));
+        item_state = c->item_state.as<uint8_t>();
+    }
+    CK(launch_paint(bg, sorted, items_sorted, idx_bits, (uint32_t)G, cb.tile_start, cb, c->tuning.paint_warps,
+                    features != 0, item_state, st));
     CK(stage_mark(c, 5, st, nullptr));
     for (SceneInput& in : scenes)
         if (in.buf->memory == CGB_MEMORY_HOST)
@@ -931,7 +946,7 @@ CGB_EXPORT cgb_status cgb_composition_free(cgb_composition* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     DevBuf* bufs[] = {&c->p0x, &c->p0y, &c->p1x, &c->p1y, &c->lids, &c->d_layers, &c->recs, &c->lengths,
                       &c->step_off, &c->bcounts, &c->boff, &c->segs_a, &c->segs_b,
-                      &c->tl_start, &c->tl_key, &c->blk_cover, &c->blk_head, &c->rlb, &c->tl_cover, &c->tl_carry, &c->tl_flags, &c->item_count, &c->item_off,
+                      &c->tl_start, &c->tl_key, &c->blk_cover, &c->blk_head, &c->rlb, &c->item_state, &c->tl_cover, &c->tl_carry, &c->tl_flags, &c->item_count, &c->item_off,
                       &c->items_a, &c->items_b, &c->tile_start, &c->d_props, &c->d_grads, &c->d_stops, &c->d_unchanged, &c->out_rgba, &c->err,
                       &c->dflt_t, &c->f_kinds, &c->f_points, &c->f_cmd_off, &c->f_pt_off, &c->f_t9, &c->f_has_t,
                       &c->f_path_layer, &c->f_counts, &c->f_off, &c->g_flags, &c->g_off, &c->s.scan_sums,

@@ -24,7 +24,10 @@
 // items in order.  The painter gives each tile one warp (2 pixels per lane), replicates
 // tile_unchanged_pass and skip_fully_covered_layers (:200-222, :310-388),
 // paints the surviving layers bottom-up in f32 with the reference's vector
-// blend formulas, and writes RGBA8 with 128-bit stores.
+// blend formulas, and writes RGBA8 with 128-bit stores.  Frames with gradient
+// fills or clip layers use the FULL variant: per-pixel gradient colours
+// (style.rs:96-174), skip_trivial_clips_pass (:224-308) as a lockstep warp
+// pass, and the painter's clip mask (painter/mod.rs:260-317, 402-416).
 #include "cgb_internal.cuh"
 
 namespace cgb {
@@ -529,16 +532,18 @@ __device__ float4 gradient_color(const GradRec& g, const GradStop* __restrict__ 
                        __uint_as_float(out[3]));
 }
 
-// blend_at with a per-pixel source (gradient fills).
+// blend_at with a per-pixel source (gradient fills) and, for clipped layers,
+// the clip mask (alpha = fill alpha * coverage * mask, in that order).
 template <int MODE>
 __device__ __forceinline__ void blend_pixels_src(float2 (&C)[4], const float4 (&src)[2], float2 cov, bool col0,
-                                                 bool col1) {
+                                                 bool col1, bool clipped, float2 mask) {
 #pragma unroll
     for (int h = 0; h < 2; h++) {
         const float cv = h ? cov.y : cov.x;
         const bool on = h ? col1 : col0;
         float c[4] = {h ? C[0].y : C[0].x, h ? C[1].y : C[1].x, h ? C[2].y : C[2].x, h ? C[3].y : C[3].x};
-        const float al = src[h].w * cv;
+        float al = src[h].w * cv;
+        if (clipped) al *= h ? mask.y : mask.x;
         const float inv = 1.0f - al;
         const float n0 = __fmaf_rn(c[0], inv, blend_vec1<MODE>(c[0], src[h].x) * al);
         const float n1 = __fmaf_rn(c[1], inv, blend_vec1<MODE>(c[1], src[h].y) * al);
@@ -552,20 +557,22 @@ __device__ __forceinline__ void blend_pixels_src(float2 (&C)[4], const float4 (&
 }
 
 __device__ void blend_dispatch_src(uint32_t mode, float2 (&C)[4], const float4 (&src)[2], float2 cov, bool col0,
-                                   bool col1) {
+                                   bool col1, bool clipped, float2 mask) {
     switch (mode) {
-        case CGB_BLEND_OVER: blend_pixels_src<CGB_BLEND_OVER>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_MULTIPLY: blend_pixels_src<CGB_BLEND_MULTIPLY>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_SCREEN: blend_pixels_src<CGB_BLEND_SCREEN>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_OVERLAY: blend_pixels_src<CGB_BLEND_OVERLAY>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_DARKEN: blend_pixels_src<CGB_BLEND_DARKEN>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_LIGHTEN: blend_pixels_src<CGB_BLEND_LIGHTEN>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_COLOR_DODGE: blend_pixels_src<CGB_BLEND_COLOR_DODGE>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_COLOR_BURN: blend_pixels_src<CGB_BLEND_COLOR_BURN>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_HARD_LIGHT: blend_pixels_src<CGB_BLEND_HARD_LIGHT>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_SOFT_LIGHT: blend_pixels_src<CGB_BLEND_SOFT_LIGHT>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_DIFFERENCE: blend_pixels_src<CGB_BLEND_DIFFERENCE>(C, src, cov, col0, col1); break;
-        default: blend_pixels_src<CGB_BLEND_EXCLUSION>(C, src, cov, col0, col1); break;
+        case CGB_BLEND_OVER: blend_pixels_src<CGB_BLEND_OVER>(C, src, cov, col0, col1, clipped, mask); break;
+        case CGB_BLEND_MULTIPLY: blend_pixels_src<CGB_BLEND_MULTIPLY>(C, src, cov, col0, col1, clipped, mask); break;
+        case CGB_BLEND_SCREEN: blend_pixels_src<CGB_BLEND_SCREEN>(C, src, cov, col0, col1, clipped, mask); break;
+        case CGB_BLEND_OVERLAY: blend_pixels_src<CGB_BLEND_OVERLAY>(C, src, cov, col0, col1, clipped, mask); break;
+        case CGB_BLEND_DARKEN: blend_pixels_src<CGB_BLEND_DARKEN>(C, src, cov, col0, col1, clipped, mask); break;
+        case CGB_BLEND_LIGHTEN: blend_pixels_src<CGB_BLEND_LIGHTEN>(C, src, cov, col0, col1, clipped, mask); break;
+        case CGB_BLEND_COLOR_DODGE:
+            blend_pixels_src<CGB_BLEND_COLOR_DODGE>(C, src, cov, col0, col1, clipped, mask);
+            break;
+        case CGB_BLEND_COLOR_BURN: blend_pixels_src<CGB_BLEND_COLOR_BURN>(C, src, cov, col0, col1, clipped, mask); break;
+        case CGB_BLEND_HARD_LIGHT: blend_pixels_src<CGB_BLEND_HARD_LIGHT>(C, src, cov, col0, col1, clipped, mask); break;
+        case CGB_BLEND_SOFT_LIGHT: blend_pixels_src<CGB_BLEND_SOFT_LIGHT>(C, src, cov, col0, col1, clipped, mask); break;
+        case CGB_BLEND_DIFFERENCE: blend_pixels_src<CGB_BLEND_DIFFERENCE>(C, src, cov, col0, col1, clipped, mask); break;
+        default: blend_pixels_src<CGB_BLEND_EXCLUSION>(C, src, cov, col0, col1, clipped, mask); break;
     }
 }
 
@@ -640,6 +647,7 @@ struct PaintArgs {
     int idx_bits;
     int order_bits;
     uint32_t G;  // TL count (item TL indices are below it)
+    uint8_t* item_state;  // per work item: ISTATE_* from the clip pass (scenes with clips)
     const uint32_t* tile_start;
     const uint32_t* tl_start;
     const uint64_t* tl_cover;
@@ -652,13 +660,20 @@ static_assert(SEGCAP == 8 * 32, "the staging owner map gives each lane 8 positio
 constexpr uint32_t META_CARRY_ONLY = 32u;  // the item only carries cover through the tile
 constexpr uint32_t META_ACTIVE = 64u;      // carry-only: some tile row has non-zero coverage
 constexpr uint32_t META_GRAD = 128u;       // a gradient fill (its GradRec index in color.x's bits)
+constexpr uint32_t META_SKIP = 256u;       // masked out by the clip pass: not painted
+constexpr uint32_t META_CLIP = 512u;       // a clip layer (the last layer it clips in color.x's bits)
+constexpr uint32_t META_APPLY_CLIP = 1024u;  // a clipped Draw layer whose clip is not trivially full
+// item_state bits written by the clip pass (skip_trivial_clips_pass)
+constexpr uint8_t ISTATE_MASKED = 1;     // masked out
+constexpr uint8_t ISTATE_SKIP_CLIP = 2;  // clipped, but its clip is full: drawn unclipped
 
 // Per-warp staging of 32 work items.
 struct WarpStage {
     float4 color[32];
     float4 rowcov[32][2];  // carry-only items: coverage of each tile row
     uint64_t carry[32];    // cover entering the tile (TL items)
-    uint32_t meta[32];     // blend_mode | fill_rule << 4 | META_CARRY_ONLY | META_ACTIVE
+    uint32_t meta[32];     // blend_mode | fill_rule << 4 | META_*
+    uint32_t order[32];    // the item's layer order
     uint32_t sb[32];     // first segment (global index)
     uint32_t cnt[32];    // segments of the item
     uint32_t soff[32];   // staging offset of its segments
@@ -669,8 +684,11 @@ struct WarpStage {
 };
 
 // Loads items [c0, c0 + n) into the stage; all loads of the chunk are in flight together.
-__device__ __forceinline__ void stage_items(const PaintArgs& a, const PaintProps* __restrict__ props, uint32_t n_orders,
-                                            WarpStage& S, uint32_t c0, uint32_t n, int lane, bool with_segments) {
+template <bool FULL>
+__device__ __forceinline__ void stage_items(const PaintArgs& a, const SceneDesc& scene, WarpStage& S, uint32_t c0,
+                                            uint32_t n, int lane, bool with_segments) {
+    const PaintProps* __restrict__ props = scene.props;
+    const uint32_t n_orders = scene.n_orders;
     uint32_t meta = 0, sb = 0, cnt = 0;
     uint64_t carry = 0;
     float4 col = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -684,9 +702,20 @@ __device__ __forceinline__ void stage_items(const PaintArgs& a, const PaintProps
         const uint32_t co = (fl & ITEM_CARRY) ? 1u : 0u;
         const uint32_t fr = hdr.x & 1u;
         meta = (hdr.y & 15u) | (fr << 4);
-        if (!(hdr.z & PROPS_SOLID)) {
-            meta |= META_GRAD;
-            col.x = __uint_as_float(hdr.w);
+        if (FULL) {
+            if (hdr.z & PROPS_CLIP) {
+                // `layer + *layers as u16` (mold's u16 arithmetic; 17 bits in the widened format)
+                meta |= META_CLIP;
+                col.x = __uint_as_float((L + hdr.w) & (scene.wide ? 0x1FFFFu : 0xFFFFu));
+            } else if (!(hdr.z & PROPS_SOLID)) {
+                meta |= META_GRAD;
+                col.x = __uint_as_float(hdr.w);
+            }
+            if (scene.features & FEAT_CLIPS) {
+                const uint32_t st = a.item_state[c0 + lane];
+                if (st & ISTATE_MASKED) meta |= META_SKIP;
+                if ((hdr.z & PROPS_DRAW) && (hdr.z & PROPS_CLIPPED) && !(st & ISTATE_SKIP_CLIP)) meta |= META_APPLY_CLIP;
+            }
         }
         if (co) {
             carry = cover_add(carry, a.tl_cover[g]);
@@ -721,6 +750,7 @@ __device__ __forceinline__ void stage_items(const PaintArgs& a, const PaintProps
     S.color[lane] = col;
     S.carry[lane] = carry;
     S.meta[lane] = meta;
+    S.order[lane] = L;
     S.sb[lane] = sb;
     S.cnt[lane] = cnt;
     S.soff[lane] = inc - cnt;
@@ -773,8 +803,8 @@ __device__ __forceinline__ void stage_items(const PaintArgs& a, const PaintProps
     __syncwarp();
 }
 
-// PAINT_WARPS tiles per CTA; GRAD: the frame holds gradient fills
-template <int PAINT_WARPS, bool GRAD>
+// PAINT_WARPS tiles per CTA; FULL: the frame holds gradient fills or clips
+template <int PAINT_WARPS, bool FULL>
 __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
     __shared__ WarpStage stages[PAINT_WARPS];
     const int lane = threadIdx.x & 31;
@@ -811,6 +841,57 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
         }
     }
 
+    // skip_trivial_clips_pass (layer_workbench.rs:224-308): a sequential pass
+    // over the tile's layers in order, run by the whole warp in lockstep (each
+    // lane holds one item of the chunk); lane 0 records each item's state.
+    const bool clips = FULL && (p.features & FEAT_CLIPS);
+    if (clips) {
+        const uint32_t lmask = p.wide ? 0x1FFFFu : 0xFFFFu;
+        bool has = false, c_full = false, c_used = false;
+        uint32_t c_last = 0, c_idx = 0;
+        for (uint32_t c0 = b; c0 < e; c0 += 32) {
+            const uint32_t n = min(32u, e - c0);
+            uint32_t L = 0, fl = 0, g = 0, pf = 0, aux = 0;
+            if ((uint32_t)lane < n) {
+                item_decode(a.items[c0 + lane], a.idx_bits, a.order_bits, L, fl, g);
+                if (L < p.n_orders) {
+                    pf = p.props[L].flags;
+                    aux = p.props[L].aux;
+                }
+            }
+            for (uint32_t q = 0; q < n; q++) {
+                const uint32_t qL = __shfl_sync(0xffffffffu, L, q);
+                const uint32_t qpf = __shfl_sync(0xffffffffu, pf, q);
+                const uint32_t qfl = __shfl_sync(0xffffffffu, fl, q);
+                const uint32_t qaux = __shfl_sync(0xffffffffu, aux, q);
+                uint8_t st = 0;
+                if (qpf & PROPS_CLIP) {
+                    has = true;
+                    c_full = (qfl & ITEM_FULL) != 0;  // layer_is_full: no segments, full carried cover
+                    c_last = (qL + qaux) & lmask;
+                    c_idx = c0 + q;
+                    c_used = false;
+                    if (c_full) st |= ISTATE_MASKED;
+                }
+                if ((qpf & PROPS_DRAW) && (qpf & PROPS_CLIPPED)) {
+                    if (has && qL <= c_last) {
+                        if (c_full) st |= ISTATE_SKIP_CLIP;
+                        else c_used = true;
+                    } else {
+                        st |= ISTATE_MASKED;
+                    }
+                }
+                if (lane == 0) a.item_state[c0 + q] = st;
+                if (has && qL > c_last) {
+                    has = false;
+                    if (!c_used && lane == 0) a.item_state[c_idx] |= ISTATE_MASKED;
+                }
+            }
+        }
+        if (has && !c_used && lane == 0) a.item_state[c_idx] |= ISTATE_MASKED;
+        __syncwarp();
+    }
+
     // skip_fully_covered_layers (layer_workbench.rs:310-388), top-down over
     // the items' precomputed full / opaque bits.
     int64_t k_op = -1;
@@ -822,6 +903,19 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
             const uint32_t fl = (uint32_t)(a.items[idx] >> a.idx_bits) & 7u;
             inc = !(fl & ITEM_FULL);
             op = (fl & ITEM_OPAQUE) != 0;
+            if (clips) {
+                const uint32_t st = a.item_state[idx];
+                uint32_t L, f2, g;
+                item_decode(a.items[idx], a.idx_bits, a.order_bits, L, f2, g);
+                const uint32_t pf = L < p.n_orders ? p.props[L].flags : 0u;
+                const bool clipped = (pf & PROPS_DRAW) && (pf & PROPS_CLIPPED) && !(st & ISTATE_SKIP_CLIP);
+                if (st & ISTATE_MASKED) {
+                    inc = op = false;
+                } else {
+                    inc = inc || clipped;
+                    op = op && !clipped;
+                }
+            }
         }
         const uint32_t bi = __ballot_sync(0xffffffffu, inc), bo = __ballot_sync(0xffffffffu, op);
         const uint32_t any = bi | bo;
@@ -838,15 +932,16 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
     bool painted = true;
     // the gradient column argument of the lane's first pixel, less one, and the tile's top row
     const float gx0 = (float)(i * 8 + x0), gy0 = (float)(j * 8);
-    if (GRAD && first != 2) {
-        // the fold takes Solid fills only (skip_fully_covered_layers, :376-383)
+    if (FULL && first != 2) {
+        // the fold takes (unmasked) Solid Draw layers only (skip_fully_covered_layers, :376-383)
         const uint32_t from0 = first == 1 ? (uint32_t)k_op + 1 : b;
         for (uint32_t c0 = from0; c0 < e && first != 2; c0 += 32) {
             bool ok = true;
             if (c0 + lane < e) {
                 uint32_t L, fl, g;
                 item_decode(a.items[c0 + lane], a.idx_bits, a.order_bits, L, fl, g);
-                ok = L < p.n_orders && (p.props[L].flags & PROPS_SOLID);
+                const bool masked = clips && (a.item_state[c0 + lane] & ISTATE_MASKED);
+                ok = masked || (L < p.n_orders && (p.props[L].flags & PROPS_SOLID) && (p.props[L].flags & PROPS_DRAW));
             }
             if (!__all_sync(0xffffffffu, ok)) first = 2;
         }
@@ -868,8 +963,9 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
         }
         for (uint32_t c0 = from; c0 < e; c0 += 32) {
             const uint32_t n = min(32u, e - c0);
-            stage_items(a, p.props, p.n_orders, S, c0, n, lane, false);
+            stage_items<FULL>(a, p, S, c0, n, lane, false);
             for (uint32_t q = 0; q < n; q++) {
+                if (FULL && (S.meta[q] & META_SKIP)) continue;
                 const float4 col = S.color[q];
                 const uint32_t mode = S.meta[q] & 15u;
                 const float al = col.w, inv = 1.0f - al;
@@ -889,6 +985,11 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
         float2 C[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) C[q] = splat(p.clear[q]);
+        // Painter's clip state (painter/mod.rs:260-317): a mask per pixel and
+        // the last layer it applies to
+        bool has_clip = false;
+        uint32_t clip_last = 0;
+        float2 clip_mask = splat(0.0f);
         const uint32_t start = k_op >= 0 ? (uint32_t)k_op : b;
         S.area[lane] = 0;
         S.area[lane + 32] = 0;
@@ -896,20 +997,38 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
         S.cov[lane + 32] = 0;
         for (uint32_t c0 = start; c0 < e; c0 += 32) {
             const uint32_t n = min(32u, e - c0);
-            stage_items(a, p.props, p.n_orders, S, c0, n, lane, true);
+            stage_items<FULL>(a, p, S, c0, n, lane, true);
             for (uint32_t q = 0; q < n; q++) {
                 const uint32_t meta = S.meta[q];
                 const uint32_t mode = meta & 15u, fr = (meta >> 4) & 1u;
+                bool apply = false;
+                if (clips) {
+                    if (meta & META_SKIP) continue;  // masked: its cover is carried, nothing is painted
+                    if (has_clip && clip_last < S.order[q]) has_clip = false;
+                    apply = (meta & META_APPLY_CLIP) != 0;
+                    if (apply && !has_clip) continue;  // a clipped layer with no clip in effect
+                }
                 float2 cov;
                 bool col0, col1;
                 if (meta & META_CARRY_ONLY) {
-                    if (!(meta & META_ACTIVE)) continue;
                     cov = splat(reinterpret_cast<const float*>(&S.rowcov[q][0])[y]);
-                    if (GRAD && (meta & META_GRAD)) {
-                        const GradRec g = p.grads[__float_as_uint(S.color[q].x)];
-                        const float4 src[2] = {gradient_color(g, p.stops, gx0 + 1.0f, gy0, (int)y),
-                                               gradient_color(g, p.stops, gx0 + 2.0f, gy0, (int)y)};
-                        blend_dispatch_src(mode, C, src, cov, true, true);
+                    if (clips && (meta & META_CLIP)) {
+                        if (!has_clip) {
+                            has_clip = true;
+                            clip_last = __float_as_uint(S.color[q].x);
+                        }
+                        clip_mask = cov;
+                        continue;
+                    }
+                    if (!(meta & META_ACTIVE)) continue;
+                    if (FULL && ((meta & META_GRAD) || apply)) {
+                        float4 src[2] = {S.color[q], S.color[q]};
+                        if (meta & META_GRAD) {
+                            const GradRec g = p.grads[__float_as_uint(S.color[q].x)];
+                            src[0] = gradient_color(g, p.stops, gx0 + 1.0f, gy0, (int)y);
+                            src[1] = gradient_color(g, p.stops, gx0 + 2.0f, gy0, (int)y);
+                        }
+                        blend_dispatch_src(mode, C, src, cov, true, true, apply, clip_mask);
                     } else {
                         blend_dispatch<false>(mode, C, S.color[q], cov, true, true);
                     }
@@ -945,6 +1064,14 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
                     cov.x = from_area(PIXEL_WIDTH * (int32_t)(int8_t)cv + (int32_t)(int16_t)a0, fr);
                     cov.y = from_area(PIXEL_WIDTH * (int32_t)(int8_t)cv1 + (int32_t)(int16_t)a1, fr);
                     __syncwarp();
+                    if (clips && (meta & META_CLIP)) {  // clip_at: every column, zero or not
+                        if (!has_clip) {
+                            has_clip = true;
+                            clip_last = __float_as_uint(S.color[q].x);
+                        }
+                        clip_mask = cov;
+                        continue;
+                    }
                     // A column is blended when any of its 8 coverages is non-zero
                     // (painter/mod.rs:287-289).
                     const uint32_t b0 = __ballot_sync(0xffffffffu, cov.x != 0.0f);
@@ -953,11 +1080,14 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
                     col0 = ((b0 >> (8 * xg)) & 0xFFu) != 0;
                     col1 = ((b1 >> (8 * xg)) & 0xFFu) != 0;
                 }
-                if (GRAD && (meta & META_GRAD)) {
-                    const GradRec g = p.grads[__float_as_uint(S.color[q].x)];
-                    const float4 src[2] = {gradient_color(g, p.stops, gx0 + 1.0f, gy0, (int)y),
-                                           gradient_color(g, p.stops, gx0 + 2.0f, gy0, (int)y)};
-                    blend_dispatch_src(mode, C, src, cov, col0, col1);
+                if (FULL && ((meta & META_GRAD) || apply)) {
+                    float4 src[2] = {S.color[q], S.color[q]};
+                    if (meta & META_GRAD) {
+                        const GradRec g = p.grads[__float_as_uint(S.color[q].x)];
+                        src[0] = gradient_color(g, p.stops, gx0 + 1.0f, gy0, (int)y);
+                        src[1] = gradient_color(g, p.stops, gx0 + 2.0f, gy0, (int)y);
+                    }
+                    blend_dispatch_src(mode, C, src, cov, col0, col1, apply, clip_mask);
                 } else {
                     blend_dispatch<true>(mode, C, S.color[q], cov, col0, col1);
                 }
@@ -1027,13 +1157,14 @@ cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_til
 }
 
 cudaError_t launch_paint(const BatchGeom& bg, const uint64_t* segs, const uint64_t* items, int idx_bits, uint32_t G,
-                         const uint32_t* tile_start, const CarryBuffers& cb, uint32_t warps, bool grad,
-                         cudaStream_t st) {
+                         const uint32_t* tile_start, const CarryBuffers& cb, uint32_t warps, bool full,
+                         uint8_t* item_state, cudaStream_t st) {
     if (bg.total_tiles == 0) return cudaSuccess;
-    PaintArgs a{bg, segs, items, idx_bits, cb.order_bits, G, tile_start, cb.tl_start, cb.tl_cover, cb.tl_carry};
+    PaintArgs a{bg,        segs,        items,       idx_bits,    cb.order_bits, G,
+                item_state, tile_start, cb.tl_start, cb.tl_cover, cb.tl_carry};
     count_launches(1);
     const uint32_t T = bg.total_tiles;
-    if (grad) {
+    if (full) {
         switch (warps) {
             case 2: k_paint<2, true><<<(T + 1) / 2, 64, 0, st>>>(a); break;
             case 4: k_paint<4, true><<<(T + 3) / 4, 128, 0, st>>>(a); break;
