@@ -66,6 +66,16 @@ class CgbBuffer(ctypes.Structure):
     ]
 
 
+class CgbCassiaStyling(ctypes.Structure):
+    """cassia's CassiaStyling (cassia/src/Cassia.h:25-30)."""
+    _fields_ = [
+        ("fill", ctypes.c_float * 4),
+        ("fill_rule", ctypes.c_uint32),
+        ("blend_mode", ctypes.c_uint32),
+        ("_padding", ctypes.c_uint32 * 2),
+    ]
+
+
 class CgbRect(ctypes.Structure):
     _fields_ = [("x0", ctypes.c_uint64), ("x1", ctypes.c_uint64), ("y0", ctypes.c_uint64), ("y1", ctypes.c_uint64)]
 
@@ -159,6 +169,7 @@ def _declare(lib):
         "cgb_create_buffer_layer_cache": ([handle, P(i32)], i32),
         "cgb_release_buffer_layer_cache": ([handle, i32], i32),
         "cgb_render": ([handle, P(CgbBuffer), fp, P(CgbRect)], i32),
+        "cgb_cassia_render": ([handle, P(u64), sz, P(CgbCassiaStyling), sz, P(CgbBuffer), fp], i32),
         "cgb_render_batch": ([handle, sz, P(vp), P(CgbBuffer), fp, P(CgbRect)], i32),
         "cgb_pixel_segments": ([handle, P(u64), sz, P(u64), P(u64), u32], i32),
         "cgb_get_stats": ([handle, P(CgbStats)], i32),

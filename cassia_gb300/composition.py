@@ -212,6 +212,22 @@ class Composition:
         _check(self._lib, st, "render")
         return pixels
 
+    def cassia_render(self, segments, stylings, pixels, width, background, height=None):
+        """cassia_render, headless: paints externally produced pixel segments
+        (reference CompactSegments, any order, NONE allowed) with
+        stylings[order] = (rgba, fill_rule, blend_mode) into `pixels`."""
+        segs = np.ascontiguousarray(segments, np.uint64)
+        arr = (abi.CgbCassiaStyling * max(len(stylings), 1))()
+        for k, (fill, fr, bm) in enumerate(stylings):
+            arr[k].fill[:] = [float(v) for v in fill]
+            arr[k].fill_rule = int(fr)
+            arr[k].blend_mode = int(bm)
+        b = _buffer(pixels, width, -1, None, height)
+        bg = (ctypes.c_float * 4)(*background)
+        st = self._lib.cgb_cassia_render(self._h, _u64p(segs), len(segs), arr, len(stylings), ctypes.byref(b), bg)
+        _check(self._lib, st, "cassia_render")
+        return pixels
+
     def count_segments(self):
         """Real pixel segments the reference's rasterizer emits for the current
         scene (Composition::pixel_segments without the copy), and its NONE count."""

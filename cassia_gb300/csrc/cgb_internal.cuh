@@ -238,6 +238,12 @@ cudaError_t launch_rasterize(int render, const BatchGeom& bg, const LineRec* rec
                              uint32_t n_lines, uint64_t n_steps, uint32_t block, uint32_t items, uint64_t* runs,
                              uint32_t* run_count, unsigned long long* produced, cudaStream_t st);
 uint32_t raster_run_slots(uint32_t block, uint32_t items);
+// Keys n reference CompactSegments (cassia_render's input) of scene 0 into
+// runs of import_run_slots() slots per block, as launch_rasterize does.
+cudaError_t launch_import_segments(const uint64_t* segs, uint64_t n, const BatchGeom& bg, uint64_t* runs,
+                                   uint32_t* run_count, unsigned long long* produced, cudaStream_t st);
+uint32_t import_grid(uint64_t n);
+uint32_t import_run_slots();
 uint32_t raster_grid(uint64_t n_steps, uint32_t block, uint32_t items);
 cudaError_t launch_compact_lines(const float* in4[4], const uint32_t* lid_in, uint32_t n, const LayerRec* layers,
                                  uint32_t n_layer_recs, float* out4[4], uint32_t* lid_out, uint32_t* flags,

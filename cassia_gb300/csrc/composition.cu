@@ -170,6 +170,10 @@ struct cgb_composition {
     std::vector<uint32_t> order_layer;
     uint32_t n_orders = 1;
     uint32_t features = 0;     // FEAT_* of the enabled layers' props
+    // cassia_render input of the current frame (import mode: no lines, props from stylings)
+    const uint64_t* import_segs = nullptr;
+    uint64_t import_n = 0;
+    DevBuf d_import;
     uint64_t props_version = 1, props_uploaded = 0;
 
     // frame buffers
@@ -616,6 +620,44 @@ cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& 
     return CGB_OK;
 }
 
+// cassia_render's segments (host memory) into packed keys of scene 0, with
+// the sort's digit histogram counted, like build_and_rasterize.
+cgb_status import_segments(cgb_composition* c, const BatchGeom& bg, int sort_lo, int sort_hi, uint64_t* n_segs,
+                           uint64_t* n_total, uint64_t** keys) {
+    cudaStream_t st = c->stream;
+    const uint64_t n = c->import_n;
+    if (n >= (1ull << 32)) return fail(CGB_ERR_LAYER_LIMIT, "cassia_render: more than 2^32 segments");
+    c->stats.lines = 0;
+    c->stats.steps = 0;
+    CK(stage_mark(c, 0, st, "cgb:import"));
+    CK(c->s.ensure(c->d_import, std::max<size_t>(n, 1) * 8));
+    if (n) CK(cudaMemcpyAsync(c->d_import.p, c->import_segs, n * 8, cudaMemcpyHostToDevice, st));
+    CK(stage_mark(c, 1, st, "cgb:import_keys"));
+    const uint32_t grid = import_grid(n), slots = import_run_slots();
+    CK(c->s.ensure(c->segs_a, std::max<size_t>((size_t)grid * slots, 1) * 8));
+    CK(c->s.ensure(c->bcounts, ((size_t)grid + 1) * 4));
+    CK(c->s.ensure(c->boff, ((size_t)grid + 1) * 4));
+    CK(c->s.ensure(c->rlb, 8));
+    CK(cudaMemsetAsync(c->rlb.p, 0, 8, st));
+    unsigned long long* produced = c->rlb.as<unsigned long long>();
+    CK(launch_import_segments(c->d_import.as<uint64_t>(), n, bg, c->segs_a.as<uint64_t>(), c->bcounts.as<uint32_t>(),
+                              produced, st));
+    CK(cudaMemcpyAsync(&c->s.pinned[3], produced, 8, cudaMemcpyDeviceToHost, st));
+    uint64_t P = 0;
+    if (grid) CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid, &c->s, st, &P));
+    else CK(cudaStreamSynchronize(st));
+    if (P >= (1ull << 30) - 1) return fail(CGB_ERR_LAYER_LIMIT, "more than 2^30 pixel segments");
+    CK(c->s.ensure(c->segs_b, std::max<size_t>(P, 1) * 8));
+    CK(radix_gather_hist(c->segs_a.as<uint64_t>(), slots, c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid,
+                         c->segs_b.as<uint64_t>(), sort_lo, sort_hi, (int)c->tuning.radix_bits, &c->s, st));
+    CK(stage_mark(c, 2, st, "cgb:sort"));
+    *n_segs = P;
+    *n_total = n ? c->s.pinned[3] : 0;
+    *keys = c->segs_b.as<uint64_t>();
+    c->stats.segments = *n_total;
+    return CGB_OK;
+}
+
 cgb_status check_device_error(cgb_composition* c) {
     uint32_t v = 0;
     CK(cudaMemcpyAsync(&v, c->err.p, 4, cudaMemcpyDeviceToHost, c->stream));
@@ -659,9 +701,11 @@ cgb_status prepare_scene(cgb_composition* c, SceneInput& in) {
             in.cache->tiles = n_tiles;
         }
     }
-    cgb_status s0 = remove_disabled(c);
-    if (s0) return s0;
-    if (c->props_dirty) rebuild_props(c);
+    if (!c->import_segs) {  // import mode: the props come from the stylings
+        cgb_status s0 = remove_disabled(c);
+        if (s0) return s0;
+        if (c->props_dirty) rebuild_props(c);
+    }
     cgb_status s1 = upload_layers(c);
     if (s1) return s1;
     if (c->props_uploaded != c->props_version) {
@@ -789,7 +833,8 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
 
     uint64_t P = 0, PT = 0;
     uint64_t* keys = nullptr;
-    cgb_status s2 = build_and_rasterize(c, 1, bg, 22, 22 + (int)bg.key_bits, &P, &PT, &keys);
+    cgb_status s2 = c->import_segs ? import_segments(c, bg, 22, 22 + (int)bg.key_bits, &P, &PT, &keys)
+                                   : build_and_rasterize(c, 1, bg, 22, 22 + (int)bg.key_bits, &P, &PT, &keys);
     if (s2) return s2;
     c->stats.painted_segments = P;
     // sort by (global row, order, tile column)
@@ -946,7 +991,7 @@ CGB_EXPORT cgb_status cgb_composition_free(cgb_composition* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     DevBuf* bufs[] = {&c->p0x, &c->p0y, &c->p1x, &c->p1y, &c->lids, &c->d_layers, &c->recs, &c->lengths,
                       &c->step_off, &c->bcounts, &c->boff, &c->segs_a, &c->segs_b,
-                      &c->tl_start, &c->tl_key, &c->blk_cover, &c->blk_head, &c->rlb, &c->item_state, &c->tl_cover, &c->tl_carry, &c->tl_flags, &c->item_count, &c->item_off,
+                      &c->tl_start, &c->tl_key, &c->blk_cover, &c->blk_head, &c->rlb, &c->item_state, &c->d_import, &c->tl_cover, &c->tl_carry, &c->tl_flags, &c->item_count, &c->item_off,
                       &c->items_a, &c->items_b, &c->tile_start, &c->d_props, &c->d_grads, &c->d_stops, &c->d_unchanged, &c->out_rgba, &c->err,
                       &c->dflt_t, &c->f_kinds, &c->f_points, &c->f_cmd_off, &c->f_pt_off, &c->f_t9, &c->f_has_t,
                       &c->f_path_layer, &c->f_counts, &c->f_off, &c->g_flags, &c->g_off, &c->s.scan_sums,
@@ -1222,6 +1267,43 @@ CGB_EXPORT cgb_status cgb_render_batch(cgb_composition* ctx, size_t n, cgb_compo
     }
     if (n == 0) return CGB_OK;
     return render_frame(ctx, scenes);
+}
+
+CGB_EXPORT cgb_status cgb_cassia_render(cgb_composition* c, const uint64_t* segments, size_t n,
+                                        const cgb_cassia_styling* stylings, size_t m, const cgb_buffer* buffer,
+                                        const float background[4]) {
+    HANDLE_CHECK();
+    if ((n && !segments) || (m && !stylings) || !buffer || !background)
+        return fail(CGB_ERR_INVALID_ARG, "cassia_render: null argument");
+    if (m > c->max_ids) return fail(CGB_ERR_LAYER_LIMIT, "cassia_render: more stylings than layer orders");
+    // each styling is Props { fill_rule, Func::Draw(Style { Fill::Solid(fill), blend_mode }) }
+    // (demo/src/cassia.rs:7-13, demo/src/circles.rs:117-131)
+    std::vector<PaintProps> props(std::max<size_t>(m, 1),
+                                  PaintProps{CGB_FILL_NONZERO, CGB_BLEND_OVER, PROPS_SOLID | PROPS_DRAW, 0, {0, 0, 0, 1}});
+    for (size_t o = 0; o < m; o++) {
+        const cgb_cassia_styling& sy = stylings[o];
+        if (sy.fill_rule > 1 || sy.blend_mode > 11) return fail(CGB_ERR_INVALID_ARG, "cassia_render: bad styling");
+        PaintProps& pp = props[o];
+        pp.fill_rule = sy.fill_rule;
+        pp.blend_mode = sy.blend_mode;
+        pp.flags = PROPS_SOLID | PROPS_DRAW | PROPS_PRESENT;
+        if (sy.blend_mode == CGB_BLEND_OVER && sy.fill[3] == 1.0f) pp.flags |= PROPS_OPAQUE_OVER;
+        std::memcpy(pp.color, sy.fill, sizeof(pp.color));
+    }
+    c->props_host.swap(props);
+    c->grads_host.clear();
+    c->stops_host.clear();
+    c->n_orders = (uint32_t)std::max<size_t>(m, 1);
+    c->features = 0;
+    c->props_dirty = false;
+    c->props_version++;
+    c->import_segs = segments;
+    c->import_n = n;
+    cgb_status s = render(c, buffer, background, nullptr);
+    c->import_segs = nullptr;
+    c->import_n = 0;
+    c->props_dirty = true;  // a later render rebuilds the props from the layers
+    return s;
 }
 
 CGB_EXPORT cgb_status cgb_pixel_segments(cgb_composition* c, uint64_t* out, size_t cap, uint64_t* out_len,

@@ -612,6 +612,90 @@ __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ r
     for (uint32_t i = threadIdx.x; i < btotal; i += blockDim.x) dst[i] = s_out[i];
 }
 
+// cassia_render's input (cassia/src/Cassia.h:25-41): reference CompactSegments
+// in any order, NONE slots allowed.  Every thread takes IMPORT_ITEMS
+// consecutive segments, drops NONE slots, segments of orders without a styling
+// and segments outside the canvas, keys the rest as the rasterizer does, and
+// the block stores them as one run (gathered with the sort's histogram).
+constexpr int IMPORT_ITEMS = 8;
+
+__global__ void __launch_bounds__(256) k_import_segments(const uint64_t* __restrict__ in, uint64_t n, BatchGeom bg,
+                                                         uint64_t* __restrict__ runs, uint32_t* __restrict__ run_count,
+                                                         unsigned long long* __restrict__ produced) {
+    extern __shared__ uint64_t s_out[];  // IMPORT_ITEMS * blockDim.x
+    const SceneDesc& sc = bg.scenes[0];
+    const SceneRaster sr{sc.wide, sc.rows, sc.row_len, sc.row_base};
+    const uint64_t s0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * IMPORT_ITEMS;
+    uint64_t keys[IMPORT_ITEMS];
+    int kept = 0, real = 0;
+#pragma unroll
+    for (int k = 0; k < IMPORT_ITEMS; k++) {
+        const uint64_t i = s0 + k;
+        if (i >= n) break;
+        const uint64_t v = in[i];
+        SegFields f;
+        uint32_t layer;
+        if (sc.wide) {  // tile_j:12 tile_i:13 layer:17 (no NONE slots)
+            f.tj = (int32_t)((v >> 52) & 0xFFFu);
+            f.tis = (int32_t)((v >> 39) & 0x1FFFu);
+            layer = (uint32_t)((v >> 22) & 0x1FFFFu);
+        } else {  // is_none:1 tile_j:12 tile_i:13 layer:16
+            if (v >> 63) continue;
+            f.tj = (int32_t)((v >> 51) & 0xFFFu);
+            f.tis = (int32_t)((v >> 38) & 0x1FFFu);
+            layer = (uint32_t)((v >> 22) & 0xFFFFu);
+        }
+        f.low = (uint32_t)(v & 0x3FFFFFu);
+        real++;
+        uint64_t key;
+        if (layer < sc.n_orders && render_key(sr, bg, layer, f, key)) keys[kept++] = key;
+    }
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t warp_tot[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t inc = kept, tinc = real;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t a = __shfl_up_sync(0xffffffffu, inc, o);
+        const uint32_t b = __shfl_up_sync(0xffffffffu, tinc, o);
+        if (lane >= o) {
+            inc += a;
+            tinc += b;
+        }
+    }
+    if (lane == 31) {
+        warp_sums[warp] = inc;
+        warp_tot[warp] = tinc;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t w = lane < nw ? warp_sums[lane] : 0, wt = lane < nw ? warp_tot[lane] : 0;
+        uint32_t wi = w, wti = wt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t a = __shfl_up_sync(0xffffffffu, wi, o);
+            const uint32_t b = __shfl_up_sync(0xffffffffu, wti, o);
+            if (lane >= o) {
+                wi += a;
+                wti += b;
+            }
+        }
+        if (lane < nw) warp_sums[lane] = wi - w;
+        if (lane == 31) {
+            warp_tot[0] = wi;
+            run_count[blockIdx.x] = wi;
+            if (wti) atomicAdd(produced, (unsigned long long)wti);
+        }
+    }
+    __syncthreads();
+    const uint32_t local = warp_sums[warp] + inc - kept;
+    const uint32_t btotal = warp_tot[0];
+    for (int q = 0; q < kept; q++) s_out[local + q] = keys[q];
+    __syncthreads();
+    uint64_t* dst = runs + (uint64_t)blockIdx.x * (IMPORT_ITEMS * blockDim.x);
+    for (uint32_t i = threadIdx.x; i < btotal; i += blockDim.x) dst[i] = s_out[i];
+}
+
 __global__ void k_keep_flags(const uint32_t* __restrict__ lids, uint32_t n, const LayerRec* __restrict__ layers,
                              uint32_t n_layer_recs, uint32_t* __restrict__ flags) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -685,6 +769,20 @@ uint32_t raster_grid(uint64_t n_steps, uint32_t block, uint32_t items) {
     const uint64_t per_block = (uint64_t)block * items;
     return (uint32_t)((n_steps + per_block - 1) / per_block);
 }
+
+cudaError_t launch_import_segments(const uint64_t* segs, uint64_t n, const BatchGeom& bg, uint64_t* runs,
+                                   uint32_t* run_count, unsigned long long* produced, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    const uint32_t block = 256;
+    const uint32_t grid = import_grid(n);
+    count_launches(1);
+    k_import_segments<<<grid, block, (size_t)IMPORT_ITEMS * block * sizeof(uint64_t), st>>>(segs, n, bg, runs,
+                                                                                         run_count, produced);
+    return cudaGetLastError();
+}
+
+uint32_t import_grid(uint64_t n) { return (uint32_t)((n + 256 * IMPORT_ITEMS - 1) / (256 * IMPORT_ITEMS)); }
+uint32_t import_run_slots() { return 256 * IMPORT_ITEMS; }
 
 cudaError_t launch_compact_lines(const float* in4[4], const uint32_t* lid_in, uint32_t n, const LayerRec* layers,
                                  uint32_t n_layer_recs, float* out4[4], uint32_t* lid_out, uint32_t* flags,

@@ -306,6 +306,26 @@ CGB_EXPORT uint64_t cgb_kernel_launches(void);
 CGB_EXPORT cgb_status cgb_sort_keys_noalloc(uint64_t* keys, uint64_t* out, size_t n, uint32_t bit_lo,
                                             uint32_t bit_hi, void* stream);
 
+/* cassia's styling record (cassia/src/Cassia.h:25-30): a Solid fill, the
+ * fill rule and the blend mode of one layer order. */
+typedef struct cgb_cassia_styling {
+    float fill[4];
+    uint32_t fill_rule;
+    uint32_t blend_mode;
+    uint32_t _padding[2];
+} cgb_cassia_styling;
+
+/* cassia_render (cassia/src/Cassia.h:34-39), headless: paints pixel segments
+ * produced elsewhere (reference CompactSegments as pixel_segments returns
+ * them, in any order, NONE slots allowed; the widened format when the handle
+ * was created with CGB_COMPOSITION_WIDE_LAYERS) with stylings[order] as
+ * Props { fill_rule, Draw(Style { Solid(fill), blend_mode }) } into `buffer`
+ * over `background`.  Segments of orders >= m are dropped.  The handle's own
+ * layers are not used.  Both arrays are read during the call. */
+CGB_EXPORT cgb_status cgb_cassia_render(cgb_composition* c, const uint64_t* segments, size_t n,
+                                        const cgb_cassia_styling* stylings, size_t m, const cgb_buffer* buffer,
+                                        const float background[4]);
+
 /* Diagnostic: exercises the bounded device-side wait of the sort's decoupled
  * look-back.  One sort CTA waits on a predecessor tile that never publishes;
  * after its iteration limit (well under a second) it records the expiry in an
