@@ -55,6 +55,10 @@ class CgbProps(ctypes.Structure):
     ]
 
 
+# cgb_flush_fn: (user, pixels, n_pixels)
+FLUSH_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t)
+
+
 class CgbBuffer(ctypes.Structure):
     _fields_ = [
         ("pixels", ctypes.c_void_p),
@@ -63,6 +67,8 @@ class CgbBuffer(ctypes.Structure):
         ("width_stride", ctypes.c_uint64),
         ("layer_cache", ctypes.c_int32),
         ("memory", ctypes.c_uint32),
+        ("flusher", FLUSH_FN),
+        ("flusher_user", ctypes.c_void_p),
     ]
 
 

@@ -200,10 +200,19 @@ class Composition:
         _check(self._lib, self._lib.cgb_release_buffer_layer_cache(self._h, cache_id), "release_cache")
 
     # ---- frames -----------------------------------------------------------------
-    def render(self, pixels, width, background, crop=None, layer_cache=-1, width_stride=None, height=None):
+    def render(self, pixels, width, background, crop=None, layer_cache=-1, width_stride=None, height=None,
+               flusher=None):
         """Composition::render.  `pixels` is a host uint8 numpy array of shape
-        (height, width_stride, 4), or a device pointer (int) with `height` given."""
+        (height, width_stride, 4), or a device pointer (int) with `height` given.
+        `flusher(view)` (host buffers) is called with an (n, 4) uint8 view of
+        each row slice of every tile written, as mold's Buffer::flusher."""
         b = _buffer(pixels, width, layer_cache, width_stride, height)
+        cb = None
+        if flusher is not None:
+            def _flush(user, ptr, n):
+                flusher(np.ctypeslib.as_array(ptr, shape=(n * 4,)).reshape(n, 4))
+            cb = abi.FLUSH_FN(_flush)
+            b.flusher = cb
         bg = (ctypes.c_float * 4)(*background)
         cr = None
         if crop is not None:

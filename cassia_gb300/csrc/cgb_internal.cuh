@@ -100,6 +100,7 @@ struct SceneDesc {
     uint32_t crop_h0, crop_h1, crop_v0, crop_v1;  // in tiles
     uint32_t features;                            // FEAT_*
     float clear[4];
+    uint8_t* written;                             // by tile: the painter wrote it (flushers), or null
 };
 
 // Frame-wide geometry of the render-mode segment key, bit fields from high

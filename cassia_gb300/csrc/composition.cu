@@ -179,7 +179,7 @@ struct cgb_composition {
     // frame buffers
     DevBuf recs, lengths, step_off, bcounts, boff, segs_a, segs_b;
     DevBuf tl_start, tl_key, tl_cover, tl_carry, tl_flags, item_count, item_off, items_a, items_b, tile_start;
-    DevBuf blk_cover, blk_head, rlb, item_state;
+    DevBuf blk_cover, blk_head, rlb, item_state, written;
     DevBuf d_props, d_grads, d_stops, d_unchanged, out_rgba, err, dflt_t, d_scenes, d_row_scene;
     // flatten staging
     DevBuf f_kinds, f_points, f_cmd_off, f_pt_off, f_t9, f_has_t, f_path_layer, f_counts, f_off;
@@ -685,6 +685,8 @@ cgb_status prepare_scene(cgb_composition* c, SceneInput& in) {
     const cgb_buffer* buf = in.buf;
     if (!buf || !in.bg || !buf->pixels || buf->width == 0 || buf->height == 0)
         return fail(CGB_ERR_INVALID_ARG, "render: empty buffer");
+    if (buf->flusher && buf->memory != CGB_MEMORY_HOST)
+        return fail(CGB_ERR_INVALID_ARG, "render: a flusher needs a host buffer");
     const uint64_t stride = buf->width_stride ? buf->width_stride : buf->width;
     if (stride < buf->width || buf->width > (1u << 20) || buf->height > (1u << 20))
         return fail(CGB_ERR_INVALID_ARG, "render: bad width/stride/height");
@@ -908,6 +910,19 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
         CK(c->s.ensure(c->item_state, std::max<uint64_t>(W, 1)));
         item_state = c->item_state.as<uint8_t>();
     }
+    bool flush = false;
+    for (const SceneInput& in : scenes) flush |= in.buf->flusher != nullptr;
+    if (flush) {  // per-tile written flags for the flushers
+        CK(c->s.ensure(c->written, std::max<uint64_t>(tiles, 1)));
+        CK(cudaMemsetAsync(c->written.p, 0, tiles, st));
+        std::vector<SceneDesc> descs2;
+        for (SceneInput& in : scenes) {
+            if (in.buf->flusher) in.d.written = c->written.as<uint8_t>() + in.d.tile_base;
+            descs2.push_back(in.d);
+        }
+        CK(cudaMemcpyAsync(c->d_scenes.p, descs2.data(), descs2.size() * sizeof(SceneDesc), cudaMemcpyHostToDevice,
+                           st));
+    }
     CK(launch_paint(bg, sorted, items_sorted, idx_bits, (uint32_t)G, cb.tile_start, cb, c->tuning.paint_warps,
                     features != 0, item_state, st));
     CK(stage_mark(c, 5, st, nullptr));
@@ -915,6 +930,11 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
         if (in.buf->memory == CGB_MEMORY_HOST)
             CK(cudaMemcpy2DAsync(in.buf->pixels, (size_t)in.d.stride * 4, in.d.out, (size_t)in.d.stride * 4,
                                  (size_t)in.d.width * 4, in.d.height, cudaMemcpyDeviceToHost, st));
+    std::vector<uint8_t> written;
+    if (flush) {
+        written.resize(tiles);
+        CK(cudaMemcpyAsync(written.data(), c->written.p, tiles, cudaMemcpyDeviceToHost, st));
+    }
     cgb_status s3 = check_device_error(c);
     if (s3) return s3;
     c->stats.build_ms = elapsed(c->ev[0], c->ev[1]);
@@ -923,6 +943,19 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
     c->stats.carry_ms = elapsed(c->ev[3], c->ev[4]);
     c->stats.paint_ms = elapsed(c->ev[4], c->ev[5]);
     c->stats.total_ms = elapsed(c->ev[0], c->ev[5]);
+    // Painter::write_to_tile's flush (painter/mod.rs:483-492): each written
+    // tile's row slices, cut to the tile width
+    for (const SceneInput& in : scenes) {
+        if (!in.buf->flusher) continue;
+        const SceneDesc& d = in.d;
+        for (uint32_t j = 0; j < d.rows; j++)
+            for (uint32_t i = 0; i < d.row_len; i++) {
+                if (!written[d.tile_base + (uint64_t)j * d.row_len + i]) continue;
+                const uint32_t x = i * 8, w = std::min<uint32_t>(8, d.width - x);
+                for (uint32_t y = j * 8; y < std::min<uint32_t>(j * 8 + 8, d.height); y++)
+                    in.buf->flusher(in.buf->flusher_user, in.buf->pixels + ((size_t)y * d.stride + x) * 4, w);
+            }
+    }
     for (SceneInput& in : scenes)
         if (in.cache)  // composition.rs:322-327
             for (HostLayer& l : in.comp->layers) {
@@ -991,7 +1024,7 @@ CGB_EXPORT cgb_status cgb_composition_free(cgb_composition* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     DevBuf* bufs[] = {&c->p0x, &c->p0y, &c->p1x, &c->p1y, &c->lids, &c->d_layers, &c->recs, &c->lengths,
                       &c->step_off, &c->bcounts, &c->boff, &c->segs_a, &c->segs_b,
-                      &c->tl_start, &c->tl_key, &c->blk_cover, &c->blk_head, &c->rlb, &c->item_state, &c->d_import, &c->tl_cover, &c->tl_carry, &c->tl_flags, &c->item_count, &c->item_off,
+                      &c->tl_start, &c->tl_key, &c->blk_cover, &c->blk_head, &c->rlb, &c->item_state, &c->d_import, &c->written, &c->tl_cover, &c->tl_carry, &c->tl_flags, &c->item_count, &c->item_off,
                       &c->items_a, &c->items_b, &c->tile_start, &c->d_props, &c->d_grads, &c->d_stops, &c->d_unchanged, &c->out_rgba, &c->err,
                       &c->dflt_t, &c->f_kinds, &c->f_points, &c->f_cmd_off, &c->f_pt_off, &c->f_t9, &c->f_has_t,
                       &c->f_path_layer, &c->f_counts, &c->f_off, &c->g_flags, &c->g_off, &c->s.scan_sums,

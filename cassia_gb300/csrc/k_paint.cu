@@ -1098,6 +1098,7 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
         px1 = pixel_bytes(C[0].y, C[1].y, C[2].y, C[3].y);
     }
 
+    if (p.written && lane == 0) p.written[lt] = 1;
     // RGBA8 store: a full tile goes out as 16 x 16-byte half rows.
     const uint32_t gx = i * 8 + x0, gy = j * 8 + y;
     const bool full_tile = (i * 8 + 8 <= p.width) && (j * 8 + 8 <= p.height) && ((p.stride & 3) == 0) &&

@@ -136,6 +136,10 @@ typedef struct cgb_props {
  * `width_stride` RGBA8 pixels of which the first `width` are painted. */
 #define CGB_MEMORY_HOST 0u
 #define CGB_MEMORY_DEVICE 1u
+/* surpass Flusher::flush (surpass/src/painter/buffer_layout.rs:52-54): called
+ * with each row slice (at most 8 pixels) of every tile the render wrote. */
+typedef void (*cgb_flush_fn)(void* user, uint8_t* pixels, size_t n_pixels);
+
 typedef struct cgb_buffer {
     uint8_t* pixels;
     uint64_t width;
@@ -143,6 +147,12 @@ typedef struct cgb_buffer {
     uint64_t width_stride; /* 0 means width */
     int32_t layer_cache;   /* BufferLayerCache id, or -1 */
     uint32_t memory;       /* CGB_MEMORY_HOST | CGB_MEMORY_DEVICE */
+    /* mold Buffer::flusher (mold/src/buffer.rs:19-25), host buffers only:
+     * after the frame, called on the host for the row slices of every tile
+     * written (not for tiles left unchanged by a layer cache or outside the
+     * crop), tile by tile in row-major order.  NULL for none. */
+    cgb_flush_fn flusher;
+    void* flusher_user;
 } cgb_buffer;
 
 /* surpass painter Rect (surpass/src/painter/buffer_layout.rs:37-50), in
