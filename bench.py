@@ -51,6 +51,26 @@ def make_scene(name):
     return scenes.glyphs(seed=w["seed"], n_layers=w["n_layers"], width=w["width"], height=w["height"])
 
 
+def over_ranks(x, op="max"):
+    """x reduced over the replicas of a multi-process run ("max" for times,
+    "sum" for counts); x itself without a process group.  NCCL groups reduce
+    on the current CUDA device, gloo groups on the host."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return x
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier():
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
 def load_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -263,11 +283,12 @@ def run_batch(args, rank, world, local):
 
     def timed(fn, reps):
         torch.cuda.synchronize()
+        barrier()
         t = time.perf_counter()
         for _ in range(reps):
             fn()
         torch.cuda.synchronize()
-        return (time.perf_counter() - t) / reps
+        return over_ranks((time.perf_counter() - t) / reps)
 
     # the autotuner picks the digit width, rasterizer block and painter block
     # for the batched pipeline; the same setting is applied to every
@@ -340,6 +361,9 @@ def run_serve(args, rank, world, local):
             done = srv.run(reqs)
         torch.cuda.synchronize()
         s = serving.latency_summary(done, w["duration"])
+        # whole-job rate: the frames of every replica over the slowest replica's span
+        span = over_ranks(s["requests"] / s["frames_per_s"])
+        s["frames_per_s_all_ranks"] = over_ranks(s["requests"], "sum") / span
         s["gpu_launches"] = kernel_launches() - l0
         s["clocks"] = clk.summary()
         if mode == "batched":
@@ -357,13 +381,13 @@ def run_serve(args, rank, world, local):
     if rank == 0:
         b, p = out["batched"], out["plain"]
         line = {
-            "metric": "frames/s", "value": world * b["frames_per_s"], "unit": "frames/s", "n_gpus": world,
+            "metric": "frames/s", "value": b["frames_per_s_all_ranks"], "unit": "frames/s", "n_gpus": world,
             "steps": b["requests"], "warmup": 0, "ms_per_step": 1e3 / b["frames_per_s"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+int (fixed point)", "data": "synthetic (seeded)",
             "config": {"workload": args.workload, "clients": w["n_clients"], "offered_rate": w["rate"],
                        "duration_s": w["duration"], "hbm_budget_gb": 40, "max_batch": 16, "workers": 2},
             "p50_ms": b["p50_ms"], "p99_ms": b["p99_ms"], "batched": b, "plain": p,
-            "speedup_vs_plain": b["frames_per_s"] / p["frames_per_s"],
+            "speedup_vs_plain": b["frames_per_s_all_ranks"] / p["frames_per_s_all_ranks"],
             "gpu_launches": b["gpu_launches"], "clocks": b["clocks"],
         }
         print(json.dumps(line))
@@ -374,7 +398,7 @@ def run_reference(args, rank, world):
     if rank != 0:
         return 0
     scene = make_scene(args.workload)
-    r = cpu_reference(scene, args.steps, args.warmup)
+    r = cpu_reference(scene, args.steps, args.warmup, budget_s=args.cpu_budget)
     line = {
         "metric": "Msegments/s", "value": r["value"], "unit": "Msegments/s", "impl": "reference",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
@@ -399,6 +423,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quiet", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=150.0,
+                    help="seconds of host work the reference arm's samples are sized to")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
@@ -409,7 +435,8 @@ def main():
     dist = None
     if world > 1:
         import torch.distributed as dist
-        torch.cuda.set_device(local)
+        if args.impl == "ours":
+            torch.cuda.set_device(local)
         dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
     if args.impl == "reference":
         rc = run_reference(args, rank, world)
@@ -466,10 +493,7 @@ def main():
         dist.barrier()
     ms_total = ev0.elapsed_time(ev1)
     ms_step = ms_total / args.steps
-    if dist:
-        t = torch.tensor([ms_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
+    ms_step = over_ranks(ms_step)
     st = stats[-1]
     segs = ref_segments
     value = world * segs / (ms_step / 1e3) / 1e6
@@ -506,10 +530,7 @@ def main():
             comp.render(host_img, W, scene.background)
         torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-        if dist:
-            t = torch.tensor([e2e_s], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s = over_ranks(e2e_s)
         h2d = scene.n_layers * (6 * 4)
         e2e = {"value": world * segs / e2e_s / 1e6, "unit": "Msegments/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": W * H * 4, "ms_per_step": e2e_s * 1e3}
