@@ -423,6 +423,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quiet", action="store_true")
+    ap.add_argument("--frame-mode", default="staged", choices=["staged", "graph"],
+                    help="graph: frames replayed from a captured CUDA graph (cgb_set_graph_mode)")
     ap.add_argument("--cpu-budget", type=float, default=150.0,
                     help="seconds of host work the reference arm's samples are sized to")
     args = ap.parse_args()
@@ -466,6 +468,8 @@ def main():
     # whose segments cannot reach the canvas.  The metric counts the
     # reference's segments, counted once here.
     ref_segments, _ = comp.count_segments()
+    if args.frame_mode == "graph":
+        comp.set_graph_mode(True)
     out = torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda")
     stream = torch.cuda.ExternalStream(comp.stream())
 
@@ -558,6 +562,7 @@ def main():
                            st["lines"] * 20 // 2**20, segs * 8 // 2**20),
                        "parallelism": f"replicas x{world}"},
             "frames_per_s": world * 1e3 / ms_step,
+            "frame_mode": args.frame_mode, "graph_replayed": int(st.get("graph_replayed", 0)),
             "stage_ms": stage_ms,
             "roofline": {"bound": "hbm", "kernel": STAGE_KERNELS[dom], "stage": dom, "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,

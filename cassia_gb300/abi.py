@@ -102,6 +102,8 @@ class CgbStats(ctypes.Structure):
         ("carry_ms", ctypes.c_float),
         ("paint_ms", ctypes.c_float),
         ("total_ms", ctypes.c_float),
+        ("graph_replayed", ctypes.c_uint32),
+        ("graphs_cached", ctypes.c_uint32),
     ]
 
     def as_dict(self):
@@ -180,6 +182,7 @@ def _declare(lib):
         "cgb_pixel_segments": ([handle, P(u64), sz, P(u64), P(u64), u32], i32),
         "cgb_get_stats": ([handle, P(CgbStats)], i32),
         "cgb_set_tuning": ([handle, P(CgbTuning)], i32),
+        "cgb_set_graph_mode": ([handle, ctypes.c_int, ctypes.c_float], i32),
         "cgb_get_tuning": ([handle, P(CgbTuning)], i32),
         "cgb_synchronize": ([handle], i32),
         "cgb_get_stream": ([handle, P(vp)], i32),

@@ -272,6 +272,13 @@ class Composition:
         t = abi.CgbTuning(**kw)
         _check(self._lib, self._lib.cgb_set_tuning(self._h, ctypes.byref(t)), "set_tuning")
 
+    def set_graph_mode(self, enabled: bool = True, headroom: float = 0.125):
+        """Replays frames whose geometry repeats from a captured CUDA graph
+        (cgb_set_graph_mode); buffers get `headroom` above the counts of the
+        frame a graph was captured after.  Pixels are identical either way."""
+        _check(self._lib, self._lib.cgb_set_graph_mode(self._h, 1 if enabled else 0, float(headroom)),
+               "set_graph_mode")
+
     def stream(self) -> int:
         """The cudaStream_t (as an int) the handle launches on."""
         out = ctypes.c_void_p()

@@ -206,6 +206,30 @@ struct DevBuf {
 };
 
 // Device scratch shared by the stages of one composition handle.
+// Counts of a frame kept on the device (graph frames).  The scans write S
+// (pixel steps), P (painted segments), G (tile-layer groups) and W (work
+// items) here instead of returning them to the host, and every kernel that
+// consumes one reads it, clamped to the capacity its buffers were sized for;
+// a count above its capacity sets its bit in `overflow` (the painter then
+// paints nothing and the host renders the frame again with larger buffers).
+enum { FC_STEPS = 0, FC_SEGS = 1, FC_TLS = 2, FC_ITEMS = 3 };
+struct FrameCounts {
+    uint32_t n[4];
+    uint32_t overflow;
+    uint32_t pad[3];
+    unsigned long long produced;  // segments the rasterizer produced, kept or not
+};
+
+// The count `k` of a frame: `cap` itself without device counts (the host's
+// exact count), else the device count clamped to `cap`.
+__device__ __forceinline__ uint32_t fc_count(FrameCounts* fc, int k, uint32_t cap, bool report) {
+    if (!fc) return cap;
+    const uint32_t v = fc->n[k];
+    if (v <= cap) return v;
+    if (report) atomicOr(&fc->overflow, 1u << k);
+    return cap;
+}
+
 struct Scratch {
     size_t budget = 0;  // 0 = unlimited
     size_t used = 0;    // bytes held by all DevBufs of the handle
@@ -235,9 +259,11 @@ cudaError_t launch_build_lines(const BatchGeom& bg, int cull, LineRec* recs, uin
 // block b stores its kept segments at runs[b * raster_run_slots(block, items)...]
 // and their count at run_count[b]; *produced (zeroed by the caller)
 // accumulates all segments, kept or not.
+// With fc, n_steps is the capacity and the step count is fc->n[FC_STEPS].
 cudaError_t launch_rasterize(int render, const BatchGeom& bg, const LineRec* recs, const uint32_t* step_off,
                              uint32_t n_lines, uint64_t n_steps, uint32_t block, uint32_t items, uint64_t* runs,
-                             uint32_t* run_count, unsigned long long* produced, cudaStream_t st);
+                             uint32_t* run_count, unsigned long long* produced, cudaStream_t st,
+                             FrameCounts* fc = nullptr);
 uint32_t raster_run_slots(uint32_t block, uint32_t items);
 // Keys n reference CompactSegments (cassia_render's input) of scene 0 into
 // runs of import_run_slots() slots per block, as launch_rasterize does.
@@ -252,25 +278,33 @@ cudaError_t launch_compact_lines(const float* in4[4], const uint32_t* lid_in, ui
 
 // k_sort.cu
 // Exclusive scan of n u32 values; out has n+1 entries (out[n] = total mod 2^32).
-// *total_host receives the exact 64-bit total (synchronizes).
+// *total_host receives the exact 64-bit total (synchronizes); *tail_dev, if
+// given, receives the total on the device as well (no synchronization).
 cudaError_t scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, Scratch* s, cudaStream_t st,
-                     uint64_t* total_host);
+                     uint64_t* total_host, uint32_t* tail_dev = nullptr);
+// Sizes the scan and sort scratch of `s` for scans of up to scan_n values and
+// sorts of up to sort_n keys (before a frame graph is captured: nothing may
+// allocate while a stream captures).
+cudaError_t reserve_frame_scratch(Scratch* s, uint32_t scan_n, uint32_t sort_n);
 // Sort n u64 keys by bits [bit_lo, bit_hi).  `keys` and `tmp` hold n keys;
 // on return *result points at the sorted array (keys or tmp).  With
 // hist_ready the digit counts of every pass are already in s->sort_hist
 // (from radix_gather_hist).
+// With fc, n is the capacity of keys and tmp and the key count is fc->n[fc_which].
 cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo, int bit_hi, int digit_bits,
                            Scratch* s, uint32_t* err_flag, cudaStream_t st, uint64_t** result, int* passes,
-                           bool hist_ready = false);
+                           bool hist_ready = false, FrameCounts* fc = nullptr, int fc_which = 0);
 // Runs one onesweep CTA whose predecessor tile never publishes; *flag_host
 // receives the kernel's error flag (1 = the bounded wait gave up).
 cudaError_t selftest_bounded_wait(cudaStream_t st, uint32_t* flag_host);
 // Packs runs of keys (run r: run_count[r] keys at runs[r * run_slots...],
 // placed at run_off[r] of out) and counts the digits of every pass of the sort
 // by bits [bit_lo, bit_hi) into s->sort_hist, for radix_sort_u64(hist_ready).
+// Keys placed at or beyond out_cap are dropped (a graph frame whose segment
+// count passed its capacity; the sort reports the overflow).
 cudaError_t radix_gather_hist(const uint64_t* runs, uint32_t run_slots, const uint32_t* run_count,
                               const uint32_t* run_off, uint32_t n_runs, uint64_t* out, int bit_lo, int bit_hi,
-                              int digit_bits, Scratch* s, cudaStream_t st);
+                              int digit_bits, Scratch* s, cudaStream_t st, uint32_t out_cap = 0xFFFFFFFFu);
 
 // k_paint.cu
 struct CarryBuffers {
@@ -287,15 +321,22 @@ struct CarryBuffers {
     uint64_t* blk_cover;  // [tl_scan_grid] per block: cover sum before its first TL head
     uint32_t* blk_head;   // [tl_scan_grid] per block: holds a TL head
     int order_bits;       // width of the order field of an item
+    // graph frames: the device counts, and the TL and item capacities (TL
+    // and item writes at or beyond them are dropped); without fc, the exact
+    // G and W bound every write
+    FrameCounts* fc;
+    uint32_t tl_cap, items_cap;
 };
+// n: the segment count (with cb.fc, the capacity of the segment arrays).
 cudaError_t launch_tl_scan(int mode, const uint64_t* segs, uint32_t n, uint32_t col_bits, uint32_t* block_counts,
                            const uint32_t* block_off, const CarryBuffers& cb, cudaStream_t st);
 uint32_t tl_scan_grid(uint32_t n);
-cudaError_t launch_tl_carry(uint32_t G, const CarryBuffers& cb, cudaStream_t st);
+// Also sets tl_start[G] = P.  G, P: the counts (with cb.fc, the capacities).
+cudaError_t launch_tl_carry(uint32_t G, uint32_t P, const CarryBuffers& cb, cudaStream_t st);
 cudaError_t launch_items(int mode, uint32_t G, const BatchGeom& bg, const CarryBuffers& cb, int idx_bits,
                          cudaStream_t st);
 cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_tiles, int tile_shift,
-                               uint32_t* tile_start, cudaStream_t st);
+                               uint32_t* tile_start, cudaStream_t st, FrameCounts* fc = nullptr);
 // full: some scene of the frame has gradient fills or clips (selects the
 // painter variant that handles them); item_state: one byte per work item
 // (clip pass results), needed when a scene has clips.

@@ -135,6 +135,22 @@ struct PinnedAllocator {
 
 }  // namespace
 
+// Capacities of a frame graph's buffers: the counts of the frame it was
+// captured after, plus headroom.
+struct FrameCaps {
+    uint32_t steps = 0, segs = 0, tls = 0, items = 0;
+};
+
+// A captured frame: replayed while the frame geometry (its signature) and
+// every buffer it uses (pointer and size) stay the same.
+struct FrameGraph {
+    cudaGraphExec_t exec = nullptr;
+    FrameCaps caps;
+    std::vector<std::pair<const void*, size_t>> bufs;
+    uint64_t launches = 0;
+    uint32_t sort_passes = 0, item_sort_passes = 0;
+};
+
 struct cgb_composition {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -192,6 +208,15 @@ struct cgb_composition {
     cudaEvent_t ev[8] = {};
     nvtxRangeId_t nvtx_range = 0;  // the open stage range (visible in Nsight tools)
     bool nvtx_open = false;
+
+    // frame graphs (cgb_set_graph_mode), by frame signature
+    bool graph_mode = false;
+    float graph_headroom = 0.125f;
+    std::map<std::string, FrameGraph> graphs;
+    DevBuf d_counts;                // FrameCounts of the frame in flight
+    FrameCounts* h_counts = nullptr;  // pinned readback of d_counts
+    bool last_replayed = false;
+    bool capturing = false;         // the stream is capturing a frame graph
 
     cgb_status cuda_fail(cudaError_t e, const char* where) {
         if (e == cudaErrorMemoryAllocation && s.over_budget) {
@@ -564,6 +589,8 @@ struct SceneInput {
 // Stage boundary: records CUDA event k on the stream (the stage times of
 // cgb_stats) and closes the open NVTX range, opening `next` if given.
 cudaError_t stage_mark(cgb_composition* c, int k, cudaStream_t st, const char* next) {
+    // in a frame graph the event is a node of the graph, recorded at each replay
+    if (c->capturing) return cudaEventRecordWithFlags(c->ev[k], st, cudaEventRecordExternal);
     if (c->nvtx_open) nvtxRangeEnd(c->nvtx_range);
     c->nvtx_open = next != nullptr;
     if (next) c->nvtx_range = nvtxRangeStartA(next);
@@ -775,64 +802,21 @@ cgb_status prepare_scene(cgb_composition* c, SceneInput& in) {
     return CGB_OK;
 }
 
-// Renders every scene of `scenes` in one pipeline on `c`'s stream and
-// buffers: build, rasterize, sort, carries / items, paint.
-cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
-    cudaStream_t st = c->stream;
-    for (SceneInput& in : scenes) {
-        cgb_status s0 = prepare_scene(in.comp, in);
-        if (s0) return s0;
-    }
-    // frame geometry: global rows / tiles, key factors, host-output staging
-    uint64_t lines = 0, rows = 0, tiles = 0, staging = 0;
-    uint32_t n_orders = 1, row_len = 1;
-    for (SceneInput& in : scenes) {
-        in.d.line_base = lines;
-        in.d.row_base = (uint32_t)rows;
-        in.d.tile_base = (uint32_t)tiles;
-        lines += in.d.n_lines;
-        rows += in.d.rows;
-        tiles += (uint64_t)in.d.rows * in.d.row_len;
-        n_orders = std::max(n_orders, in.d.n_orders);
-        row_len = std::max(row_len, in.d.row_len);
-        in.staging_off = staging;
-        if (in.buf->memory == CGB_MEMORY_HOST) staging += ((size_t)in.d.height * in.d.stride * 4 + 255) & ~(size_t)255;
-    }
-    if (tiles >= (1ull << 31)) return fail(CGB_ERR_LAYER_LIMIT, "render: too many tiles in a frame");
+// Frame geometry shared by the staged and the graph form of a frame.
+struct FrameSetup {
     BatchGeom bg{};
-    bg.n_scenes = (uint32_t)scenes.size();
-    bg.total_rows = (uint32_t)rows;
-    bg.total_tiles = (uint32_t)tiles;
-    bg.n_orders = n_orders;
-    bg.row_len = row_len;
-    bg.total_lines = lines;
-    bg.order_bits = bits_for(std::max<uint32_t>(n_orders, 1) - 1);
-    bg.col_bits = bits_for(row_len);
-    bg.key_bits = bits_for(std::max<uint64_t>(rows, 1) - 1) + bg.order_bits + bg.col_bits;
-    if (bg.key_bits > 42) return fail(CGB_ERR_LAYER_LIMIT, "render: rows x orders x tiles too large for the segment key");
-    if (staging) CK(c->s.ensure(c->out_rgba, staging));
-    std::vector<SceneDesc> descs;
-    std::vector<uint32_t> row_scene(std::max<uint64_t>(rows, 1), 0);
-    for (size_t k = 0; k < scenes.size(); k++) {
-        SceneInput& in = scenes[k];
-        if (in.buf->memory == CGB_MEMORY_HOST) {
-            in.d.out = c->out_rgba.as<uint8_t>() + in.staging_off;
-            if (in.cache || in.crop)  // tiles that are not repainted keep the caller's pixels
-                CK(cudaMemcpy2DAsync(in.d.out, (size_t)in.d.stride * 4, in.buf->pixels, (size_t)in.d.stride * 4,
-                                     (size_t)in.d.width * 4, in.d.height, cudaMemcpyHostToDevice, st));
-        } else {
-            in.d.out = in.buf->pixels;
-        }
-        for (uint32_t r = 0; r < in.d.rows; r++) row_scene[in.d.row_base + r] = (uint32_t)k;
-        descs.push_back(in.d);
-    }
-    CK(c->s.ensure(c->d_scenes, descs.size() * sizeof(SceneDesc)));
-    CK(c->s.ensure(c->d_row_scene, row_scene.size() * 4));
-    CK(cudaMemcpyAsync(c->d_scenes.p, descs.data(), descs.size() * sizeof(SceneDesc), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(c->d_row_scene.p, row_scene.data(), row_scene.size() * 4, cudaMemcpyHostToDevice, st));
-    bg.scenes = c->d_scenes.as<SceneDesc>();
-    bg.row_scene = c->d_row_scene.as<uint32_t>();
+    uint64_t tiles = 0;
+    uint32_t features = 0;
+    bool flush = false;
+};
 
+// Build -> rasterize -> sort -> carries / items -> paint, stage by stage:
+// the host reads S, P, G and W as they are produced and sizes each buffer
+// to them.
+cgb_status staged_frame(cgb_composition* c, const FrameSetup& f) {
+    cudaStream_t st = c->stream;
+    const BatchGeom& bg = f.bg;
+    const uint64_t tiles = f.tiles;
     uint64_t P = 0, PT = 0;
     uint64_t* keys = nullptr;
     cgb_status s2 = c->import_segs ? import_segments(c, bg, 22, 22 + (int)bg.key_bits, &P, &PT, &keys)
@@ -876,9 +860,7 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
     cb.item_off = c->item_off.as<uint32_t>();
     cb.order_bits = (int)bg.order_bits;
     CK(launch_tl_scan(1, sorted, (uint32_t)P, bg.col_bits, nullptr, c->boff.as<uint32_t>(), cb, st));
-    c->s.pinned[1] = P;  // tl_start[G] = P
-    CK(cudaMemcpyAsync(cb.tl_start + G, &c->s.pinned[1], 4, cudaMemcpyHostToDevice, st));
-    CK(launch_tl_carry((uint32_t)G, cb, st));
+    CK(launch_tl_carry((uint32_t)G, (uint32_t)P, cb, st));
     CK(launch_items(0, (uint32_t)G, bg, cb, 0, st));
     uint64_t W = 0;
     if (G) CK(scan_u32(cb.item_count, cb.item_off, (uint32_t)G, &c->s, st, &W));
@@ -903,37 +885,233 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
     c->stats.item_sort_passes = ipasses;
     CK(launch_tile_ranges(items_sorted, (uint32_t)W, (uint32_t)tiles, tile_shift, cb.tile_start, st));
     CK(stage_mark(c, 4, st, "cgb:paint"));
-    uint32_t features = 0;
-    for (const SceneInput& in : scenes) features |= in.d.features;
     uint8_t* item_state = nullptr;
-    if (features & FEAT_CLIPS) {
+    if (f.features & FEAT_CLIPS) {
         CK(c->s.ensure(c->item_state, std::max<uint64_t>(W, 1)));
         item_state = c->item_state.as<uint8_t>();
     }
-    bool flush = false;
-    for (const SceneInput& in : scenes) flush |= in.buf->flusher != nullptr;
-    if (flush) {  // per-tile written flags for the flushers
-        CK(c->s.ensure(c->written, std::max<uint64_t>(tiles, 1)));
-        CK(cudaMemsetAsync(c->written.p, 0, tiles, st));
-        std::vector<SceneDesc> descs2;
-        for (SceneInput& in : scenes) {
-            if (in.buf->flusher) in.d.written = c->written.as<uint8_t>() + in.d.tile_base;
-            descs2.push_back(in.d);
-        }
-        CK(cudaMemcpyAsync(c->d_scenes.p, descs2.data(), descs2.size() * sizeof(SceneDesc), cudaMemcpyHostToDevice,
-                           st));
-    }
+    if (f.flush) CK(cudaMemsetAsync(c->written.p, 0, tiles, st));
     CK(launch_paint(bg, sorted, items_sorted, idx_bits, (uint32_t)G, cb.tile_start, cb, c->tuning.paint_warps,
-                    features != 0, item_state, st));
+                    f.features != 0, item_state, st));
     CK(stage_mark(c, 5, st, nullptr));
+    return CGB_OK;
+}
+
+uint32_t with_headroom(uint64_t n, float headroom) {
+    const uint64_t v = n + (uint64_t)((double)n * headroom) + 4096;
+    return (uint32_t)std::min<uint64_t>(v, (1ull << 30) - 2);
+}
+
+// The frame-graph signature: what a captured frame bakes into its launches
+// besides buffer pointers (those are compared separately).  Scene
+// descriptors, layer tables, props and output pointers are read by the
+// kernels from device memory, so they may change between replays.
+std::string frame_signature(const cgb_composition* c, const FrameSetup& f) {
+    const BatchGeom& bg = f.bg;
+    const uint64_t v[] = {bg.n_scenes,        bg.total_rows,   bg.total_tiles,           bg.n_orders,
+                          bg.row_len,         bg.order_bits,   bg.col_bits,              bg.key_bits,
+                          bg.total_lines,     c->tuning.radix_bits, c->tuning.raster_block, c->tuning.steps_per_block,
+                          c->tuning.paint_warps, f.features,   f.flush ? 1u : 0u};
+    return std::string(reinterpret_cast<const char*>(v), sizeof(v));
+}
+
+// (pointer, size) of every buffer that a frame graph launches on.
+std::vector<std::pair<const void*, size_t>> graph_buffers(cgb_composition* c) {
+    const DevBuf* b[] = {&c->recs,       &c->lengths,   &c->step_off,  &c->bcounts,         &c->boff,
+                         &c->segs_a,     &c->segs_b,    &c->blk_cover, &c->blk_head,        &c->tl_start,
+                         &c->tl_key,     &c->tl_cover,  &c->tl_carry,  &c->tl_flags,        &c->item_count,
+                         &c->item_off,   &c->items_a,   &c->items_b,   &c->tile_start,      &c->item_state,
+                         &c->written,    &c->d_scenes,  &c->d_row_scene, &c->err,           &c->d_counts,
+                         &c->s.scan_sums, &c->s.sort_hist, &c->s.sort_lookback, &c->s.sort_counter};
+    std::vector<std::pair<const void*, size_t>> r;
+    for (const DevBuf* x : b) r.emplace_back(x->p, x->cap);
+    return r;
+}
+
+// Every buffer of a graph frame at its capacity (nothing may allocate while
+// the stream captures).
+cudaError_t ensure_graph_buffers(cgb_composition* c, const FrameSetup& f, const FrameCaps& k) {
+    Scratch& s = c->s;
+    const uint64_t L = f.bg.total_lines;
+    const uint32_t block = c->tuning.raster_block, items = c->tuning.steps_per_block / block;
+    const uint64_t grid = raster_grid(k.steps, block, items), slots = raster_run_slots(block, items);
+    const uint64_t hg = tl_scan_grid(k.segs);
+    cudaError_t e = cudaSuccess;
+    auto need = [&](DevBuf& b, uint64_t bytes) {
+        if (e == cudaSuccess) e = s.ensure(b, std::max<uint64_t>(bytes, 8));
+    };
+    need(c->recs, L * sizeof(LineRec));
+    need(c->lengths, L * 4);
+    need(c->step_off, (L + 1) * 4);
+    need(c->segs_a, std::max<uint64_t>(grid * slots, k.segs) * 8);
+    need(c->segs_b, (uint64_t)k.segs * 8);
+    need(c->bcounts, (std::max(grid, hg) + 1) * 4);
+    need(c->boff, (std::max(grid, hg) + 1) * 4);
+    need(c->blk_cover, (hg + 1) * 8);
+    need(c->blk_head, (hg + 1) * 4);
+    need(c->tl_start, ((uint64_t)k.tls + 1) * 4);
+    need(c->tl_key, (uint64_t)k.tls * 8);
+    need(c->tl_cover, (uint64_t)k.tls * 8);
+    need(c->tl_carry, (uint64_t)k.tls * 8);
+    need(c->tl_flags, (uint64_t)k.tls * 4);
+    need(c->item_count, (uint64_t)k.tls * 4);
+    need(c->item_off, ((uint64_t)k.tls + 1) * 4);
+    need(c->items_a, (uint64_t)k.items * 8);
+    need(c->items_b, (uint64_t)k.items * 8);
+    need(c->tile_start, (f.tiles + 1) * 4);
+    if (f.features & FEAT_CLIPS) need(c->item_state, k.items);
+    need(c->d_counts, sizeof(FrameCounts));
+    if (e == cudaSuccess) {
+        const uint64_t scan_n = std::max<uint64_t>(std::max<uint64_t>(L, grid), std::max<uint64_t>(hg, k.tls));
+        e = reserve_frame_scratch(&s, (uint32_t)std::min<uint64_t>(scan_n, UINT32_MAX), std::max(k.segs, k.items));
+    }
+    return e;
+}
+
+// The body of a frame graph: the staged frame's launches with the counts
+// kept on the device (no host synchronization) and every grid sized for
+// the capacities.
+cgb_status enqueue_counted_frame(cgb_composition* c, const FrameSetup& f, const FrameCaps& k, FrameGraph* g) {
+    cudaStream_t st = c->stream;
+    const BatchGeom& bg = f.bg;
+    FrameCounts* fc = c->d_counts.as<FrameCounts>();
+    uint32_t* err = c->err.as<uint32_t>();
+    const uint32_t L = (uint32_t)bg.total_lines;
+    const uint32_t block = c->tuning.raster_block, items = c->tuning.steps_per_block / block;
+    const uint32_t grid = raster_grid(k.steps, block, items), slots = raster_run_slots(block, items);
+    const int rbits = (int)c->tuning.radix_bits;
+    CK(cudaMemsetAsync(fc, 0, sizeof(FrameCounts), st));
+    CK(stage_mark(c, 0, st, nullptr));
+    CK(launch_build_lines(bg, 1, c->recs.as<LineRec>(), c->lengths.as<uint32_t>(), st));
+    CK(scan_u32(c->lengths.as<uint32_t>(), c->step_off.as<uint32_t>(), L, &c->s, st, nullptr, &fc->n[FC_STEPS]));
+    CK(stage_mark(c, 1, st, nullptr));
+    CK(launch_rasterize(1, bg, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, k.steps, block, items,
+                        c->segs_a.as<uint64_t>(), c->bcounts.as<uint32_t>(), &fc->produced, st, fc));
+    CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid, &c->s, st, nullptr, &fc->n[FC_SEGS]));
+    CK(radix_gather_hist(c->segs_a.as<uint64_t>(), slots, c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid,
+                         c->segs_b.as<uint64_t>(), 22, 22 + (int)bg.key_bits, rbits, &c->s, st, k.segs));
+    CK(stage_mark(c, 2, st, nullptr));
+    uint64_t* sorted = nullptr;
+    int passes = 0;
+    CK(radix_sort_u64(c->segs_b.as<uint64_t>(), c->segs_a.as<uint64_t>(), k.segs, 22, 22 + (int)bg.key_bits, rbits,
+                      &c->s, err, st, &sorted, &passes, true, fc, FC_SEGS));
+    g->sort_passes = (uint32_t)passes;
+    CK(stage_mark(c, 3, st, nullptr));
+
+    CarryBuffers cb{};
+    const uint32_t hg = tl_scan_grid(k.segs);
+    cb.blk_cover = c->blk_cover.as<uint64_t>();
+    cb.blk_head = c->blk_head.as<uint32_t>();
+    cb.tl_start = c->tl_start.as<uint32_t>();
+    cb.tl_key = c->tl_key.as<uint64_t>();
+    cb.tl_cover = c->tl_cover.as<uint64_t>();
+    cb.tl_carry = c->tl_carry.as<uint64_t>();
+    cb.tl_flags = c->tl_flags.as<uint32_t>();
+    cb.item_count = c->item_count.as<uint32_t>();
+    cb.item_off = c->item_off.as<uint32_t>();
+    cb.items = c->items_a.as<uint64_t>();
+    cb.items_tmp = c->items_b.as<uint64_t>();
+    cb.tile_start = c->tile_start.as<uint32_t>();
+    cb.order_bits = (int)bg.order_bits;
+    cb.fc = fc;
+    cb.tl_cap = k.tls;
+    cb.items_cap = k.items;
+    CK(launch_tl_scan(0, sorted, k.segs, bg.col_bits, c->bcounts.as<uint32_t>(), nullptr, cb, st));
+    CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), hg, &c->s, st, nullptr, &fc->n[FC_TLS]));
+    CK(launch_tl_scan(1, sorted, k.segs, bg.col_bits, nullptr, c->boff.as<uint32_t>(), cb, st));
+    CK(launch_tl_carry(k.tls, k.segs, cb, st));
+    CK(launch_items(0, k.tls, bg, cb, 0, st));
+    CK(scan_u32(cb.item_count, cb.item_off, k.tls, &c->s, st, nullptr, &fc->n[FC_ITEMS]));
+    const int idx_bits = bits_for((uint64_t)k.tls - 1);
+    const int tile_bits = bits_for(std::max<uint64_t>(f.tiles, 1) - 1);
+    const int tile_shift = idx_bits + 3 + cb.order_bits;
+    if (tile_shift + tile_bits > 64) return fail(CGB_ERR_LAYER_LIMIT, "render: frame graph item key too wide");
+    CK(launch_items(1, k.tls, bg, cb, idx_bits, st));
+    uint64_t* items_sorted = nullptr;
+    int ipasses = 0;
+    CK(radix_sort_u64(cb.items, cb.items_tmp, k.items, tile_shift, tile_shift + tile_bits, rbits, &c->s, err, st,
+                      &items_sorted, &ipasses, false, fc, FC_ITEMS));
+    g->item_sort_passes = (uint32_t)ipasses;
+    CK(launch_tile_ranges(items_sorted, k.items, (uint32_t)f.tiles, tile_shift, cb.tile_start, st, fc));
+    CK(stage_mark(c, 4, st, nullptr));
+    uint8_t* item_state = (f.features & FEAT_CLIPS) ? c->item_state.as<uint8_t>() : nullptr;
+    if (f.flush) CK(cudaMemsetAsync(c->written.p, 0, f.tiles, st));
+    CK(launch_paint(bg, sorted, items_sorted, idx_bits, k.tls, cb.tile_start, cb, c->tuning.paint_warps,
+                    f.features != 0, item_state, st));
+    CK(stage_mark(c, 5, st, nullptr));
+    CK(cudaMemcpyAsync(c->h_counts, fc, sizeof(FrameCounts), cudaMemcpyDeviceToHost, st));
+    return CGB_OK;
+}
+
+void destroy_graph(FrameGraph& g) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g.exec = nullptr;
+}
+
+// Captures the frame graph of `f` with capacities from the counts of the
+// frame just rendered.  A frame that cannot be captured (memory budget, an
+// item key too wide) is simply rendered stage by stage next time.
+void capture_frame_graph(cgb_composition* c, const FrameSetup& f, const std::string& sig) {
+    FrameCaps k;
+    k.steps = with_headroom(c->stats.steps, c->graph_headroom);
+    k.segs = with_headroom(c->stats.painted_segments, c->graph_headroom);
+    k.tls = with_headroom(c->stats.tile_layers, c->graph_headroom);
+    k.items = with_headroom(c->stats.work_items, c->graph_headroom);
+    if (!c->h_counts && cudaMallocHost(&c->h_counts, sizeof(FrameCounts)) != cudaSuccess) {
+        cudaGetLastError();
+        c->h_counts = nullptr;
+        return;
+    }
+    if (ensure_graph_buffers(c, f, k) != cudaSuccess) {
+        cudaGetLastError();
+        c->s.over_budget = false;
+        return;
+    }
+    FrameGraph g;
+    g.caps = k;
+    const uint64_t l0 = g_launches.load();
+    cudaStream_t st = c->stream;
+    c->capturing = true;
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    cgb_status s1 = e == cudaSuccess ? enqueue_counted_frame(c, f, k, &g) : CGB_ERR_DEVICE;
+    cudaGraph_t graph = nullptr;
+    if (e == cudaSuccess) e = cudaStreamEndCapture(st, &graph);
+    c->capturing = false;
+    g.launches = g_launches.load() - l0;
+    g_launches.fetch_sub(g.launches);  // captured, not launched: counted at each replay
+    if (s1 == CGB_OK && e == cudaSuccess && graph) e = cudaGraphInstantiate(&g.exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (s1 != CGB_OK || e != cudaSuccess || !g.exec) {
+        cudaGetLastError();
+        destroy_graph(g);
+        return;
+    }
+    g.bufs = graph_buffers(c);
+    auto it = c->graphs.find(sig);
+    if (it != c->graphs.end()) {
+        destroy_graph(it->second);
+        c->graphs.erase(it);
+    }
+    constexpr size_t MAX_GRAPHS = 32;  // frame geometries kept per handle
+    if (c->graphs.size() >= MAX_GRAPHS) {
+        destroy_graph(c->graphs.begin()->second);
+        c->graphs.erase(c->graphs.begin());
+    }
+    c->graphs.emplace(sig, std::move(g));
+}
+
+// After the device frame: RGBA8 back into host buffers, the written-tile
+// flags, the error flag and the stage times.
+cgb_status finish_frame(cgb_composition* c, std::vector<SceneInput>& scenes, const FrameSetup& f,
+                        std::vector<uint8_t>& written) {
+    cudaStream_t st = c->stream;
     for (SceneInput& in : scenes)
         if (in.buf->memory == CGB_MEMORY_HOST)
             CK(cudaMemcpy2DAsync(in.buf->pixels, (size_t)in.d.stride * 4, in.d.out, (size_t)in.d.stride * 4,
                                  (size_t)in.d.width * 4, in.d.height, cudaMemcpyDeviceToHost, st));
-    std::vector<uint8_t> written;
-    if (flush) {
-        written.resize(tiles);
-        CK(cudaMemcpyAsync(written.data(), c->written.p, tiles, cudaMemcpyDeviceToHost, st));
+    if (f.flush) {
+        written.resize(f.tiles);
+        CK(cudaMemcpyAsync(written.data(), c->written.p, f.tiles, cudaMemcpyDeviceToHost, st));
     }
     cgb_status s3 = check_device_error(c);
     if (s3) return s3;
@@ -943,6 +1121,11 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
     c->stats.carry_ms = elapsed(c->ev[3], c->ev[4]);
     c->stats.paint_ms = elapsed(c->ev[4], c->ev[5]);
     c->stats.total_ms = elapsed(c->ev[0], c->ev[5]);
+    return CGB_OK;
+}
+
+// The host side of a finished frame: the flushers and the layer caches.
+void post_frame(std::vector<SceneInput>& scenes, const std::vector<uint8_t>& written) {
     // Painter::write_to_tile's flush (painter/mod.rs:483-492): each written
     // tile's row slices, cut to the tile width
     for (const SceneInput& in : scenes) {
@@ -963,6 +1146,114 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
                 if (l.enabled) l.unchanged |= 1u << in.buf->layer_cache;
                 else l.unchanged &= ~(1u << in.buf->layer_cache);
             }
+}
+
+// Renders every scene of `scenes` in one pipeline on `c`'s stream and
+// buffers: build, rasterize, sort, carries / items, paint.  In graph mode a
+// frame whose signature and buffers match a captured one is replayed from
+// its graph; a replay whose counts passed the graph's capacities paints
+// nothing and the frame is rendered again stage by stage.
+cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
+    cudaStream_t st = c->stream;
+    for (SceneInput& in : scenes) {
+        cgb_status s0 = prepare_scene(in.comp, in);
+        if (s0) return s0;
+    }
+    // frame geometry: global rows / tiles, key factors, host-output staging
+    uint64_t lines = 0, rows = 0, tiles = 0, staging = 0;
+    uint32_t n_orders = 1, row_len = 1;
+    FrameSetup f;
+    for (SceneInput& in : scenes) {
+        in.d.line_base = lines;
+        in.d.row_base = (uint32_t)rows;
+        in.d.tile_base = (uint32_t)tiles;
+        lines += in.d.n_lines;
+        rows += in.d.rows;
+        tiles += (uint64_t)in.d.rows * in.d.row_len;
+        n_orders = std::max(n_orders, in.d.n_orders);
+        row_len = std::max(row_len, in.d.row_len);
+        in.staging_off = staging;
+        if (in.buf->memory == CGB_MEMORY_HOST) staging += ((size_t)in.d.height * in.d.stride * 4 + 255) & ~(size_t)255;
+        f.features |= in.d.features;
+        f.flush |= in.buf->flusher != nullptr;
+    }
+    if (tiles >= (1ull << 31)) return fail(CGB_ERR_LAYER_LIMIT, "render: too many tiles in a frame");
+    BatchGeom& bg = f.bg;
+    f.tiles = tiles;
+    bg.n_scenes = (uint32_t)scenes.size();
+    bg.total_rows = (uint32_t)rows;
+    bg.total_tiles = (uint32_t)tiles;
+    bg.n_orders = n_orders;
+    bg.row_len = row_len;
+    bg.total_lines = lines;
+    bg.order_bits = bits_for(std::max<uint32_t>(n_orders, 1) - 1);
+    bg.col_bits = bits_for(row_len);
+    bg.key_bits = bits_for(std::max<uint64_t>(rows, 1) - 1) + bg.order_bits + bg.col_bits;
+    if (bg.key_bits > 42) return fail(CGB_ERR_LAYER_LIMIT, "render: rows x orders x tiles too large for the segment key");
+    if (staging) CK(c->s.ensure(c->out_rgba, staging));
+    if (f.flush) CK(c->s.ensure(c->written, std::max<uint64_t>(tiles, 1)));  // per-tile written flags
+    std::vector<SceneDesc> descs;
+    std::vector<uint32_t> row_scene(std::max<uint64_t>(rows, 1), 0);
+    for (size_t k = 0; k < scenes.size(); k++) {
+        SceneInput& in = scenes[k];
+        if (in.buf->memory == CGB_MEMORY_HOST) {
+            in.d.out = c->out_rgba.as<uint8_t>() + in.staging_off;
+            if (in.cache || in.crop)  // tiles that are not repainted keep the caller's pixels
+                CK(cudaMemcpy2DAsync(in.d.out, (size_t)in.d.stride * 4, in.buf->pixels, (size_t)in.d.stride * 4,
+                                     (size_t)in.d.width * 4, in.d.height, cudaMemcpyHostToDevice, st));
+        } else {
+            in.d.out = in.buf->pixels;
+        }
+        if (in.buf->flusher) in.d.written = c->written.as<uint8_t>() + in.d.tile_base;
+        for (uint32_t r = 0; r < in.d.rows; r++) row_scene[in.d.row_base + r] = (uint32_t)k;
+        descs.push_back(in.d);
+    }
+    CK(c->s.ensure(c->d_scenes, descs.size() * sizeof(SceneDesc)));
+    CK(c->s.ensure(c->d_row_scene, row_scene.size() * 4));
+    CK(cudaMemcpyAsync(c->d_scenes.p, descs.data(), descs.size() * sizeof(SceneDesc), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->d_row_scene.p, row_scene.data(), row_scene.size() * 4, cudaMemcpyHostToDevice, st));
+    bg.scenes = c->d_scenes.as<SceneDesc>();
+    bg.row_scene = c->d_row_scene.as<uint32_t>();
+
+    c->last_replayed = false;
+    std::vector<uint8_t> written;
+    const bool graphable = c->graph_mode && !c->import_segs && lines > 0;
+    std::string sig;
+    if (graphable) {
+        sig = frame_signature(c, f);
+        auto it = c->graphs.find(sig);
+        if (it != c->graphs.end() && it->second.bufs == graph_buffers(c)) {
+            FrameGraph& g = it->second;
+            CK(cudaGraphLaunch(g.exec, st));
+            count_launches(g.launches);
+            cgb_status s3 = finish_frame(c, scenes, f, written);
+            if (s3) return s3;
+            const FrameCounts& k = *c->h_counts;
+            if (!k.overflow) {
+                c->stats.lines = lines;
+                c->stats.steps = k.n[FC_STEPS];
+                c->stats.segments = k.produced;
+                c->stats.painted_segments = k.n[FC_SEGS];
+                c->stats.tile_layers = k.n[FC_TLS];
+                c->stats.work_items = k.n[FC_ITEMS];
+                c->stats.sort_passes = g.sort_passes;
+                c->stats.item_sort_passes = g.item_sort_passes;
+                c->last_replayed = true;
+                post_frame(scenes, written);
+                return CGB_OK;
+            }
+            // a count passed its capacity: nothing was painted; render the
+            // frame stage by stage and capture again with the new counts
+            destroy_graph(g);
+            c->graphs.erase(it);
+        }
+    }
+    cgb_status s2 = staged_frame(c, f);
+    if (s2) return s2;
+    cgb_status s3 = finish_frame(c, scenes, f, written);
+    if (s3) return s3;
+    post_frame(scenes, written);
+    if (graphable) capture_frame_graph(c, f, sig);
     return CGB_OK;
 }
 
@@ -1028,7 +1319,11 @@ CGB_EXPORT cgb_status cgb_composition_free(cgb_composition* c) {
                       &c->items_a, &c->items_b, &c->tile_start, &c->d_props, &c->d_grads, &c->d_stops, &c->d_unchanged, &c->out_rgba, &c->err,
                       &c->dflt_t, &c->f_kinds, &c->f_points, &c->f_cmd_off, &c->f_pt_off, &c->f_t9, &c->f_has_t,
                       &c->f_path_layer, &c->f_counts, &c->f_off, &c->g_flags, &c->g_off, &c->s.scan_sums,
-                      &c->s.sort_hist, &c->s.sort_lookback, &c->s.sort_counter};
+                      &c->s.sort_hist, &c->s.sort_lookback, &c->s.sort_counter, &c->d_scenes, &c->d_row_scene,
+                      &c->d_counts};
+    for (auto& kv : c->graphs) destroy_graph(kv.second);
+    c->graphs.clear();
+    if (c->h_counts) cudaFreeHost(c->h_counts);
     for (DevBuf* b : bufs) c->s.release(*b);
     for (auto& b : c->g_tmp) c->s.release(b);
     for (auto& kv : c->caches) c->s.release(kv.second.prev);
@@ -1398,6 +1693,21 @@ CGB_EXPORT cgb_status cgb_pixel_segments(cgb_composition* c, uint64_t* out, size
 CGB_EXPORT cgb_status cgb_get_stats(cgb_composition* c, cgb_stats* out) {
     if (!c || !out) return fail(CGB_ERR_INVALID_ARG, "null argument");
     *out = c->stats;
+    out->graph_replayed = c->last_replayed ? 1u : 0u;
+    out->graphs_cached = (uint32_t)c->graphs.size();
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_set_graph_mode(cgb_composition* c, int enabled, float headroom) {
+    HANDLE_CHECK();
+    if (!(headroom >= 0.0f && headroom <= 4.0f)) return fail(CGB_ERR_INVALID_ARG, "graph headroom must be in [0, 4]");
+    CK(cudaStreamSynchronize(c->stream));
+    c->graph_mode = enabled != 0;
+    if (headroom != c->graph_headroom || !c->graph_mode) {
+        for (auto& kv : c->graphs) destroy_graph(kv.second);
+        c->graphs.clear();
+    }
+    c->graph_headroom = headroom;
     return CGB_OK;
 }
 

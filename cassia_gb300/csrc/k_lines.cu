@@ -531,8 +531,9 @@ template <int RENDER, int RASTER_ITEMS>
 __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ recs, const uint32_t* __restrict__ off,
                                                    uint32_t n_lines, uint64_t n_steps, BatchGeom bg,
                                                    uint64_t* __restrict__ runs, uint32_t* __restrict__ run_count,
-                                                   unsigned long long* __restrict__ produced) {
+                                                   unsigned long long* __restrict__ produced, FrameCounts* fc) {
     extern __shared__ uint64_t s_out[];  // 2 * RASTER_ITEMS * blockDim.x
+    if (fc) n_steps = fc_count(fc, FC_STEPS, (uint32_t)n_steps, blockIdx.x == 0 && threadIdx.x == 0);
     const uint64_t s0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * RASTER_ITEMS;
     uint64_t segs[2 * RASTER_ITEMS];
     int n = 0, total = 0;
@@ -743,22 +744,24 @@ cudaError_t launch_build_lines(const BatchGeom& bg, int cull, LineRec* recs, uin
 
 cudaError_t launch_rasterize(int render, const BatchGeom& bg, const LineRec* recs, const uint32_t* step_off,
                              uint32_t n_lines, uint64_t n_steps, uint32_t block, uint32_t items, uint64_t* runs,
-                             uint32_t* run_count, unsigned long long* produced, cudaStream_t st) {
+                             uint32_t* run_count, unsigned long long* produced, cudaStream_t st,
+                             FrameCounts* fc) {
     if (n_steps == 0) return cudaSuccess;
+    if (fc && n_steps >= (1ull << 32)) return cudaErrorInvalidValue;
     if (block == 0 || block % 32 || block > 256 || (items != 4 && items != 8)) return cudaErrorInvalidValue;
     const uint32_t grid = raster_grid(n_steps, block, items);
     const size_t smem = (size_t)raster_run_slots(block, items) * sizeof(uint64_t);
     count_launches(1);
     if (render) {
         if (items == 4)
-            k_rasterize<1, 4><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced);
+            k_rasterize<1, 4><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced, fc);
         else
-            k_rasterize<1, 8><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced);
+            k_rasterize<1, 8><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced, fc);
     } else {
         if (items == 4)
-            k_rasterize<0, 4><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced);
+            k_rasterize<0, 4><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced, fc);
         else
-            k_rasterize<0, 8><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced);
+            k_rasterize<0, 8><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced, fc);
     }
     return cudaGetLastError();
 }

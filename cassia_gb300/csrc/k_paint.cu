@@ -61,6 +61,7 @@ __global__ void __launch_bounds__(HEAD_THREADS) k_tl_scan(const uint64_t* __rest
                                                           uint32_t col_bits, uint32_t* __restrict__ block_counts,
                                                           const uint32_t* __restrict__ block_off, CarryBuffers cb) {
     constexpr int mode = MODE;
+    n = fc_count(cb.fc, FC_SEGS, n, false);
     const uint64_t s0 = ((uint64_t)blockIdx.x * HEAD_THREADS + threadIdx.x) * HEAD_ITEMS;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint64_t key[HEAD_ITEMS];
@@ -120,7 +121,10 @@ __global__ void __launch_bounds__(HEAD_THREADS) k_tl_scan(const uint64_t* __rest
     if (lane == 31) w_sums[warp] = inc;
     if (mode == 1 && threadIdx.x == 0) {
         uint64_t x = 0;
-        for (uint32_t b = blockIdx.x + 1; b < gridDim.x; b++) {
+        // (graph frames launch blocks for the capacity: those past the
+        // count hold no segments and are not walked)
+        const uint32_t nb = min(gridDim.x, (uint32_t)((n + HEAD_THREADS * HEAD_ITEMS - 1) / (HEAD_THREADS * HEAD_ITEMS)));
+        for (uint32_t b = blockIdx.x + 1; b < nb; b++) {
             x = cover_add(x, cb.blk_cover[b]);
             if (cb.blk_head[b]) break;
         }
@@ -152,6 +156,7 @@ __global__ void __launch_bounds__(HEAD_THREADS) k_tl_scan(const uint64_t* __rest
     const uint64_t r_next_lane = __shfl_down_sync(0xffffffffu, R, 1);
     const uint64_t cont = lane == 31 ? w_carry[warp] : r_next_lane;  // R(t + 1)
     if (!flags) return;
+    const uint32_t cap = cb.fc ? cb.tl_cap : 0xFFFFFFFFu;
     uint32_t o = block_off[blockIdx.x] + w_sums[warp] + inc - cnt;
     uint64_t pk = first_prev;
     uint64_t acc = 0;
@@ -160,36 +165,41 @@ __global__ void __launch_bounds__(HEAD_THREADS) k_tl_scan(const uint64_t* __rest
     for (int k = 0; k < HEAD_ITEMS; k++) {
         if (flags & (1u << k)) {
             if (open >= 0) {
-                cb.tl_cover[o] = acc;
+                if (o < cap) cb.tl_cover[o] = acc;
                 o++;
             }
             open = k;
             acc = 0;
-            cb.tl_start[o] = (uint32_t)(s0 + k);
-            cb.tl_key[o] = key[k];
-            // a run is one (row, order) pair: a new run starts unless the
-            // previous segment is in the same row and order
-            cb.tl_flags[o] = (pk == ~0ull || key_run(pk, col_bits) != key_run(key[k], col_bits)) ? 1u : 0u;
+            if (o < cap) {
+                cb.tl_start[o] = (uint32_t)(s0 + k);
+                cb.tl_key[o] = key[k];
+                // a run is one (row, order) pair: a new run starts unless the
+                // previous segment is in the same row and order
+                cb.tl_flags[o] = (pk == ~0ull || key_run(pk, col_bits) != key_run(key[k], col_bits)) ? 1u : 0u;
+            }
         }
         if (s0 + k < n) acc = cover_add(acc, seg_cover(low[k]));
         pk = key[k];
     }
-    cb.tl_cover[o] = cover_add(acc, cont);
+    if (o < cap) cb.tl_cover[o] = cover_add(acc, cont);
 }
 
 // Exclusive prefix of the cover sums along each (j, L) run: one thread walks
-// each run (runs are a layer's few tile groups in one tile row).
-__global__ void k_tl_carry(uint32_t G, const uint64_t* __restrict__ tl_cover, const uint32_t* __restrict__ tl_flags,
-                           uint64_t* __restrict__ tl_carry) {
-    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= G || !tl_flags[g]) return;
+// each run (runs are a layer's few tile groups in one tile row).  Thread 0
+// also closes the TL segment ranges: tl_start[G] = P.
+__global__ void k_tl_carry(uint32_t G, uint32_t P, CarryBuffers cb) {
+    G = fc_count(cb.fc, FC_TLS, G, blockIdx.x == 0 && threadIdx.x == 0);
+    P = fc_count(cb.fc, FC_SEGS, P, false);
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g == 0) cb.tl_start[G] = P;
+    if (g >= G || !cb.tl_flags[g]) return;
     uint64_t acc = 0;
     uint32_t h = g;
     do {
-        tl_carry[h] = acc;
-        acc = cover_add(acc, tl_cover[h]);
+        cb.tl_carry[h] = acc;
+        acc = cover_add(acc, cb.tl_cover[h]);
         h++;
-    } while (h < G && !tl_flags[h]);
+    } while (h < G && !cb.tl_flags[h]);
 }
 
 // Work-item payload bits above the TL index: the item holds only a cover carry;
@@ -257,10 +267,13 @@ __device__ __forceinline__ TlItems tl_items(uint32_t g, uint32_t G, const CarryB
     return r;
 }
 
+// G: the TL count, or with cb.fc the TL capacity (the entries past the
+// device count are zeroed for the scan over the capacity).
 __global__ void k_items_count(uint32_t G, CarryBuffers cb, BatchGeom bg) {
+    const uint32_t Gd = fc_count(cb.fc, FC_TLS, G, false);
     uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= G) return;
-    cb.item_count[g] = tl_items(g, G, cb, bg).count();
+    cb.item_count[g] = g < Gd ? tl_items(g, Gd, cb, bg).count() : 0u;
 }
 
 // Item = tile | order | flags | TL index, high to low; the tile field is the
@@ -275,7 +288,10 @@ __global__ void __launch_bounds__(IW_THREADS) k_items_write(uint32_t G, CarryBuf
     __shared__ uint64_t s_row[IW_THREADS];
     __shared__ int32_t s_own[IW_THREADS], s_ta[IW_THREADS];
     __shared__ uint32_t s_lf[IW_THREADS];  // order << 3 | carry-only flags
+    G = fc_count(cb.fc, FC_TLS, G, false);
     const uint32_t g0 = blockIdx.x * IW_THREADS, g = g0 + threadIdx.x;
+    if (g0 >= G) return;  // graph frames: blocks past the TL count
+    const uint32_t icap = cb.fc ? cb.items_cap : 0xFFFFFFFFu;
     const uint32_t nt = min(G - g0, (uint32_t)IW_THREADS);
     const uint32_t base = cb.item_off[g0];
     if (g < G) {
@@ -312,12 +328,13 @@ __global__ void __launch_bounds__(IW_THREADS) k_items_write(uint32_t G, CarryBuf
         }
         const uint64_t tile = s_row[lo] + (uint64_t)col;
         const uint64_t key = (((tile << ob) | (lf >> ITEM_FLAG_BITS)) << ITEM_FLAG_BITS) | fl;
-        cb.items[base + idx] = (key << idx_bits) | (g0 + lo);
+        if (base + idx < icap) cb.items[base + idx] = (key << idx_bits) | (g0 + lo);
     }
 }
 
 __global__ void k_tile_ranges(const uint64_t* __restrict__ items, uint32_t W, uint32_t n_tiles, int tile_shift,
-                              uint32_t* __restrict__ tile_start) {
+                              uint32_t* __restrict__ tile_start, FrameCounts* fc) {
+    W = fc_count(fc, FC_ITEMS, W, blockIdx.x == 0 && threadIdx.x == 0);
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k > W) return;
     int64_t cur = k < W ? (int64_t)min(items[k] >> tile_shift, (uint64_t)n_tiles) : (int64_t)n_tiles;
@@ -652,6 +669,7 @@ struct PaintArgs {
     const uint32_t* tl_start;
     const uint64_t* tl_cover;
     const uint64_t* tl_carry;
+    const FrameCounts* fc;  // graph frames: nothing is painted after an overflow
 };
 
 constexpr int SEGCAP = 256;     // staged segments per warp and chunk of 32 items
@@ -811,6 +829,7 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
     WarpStage& S = stages[threadIdx.x >> 5];
     const uint32_t t = blockIdx.x * PAINT_WARPS + (threadIdx.x >> 5);
     if (t >= a.bg.total_tiles) return;
+    if (a.fc && a.fc->overflow) return;
     // the scene holding global tile t
     uint32_t lo = 0, hi = a.bg.n_scenes;
     while (hi - lo > 1) {
@@ -1132,10 +1151,9 @@ cudaError_t launch_tl_scan(int mode, const uint64_t* segs, uint32_t n, uint32_t 
 
 uint32_t tl_scan_grid(uint32_t n) { return (n + HEAD_THREADS * HEAD_ITEMS - 1) / (HEAD_THREADS * HEAD_ITEMS); }
 
-cudaError_t launch_tl_carry(uint32_t G, const CarryBuffers& cb, cudaStream_t st) {
-    if (G == 0) return cudaSuccess;
+cudaError_t launch_tl_carry(uint32_t G, uint32_t P, const CarryBuffers& cb, cudaStream_t st) {
     count_launches(1);
-    k_tl_carry<<<(G + 255) / 256, 256, 0, st>>>(G, cb.tl_cover, cb.tl_flags, cb.tl_carry);
+    k_tl_carry<<<std::max<uint32_t>(1, (G + 255) / 256), 256, 0, st>>>(G, P, cb);
     return cudaGetLastError();
 }
 
@@ -1151,9 +1169,9 @@ cudaError_t launch_items(int mode, uint32_t G, const BatchGeom& bg, const CarryB
 }
 
 cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_tiles, int tile_shift,
-                               uint32_t* tile_start, cudaStream_t st) {
+                               uint32_t* tile_start, cudaStream_t st, FrameCounts* fc) {
     count_launches(1);
-    k_tile_ranges<<<(W + 1 + 255) / 256, 256, 0, st>>>(items, W, n_tiles, tile_shift, tile_start);
+    k_tile_ranges<<<(W + 1 + 255) / 256, 256, 0, st>>>(items, W, n_tiles, tile_shift, tile_start, fc);
     return cudaGetLastError();
 }
 
@@ -1161,8 +1179,8 @@ cudaError_t launch_paint(const BatchGeom& bg, const uint64_t* segs, const uint64
                          const uint32_t* tile_start, const CarryBuffers& cb, uint32_t warps, bool full,
                          uint8_t* item_state, cudaStream_t st) {
     if (bg.total_tiles == 0) return cudaSuccess;
-    PaintArgs a{bg,        segs,        items,       idx_bits,    cb.order_bits, G,
-                item_state, tile_start, cb.tl_start, cb.tl_cover, cb.tl_carry};
+    PaintArgs a{bg,         segs,       items,       idx_bits,    cb.order_bits, G,
+                item_state, tile_start, cb.tl_start, cb.tl_cover, cb.tl_carry,   cb.fc};
     count_launches(1);
     const uint32_t T = bg.total_tiles;
     if (full) {

@@ -85,8 +85,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t* __
     }
 }
 
-// Exclusive scan of nb u64 block sums in place; sums[nb] = total; out_tail = total (u32).
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_sums(uint64_t* sums, uint32_t nb, uint32_t* out_tail) {
+// Exclusive scan of nb u64 block sums in place; sums[nb] = total; out_tail
+// (and tail2, if given) = total (u32).
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_sums(uint64_t* sums, uint32_t nb, uint32_t* out_tail,
+                                                           uint32_t* tail2) {
     __shared__ uint64_t carry;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
@@ -104,6 +106,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_sums(uint64_t* sums, uint
     if (threadIdx.x == 0) {
         sums[nb] = carry;
         if (out_tail) *out_tail = (uint32_t)carry;
+        if (tail2) *tail2 = (uint32_t)carry;
     }
 }
 
@@ -161,8 +164,9 @@ __device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
 
 // One pass over the keys that histograms every digit of every pass.
 __global__ void __launch_bounds__(512) k_radix_hist(const uint64_t* __restrict__ keys, uint32_t n, PassPlan plan,
-                                                    uint32_t* __restrict__ hist) {
+                                                    uint32_t* __restrict__ hist, FrameCounts* fc, int fc_which) {
     __shared__ uint32_t sh[MAX_PASSES][RADIX];
+    n = fc_count(fc, fc_which, n, false);
     for (int i = threadIdx.x; i < plan.n * RADIX; i += blockDim.x) (&sh[0][0])[i] = 0;
     __syncthreads();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -184,15 +188,16 @@ __global__ void __launch_bounds__(512) k_radix_hist(const uint64_t* __restrict__
 __global__ void __launch_bounds__(512) k_gather_hist(const uint64_t* __restrict__ runs, uint32_t run_slots,
                                                      const uint32_t* __restrict__ run_count,
                                                      const uint32_t* __restrict__ run_off, uint32_t n_runs,
-                                                     uint64_t* __restrict__ out, PassPlan plan,
+                                                     uint64_t* __restrict__ out, uint32_t out_cap, PassPlan plan,
                                                      uint32_t* __restrict__ hist) {
     __shared__ uint32_t sh[MAX_PASSES][RADIX];
     for (int i = threadIdx.x; i < plan.n * RADIX; i += blockDim.x) (&sh[0][0])[i] = 0;
     __syncthreads();
     for (uint32_t r = blockIdx.x; r < n_runs; r += gridDim.x) {
-        const uint32_t cnt = run_count[r];
+        const uint32_t o = run_off[r];
+        const uint32_t cnt = o < out_cap ? min(run_count[r], out_cap - o) : 0u;
         const uint64_t* src = runs + (uint64_t)r * run_slots;
-        uint64_t* dst = out + run_off[r];
+        uint64_t* dst = out + o;
         for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) {
             const uint64_t k = src[i];
             dst[i] = k;
@@ -221,7 +226,7 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) k_onesweep(const uint64_t* __
                                                            uint32_t n, int shift, int bits,
                                                            const uint32_t* __restrict__ global_off,
                                                            uint32_t* lookback, uint32_t* tile_counter,
-                                                           uint32_t* err) {
+                                                           uint32_t* err, FrameCounts* fc, int fc_which) {
     __shared__ uint16_t s_hist[SORT_WARPS][RADIX];  // per-warp counts, then offsets (< 4096)
     __shared__ uint32_t s_count[RADIX];
     __shared__ uint32_t s_start[RADIX];
@@ -240,6 +245,10 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) k_onesweep(const uint64_t* __
     __syncthreads();
     const uint32_t tile = s_tile;
     const uint64_t base = (uint64_t)tile * SORT_TILE;
+    // graph frames launch one CTA per tile of the capacity: the tiles past
+    // the count have no keys and no successor that waits for them
+    n = fc_count(fc, fc_which, n, tile == 0 && tid == 0);
+    if (fc && base >= n && tile > 0) return;
 
     uint64_t key[SORT_ITEMS];
     uint32_t dr[SORT_ITEMS];  // digit (RADIX = none) | rank within the warp << 16
@@ -367,14 +376,14 @@ cudaError_t onesweep_setup() {
 size_t scan_scratch_bytes(uint32_t n) { return ((size_t)n / SCAN_TILE + 2) * sizeof(uint64_t); }
 
 cudaError_t scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, Scratch* s, cudaStream_t st,
-                     uint64_t* total_host) {
+                     uint64_t* total_host, uint32_t* tail_dev) {
     uint32_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
     cudaError_t e = s->ensure(s->scan_sums, ((size_t)nb + 1) * sizeof(uint64_t));
     if (e != cudaSuccess) return e;
     uint64_t* sums = s->scan_sums.as<uint64_t>();
     count_launches(nb > 0 ? 3 : 1);
     if (nb > 0) k_scan_reduce<<<nb, SCAN_THREADS, 0, st>>>(in, n, sums);
-    k_scan_sums<<<1, SCAN_THREADS, 0, st>>>(sums, nb, out + n);
+    k_scan_sums<<<1, SCAN_THREADS, 0, st>>>(sums, nb, out + n, tail_dev);
     if (nb > 0) k_scan_apply<<<nb, SCAN_THREADS, 0, st>>>(in, n, sums, out);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -386,6 +395,16 @@ cudaError_t scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, Scratch* s, 
         *total_host = s->pinned[0];
     }
     return cudaSuccess;
+}
+
+cudaError_t reserve_frame_scratch(Scratch* s, uint32_t scan_n, uint32_t sort_n) {
+    const size_t tiles = ((size_t)sort_n + SORT_TILE - 1) / SORT_TILE;
+    cudaError_t e = s->ensure(s->scan_sums, ((size_t)scan_n / SCAN_TILE + 2) * sizeof(uint64_t));
+    if (e == cudaSuccess) e = s->ensure(s->sort_hist, (size_t)MAX_PASSES * RADIX * 4);
+    if (e == cudaSuccess) e = s->ensure(s->sort_lookback, std::max<size_t>(tiles, 1) * RADIX * 4);
+    if (e == cudaSuccess) e = s->ensure(s->sort_counter, MAX_PASSES * 4);
+    if (e == cudaSuccess) e = onesweep_setup();
+    return e;
 }
 
 cudaError_t scan_block_counts(const uint32_t* counts, uint32_t* offsets, uint32_t n_blocks, Scratch* s,
@@ -424,7 +443,7 @@ static int sm_count() {
 
 cudaError_t radix_gather_hist(const uint64_t* runs, uint32_t run_slots, const uint32_t* run_count,
                               const uint32_t* run_off, uint32_t n_runs, uint64_t* out, int bit_lo, int bit_hi,
-                              int digit_bits, Scratch* s, cudaStream_t st) {
+                              int digit_bits, Scratch* s, cudaStream_t st, uint32_t out_cap) {
     const PassPlan plan = make_plan(bit_lo, bit_hi, digit_bits);
     cudaError_t e = s->ensure(s->sort_hist, (size_t)MAX_PASSES * RADIX * 4);
     if (e != cudaSuccess) return e;
@@ -433,13 +452,13 @@ cudaError_t radix_gather_hist(const uint64_t* runs, uint32_t run_slots, const ui
     if (n_runs == 0) return cudaSuccess;
     const uint32_t blocks = std::min<uint32_t>(n_runs, (uint32_t)sm_count() * 4);
     count_launches(1);
-    k_gather_hist<<<blocks, 512, 0, st>>>(runs, run_slots, run_count, run_off, n_runs, out, plan, hist);
+    k_gather_hist<<<blocks, 512, 0, st>>>(runs, run_slots, run_count, run_off, n_runs, out, out_cap, plan, hist);
     return cudaGetLastError();
 }
 
 cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo, int bit_hi, int digit_bits,
                            Scratch* s, uint32_t* err_flag, cudaStream_t st, uint64_t** result, int* passes,
-                           bool hist_ready) {
+                           bool hist_ready, FrameCounts* fc, int fc_which) {
     PassPlan plan = make_plan(bit_lo, bit_hi, digit_bits);
     *result = keys;
     if (passes) *passes = plan.n;
@@ -459,7 +478,7 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo
         if ((e = cudaMemsetAsync(hist, 0, (size_t)plan.n * RADIX * 4, st)) != cudaSuccess) return e;
         uint32_t hist_blocks = std::min<uint32_t>((n + 511) / 512, (uint32_t)sm_count() * 4);
         count_launches(1);
-        k_radix_hist<<<hist_blocks, 512, 0, st>>>(keys, n, plan, hist);
+        k_radix_hist<<<hist_blocks, 512, 0, st>>>(keys, n, plan, hist, fc, fc_which);
     }
     count_launches(1 + plan.n);
     k_radix_hist_scan<<<plan.n, RADIX, 0, st>>>(hist);
@@ -468,7 +487,8 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo
     for (int p = 0; p < plan.n; p++) {
         if ((e = cudaMemsetAsync(lb, 0, (size_t)tiles * RADIX * 4, st)) != cudaSuccess) return e;
         k_onesweep<<<tiles, SORT_THREADS, ONESWEEP_DYN_SMEM, st>>>(src, dst, n, plan.shift[p], plan.bits[p],
-                                                                   hist + p * RADIX, lb, ctr + p, err_flag);
+                                                                   hist + p * RADIX, lb, ctr + p, err_flag, fc,
+                                                                   fc_which);
         std::swap(src, dst);
     }
     *result = src;
@@ -498,7 +518,7 @@ cudaError_t selftest_bounded_wait(cudaStream_t st, uint32_t* flag_host) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(ctr, &one, 4, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
         count_launches(1);
-        k_onesweep<<<1, SORT_THREADS, ONESWEEP_DYN_SMEM, st>>>(in, out, n, 0, 8, hist, lb, ctr, err);
+        k_onesweep<<<1, SORT_THREADS, ONESWEEP_DYN_SMEM, st>>>(in, out, n, 0, 8, hist, lb, ctr, err, nullptr, 0);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(flag_host, err, 4, cudaMemcpyDeviceToHost, st);
@@ -592,7 +612,7 @@ extern "C" CGB_EXPORT cgb_status cgb_sort_keys_noalloc(uint64_t* keys, uint64_t*
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint32_t hist_blocks = std::min<uint32_t>((nn + 511) / 512, (uint32_t)sms * 4);
     if (e == cudaSuccess) {
-        k_radix_hist<<<hist_blocks, 512, 0, st>>>(keys, nn, plan, hist);
+        k_radix_hist<<<hist_blocks, 512, 0, st>>>(keys, nn, plan, hist, nullptr, 0);
         k_radix_hist_scan<<<plan.n, RADIX, 0, st>>>(hist);
         e = cudaGetLastError();
     }
@@ -603,7 +623,7 @@ extern "C" CGB_EXPORT cgb_status cgb_sort_keys_noalloc(uint64_t* keys, uint64_t*
         e = cudaMemsetAsync(lb, 0, (size_t)tiles * RADIX * 4, st);
         if (e != cudaSuccess) break;
         k_onesweep<<<tiles, SORT_THREADS, ONESWEEP_DYN_SMEM, st>>>(src, dst, nn, plan.shift[p], plan.bits[p],
-                                                                   hist + p * RADIX, lb, ctr + p, err);
+                                                                   hist + p * RADIX, lb, ctr + p, err, nullptr, 0);
         e = cudaGetLastError();
         std::swap(src, dst);
     }

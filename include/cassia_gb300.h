@@ -172,6 +172,8 @@ typedef struct cgb_stats {
     uint32_t sort_passes;      /* radix passes of the segment sort */
     uint32_t item_sort_passes; /* radix passes of the work-item sort */
     float build_ms, rasterize_ms, sort_ms, carry_ms, paint_ms, total_ms;
+    uint32_t graph_replayed;   /* 1: the frame was replayed from a frame graph (cgb_set_graph_mode) */
+    uint32_t graphs_cached;    /* frame graphs held by the handle */
 } cgb_stats;
 
 /* Autotuned knobs (0 keeps the current value).  Every setting renders the
@@ -285,6 +287,18 @@ CGB_EXPORT cgb_status cgb_pixel_segments(cgb_composition* c, uint64_t* out, size
 
 /* Sizes and stage times of the last render / pixel_segments. */
 CGB_EXPORT cgb_status cgb_get_stats(cgb_composition* c, cgb_stats* out);
+/* Frame graphs (replaces the per-stage launches of mold's Composition::render,
+ * mold/src/composition.rs:212-329, by one CUDA graph launch).  With enabled
+ * != 0, a frame whose geometry repeats -- the same compositions, line counts,
+ * canvases, clear-colour-independent layout and tuning -- is replayed from a
+ * CUDA graph captured after the first frame of that geometry.  The graph
+ * keeps every count of the frame on the device (no host synchronization
+ * between stages); its buffers are sized `headroom` (a fraction, e.g. 0.125)
+ * above the counts of the frame it was captured after.  A replayed frame
+ * whose counts pass them paints nothing and is rendered again stage by stage,
+ * then captured anew.  Pixels are identical in both forms.  Up to 32
+ * geometries are kept per handle (cgb_render_batch groups included). */
+CGB_EXPORT cgb_status cgb_set_graph_mode(cgb_composition* c, int enabled, float headroom);
 CGB_EXPORT cgb_status cgb_set_tuning(cgb_composition* c, const cgb_tuning* tuning);
 CGB_EXPORT cgb_status cgb_get_tuning(cgb_composition* c, cgb_tuning* out);
 
