@@ -511,6 +511,8 @@ __device__ __forceinline__ int raster_step(const SceneRaster& sr, const BatchGeo
 }
 
 
+constexpr uint32_t RASTER_LINE_STAGE = 1024;  // line offsets staged per rasterizer block
+
 __device__ __forceinline__ uint32_t find_line(const uint32_t* __restrict__ off, uint32_t n_lines, uint64_t s) {
     // largest l with off[l] <= s (off has n_lines + 1 entries, off[0] = 0)
     uint32_t lo = 0, hi = n_lines;
@@ -533,13 +535,43 @@ __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ r
                                                    uint64_t* __restrict__ runs, uint32_t* __restrict__ run_count,
                                                    unsigned long long* __restrict__ produced, FrameCounts* fc) {
     extern __shared__ uint64_t s_out[];  // 2 * RASTER_ITEMS * blockDim.x
+    // The line offsets of the block's step range, staged once: two searches
+    // over the whole offset array per block instead of one per thread.
+    __shared__ uint32_t s_off[RASTER_LINE_STAGE + 1];
+    __shared__ uint32_t s_lines[2];
     if (fc) n_steps = fc_count(fc, FC_STEPS, (uint32_t)n_steps, blockIdx.x == 0 && threadIdx.x == 0);
+    const uint64_t bs0 = (uint64_t)blockIdx.x * blockDim.x * RASTER_ITEMS;
+    const uint64_t bs1 = min(bs0 + (uint64_t)blockDim.x * RASTER_ITEMS, n_steps);  // exclusive
+    if (bs0 < n_steps) {
+        if (threadIdx.x == 0) s_lines[0] = find_line(off, n_lines, bs0);
+        if (threadIdx.x == 32 % blockDim.x) s_lines[1] = find_line(off, n_lines, bs1 - 1);
+    }
+    __syncthreads();
+    // lines l0..l1 hold the block's steps; off[l0 .. l1 + 1] go to s_off
+    const uint32_t l0 = bs0 < n_steps ? s_lines[0] : 0u;
+    const uint32_t nl = bs0 < n_steps ? s_lines[1] - l0 + 1 : 0u;
+    const bool staged = nl > 0 && nl <= RASTER_LINE_STAGE;
+    if (staged)
+        for (uint32_t q = threadIdx.x; q <= nl; q += blockDim.x) s_off[q] = off[l0 + q];
+    __syncthreads();
     const uint64_t s0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * RASTER_ITEMS;
     uint64_t segs[2 * RASTER_ITEMS];
     int n = 0, total = 0;
     if (s0 < n_steps) {
-        uint32_t l = find_line(off, n_lines, s0);
-        uint32_t next = off[l + 1];
+        uint32_t l;
+        if (staged) {  // largest q with s_off[q] <= s0 (s_off[0] <= s0 < s_off[nl])
+            uint32_t lo = 0, hi = nl;
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if ((uint64_t)s_off[mid] <= s0) lo = mid;
+                else hi = mid;
+            }
+            l = l0 + lo;
+        } else {
+            l = find_line(off, n_lines, s0);
+        }
+        uint32_t cur = staged ? s_off[l - l0] : off[l];
+        uint32_t next = staged ? s_off[l - l0 + 1] : off[l + 1];
         LineRec rec = recs[l];
         uint32_t sc = rec.order_octant >> LINE_SCENE_SHIFT;
         SceneRaster sr{bg.scenes[sc].wide, bg.scenes[sc].rows, bg.scenes[sc].row_len, bg.scenes[sc].row_base};
@@ -547,9 +579,13 @@ __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ r
         for (int k = 0; k < RASTER_ITEMS; k++) {
             uint64_t s = s0 + k;
             if (s < n_steps) {
-                while (s >= next) {
-                    l++;
-                    next = off[l + 1];
+                if (s >= next) {
+                    // the next line with steps (lines culled to length 0 are passed over)
+                    do {
+                        l++;
+                        cur = next;
+                        next = staged ? s_off[l - l0 + 1] : off[l + 1];
+                    } while (s >= next);
                     rec = recs[l];
                     if ((rec.order_octant >> LINE_SCENE_SHIFT) != sc) {
                         sc = rec.order_octant >> LINE_SCENE_SHIFT;
@@ -558,7 +594,7 @@ __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ r
                     }
                 }
                 uint64_t o[2];
-                const int m = raster_step<RENDER>(sr, bg, rec, (int32_t)(s - off[l]), o, total);
+                const int m = raster_step<RENDER>(sr, bg, rec, (int32_t)(s - cur), o, total);
 #pragma unroll
                 for (int q = 0; q < 2; q++)
                     if (q < m) segs[n++] = o[q];

@@ -57,7 +57,7 @@ __device__ __forceinline__ uint64_t seg_cover(uint32_t low) {
 // mode 0: per block, the TL count, blk_cover and blk_head.
 // mode 1: per TL g, its first segment, key, cover sum and run-start flag.
 template <int MODE>
-__global__ void __launch_bounds__(HEAD_THREADS) k_tl_scan(const uint64_t* __restrict__ segs, uint32_t n,
+__global__ void __launch_bounds__(HEAD_THREADS, 5) k_tl_scan(const uint64_t* __restrict__ segs, uint32_t n,
                                                           uint32_t col_bits, uint32_t* __restrict__ block_counts,
                                                           const uint32_t* __restrict__ block_off, CarryBuffers cb) {
     constexpr int mode = MODE;
