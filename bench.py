@@ -235,16 +235,28 @@ def cpu_reference(scene, steps, warmup, budget_s=150.0):
             "ms_per_step": t * 1e3, "frames_per_s": 1.0 / t}
 
 
-def group_scenes(comps, line_budget=16_000_000):
-    """Consecutive scenes whose lines fit one frame's budget."""
-    groups, cur, lines = [], [], 0
-    for k, c in enumerate(comps):
+def _bits(v):
+    """Bits that hold values in [0, v] (at least 1)."""
+    return max(1, int(v).bit_length())
+
+
+def group_scenes(comps, sset, line_budget=16_000_000, key_bits=36):
+    """Consecutive scenes whose lines fit one frame's budget and whose
+    batched segment key -- the tile rows of all of them, the largest order,
+    the widest tile row -- stays within key_bits (4 radix passes of 9 bits;
+    one more bit would cost a fifth pass over every segment of the group)."""
+    groups, cur, lines, rows, orders, cols = [], [], 0, 0, 1, 1
+    for k, (c, sc) in enumerate(zip(comps, sset)):
         n = c.lens()[0]
-        if cur and lines + n > line_budget:
+        r, cl, o = (sc.height + 7) // 8, (sc.width + 7) // 8, max(1, sc.n_layers)
+        nrows, nord, ncol = rows + r, max(orders, o), max(cols, cl)
+        if cur and (lines + n > line_budget or _bits(nrows - 1) + _bits(nord - 1) + _bits(ncol) > key_bits):
             groups.append(cur)
             cur, lines = [], 0
+            nrows, nord, ncol = r, o, cl
         cur.append(k)
         lines += n
+        rows, orders, cols = nrows, nord, ncol
     if cur:
         groups.append(cur)
     return groups
@@ -270,7 +282,7 @@ def run_batch(args, rank, world, local):
     outs_b = [torch.zeros((sc.height, sc.width, 4), dtype=torch.uint8, device="cuda") for sc in sset]
     outs_p = [torch.zeros_like(o) for o in outs_b]
     ctx = Composition()
-    groups = group_scenes(comps)
+    groups = group_scenes(comps, sset)
 
     def batched():
         for g in groups:
@@ -298,6 +310,10 @@ def run_batch(args, rank, world, local):
     tuning, trials = autotune.tune(ctx, batched, snapshot=lambda: [o.clone() for o in outs_b],
                                    same=lambda a, b: all(torch.equal(x, y) for x, y in zip(a, b)), reps=2)
     tune_s = time.time() - t_tune
+    if args.frame_mode == "graph":  # after tuning: each tuning is a new frame geometry
+        ctx.set_graph_mode(True)
+        for c in comps:
+            c.set_graph_mode(True)
     for c in comps:
         c.set_tuning(**tuning)
     for _ in range(args.warmup):
@@ -329,7 +345,7 @@ def run_batch(args, rank, world, local):
                        "frames_per_pass": len(groups), "segments_per_pass": int(segs),
                        "l2": "inputs larger than L2"},
             "plain_scenes_per_s": world * len(sset) / tp, "plain_ms_per_pass": tp * 1e3,
-            "speedup_vs_plain": tp / tb, "bit_exact_batched_vs_plain": bool(exact),
+            "speedup_vs_plain": tp / tb, "bit_exact_batched_vs_plain": bool(exact), "frame_mode": args.frame_mode,
             "tuning": tuning, "autotune": {"trials": len(trials), "seconds": tune_s,
                                            "ms_per_pass": {str(i): t["ms"] for i, t in enumerate(trials)}},
             "e2e": {"value": world * len(sset) / te, "unit": "scenes/s", "h2d_bytes_per_step": 0,
