@@ -6,9 +6,12 @@ Workload (default): the mixed 100,000-layer scene on a 2560x1600 canvas
 blend modes, NonZero/EvenOdd; ~7.6M lines, ~65M pixel segments), seeded and
 synthetic.  Lines are flattened once on the GPU and stay resident in HBM; one
 step is one frame: LinesBuilder::build -> rasterize -> sort -> paint into an
-RGBA8 device buffer.  value = pixel segments / second over all ranks.
+RGBA8 device buffer.  value = pixel segments / second over all ranks.  By
+default frames are replayed from a captured CUDA graph (the library's graph
+mode: counts stay on the device); --frame-mode staged enqueues each stage and
+reads the counts back between stages.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--frame-mode staged|graph]
 
 --impl reference times the CPU restatement of the reference path (the
 oracle, std::thread-parallel over the host cores) on the same workload,
@@ -312,8 +315,6 @@ def run_batch(args, rank, world, local):
     tune_s = time.time() - t_tune
     if args.frame_mode == "graph":  # after tuning: each tuning is a new frame geometry
         ctx.set_graph_mode(True)
-        for c in comps:
-            c.set_graph_mode(True)
     for c in comps:
         c.set_tuning(**tuning)
     for _ in range(args.warmup):
@@ -324,7 +325,16 @@ def run_batch(args, rank, world, local):
     with ClockSampler(local) as clk:
         tb = timed(batched, args.steps)
     launches = kernel_launches() - launches0
+    # the plain loop both ways: every frame enqueued stage by stage, and
+    # every scene replayed from its own frame graph
     tp = timed(plain, max(1, args.steps // 2))
+    for c in comps:
+        c.set_graph_mode(True)
+    for _ in range(2):
+        plain()
+    tpg = timed(plain, max(1, args.steps // 2))
+    exact = exact and all(torch.equal(a, b) for a, b in zip(outs_b, outs_p))
+    tp_ref = tpg if args.frame_mode == "graph" else tp
     segs = sum(c.count_segments()[0] for c in comps)
     # e2e: the same batched pass into pinned host buffers (RGBA8 read back each pass)
     host = [torch.zeros((sc.height, sc.width, 4), dtype=torch.uint8).pin_memory().numpy() for sc in sset]
@@ -344,8 +354,10 @@ def run_batch(args, rank, world, local):
             "config": {"workload": args.workload, "scenes": len(sset), "layers": int(sum(s.n_layers for s in sset)),
                        "frames_per_pass": len(groups), "segments_per_pass": int(segs),
                        "l2": "inputs larger than L2"},
-            "plain_scenes_per_s": world * len(sset) / tp, "plain_ms_per_pass": tp * 1e3,
-            "speedup_vs_plain": tp / tb, "bit_exact_batched_vs_plain": bool(exact), "frame_mode": args.frame_mode,
+            "plain_scenes_per_s": world * len(sset) / tp_ref, "plain_ms_per_pass": tp_ref * 1e3,
+            "speedup_vs_plain": tp_ref / tb, "bit_exact_batched_vs_plain": bool(exact), "frame_mode": args.frame_mode,
+            "plain_staged_ms_per_pass": tp * 1e3, "plain_graph_ms_per_pass": tpg * 1e3,
+            "speedup_vs_plain_staged": tp / tb, "speedup_vs_plain_graph": tpg / tb,
             "tuning": tuning, "autotune": {"trials": len(trials), "seconds": tune_s,
                                            "ms_per_pass": {str(i): t["ms"] for i, t in enumerate(trials)}},
             "e2e": {"value": world * len(sset) / te, "unit": "scenes/s", "h2d_bytes_per_step": 0,
@@ -439,7 +451,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quiet", action="store_true")
-    ap.add_argument("--frame-mode", default="staged", choices=["staged", "graph"],
+    ap.add_argument("--frame-mode", default="graph", choices=["staged", "graph"],
                     help="graph: frames replayed from a captured CUDA graph (cgb_set_graph_mode)")
     ap.add_argument("--cpu-budget", type=float, default=150.0,
                     help="seconds of host work the reference arm's samples are sized to")

@@ -27,7 +27,7 @@ constexpr int TILE_MASK = 7;
 // ---------------------------------------------------------------------------
 
 // surpass::Layer (surpass/src/layer.rs:5-20) indexed by layer id.
-struct LayerRec {
+struct alignas(16) LayerRec {  // two 16-byte loads
     uint32_t flags;  // LAYER_PRESENT | LAYER_ENABLED | LAYER_HAS_TRANSFORM
     uint32_t order;  // Layer::order (defaults to the id when LAYER_HAS_ORDER is clear)
     float t[6];      // affine_transform
@@ -38,13 +38,15 @@ constexpr uint32_t LAYER_HAS_TRANSFORM = 4u;
 constexpr uint32_t LAYER_HAS_ORDER = 8u;
 
 // Output of LinesBuilder::build for one line (surpass/src/segment.rs:208-219),
-// packed into 32 bytes.  `length` lives in a separate array (it is scanned).
-struct LineRec {
+// packed into 32 bytes (two 16-byte stores and loads).  `length` lives in a
+// separate array (it is scanned).
+struct alignas(16) LineRec {
     int32_t start;
     float start_f32, end_f32;
     float slope, slope_recip, py_slope_px, px_slope_recip_py;
     uint32_t order_octant;  // order << 3 | octant
 };
+static_assert(sizeof(LineRec) == 32 && sizeof(LayerRec) == 32, "32-byte line and layer records");
 
 // Painter-side props of one order (LayerProps::get, painter/mod.rs:143-146).
 struct PaintProps {

@@ -325,11 +325,9 @@ __global__ void k_build_lines(BatchGeom bg, int cull, LineRec* __restrict__ recs
     const float* __restrict__ default_t = S.default_t;
     LineRec r{0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0u};
     uint32_t length = 0;
-    uint32_t flags = 0, lorder = 0;
-    if (lid < n_layer_recs) {
-        flags = layers[lid].flags;
-        lorder = layers[lid].order;
-    }
+    LayerRec lrec{};
+    if (lid < n_layer_recs) lrec = layers[lid];
+    const uint32_t flags = lrec.flags, lorder = lrec.order;
     const bool present = (flags & LAYER_PRESENT) != 0;
     if (!(present && !(flags & LAYER_ENABLED))) {
         const uint32_t order = (present && (flags & LAYER_HAS_ORDER)) ? lorder : lid;
@@ -337,7 +335,7 @@ __global__ void k_build_lines(BatchGeom bg, int cull, LineRec* __restrict__ recs
         bool has_t = false;
         float t0 = 0.f, t1 = 0.f, t2 = 0.f, t3 = 0.f, t4 = 0.f, t5 = 0.f;
         if (present && (flags & LAYER_HAS_TRANSFORM)) {
-            const float* tr = layers[lid].t;
+            const float* tr = lrec.t;
             t0 = tr[0], t1 = tr[1], t2 = tr[2], t3 = tr[3], t4 = tr[4], t5 = tr[5];
             has_t = true;
         } else if (default_t) {
