@@ -373,7 +373,10 @@ def run_serve(args, rank, world, local):
     distribution), Poisson arrivals at 2,000 requests/s; each frame gives 20%
     of a client's layers a new affine and adds/removes 1%.  Continuous
     batching (2 workers, batches of up to 16, 40 GB HBM budget) against the
-    plain loop (one render call per request), on identical request streams."""
+    plain loop (one render call per request), on identical request streams.
+    The offered rate saturates the server (its latency then grows with the
+    run), so the batched server is also run at 75% of the throughput it
+    reached ("sustained": p50/p99 of a server that keeps up)."""
     import torch
     from cassia_gb300 import serving
     from cassia_gb300.composition import kernel_launches
@@ -381,14 +384,23 @@ def run_serve(args, rank, world, local):
     reqs_b = serving.poisson_arrivals(w["rate"], w["n_clients"], w["duration"], seed=w["seed"] + rank)
     reqs_p = serving.poisson_arrivals(w["rate"], w["n_clients"], w["duration"], seed=w["seed"] + rank)
     out = {}
-    for mode, reqs in (("batched", reqs_b), ("plain", reqs_p)):
+    runs = [("batched", reqs_b), ("plain", reqs_p), ("sustained", None)]
+    for mode, reqs in runs:
+        if mode == "sustained":
+            # the batched server at 75% of the throughput it reached at the
+            # offered rate: latency of a server that keeps up with its load
+            rate = 0.75 * out["batched"]["frames_per_s"]
+            reqs = serving.poisson_arrivals(rate, w["n_clients"], w["duration"], seed=w["seed"] + rank + 1)
         clients = serving.make_clients(w["n_clients"], seed=w["seed"] + rank, device_out=True)
-        srv = serving.Server(clients, mode=mode, workers=2, max_batch=16, hbm_budget=40e9)
+        srv = serving.Server(clients, mode="plain" if mode == "plain" else "batched", workers=2, max_batch=16,
+                             hbm_budget=40e9)
         l0 = kernel_launches()
         with ClockSampler(local) as clk:
             done = srv.run(reqs)
         torch.cuda.synchronize()
         s = serving.latency_summary(done, w["duration"])
+        if mode == "sustained":
+            s["offered_rate"] = rate
         # whole-job rate: the frames of every replica over the slowest replica's span
         span = over_ranks(s["requests"] / s["frames_per_s"])
         s["frames_per_s_all_ranks"] = over_ranks(s["requests"], "sum") / span
@@ -415,6 +427,8 @@ def run_serve(args, rank, world, local):
             "config": {"workload": args.workload, "clients": w["n_clients"], "offered_rate": w["rate"],
                        "duration_s": w["duration"], "hbm_budget_gb": 40, "max_batch": 16, "workers": 2},
             "p50_ms": b["p50_ms"], "p99_ms": b["p99_ms"], "batched": b, "plain": p,
+            "sustained": {k: out["sustained"][k] for k in ("offered_rate", "frames_per_s", "p50_ms", "p99_ms",
+                                                           "mean_batch")},
             "speedup_vs_plain": b["frames_per_s_all_ranks"] / p["frames_per_s_all_ranks"],
             "gpu_launches": b["gpu_launches"], "clocks": b["clocks"],
         }

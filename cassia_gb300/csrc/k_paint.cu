@@ -70,13 +70,27 @@ __global__ void __launch_bounds__(HEAD_THREADS, 5) k_tl_scan(const uint64_t* __r
     uint64_t prev = ~0ull;
     if (s0 < n && s0 > 0) prev = segs[s0 - 1] >> 22;
     const uint64_t first_prev = prev;
+    // the thread's segments as 16-byte pairs (s0 is a multiple of HEAD_ITEMS)
+    uint64_t sv[HEAD_ITEMS];
+    if (s0 + HEAD_ITEMS <= n) {
+        const ulonglong2* p2 = reinterpret_cast<const ulonglong2*>(segs + s0);
+#pragma unroll
+        for (int k = 0; k < HEAD_ITEMS / 2; k++) {
+            const ulonglong2 v = p2[k];
+            sv[2 * k] = v.x;
+            sv[2 * k + 1] = v.y;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < HEAD_ITEMS; k++) sv[k] = s0 + k < n ? segs[s0 + k] : 0ull;
+    }
 #pragma unroll
     for (int k = 0; k < HEAD_ITEMS; k++) {
         const uint64_t s = s0 + k;
         key[k] = ~0ull;
         low[k] = 0;
         if (s < n) {
-            const uint64_t v = segs[s];
+            const uint64_t v = sv[k];
             key[k] = v >> 22;
             low[k] = (uint32_t)v;
             if (key[k] != prev) {

@@ -85,16 +85,26 @@ def make_clients(n_clients: int, seed: int, device_out: bool = True, max_layers:
     return clients
 
 
+def _mix64(ids: np.ndarray, salt: int) -> np.ndarray:
+    """splitmix64 of each id and a salt, vectorized (array integer arithmetic
+    wraps silently)."""
+    z = ids.astype(np.uint64) * np.uint64(0x9E3779B97F4A7C15) + np.uint64(salt & 0xFFFFFFFFFFFFFFFF)
+    z ^= z >> np.uint64(30)
+    z *= np.uint64(0xBF58476D1CE4E5B9)
+    z ^= z >> np.uint64(27)
+    z *= np.uint64(0x94D049BB133111EB)
+    z ^= z >> np.uint64(31)
+    return z
+
+
+def _bits01(z: np.ndarray, shift: int, bits: int) -> np.ndarray:
+    """Uniform [0, 1) from `bits` bits of z starting at `shift`."""
+    return ((z >> np.uint64(shift)) & np.uint64((1 << bits) - 1)).astype(np.float64) * (1.0 / (1 << bits))
+
+
 def _u01(ids: np.ndarray, salt: int) -> np.ndarray:
-    """Seeded uniform [0, 1) per id (splitmix64 of id and salt), vectorized."""
-    with np.errstate(over="ignore"):
-        z = ids.astype(np.uint64) * np.uint64(0x9E3779B97F4A7C15) + np.uint64(salt & 0xFFFFFFFFFFFFFFFF)
-        z ^= z >> np.uint64(30)
-        z *= np.uint64(0xBF58476D1CE4E5B9)
-        z ^= z >> np.uint64(27)
-        z *= np.uint64(0x94D049BB133111EB)
-        z ^= z >> np.uint64(31)
-    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / (1 << 53))
+    """Seeded uniform [0, 1) per id (splitmix64 of id and salt)."""
+    return _bits01(_mix64(ids, salt), 11, 53)
 
 
 def apply_update(cl: Client, client_id: int, seq: int, changed: float = 0.2, churn: float = 0.01):
@@ -105,22 +115,24 @@ def apply_update(cl: Client, client_id: int, seq: int, changed: float = 0.2, chu
     if len(live) == 0:
         return
     salt = (client_id << 40) ^ (seq * 0x9E3779B1)
-    u = _u01(live, salt)
-    ids = live[u < changed]
+    # one hash per live layer: 24 bits decide the new affine, 24 others the removal
+    z = _mix64(live, salt)
+    ids = live[_bits01(z, 40, 24) < changed]
     if len(ids) == 0:
         ids = live[:1]
-    rng = np.random.default_rng((client_id << 32) ^ (seq * 2654435761 % (1 << 32)))
+    # one hash per changed layer: rotation U[-0.05, 0.05), shift U[-3, 3)^2
+    w = _mix64(ids, salt ^ 0x2545F4914F6CDD1D)
+    th = ((_bits01(w, 42, 21) - 0.5) * 0.1).astype(np.float32)
     t = cl.transforms[ids]
-    th = rng.uniform(-0.05, 0.05, size=len(ids)).astype(np.float32)
     c, s = np.cos(th), np.sin(th)
     a, b, cc, d = t[:, 0].copy(), t[:, 1].copy(), t[:, 2].copy(), t[:, 3].copy()
     t[:, 0], t[:, 1] = c * a - s * cc, c * b - s * d
     t[:, 2], t[:, 3] = s * a + c * cc, s * b + c * d
-    t[:, 4] += rng.uniform(-3, 3, size=len(ids)).astype(np.float32)
-    t[:, 5] += rng.uniform(-3, 3, size=len(ids)).astype(np.float32)
+    t[:, 4] += ((_bits01(w, 21, 21) - 0.5) * 6.0).astype(np.float32)
+    t[:, 5] += ((_bits01(w, 0, 21) - 0.5) * 6.0).astype(np.float32)
     cl.transforms[ids] = t
     cl.comp.set_transforms(ids, t)
-    gone = live[_u01(live, salt ^ 0x5DEECE66D) < churn]
+    gone = live[_bits01(z, 16, 24) < churn]
     if len(gone):
         cl.comp.set_enabled_many(gone, np.zeros(len(gone), np.uint8))
         cl.enabled[gone] = False
