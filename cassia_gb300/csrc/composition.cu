@@ -78,16 +78,17 @@ HostProps default_props() {
     return p;
 }
 
-struct HostLayer {
+// The fields a per-frame transform update touches share the first cache line.
+struct alignas(64) HostLayer {
     bool present = false;  // the layer exists in mold's `layers` map
     bool enabled = true;
     bool has_transform = false;
-    float t[6] = {1, 0, 0, 1, 0, 0};
     bool has_order = false;
     uint32_t order = 0;
-    HostProps props = default_props();
     uint32_t unchanged = 0;  // SmallBitSet of cache ids (mold/src/layer.rs:101-142)
+    float t[6] = {1, 0, 0, 1, 0, 0};
     uint64_t len = 0;
+    HostProps props = default_props();
 };
 
 struct CacheState {
