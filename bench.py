@@ -181,9 +181,11 @@ STAGE_KERNELS = {
 # What bounds each stage's dominant kernel, from the ncu captures summarised
 # in profiles/kernels_mixed20k.md.
 STAGE_LIMITERS = {
-    "rasterize": "SM issue and line-record load latency (52% issue active, long-scoreboard stalls)",
-    "sort": "latency of the onesweep tile (65% issue active, 2.2 TB/s)",
-    "paint": "SM issue (78% of issue slots); its DRAM traffic equals its algorithmic input",
+    "rasterize": "fixed-point step arithmetic and barriers of the per-block runs (55% issue active)",
+    "sort": "latency of the onesweep tile (64% issue active, 2.1 TB/s)",
+    "paint": "instruction issue and dependent-instruction latency (64% of issue slots, fixed-latency "
+             "waits the top stall; not occupancy: more resident warps did not help); its DRAM traffic "
+             "equals its algorithmic input",
 }
 
 
