@@ -183,6 +183,7 @@ def _declare(lib):
         "cgb_get_stats": ([handle, P(CgbStats)], i32),
         "cgb_set_tuning": ([handle, P(CgbTuning)], i32),
         "cgb_set_graph_mode": ([handle, ctypes.c_int, ctypes.c_float], i32),
+        "cgb_set_incremental": ([handle, ctypes.c_int], i32),
         "cgb_get_tuning": ([handle, P(CgbTuning)], i32),
         "cgb_synchronize": ([handle], i32),
         "cgb_get_stream": ([handle, P(vp)], i32),

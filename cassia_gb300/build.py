@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libcassia_gb300.so")
-SOURCES = ["k_lines.cu", "k_sort.cu", "k_paint.cu", "composition.cu"]
+SOURCES = ["k_lines.cu", "k_sort.cu", "k_paint.cu", "k_incr.cu", "composition.cu"]
 HEADERS = ["cgb_internal.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -279,6 +279,11 @@ class Composition:
         _check(self._lib, self._lib.cgb_set_graph_mode(self._h, 1 if enabled else 0, float(headroom)),
                "set_graph_mode")
 
+    def set_incremental(self, enabled: bool = True):
+        """Keep the last frame's sorted segments on the device and rasterize
+        only the layers whose geometry changed (cgb_set_incremental)."""
+        _check(self._lib, self._lib.cgb_set_incremental(self._h, 1 if enabled else 0), "set_incremental")
+
     def stream(self) -> int:
         """The cudaStream_t (as an int) the handle launches on."""
         out = ctypes.c_void_p()

@@ -103,6 +103,7 @@ struct SceneDesc {
     uint32_t features;                            // FEAT_*
     float clear[4];
     uint8_t* written;                             // by tile: the painter wrote it (flushers), or null
+    const uint8_t* rast_dirty;  // incremental frames: by order, 1 = rasterize its lines; null = all lines
 };
 
 // Frame-wide geometry of the render-mode segment key, bit fields from high
@@ -307,6 +308,46 @@ cudaError_t selftest_bounded_wait(cudaStream_t st, uint32_t* flag_host);
 cudaError_t radix_gather_hist(const uint64_t* runs, uint32_t run_slots, const uint32_t* run_count,
                               const uint32_t* run_off, uint32_t n_runs, uint64_t* out, int bit_lo, int bit_hi,
                               int digit_bits, Scratch* s, cudaStream_t st, uint32_t out_cap = 0xFFFFFFFFu);
+
+// k_incr.cu: incremental frames
+// Local key layout of a composition's resident segments (bits 22..63):
+// tile row (12 bits) | order (17) | tile column + 1 (13).
+constexpr int LOCAL_ORDER_BITS = 17;
+constexpr int LOCAL_COL_BITS = 13;
+constexpr uint32_t LOCAL_MAX_ROWS = 1u << (42 - LOCAL_ORDER_BITS - LOCAL_COL_BITS);
+constexpr uint32_t MAX_KEEP_SOURCES = 256;  // scenes of one incremental frame
+// Resident segments of one scene, flattened at `start` among all sources.
+struct KeepSource {
+    const uint64_t* seg;
+    uint64_t start, n;
+    const uint8_t* dirty;  // by order: 1 = the order's segments are rasterized again
+    uint32_t n_dirty;
+    uint32_t row_base;     // the scene's first tile row in the frame
+};
+// A scene's range of the sorted frame and where its resident copy goes.
+struct ExtractTarget {
+    uint64_t* dst;
+    uint64_t start, n, cap;  // flattened start, count, capacity of dst
+    uint32_t first;          // first segment of the range in the frame
+    uint32_t row_base;
+};
+uint32_t keep_grid(uint64_t total);
+uint32_t merge_tiles(uint64_t n);
+// mode 0: per block of keep_grid(total), the kept (clean-order) resident
+// segments; mode 1: write them at block_off, in order, in the frame's key
+// layout (out holds out_cap keys).
+cudaError_t launch_keep(int mode, const KeepSource* srcs, uint32_t n_srcs, uint64_t total, const BatchGeom& bg,
+                        uint32_t* block_count, const uint32_t* block_off, uint64_t* out, uint64_t out_cap,
+                        cudaStream_t st);
+// Stable merge of two key-sorted arrays (by bits 22..63; a first on ties);
+// split holds merge_tiles(na + nb) + 1 entries.
+cudaError_t launch_merge(const uint64_t* a, uint32_t na, const uint64_t* b, uint32_t nb, uint32_t* split,
+                         uint64_t* out, cudaStream_t st);
+// ranges[2k], ranges[2k + 1]: the segments of scene scene_ids[k]'s tile rows in the sorted frame.
+cudaError_t launch_scene_ranges(const uint64_t* segs, uint32_t n, const BatchGeom& bg, const uint32_t* scene_ids,
+                                uint32_t n_ids, uint32_t* ranges, cudaStream_t st);
+cudaError_t launch_extract(const uint64_t* segs, const ExtractTarget* tg, uint32_t n_tg, uint64_t total,
+                           const BatchGeom& bg, cudaStream_t st);
 
 // k_paint.cu
 struct CarryBuffers {

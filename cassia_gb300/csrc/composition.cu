@@ -219,6 +219,21 @@ struct cgb_composition {
     bool last_replayed = false;
     bool capturing = false;         // the stream is capturing a frame graph
 
+    // incremental frames (cgb_set_incremental): the sorted segments of the
+    // last frame stay resident and only changed layers are rasterized again
+    bool incremental = false;
+    std::vector<uint32_t> rast_ids;   // layers whose geometry changed since the last frame
+    std::vector<uint8_t> rast_flag;   // by id: listed in rast_ids
+    std::vector<int32_t> rast_order;  // by id: the order its resident segments carry, -1 none
+    std::vector<uint8_t> h_rast_dirty;
+    DevBuf d_rast_dirty;              // by order (max_ids bytes): 1 = rasterize again
+    DevBuf resident;                  // sorted segments of the last frame, local key layout
+    uint64_t resident_n = 0;
+    bool resident_valid = false;
+    uint32_t resident_rows = 0, resident_row_len = 0;
+    // frame-level buffers of an incremental frame (on the handle that renders it)
+    DevBuf segs_k, segs_m, d_keep, d_scene_ids, d_ranges, d_extract, merge_split;
+
     cgb_status cuda_fail(cudaError_t e, const char* where) {
         if (e == cudaErrorMemoryAllocation && s.over_budget) {
             s.over_budget = false;
@@ -321,8 +336,20 @@ HostLayer* find_layer(cgb_composition* c, uint32_t id) {
     return id < c->layers.size() && c->layers[id].present ? &c->layers[id] : nullptr;
 }
 
+// Incremental frames: layer `id`'s geometry changed (transform, enabled,
+// order, lines, removal), so its old and new orders are rasterized again.
+void mark_raster(cgb_composition* c, uint32_t id) {
+    if (!c->incremental) return;
+    if (id >= c->rast_flag.size()) c->rast_flag.resize((size_t)id + 1, 0);
+    if (!c->rast_flag[id]) {
+        c->rast_flag[id] = 1;
+        c->rast_ids.push_back(id);
+    }
+}
+
 // Refreshes the device-table record of layer `id` and marks it for upload.
 void touch(cgb_composition* c, uint32_t id) {
+    mark_raster(c, id);
     if (id >= c->layer_recs.size()) {
         c->layer_recs.resize((size_t)id + 1);
         c->layers_grew = true;
@@ -585,6 +612,9 @@ struct SceneInput {
     CacheState* cache;
     SceneDesc d;
     size_t staging_off;  // offset in the frame's host-output staging buffer
+    // incremental frames: 0 no; 1 all lines rasterized, the resident
+    // segments rebuilt; 2 only changed layers rasterized, the resident ones kept
+    int incr = 0;
 };
 
 // Stage boundary: records CUDA event k on the stream (the stage times of
@@ -706,6 +736,54 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
     return ms;
 }
 
+// Incremental frames: which orders of composition c are rasterized again.
+// The resident segments are usable when the canvas (tile rows and row
+// length) is the one they were made for; the orders to redo are the old and
+// new orders of every layer whose geometry changed since the last frame,
+// and every order no present layer holds.
+cgb_status prepare_incremental(cgb_composition* c, SceneInput& in) {
+    in.incr = 0;
+    in.d.rast_dirty = nullptr;
+    if (!c->incremental || c->import_segs) return CGB_OK;
+    const uint32_t rows = in.d.rows, row_len = in.d.row_len;
+    if (rows > LOCAL_MAX_ROWS || row_len + 1 >= (1u << LOCAL_COL_BITS)) {  // beyond the local key layout
+        c->resident_valid = false;
+        return CGB_OK;
+    }
+    const bool valid = c->resident_valid && c->resident_rows == rows && c->resident_row_len == row_len;
+    auto current_order = [&](uint32_t id) -> int32_t {
+        if (id >= c->layers.size()) return -1;
+        const HostLayer& l = c->layers[id];
+        return (l.present && l.enabled) ? (int32_t)(l.has_order ? l.order : id) : -1;
+    };
+    if (!valid) {  // every line rasterized; the resident segments are rebuilt after the frame
+        c->rast_order.assign(c->layers.size(), -1);
+        for (uint32_t id = 0; id < c->layers.size(); id++) c->rast_order[id] = current_order(id);
+        for (uint32_t id : c->rast_ids) c->rast_flag[id] = 0;
+        c->rast_ids.clear();
+        in.incr = 1;
+        return CGB_OK;
+    }
+    c->h_rast_dirty.assign(c->max_ids, 0);
+    for (uint32_t o = c->n_orders; o < c->max_ids; o++) c->h_rast_dirty[o] = 1;  // orders no layer holds
+    if (c->rast_order.size() < c->layers.size()) c->rast_order.resize(c->layers.size(), -1);
+    for (uint32_t id : c->rast_ids) {
+        if (id < c->rast_order.size() && c->rast_order[id] >= 0) c->h_rast_dirty[(uint32_t)c->rast_order[id]] = 1;
+        const int32_t cur = current_order(id);
+        if (cur >= 0 && (uint32_t)cur < c->max_ids) c->h_rast_dirty[(uint32_t)cur] = 1;
+        if (id >= c->rast_order.size()) c->rast_order.resize((size_t)id + 1, -1);
+        c->rast_order[id] = cur;
+        c->rast_flag[id] = 0;
+    }
+    c->rast_ids.clear();
+    CK(c->s.ensure(c->d_rast_dirty, c->max_ids));
+    CK(cudaMemcpyAsync(c->d_rast_dirty.p, c->h_rast_dirty.data(), c->max_ids, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    in.d.rast_dirty = c->d_rast_dirty.as<uint8_t>();
+    in.incr = 2;
+    return CGB_OK;
+}
+
 // Host-side preparation of one composition for a frame: mold's
 // remove_disabled, orders_to_layers / props, the layer table and the layer
 // cache (composition.rs:212-241).
@@ -800,7 +878,7 @@ cgb_status prepare_scene(cgb_composition* c, SceneInput& in) {
         d.crop_v1 = (uint32_t)std::min<uint64_t>((in.crop->y1 + 7) / 8, rows);
     }
     std::memcpy(d.clear, in.bg, sizeof(d.clear));
-    return CGB_OK;
+    return prepare_incremental(c, in);
 }
 
 // Frame geometry shared by the staged and the graph form of a frame.
@@ -809,12 +887,99 @@ struct FrameSetup {
     uint64_t tiles = 0;
     uint32_t features = 0;
     bool flush = false;
+    bool incremental = false;  // some scene is rendered incrementally (staged frames only)
 };
+
+// Incremental frames, after the sort of the new segments (*sorted, *P): the
+// kept resident segments of the scenes rendered incrementally are merged
+// in, then every incremental scene's range of the frame becomes its new
+// resident segments (local key layout).
+cgb_status incremental_merge(cgb_composition* c, const FrameSetup& f, std::vector<SceneInput>& scenes,
+                             uint64_t** sorted, uint64_t* P) {
+    cudaStream_t st = c->stream;
+    const BatchGeom& bg = f.bg;
+    // kept segments: resident segments of clean orders, scene after scene
+    std::vector<KeepSource> src;
+    uint64_t total = 0;
+    for (const SceneInput& in : scenes) {
+        if (in.incr != 2 || in.comp->resident_n == 0) continue;
+        const cgb_composition* sc = in.comp;
+        src.push_back(KeepSource{sc->resident.as<uint64_t>(), total, sc->resident_n, sc->d_rast_dirty.as<uint8_t>(),
+                                 sc->max_ids, in.d.row_base});
+        total += sc->resident_n;
+    }
+    if (src.size() > MAX_KEEP_SOURCES) return fail(CGB_ERR_INVALID_ARG, "incremental frame: too many scenes");
+    uint64_t K = 0;
+    if (total) {
+        const uint32_t grid = keep_grid(total);
+        CK(c->s.ensure(c->d_keep, src.size() * sizeof(KeepSource)));
+        CK(cudaMemcpyAsync(c->d_keep.p, src.data(), src.size() * sizeof(KeepSource), cudaMemcpyHostToDevice, st));
+        CK(c->s.ensure(c->bcounts, ((size_t)grid + 1) * 4));
+        CK(c->s.ensure(c->boff, ((size_t)grid + 1) * 4));
+        CK(launch_keep(0, c->d_keep.as<KeepSource>(), (uint32_t)src.size(), total, bg, c->bcounts.as<uint32_t>(),
+                       nullptr, nullptr, 0, st));
+        CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid, &c->s, st, &K));
+        if (*P + K >= (1ull << 30) - 1) return fail(CGB_ERR_LAYER_LIMIT, "more than 2^30 pixel segments");
+        if (K) {
+            CK(c->s.ensure(c->segs_k, K * 8));
+            CK(launch_keep(1, c->d_keep.as<KeepSource>(), (uint32_t)src.size(), total, bg, nullptr,
+                           c->boff.as<uint32_t>(), c->segs_k.as<uint64_t>(), K, st));
+            CK(c->s.ensure(c->segs_m, (K + *P) * 8));
+            CK(c->s.ensure(c->merge_split, ((size_t)merge_tiles(K + *P) + 1) * 4));
+            CK(launch_merge(c->segs_k.as<uint64_t>(), (uint32_t)K, *sorted, (uint32_t)*P,
+                            c->merge_split.as<uint32_t>(), c->segs_m.as<uint64_t>(), st));
+            *sorted = c->segs_m.as<uint64_t>();
+            *P += K;
+        }
+    }
+    // the frame's segments of each incremental scene become its resident ones
+    std::vector<uint32_t> ids;
+    for (uint32_t k = 0; k < scenes.size(); k++)
+        if (scenes[k].incr) ids.push_back(k);
+    if (ids.size() > MAX_KEEP_SOURCES) return fail(CGB_ERR_INVALID_ARG, "incremental frame: too many scenes");
+    CK(c->s.ensure(c->d_scene_ids, ids.size() * 4));
+    CK(c->s.ensure(c->d_ranges, ids.size() * 8));
+    CK(cudaMemcpyAsync(c->d_scene_ids.p, ids.data(), ids.size() * 4, cudaMemcpyHostToDevice, st));
+    CK(launch_scene_ranges(*sorted, (uint32_t)*P, bg, c->d_scene_ids.as<uint32_t>(), (uint32_t)ids.size(),
+                           c->d_ranges.as<uint32_t>(), st));
+    std::vector<uint32_t> ranges(2 * ids.size());
+    CK(cudaMemcpyAsync(ranges.data(), c->d_ranges.p, ranges.size() * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::vector<ExtractTarget> tg;
+    uint64_t n_all = 0;
+    for (size_t q = 0; q < ids.size(); q++) {
+        SceneInput& in = scenes[ids[q]];
+        cgb_composition* sc = in.comp;
+        const uint64_t n = ranges[2 * q + 1] >= ranges[2 * q] ? ranges[2 * q + 1] - ranges[2 * q] : 0;
+        cudaError_t e = sc->s.ensure(sc->resident, std::max<uint64_t>(n, 1) * 8);
+        if (e != cudaSuccess) {  // no room to keep them: the next frame rasterizes every line
+            cudaGetLastError();
+            sc->s.over_budget = false;
+            sc->resident_valid = false;
+            sc->resident_n = 0;
+            continue;
+        }
+        tg.push_back(ExtractTarget{sc->resident.as<uint64_t>(), n_all, n, sc->resident.cap / 8, ranges[2 * q],
+                                   in.d.row_base});
+        n_all += n;
+        sc->resident_n = n;
+        sc->resident_valid = true;
+        sc->resident_rows = in.d.rows;
+        sc->resident_row_len = in.d.row_len;
+    }
+    if (!tg.empty()) {
+        CK(c->s.ensure(c->d_extract, tg.size() * sizeof(ExtractTarget)));
+        CK(cudaMemcpyAsync(c->d_extract.p, tg.data(), tg.size() * sizeof(ExtractTarget), cudaMemcpyHostToDevice, st));
+        CK(launch_extract(*sorted, c->d_extract.as<ExtractTarget>(), (uint32_t)tg.size(), n_all, bg, st));
+        CK(cudaStreamSynchronize(st));  // the host vectors above go out of scope
+    }
+    return CGB_OK;
+}
 
 // Build -> rasterize -> sort -> carries / items -> paint, stage by stage:
 // the host reads S, P, G and W as they are produced and sizes each buffer
 // to them.
-cgb_status staged_frame(cgb_composition* c, const FrameSetup& f) {
+cgb_status staged_frame(cgb_composition* c, const FrameSetup& f, std::vector<SceneInput>& scenes) {
     cudaStream_t st = c->stream;
     const BatchGeom& bg = f.bg;
     const uint64_t tiles = f.tiles;
@@ -830,6 +995,11 @@ cgb_status staged_frame(cgb_composition* c, const FrameSetup& f) {
     CK(radix_sort_u64(keys, c->segs_a.as<uint64_t>(), (uint32_t)P, 22, 22 + (int)bg.key_bits,
                       (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &sorted, &passes, true));
     c->stats.sort_passes = passes;
+    if (f.incremental) {
+        cgb_status si = incremental_merge(c, f, scenes, &sorted, &P);
+        if (si) return si;
+        c->stats.painted_segments = P;
+    }
     CK(stage_mark(c, 3, st, "cgb:carry"));
 
     // tile-layer groups, carries, work items
@@ -1177,6 +1347,7 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
         if (in.buf->memory == CGB_MEMORY_HOST) staging += ((size_t)in.d.height * in.d.stride * 4 + 255) & ~(size_t)255;
         f.features |= in.d.features;
         f.flush |= in.buf->flusher != nullptr;
+        f.incremental |= in.incr != 0;
     }
     if (tiles >= (1ull << 31)) return fail(CGB_ERR_LAYER_LIMIT, "render: too many tiles in a frame");
     BatchGeom& bg = f.bg;
@@ -1218,7 +1389,7 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
 
     c->last_replayed = false;
     std::vector<uint8_t> written;
-    const bool graphable = c->graph_mode && !c->import_segs && lines > 0;
+    const bool graphable = c->graph_mode && !c->import_segs && lines > 0 && !f.incremental;
     std::string sig;
     if (graphable) {
         sig = frame_signature(c, f);
@@ -1249,10 +1420,15 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
             c->graphs.erase(it);
         }
     }
-    cgb_status s2 = staged_frame(c, f);
-    if (s2) return s2;
-    cgb_status s3 = finish_frame(c, scenes, f, written);
-    if (s3) return s3;
+    cgb_status s2 = staged_frame(c, f, scenes);
+    cgb_status s3 = s2 ? s2 : finish_frame(c, scenes, f, written);
+    if (s3) {
+        // the changed layers of this frame were taken off the dirty lists:
+        // the next frame of an incremental scene rasterizes every line
+        for (SceneInput& in : scenes)
+            if (in.incr) in.comp->resident_valid = false;
+        return s3;
+    }
     post_frame(scenes, written);
     if (graphable) capture_frame_graph(c, f, sig);
     return CGB_OK;
@@ -1321,7 +1497,8 @@ CGB_EXPORT cgb_status cgb_composition_free(cgb_composition* c) {
                       &c->dflt_t, &c->f_kinds, &c->f_points, &c->f_cmd_off, &c->f_pt_off, &c->f_t9, &c->f_has_t,
                       &c->f_path_layer, &c->f_counts, &c->f_off, &c->g_flags, &c->g_off, &c->s.scan_sums,
                       &c->s.sort_hist, &c->s.sort_lookback, &c->s.sort_counter, &c->d_scenes, &c->d_row_scene,
-                      &c->d_counts};
+                      &c->d_counts, &c->d_rast_dirty, &c->resident, &c->segs_k, &c->segs_m, &c->d_keep,
+                      &c->d_scene_ids, &c->d_ranges, &c->d_extract, &c->merge_split};
     for (auto& kv : c->graphs) destroy_graph(kv.second);
     c->graphs.clear();
     if (c->h_counts) cudaFreeHost(c->h_counts);
@@ -1472,6 +1649,7 @@ CGB_EXPORT cgb_status cgb_layers_set_transforms(cgb_composition* c, size_t n, co
         l->unchanged = 0;
         std::memcpy(l->t, t, sizeof(l->t));
         std::memcpy(c->layer_recs[id].t, t, sizeof(l->t));
+        mark_raster(c, id);
         c->dirty_lo = std::min(c->dirty_lo, id);
         c->dirty_hi = std::max(c->dirty_hi, id + 1);
     }
@@ -1699,6 +1877,19 @@ CGB_EXPORT cgb_status cgb_get_stats(cgb_composition* c, cgb_stats* out) {
     return CGB_OK;
 }
 
+CGB_EXPORT cgb_status cgb_set_incremental(cgb_composition* c, int enabled) {
+    HANDLE_CHECK();
+    CK(cudaStreamSynchronize(c->stream));
+    c->incremental = enabled != 0;
+    c->resident_valid = false;
+    c->resident_n = 0;
+    c->rast_ids.clear();
+    c->rast_flag.clear();
+    c->rast_order.clear();
+    if (!c->incremental) c->s.release(c->resident);
+    return CGB_OK;
+}
+
 CGB_EXPORT cgb_status cgb_set_graph_mode(cgb_composition* c, int enabled, float headroom) {
     HANDLE_CHECK();
     if (!(headroom >= 0.0f && headroom <= 4.0f)) return fail(CGB_ERR_INVALID_ARG, "graph headroom must be in [0, 4]");
@@ -1802,6 +1993,10 @@ CGB_EXPORT cgb_status cgb_composition_clear(cgb_composition* c) {
     c->dirty_hi = 0;
     c->props_dirty = true;
     for (auto& kv : c->caches) kv.second.tiles = 0;
+    c->resident_valid = false;
+    c->rast_ids.clear();
+    c->rast_flag.clear();
+    c->rast_order.clear();
     return CGB_OK;
 }
 

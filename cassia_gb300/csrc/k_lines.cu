@@ -359,12 +359,13 @@ __global__ void k_build_lines(BatchGeom bg, int cull, LineRec* __restrict__ recs
         // a pixel of margin for rounding) yields only segments the painter
         // never reads, unless the 12-bit tile_j / 13-bit tile_i fields could
         // wrap back into the canvas (|y| >= 16,384 px, x >= 30,720 px).
-        bool off_canvas = false;
-        if (cull) {
+        // incremental frames: only the lines of changed layers (by order)
+        bool off_canvas = cull && S.rast_dirty && !S.rast_dirty[order];
+        if (cull && !off_canvas) {
             const int32_t ymin = min(p0y_sub, p1y_sub), ymax = max(p0y_sub, p1y_sub);
             const int32_t xmin = min(p0x_sub, p1x_sub), xmax = max(p0x_sub, p1x_sub);
             const int32_t lim_y = 16384 * PIXEL_WIDTH, lim_x = 30720 * PIXEL_WIDTH;
-            off_canvas = (ymax < -PIXEL_WIDTH && ymin > -lim_y) ||
+            off_canvas = off_canvas || (ymax < -PIXEL_WIDTH && ymin > -lim_y) ||
                          (ymin >= (int32_t)(S.rows * 8 + 1) * PIXEL_WIDTH && ymax < lim_y) ||
                          (xmin >= (int32_t)(S.row_len * 8 + 1) * PIXEL_WIDTH && xmax < lim_x);
         }

@@ -299,6 +299,16 @@ CGB_EXPORT cgb_status cgb_get_stats(cgb_composition* c, cgb_stats* out);
  * then captured anew.  Pixels are identical in both forms.  Up to 32
  * geometries are kept per handle (cgb_render_batch groups included). */
 CGB_EXPORT cgb_status cgb_set_graph_mode(cgb_composition* c, int enabled, float headroom);
+/* Incremental frames (replaces the full re-rasterization of every frame in
+ * mold's Composition::render, mold/src/composition.rs:212-329).  With
+ * enabled != 0 the handle keeps the sorted segments of its last frame on the
+ * device; the next frame on the same canvas rasterizes and sorts only the
+ * lines of layers whose geometry changed since (transform, enabled, order,
+ * inserted lines, removal), drops those layers' old segments and merges the
+ * rest back in.  Pixels are identical to a full frame.  Works for cgb_render
+ * and for the compositions of cgb_render_batch; such frames are staged (no
+ * frame graph).  Costs 8 bytes of device memory per segment of the frame. */
+CGB_EXPORT cgb_status cgb_set_incremental(cgb_composition* c, int enabled);
 CGB_EXPORT cgb_status cgb_set_tuning(cgb_composition* c, const cgb_tuning* tuning);
 CGB_EXPORT cgb_status cgb_get_tuning(cgb_composition* c, cgb_tuning* out);
 
