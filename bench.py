@@ -374,8 +374,10 @@ def run_serve(args, rank, world, local):
     """Serving workload: 64 clients with resident compositions (batched-workload
     distribution), Poisson arrivals at 2,000 requests/s; each frame gives 20%
     of a client's layers a new affine and adds/removes 1%.  Continuous
-    batching (2 workers, batches of up to 16, 40 GB HBM budget) against the
-    plain loop (one render call per request), on identical request streams.
+    batching (2 workers, batches of up to 16, 40 GB HBM budget) of
+    incremental frames (each client's sorted segments stay resident; only
+    changed layers are rasterized) against the plain loop (one full render
+    call per request), on identical request streams.
     The offered rate saturates the server (its latency then grows with the
     run), so the batched server is also run at 75% of the throughput it
     reached ("sustained": p50/p99 of a server that keeps up)."""
@@ -393,7 +395,10 @@ def run_serve(args, rank, world, local):
             # offered rate: latency of a server that keeps up with its load
             rate = 0.75 * out["batched"]["frames_per_s"]
             reqs = serving.poisson_arrivals(rate, w["n_clients"], w["duration"], seed=w["seed"] + rank + 1)
-        clients = serving.make_clients(w["n_clients"], seed=w["seed"] + rank, device_out=True)
+        # the served form keeps each client's segments resident and
+        # re-rasterizes only changed layers; the plain loop re-renders in full
+        clients = serving.make_clients(w["n_clients"], seed=w["seed"] + rank, device_out=True,
+                                       incremental=mode != "plain")
         srv = serving.Server(clients, mode="plain" if mode == "plain" else "batched", workers=2, max_batch=16,
                              hbm_budget=40e9)
         l0 = kernel_launches()
@@ -427,7 +432,8 @@ def run_serve(args, rank, world, local):
             "steps": b["requests"], "warmup": 0, "ms_per_step": 1e3 / b["frames_per_s"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+int (fixed point)", "data": "synthetic (seeded)",
             "config": {"workload": args.workload, "clients": w["n_clients"], "offered_rate": w["rate"],
-                       "duration_s": w["duration"], "hbm_budget_gb": 40, "max_batch": 16, "workers": 2},
+                       "duration_s": w["duration"], "hbm_budget_gb": 40, "max_batch": 16, "workers": 2,
+                       "served": "continuous batching, incremental frames", "plain": "one full render per request"},
             "p50_ms": b["p50_ms"], "p99_ms": b["p99_ms"], "batched": b, "plain": p,
             "sustained": {k: out["sustained"][k] for k in ("offered_rate", "frames_per_s", "p50_ms", "p99_ms",
                                                            "mean_batch")},
@@ -465,6 +471,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="mixed100k", choices=list(WORKLOADS))
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--update-steps", type=int, default=5,
+                    help="frames re-transforming 20%% of the layers, full vs incremental (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quiet", action="store_true")
     ap.add_argument("--frame-mode", default="graph", choices=["staged", "graph"],
@@ -583,6 +591,52 @@ def main():
         e2e = {"value": world * segs / e2e_s / 1e6, "unit": "Msegments/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": W * H * 4, "ms_per_step": e2e_s * 1e3}
 
+    # Frames that give 20% of the layers a new affine (the serving workload's
+    # update on this scene): every frame in full, replayed from the frame
+    # graph, against incremental frames (only the changed layers rasterized
+    # and sorted, the rest kept resident and merged).  Same seeded updates.
+    updates = None
+    if args.update_steps > 0:
+        ids = np.arange(scene.n_layers, dtype=np.uint32)
+        base = (scene.transforms if scene.transforms is not None
+                else np.tile(np.array([[1, 0, 0, 1, 0, 0]], np.float32), (scene.n_layers, 1))).astype(np.float32)
+
+        def update(k):
+            rng = np.random.default_rng(7000 + k)
+            sel = ids[rng.random(len(ids)) < 0.2]
+            t = base[sel].copy()
+            th = rng.uniform(-0.05, 0.05, len(sel)).astype(np.float32)
+            c, s_ = np.cos(th), np.sin(th)
+            a, b, cc, d = t[:, 0].copy(), t[:, 1].copy(), t[:, 2].copy(), t[:, 3].copy()
+            t[:, 0], t[:, 1], t[:, 2], t[:, 3] = c * a - s_ * cc, c * b - s_ * d, s_ * a + c * cc, s_ * b + c * d
+            t[:, 4] += rng.uniform(-3, 3, len(sel)).astype(np.float32)
+            t[:, 5] += rng.uniform(-3, 3, len(sel)).astype(np.float32)
+            base[sel] = t
+            comp.set_transforms(sel, t)
+
+        updates = {"changed_fraction": 0.2, "steps": args.update_steps}
+        start = base.copy()
+        for mode in ("full", "incremental"):
+            base[:] = start
+            comp.set_transforms(ids, base)
+            comp.set_incremental(mode == "incremental")
+            comp.render(out.data_ptr(), W, scene.background, height=H)  # the first frame of the mode
+            torch.cuda.synchronize()
+            ms, dev = [], []
+            for k in range(1, args.update_steps + 1):
+                update(k)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                comp.render(out.data_ptr(), W, scene.background, height=H)
+                ms.append((time.perf_counter() - t0) * 1e3)
+                st_k = comp.stats()
+                dev.append(st_k["total_ms"])
+            updates[mode] = {"ms_per_frame": statistics.mean(ms), "device_ms_per_frame": statistics.mean(dev),
+                             "segments_rasterized": int(st_k["segments"]),
+                             "graph_replayed": int(st_k["graph_replayed"])}
+        comp.set_incremental(False)
+        updates["speedup"] = updates["full"]["ms_per_frame"] / updates["incremental"]["ms_per_frame"]
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
@@ -617,6 +671,7 @@ def main():
                                "frac": frame_bytes / (ms_step / 1e3) / 1e9 / peak},
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "update_frames": updates,
             "gpu_launches": launches,
             "clocks": clk.summary(),
             "setup_s": {"scene_gen": gen_s, "load_insert_paths": load_s},

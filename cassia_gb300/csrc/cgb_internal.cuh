@@ -263,10 +263,12 @@ cudaError_t launch_build_lines(const BatchGeom& bg, int cull, LineRec* recs, uin
 // and their count at run_count[b]; *produced (zeroed by the caller)
 // accumulates all segments, kept or not.
 // With fc, n_steps is the capacity and the step count is fc->n[FC_STEPS].
+// sparse: most lines have length 0 (an incremental frame); their runs are
+// searched instead of walked.
 cudaError_t launch_rasterize(int render, const BatchGeom& bg, const LineRec* recs, const uint32_t* step_off,
                              uint32_t n_lines, uint64_t n_steps, uint32_t block, uint32_t items, uint64_t* runs,
                              uint32_t* run_count, unsigned long long* produced, cudaStream_t st,
-                             FrameCounts* fc = nullptr);
+                             FrameCounts* fc = nullptr, bool sparse = false);
 uint32_t raster_run_slots(uint32_t block, uint32_t items);
 // Keys n reference CompactSegments (cassia_render's input) of scene 0 into
 // runs of import_run_slots() slots per block, as launch_rasterize does.
@@ -310,8 +312,9 @@ cudaError_t radix_gather_hist(const uint64_t* runs, uint32_t run_slots, const ui
                               int digit_bits, Scratch* s, cudaStream_t st, uint32_t out_cap = 0xFFFFFFFFu);
 
 // k_incr.cu: incremental frames
-// Local key layout of a composition's resident segments (bits 22..63):
-// tile row (12 bits) | order (17) | tile column + 1 (13).
+// Local key layout of a composition's resident segments after a batched
+// frame (bits 22..63): tile row (12 bits) | order (17) | tile column + 1 (13).
+// After a frame of the composition alone they stay in that frame's layout.
 constexpr int LOCAL_ORDER_BITS = 17;
 constexpr int LOCAL_COL_BITS = 13;
 constexpr uint32_t LOCAL_MAX_ROWS = 1u << (42 - LOCAL_ORDER_BITS - LOCAL_COL_BITS);
@@ -323,6 +326,7 @@ struct KeepSource {
     const uint8_t* dirty;  // by order: 1 = the order's segments are rasterized again
     uint32_t n_dirty;
     uint32_t row_base;     // the scene's first tile row in the frame
+    uint32_t order_bits, col_bits;  // the key layout the resident segments are stored in
 };
 // A scene's range of the sorted frame and where its resident copy goes.
 struct ExtractTarget {

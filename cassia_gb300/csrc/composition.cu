@@ -229,6 +229,7 @@ struct cgb_composition {
     DevBuf d_rast_dirty;              // by order (max_ids bytes): 1 = rasterize again
     DevBuf resident;                  // sorted segments of the last frame, local key layout
     uint64_t resident_n = 0;
+    uint32_t resident_ob = LOCAL_ORDER_BITS, resident_cb = LOCAL_COL_BITS;  // its key layout
     bool resident_valid = false;
     uint32_t resident_rows = 0, resident_row_len = 0;
     // frame-level buffers of an incremental frame (on the handle that renders it)
@@ -635,7 +636,7 @@ cudaError_t stage_mark(cgb_composition* c, int k, cudaStream_t st, const char* n
 // *keys (segs_b; segs_a is free for the sort) with the digit histogram of the
 // sort by bits [sort_lo, sort_hi) counted.
 cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& bg, int sort_lo, int sort_hi,
-                               uint64_t* n_segs, uint64_t* n_total, uint64_t** keys) {
+                               uint64_t* n_segs, uint64_t* n_total, uint64_t** keys, bool sparse = false) {
     cudaStream_t st = c->stream;
     if (bg.total_lines >= (1ull << 32)) return fail(CGB_ERR_LAYER_LIMIT, "more than 2^32 lines in a frame");
     const uint32_t L = (uint32_t)bg.total_lines;
@@ -661,7 +662,7 @@ cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& 
     CK(cudaMemsetAsync(c->rlb.p, 0, 8, st));
     unsigned long long* produced = c->rlb.as<unsigned long long>();
     CK(launch_rasterize(render, bg, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, S, block, items,
-                        c->segs_a.as<uint64_t>(), c->bcounts.as<uint32_t>(), produced, st));
+                        c->segs_a.as<uint64_t>(), c->bcounts.as<uint32_t>(), produced, st, nullptr, sparse));
     CK(cudaMemcpyAsync(&c->s.pinned[3], produced, 8, cudaMemcpyDeviceToHost, st));
     uint64_t P = 0;
     if (grid) CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid, &c->s, st, &P));
@@ -905,7 +906,7 @@ cgb_status incremental_merge(cgb_composition* c, const FrameSetup& f, std::vecto
         if (in.incr != 2 || in.comp->resident_n == 0) continue;
         const cgb_composition* sc = in.comp;
         src.push_back(KeepSource{sc->resident.as<uint64_t>(), total, sc->resident_n, sc->d_rast_dirty.as<uint8_t>(),
-                                 sc->max_ids, in.d.row_base});
+                                 sc->max_ids, in.d.row_base, sc->resident_ob, sc->resident_cb});
         total += sc->resident_n;
     }
     if (src.size() > MAX_KEEP_SOURCES) return fail(CGB_ERR_INVALID_ARG, "incremental frame: too many scenes");
@@ -931,6 +932,23 @@ cgb_status incremental_merge(cgb_composition* c, const FrameSetup& f, std::vecto
             *sorted = c->segs_m.as<uint64_t>();
             *P += K;
         }
+    }
+    // A frame of one composition on its own handle: its sorted segments are
+    // kept as they are, in this frame's key layout.
+    if (scenes.size() == 1 && scenes[0].incr && scenes[0].comp == c) {
+        if (*sorted == c->segs_m.as<uint64_t>()) {
+            std::swap(c->resident, c->segs_m);
+        } else {
+            CK(c->s.ensure(c->resident, std::max<uint64_t>(*P, 1) * 8));
+            if (*P) CK(cudaMemcpyAsync(c->resident.p, *sorted, *P * 8, cudaMemcpyDeviceToDevice, st));
+        }
+        c->resident_n = *P;
+        c->resident_ob = bg.order_bits;
+        c->resident_cb = bg.col_bits;
+        c->resident_valid = true;
+        c->resident_rows = scenes[0].d.rows;
+        c->resident_row_len = scenes[0].d.row_len;
+        return CGB_OK;
     }
     // the frame's segments of each incremental scene become its resident ones
     std::vector<uint32_t> ids;
@@ -963,6 +981,8 @@ cgb_status incremental_merge(cgb_composition* c, const FrameSetup& f, std::vecto
                                    in.d.row_base});
         n_all += n;
         sc->resident_n = n;
+        sc->resident_ob = LOCAL_ORDER_BITS;
+        sc->resident_cb = LOCAL_COL_BITS;
         sc->resident_valid = true;
         sc->resident_rows = in.d.rows;
         sc->resident_row_len = in.d.row_len;
@@ -985,8 +1005,10 @@ cgb_status staged_frame(cgb_composition* c, const FrameSetup& f, std::vector<Sce
     const uint64_t tiles = f.tiles;
     uint64_t P = 0, PT = 0;
     uint64_t* keys = nullptr;
+    bool sparse = false;  // some scene rasterizes only its changed layers
+    for (const SceneInput& in : scenes) sparse |= in.incr == 2;
     cgb_status s2 = c->import_segs ? import_segments(c, bg, 22, 22 + (int)bg.key_bits, &P, &PT, &keys)
-                                   : build_and_rasterize(c, 1, bg, 22, 22 + (int)bg.key_bits, &P, &PT, &keys);
+                                   : build_and_rasterize(c, 1, bg, 22, 22 + (int)bg.key_bits, &P, &PT, &keys, sparse);
     if (s2) return s2;
     c->stats.painted_segments = P;
     // sort by (global row, order, tile column)

@@ -1,18 +1,20 @@
 // Incremental frames: re-rasterize only the layers whose geometry changed.
 //
 // A composition in incremental mode keeps the sorted segments of its last
-// frame on the device ("resident" segments) in a fixed local key layout:
-// bits 22..63 of each segment = row:12 | order:17 | tile column + 1:13 (the
-// render key of the composition alone, with the widest fields).  The next
+// frame on the device ("resident" segments): after a frame of its own, that
+// frame's sorted segments as they are (a buffer swap); after a batched
+// frame, its range of the batch re-keyed to a fixed local layout, bits
+// 22..63 = row:12 | order:17 | tile column + 1:13.  The next
 // frame rasterizes only the lines of changed layers (their orders are marked
 // dirty; a layer whose order changed marks both orders), sorts those
 // segments, keeps the resident segments of clean orders, re-keys them into
 // the frame's key space and merges the two sorted streams.  Keys of one
 // order never come from both streams, so the merge needs no tie rule beyond
 // "kept first"; within one tile-layer group the order of segments does not
-// change any pixel (their areas and covers are summed).  Afterwards each
-// composition's range of the merged frame (its tile rows) is copied back,
-// re-keyed to the local layout, as its new resident segments.
+// change any pixel (their areas and covers are summed).  Afterwards the
+// merged frame is the composition's new resident segments (a frame of its
+// own), or each composition's range of it (its tile rows) is copied back,
+// re-keyed to the local layout (a batched frame).
 //
 // In a batch, scenes occupy disjoint, increasing row ranges of the frame key,
 // so the kept segments of all scenes, taken scene after scene, are already
@@ -56,9 +58,9 @@ __device__ __forceinline__ uint32_t keep_source(const KeepSource* s, uint32_t n,
 // and its key re-packed into the frame's layout.
 __device__ __forceinline__ bool keep_segment(const KeepSource& src, const BatchGeom& bg, uint64_t v, uint64_t* out) {
     const uint64_t k = v >> 22;
-    const uint32_t col1 = (uint32_t)(k & ((1u << LOCAL_COL_BITS) - 1));
-    const uint32_t order = (uint32_t)((k >> LOCAL_COL_BITS) & ((1u << LOCAL_ORDER_BITS) - 1));
-    const uint32_t row = (uint32_t)(k >> (LOCAL_ORDER_BITS + LOCAL_COL_BITS));
+    const uint32_t col1 = (uint32_t)(k & ((1ull << src.col_bits) - 1));
+    const uint32_t order = (uint32_t)((k >> src.col_bits) & ((1ull << src.order_bits) - 1));
+    const uint32_t row = (uint32_t)(k >> (src.order_bits + src.col_bits));
     if (order >= src.n_dirty || src.dirty[order]) return false;
     *out = (make_render_key(bg, src.row_base + row, order, col1) << 22) | (v & 0x3FFFFFull);
     return true;
@@ -79,16 +81,37 @@ __global__ void __launch_bounds__(KEEP_THREADS) k_keep(const KeepSource* __restr
     uint32_t keep = 0, cnt = 0;
     if (g0 < total) {
         uint32_t si = keep_source(s_src, n_srcs, g0);
+        const KeepSource& s0 = s_src[si];
+        const uint64_t i0 = g0 - s0.start;
+        const uint64_t* p0 = s0.seg + i0;
+        if (i0 + KEEP_ITEMS <= s0.n && (((uintptr_t)p0) & 15) == 0) {
+            // the thread's segments lie in one source: 16-byte pairs
+            uint64_t v[KEEP_ITEMS];
+            const ulonglong2* p2 = reinterpret_cast<const ulonglong2*>(p0);
 #pragma unroll
-        for (int k = 0; k < KEEP_ITEMS; k++) {
-            const uint64_t g = g0 + k;
-            if (g >= total) break;
-            while (si + 1 < n_srcs && s_src[si + 1].start <= g) si++;
-            const KeepSource& src = s_src[si];
-            const uint64_t i = g - src.start;
-            if (i < src.n && keep_segment(src, bg, src.seg[i], &keys[k])) {
-                keep |= 1u << k;
-                cnt++;
+            for (int k = 0; k < KEEP_ITEMS / 2; k++) {
+                const ulonglong2 w = p2[k];
+                v[2 * k] = w.x;
+                v[2 * k + 1] = w.y;
+            }
+#pragma unroll
+            for (int k = 0; k < KEEP_ITEMS; k++)
+                if (keep_segment(s0, bg, v[k], &keys[k])) {
+                    keep |= 1u << k;
+                    cnt++;
+                }
+        } else {
+#pragma unroll
+            for (int k = 0; k < KEEP_ITEMS; k++) {
+                const uint64_t g = g0 + k;
+                if (g >= total) break;
+                while (si + 1 < n_srcs && s_src[si + 1].start <= g) si++;
+                const KeepSource& src = s_src[si];
+                const uint64_t i = g - src.start;
+                if (i < src.n && keep_segment(src, bg, src.seg[i], &keys[k])) {
+                    keep |= 1u << k;
+                    cnt++;
+                }
             }
         }
     }

@@ -528,7 +528,7 @@ __device__ __forceinline__ uint32_t find_line(const uint32_t* __restrict__ off, 
 // 2 * RASTER_ITEMS * blockDim.x slots (a step yields at most two segments);
 // run_count[block] receives how many.  No block waits on another: a later
 // gather (fused with the sort's digit histogram) packs the runs.
-template <int RENDER, int RASTER_ITEMS>
+template <int RENDER, int RASTER_ITEMS, bool SPARSE>
 __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ recs, const uint32_t* __restrict__ off,
                                                    uint32_t n_lines, uint64_t n_steps, BatchGeom bg,
                                                    uint64_t* __restrict__ runs, uint32_t* __restrict__ run_count,
@@ -566,6 +566,14 @@ __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ r
                 else hi = mid;
             }
             l = l0 + lo;
+        } else if (SPARSE) {  // the block's lines l0..l1 do not fit the stage: search them in place
+            uint32_t lo = l0, hi = l0 + nl;
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if ((uint64_t)off[mid] <= s0) lo = mid;
+                else hi = mid;
+            }
+            l = lo;
         } else {
             l = find_line(off, n_lines, s0);
         }
@@ -579,12 +587,30 @@ __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ r
             uint64_t s = s0 + k;
             if (s < n_steps) {
                 if (s >= next) {
-                    // the next line with steps (lines culled to length 0 are passed over)
-                    do {
+                    // the next line with steps: usually the next line; lines of
+                    // length 0 (culled) are passed over one by one, except in
+                    // incremental frames (SPARSE: most lines belong to unchanged
+                    // layers and have length 0), which search the block's range,
+                    // off[l] <= s < off[l0 + nl]
+                    l++;
+                    cur = next;
+                    next = staged ? s_off[l - l0 + 1] : off[l + 1];
+                    while (!SPARSE && s >= next) {
                         l++;
                         cur = next;
                         next = staged ? s_off[l - l0 + 1] : off[l + 1];
-                    } while (s >= next);
+                    }
+                    if (SPARSE && s >= next) {
+                        uint32_t lo = l + 1, hi = l0 + nl;
+                        while (hi - lo > 1) {
+                            const uint32_t mid = (lo + hi) >> 1;
+                            if ((uint64_t)(staged ? s_off[mid - l0] : off[mid]) <= s) lo = mid;
+                            else hi = mid;
+                        }
+                        l = lo;
+                        cur = staged ? s_off[l - l0] : off[l];
+                        next = staged ? s_off[l - l0 + 1] : off[l + 1];
+                    }
                     rec = recs[l];
                     if ((rec.order_octant >> LINE_SCENE_SHIFT) != sc) {
                         sc = rec.order_octant >> LINE_SCENE_SHIFT;
@@ -780,24 +806,26 @@ cudaError_t launch_build_lines(const BatchGeom& bg, int cull, LineRec* recs, uin
 cudaError_t launch_rasterize(int render, const BatchGeom& bg, const LineRec* recs, const uint32_t* step_off,
                              uint32_t n_lines, uint64_t n_steps, uint32_t block, uint32_t items, uint64_t* runs,
                              uint32_t* run_count, unsigned long long* produced, cudaStream_t st,
-                             FrameCounts* fc) {
+                             FrameCounts* fc, bool sparse) {
     if (n_steps == 0) return cudaSuccess;
     if (fc && n_steps >= (1ull << 32)) return cudaErrorInvalidValue;
     if (block == 0 || block % 32 || block > 256 || (items != 4 && items != 8)) return cudaErrorInvalidValue;
     const uint32_t grid = raster_grid(n_steps, block, items);
     const size_t smem = (size_t)raster_run_slots(block, items) * sizeof(uint64_t);
     count_launches(1);
-    if (render) {
-        if (items == 4)
-            k_rasterize<1, 4><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced, fc);
-        else
-            k_rasterize<1, 8><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced, fc);
+#define CGB_RASTER(R, I, S) \
+    k_rasterize<R, I, S><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced, fc)
+    if (render && sparse) {
+        if (items == 4) CGB_RASTER(1, 4, true);
+        else CGB_RASTER(1, 8, true);
+    } else if (render) {
+        if (items == 4) CGB_RASTER(1, 4, false);
+        else CGB_RASTER(1, 8, false);
     } else {
-        if (items == 4)
-            k_rasterize<0, 4><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced, fc);
-        else
-            k_rasterize<0, 8><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced, fc);
+        if (items == 4) CGB_RASTER(0, 4, false);
+        else CGB_RASTER(0, 8, false);
     }
+#undef CGB_RASTER
     return cudaGetLastError();
 }
 

@@ -65,8 +65,11 @@ def poisson_arrivals(rate: float, n_clients: int, duration: float, seed: int = 0
     return out
 
 
-def make_clients(n_clients: int, seed: int, device_out: bool = True, max_layers: int = 50_000):
-    """Clients with compositions drawn from the batched-workload distribution."""
+def make_clients(n_clients: int, seed: int, device_out: bool = True, max_layers: int = 50_000,
+                 incremental: bool = False):
+    """Clients with compositions drawn from the batched-workload distribution.
+    incremental: each composition keeps its last frame's sorted segments on
+    the device and re-rasterizes only the layers an update changed."""
     import torch
     sset = scenes.batch(seed=seed, n_scenes=n_clients, max_layers=max_layers)
     clients = []
@@ -76,6 +79,8 @@ def make_clients(n_clients: int, seed: int, device_out: bool = True, max_layers:
         # clients use the widened 17-bit layer format
         c = Composition(wide=sc.wide or sc.n_layers > 30_000, priority="high")
         scenes.load(sc, c)
+        if incremental:
+            c.set_incremental(True)
         if device_out:
             out = torch.zeros((sc.height, sc.width, 4), dtype=torch.uint8, device="cuda")
         else:

@@ -25,11 +25,11 @@ def _oracle_replay(cl, client_id, last_seq):
     return img
 
 
-@pytest.mark.parametrize("mode", ["batched", "plain"])
-def test_server_results_match_alone_and_oracle(gpu_lib, mode):
+@pytest.mark.parametrize("mode,incremental", [("batched", False), ("plain", False), ("batched", True)])
+def test_server_results_match_alone_and_oracle(gpu_lib, mode, incremental):
     import torch
     from cassia_gb300 import serving
-    clients = serving.make_clients(6, seed=42, device_out=True, max_layers=400)
+    clients = serving.make_clients(6, seed=42, device_out=True, max_layers=400, incremental=incremental)
     reqs = serving.poisson_arrivals(rate=400.0, n_clients=len(clients), duration=0.25, seed=1)
     srv = serving.Server(clients, mode=mode, workers=2, max_batch=4)
     done = srv.run(reqs)
