@@ -111,18 +111,27 @@ struct PinnedAllocator {
             cudaGetLastError();
             p = std::malloc(n * sizeof(T));
             if (!p) throw std::bad_alloc();
+            std::lock_guard<std::mutex> lock(registry_mutex());
             pageable().insert(p);
         }
         return static_cast<T*>(p);
     }
     void deallocate(T* p, size_t) {
-        auto it = pageable().find(p);
-        if (it != pageable().end()) {
-            pageable().erase(it);
-            std::free(p);
-        } else {
-            cudaFreeHost(p);
+        bool was_pageable = false;
+        {
+            std::lock_guard<std::mutex> lock(registry_mutex());
+            auto it = pageable().find(p);
+            if (it != pageable().end()) {
+                pageable().erase(it);
+                was_pageable = true;
+            }
         }
+        if (was_pageable) std::free(p);
+        else cudaFreeHost(p);
+    }
+    static std::mutex& registry_mutex() {  // handles are used from several threads
+        static std::mutex m;
+        return m;
     }
     static std::set<void*>& pageable() {
         static std::set<void*> s;
@@ -225,7 +234,7 @@ struct cgb_composition {
     std::vector<uint32_t> rast_ids;   // layers whose geometry changed since the last frame
     std::vector<uint8_t> rast_flag;   // by id: listed in rast_ids
     std::vector<int32_t> rast_order;  // by id: the order its resident segments carry, -1 none
-    std::vector<uint8_t> h_rast_dirty;
+    std::vector<uint8_t, PinnedAllocator<uint8_t>> h_rast_dirty;  // uploaded asynchronously
     DevBuf d_rast_dirty;              // by order (max_ids bytes): 1 = rasterize again
     DevBuf resident;                  // sorted segments of the last frame, local key layout
     uint64_t resident_n = 0;
@@ -778,8 +787,9 @@ cgb_status prepare_incremental(cgb_composition* c, SceneInput& in) {
     }
     c->rast_ids.clear();
     CK(c->s.ensure(c->d_rast_dirty, c->max_ids));
+    // pinned source, rewritten only by the next frame (every render returns
+    // after its frame is done)
     CK(cudaMemcpyAsync(c->d_rast_dirty.p, c->h_rast_dirty.data(), c->max_ids, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
     in.d.rast_dirty = c->d_rast_dirty.as<uint8_t>();
     in.incr = 2;
     return CGB_OK;
@@ -1651,6 +1661,7 @@ CGB_EXPORT cgb_status cgb_layers_set_transforms(cgb_composition* c, size_t n, co
                                                 const float* affine6, uint32_t flags) {
     if (!c || (n && (!layer_ids || !affine6))) return fail(CGB_ERR_INVALID_ARG, "null argument");
     const bool check = !(flags & CGB_TRANSFORM_UNCHECKED);
+    const bool incremental = c->incremental;
     for (size_t i = 0; i < n; i++) {
         const uint32_t id = layer_ids[i];
         const float* t = affine6 + 6 * i;
@@ -1671,7 +1682,7 @@ CGB_EXPORT cgb_status cgb_layers_set_transforms(cgb_composition* c, size_t n, co
         l->unchanged = 0;
         std::memcpy(l->t, t, sizeof(l->t));
         std::memcpy(c->layer_recs[id].t, t, sizeof(l->t));
-        mark_raster(c, id);
+        if (incremental) mark_raster(c, id);
         c->dirty_lo = std::min(c->dirty_lo, id);
         c->dirty_hi = std::max(c->dirty_hi, id + 1);
     }
