@@ -472,7 +472,7 @@ def main():
     ap.add_argument("--workload", default="mixed100k", choices=list(WORKLOADS))
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--update-steps", type=int, default=5,
-                    help="frames re-transforming 20%% of the layers, full vs incremental (0: skip)")
+                    help="frames re-transforming 20%% / 5%% of the layers, full vs incremental (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quiet", action="store_true")
     ap.add_argument("--frame-mode", default="graph", choices=["staged", "graph"],
@@ -591,19 +591,19 @@ def main():
         e2e = {"value": world * segs / e2e_s / 1e6, "unit": "Msegments/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": W * H * 4, "ms_per_step": e2e_s * 1e3}
 
-    # Frames that give 20% of the layers a new affine (the serving workload's
-    # update on this scene): every frame in full, replayed from the frame
-    # graph, against incremental frames (only the changed layers rasterized
-    # and sorted, the rest kept resident and merged).  Same seeded updates.
+    # Frames that give 20% (the serving workload's update) or 5% of the
+    # layers a new affine: every frame in full, replayed from the frame graph,
+    # against incremental frames (only the changed layers rasterized and
+    # sorted, the rest kept resident and merged).  Same seeded updates.
     updates = None
     if args.update_steps > 0:
         ids = np.arange(scene.n_layers, dtype=np.uint32)
         base = (scene.transforms if scene.transforms is not None
                 else np.tile(np.array([[1, 0, 0, 1, 0, 0]], np.float32), (scene.n_layers, 1))).astype(np.float32)
 
-        def update(k):
+        def update(k, frac):
             rng = np.random.default_rng(7000 + k)
-            sel = ids[rng.random(len(ids)) < 0.2]
+            sel = ids[rng.random(len(ids)) < frac]
             t = base[sel].copy()
             th = rng.uniform(-0.05, 0.05, len(sel)).astype(np.float32)
             c, s_ = np.cos(th), np.sin(th)
@@ -614,28 +614,31 @@ def main():
             base[sel] = t
             comp.set_transforms(sel, t)
 
-        updates = {"changed_fraction": 0.2, "steps": args.update_steps}
+        updates = {"steps": args.update_steps}
         start = base.copy()
-        for mode in ("full", "incremental"):
-            base[:] = start
-            comp.set_transforms(ids, base)
-            comp.set_incremental(mode == "incremental")
-            comp.render(out.data_ptr(), W, scene.background, height=H)  # the first frame of the mode
-            torch.cuda.synchronize()
-            ms, dev = [], []
-            for k in range(1, args.update_steps + 1):
-                update(k)
+        for frac in (0.2, 0.05):
+            res = {}
+            for mode in ("full", "incremental"):
+                base[:] = start
+                comp.set_transforms(ids, base)
+                comp.set_incremental(mode == "incremental")
+                comp.render(out.data_ptr(), W, scene.background, height=H)  # the first frame of the mode
                 torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                comp.render(out.data_ptr(), W, scene.background, height=H)
-                ms.append((time.perf_counter() - t0) * 1e3)
-                st_k = comp.stats()
-                dev.append(st_k["total_ms"])
-            updates[mode] = {"ms_per_frame": statistics.mean(ms), "device_ms_per_frame": statistics.mean(dev),
+                ms, dev = [], []
+                for k in range(1, args.update_steps + 1):
+                    update(k, frac)
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    comp.render(out.data_ptr(), W, scene.background, height=H)
+                    ms.append((time.perf_counter() - t0) * 1e3)
+                    st_k = comp.stats()
+                    dev.append(st_k["total_ms"])
+                res[mode] = {"ms_per_frame": statistics.mean(ms), "device_ms_per_frame": statistics.mean(dev),
                              "segments_rasterized": int(st_k["segments"]),
                              "graph_replayed": int(st_k["graph_replayed"])}
+            res["speedup"] = res["full"]["ms_per_frame"] / res["incremental"]["ms_per_frame"]
+            updates[f"changed_{int(frac * 100)}pct"] = res
         comp.set_incremental(False)
-        updates["speedup"] = updates["full"]["ms_per_frame"] / updates["incremental"]["ms_per_frame"]
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
