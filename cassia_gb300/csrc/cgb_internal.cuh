@@ -208,7 +208,6 @@ struct DevBuf {
     T* as() const { return (T*)p; }
 };
 
-// Device scratch shared by the stages of one composition handle.
 // Counts of a frame kept on the device (graph frames).  The scans write S
 // (pixel steps), P (painted segments), G (tile-layer groups) and W (work
 // items) here instead of returning them to the host, and every kernel that
@@ -233,6 +232,7 @@ __device__ __forceinline__ uint32_t fc_count(FrameCounts* fc, int k, uint32_t ca
     return cap;
 }
 
+// Device scratch shared by the stages of one composition handle.
 struct Scratch {
     size_t budget = 0;  // 0 = unlimited
     size_t used = 0;    // bytes held by all DevBufs of the handle

@@ -311,8 +311,6 @@ cudaError_t grow_keep(cgb_composition* c, DevBuf& b, size_t bytes, size_t keep) 
     if (bytes <= b.cap) return cudaSuccess;
     DevBuf nb;
     size_t want = std::max(bytes, b.cap * 2);
-    Scratch tmp = c->s;
-    (void)tmp;
     cudaError_t e = c->s.ensure(nb, want);
     if (e != cudaSuccess) {
         e = c->s.ensure(nb, bytes);
@@ -639,11 +637,10 @@ cudaError_t stage_mark(cgb_composition* c, int k, cudaStream_t st, const char* n
 }
 
 // LinesBuilder::build + Rasterizer::rasterize (+ re-keying / culling in
-// render mode) over every scene of the frame.  Leaves n_segs keys in segs_a.
-// LinesBuilder::build + Rasterizer::rasterize (+ re-keying / culling in
 // render mode) over every scene of the frame.  Leaves n_segs keys packed at
 // *keys (segs_b; segs_a is free for the sort) with the digit histogram of the
-// sort by bits [sort_lo, sort_hi) counted.
+// sort by bits [sort_lo, sort_hi) counted.  sparse: only changed layers'
+// lines have steps (an incremental frame).
 cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& bg, int sort_lo, int sort_hi,
                                uint64_t* n_segs, uint64_t* n_total, uint64_t** keys, bool sparse = false) {
     cudaStream_t st = c->stream;

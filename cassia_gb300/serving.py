@@ -17,7 +17,7 @@ call at a time for comparison.
 import collections
 import threading
 import time
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 from typing import Dict, List, Optional
 
 import numpy as np

@@ -3,7 +3,6 @@ the oracle (tests/golden/golden.json): for config 1 (1,000 circles), config
 2a (65,535 layers, 2560x1600), config 2 (100,000 layers, widened format)
 and config 3 (50,000 glyph layers, 3840x2160), the canonical pixel segments
 (count, NONE slots, SHA-256) and the RGBA8 frame (SHA-256) are bit-exact."""
-import numpy as np
 import pytest
 
 from tests.golden import make_golden

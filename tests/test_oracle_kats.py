@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import oracle
-from cassia_gb300.types import BlendMode, FillRule, Gradient, GradientType, Path, Point, Props, Style, solid
+from cassia_gb300.types import BlendMode, FillRule, Gradient, GradientType, Path, Props, Style, solid
 
 F32_EPS = np.float32(np.finfo(np.float32).eps)
 
