@@ -374,7 +374,7 @@ def run_serve(args, rank, world, local):
     """Serving workload: 64 clients with resident compositions (batched-workload
     distribution), Poisson arrivals at 2,000 requests/s; each frame gives 20%
     of a client's layers a new affine and adds/removes 1%.  Continuous
-    batching (2 workers, batches of up to 16, 40 GB HBM budget) of
+    batching (3 workers, batches of up to 16, 40 GB HBM budget) of
     incremental frames (each client's sorted segments stay resident; only
     changed layers are rasterized) against the plain loop (one full render
     call per request), on identical request streams.
@@ -399,8 +399,8 @@ def run_serve(args, rank, world, local):
         # re-rasterizes only changed layers; the plain loop re-renders in full
         clients = serving.make_clients(w["n_clients"], seed=w["seed"] + rank, device_out=True,
                                        incremental=mode != "plain")
-        srv = serving.Server(clients, mode="plain" if mode == "plain" else "batched", workers=2, max_batch=16,
-                             hbm_budget=40e9)
+        srv = serving.Server(clients, mode="plain" if mode == "plain" else "batched", workers=args.serve_workers,
+                             max_batch=16, hbm_budget=40e9)
         l0 = kernel_launches()
         with ClockSampler(local) as clk:
             done = srv.run(reqs)
@@ -432,7 +432,7 @@ def run_serve(args, rank, world, local):
             "steps": b["requests"], "warmup": 0, "ms_per_step": 1e3 / b["frames_per_s"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+int (fixed point)", "data": "synthetic (seeded)",
             "config": {"workload": args.workload, "clients": w["n_clients"], "offered_rate": w["rate"],
-                       "duration_s": w["duration"], "hbm_budget_gb": 40, "max_batch": 16, "workers": 2,
+                       "duration_s": w["duration"], "hbm_budget_gb": 40, "max_batch": 16, "workers": args.serve_workers,
                        "served": "continuous batching, incremental frames", "plain": "one full render per request"},
             "p50_ms": b["p50_ms"], "p99_ms": b["p99_ms"], "batched": b, "plain": p,
             "sustained": {k: out["sustained"][k] for k in ("offered_rate", "frames_per_s", "p50_ms", "p99_ms",
@@ -477,6 +477,9 @@ def main():
     ap.add_argument("--quiet", action="store_true")
     ap.add_argument("--frame-mode", default="graph", choices=["staged", "graph"],
                     help="graph: frames replayed from a captured CUDA graph (cgb_set_graph_mode)")
+    ap.add_argument("--serve-workers", type=int, default=3,
+                    help="render workers of the served form (3 measured best: 2 leave the GPU idle during "
+                         "host updates, 4 contend for the interpreter)")
     ap.add_argument("--cpu-budget", type=float, default=150.0,
                     help="seconds of host work the reference arm's samples are sized to")
     args = ap.parse_args()
