@@ -4,13 +4,15 @@ renders every frame bit-exact with a composition that rasterizes everything.
 
 Frames change 20% of the layers' transforms, remove and add layers (the
 serving workload's seeded updates), swap layer orders, disable and re-enable
-layers and change the canvas; single renders, batched renders and the oracle.
+layers and change the canvas; single renders, batched renders and the oracle;
+and with layer caches, crops, gradient fills and clip layers in the painter.
 """
 import numpy as np
 import pytest
 
 import oracle
 from cassia_gb300 import scenes, serving
+from cassia_gb300.types import BlendMode, FillRule, Gradient, Props, Style
 
 pytestmark = pytest.mark.gpu
 
@@ -133,3 +135,35 @@ def test_incremental_batch(gpu_lib, wide):
             _assert_same(outs[k], _render(cr.comp, sc), f"frame {seq}, scene {k}")
             # and the same composition rendered alone, incrementally
             _assert_same(_render(cg.comp, sc), outs[k], f"frame {seq}, scene {k} alone")
+
+
+def test_incremental_with_caches_crops_gradients_and_clips(gpu_lib):
+    sc = scenes.mixed(seed=99, n_layers=1200, width=320, height=200)
+    pool = scenes.mixed(seed=100, n_layers=32, width=320, height=200)
+    cg, cr = _pair(sc, pool)
+    rng = np.random.default_rng(99)
+    kinds = rng.integers(0, 10, size=sc.n_layers)
+    clip_n = rng.integers(1, 12, size=sc.n_layers)
+    grad = Gradient(start=(20.0, 10.0), end=(250.0, 180.0),
+                    stops=[((1.0, 0.2, 0.0, 1.0), None), ((0.0, 0.4, 1.0, 0.6), None)])
+    for cl in (cg, cr):
+        for k in range(sc.n_layers):
+            fr = FillRule(int(sc.fill_rule[k]))
+            mode = BlendMode(int(sc.blend_mode[k]))
+            if kinds[k] == 0:
+                cl.comp.set_props(k, Props(fill_rule=fr, func=int(clip_n[k])))
+            elif kinds[k] == 1:
+                col = tuple(float(v) for v in sc.color[k])
+                cl.comp.set_props(k, Props(fill_rule=fr, func=Style(fill=col, blend_mode=mode, is_clipped=True)))
+            elif kinds[k] == 2:
+                cl.comp.set_props(k, Props(fill_rule=fr, func=Style(fill=grad, blend_mode=mode)))
+    caches = [cl.comp.create_buffer_layer_cache() for cl in (cg, cr)]
+    crop = (24, 290, 16, 170)
+    imgs = [np.zeros((sc.height, sc.width, 4), np.uint8) for _ in range(2)]
+    for seq in range(6):
+        if seq:
+            for cl in (cg, cr):
+                serving.apply_update(cl, 3, seq, changed=0.1, churn=0.02)
+        for cl, cache, img in zip((cg, cr), caches, imgs):
+            cl.comp.render(img, sc.width, sc.background, crop=crop if seq % 2 else None, layer_cache=cache)
+        _assert_same(imgs[0], imgs[1], f"frame {seq}")
