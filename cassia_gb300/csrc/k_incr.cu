@@ -36,7 +36,7 @@ constexpr int KEEP_THREADS = 256;
 constexpr int KEEP_ITEMS = 8;
 constexpr int KEEP_TILE = KEEP_THREADS * KEEP_ITEMS;
 constexpr int MERGE_THREADS = 256;
-constexpr int MERGE_ITEMS = 8;
+constexpr int MERGE_ITEMS = 4;
 constexpr int MERGE_TILE = MERGE_THREADS * MERGE_ITEMS;
 
 __device__ __forceinline__ uint64_t local_key(uint32_t row, uint32_t order, uint32_t col1) {
@@ -137,13 +137,18 @@ __global__ void __launch_bounds__(KEEP_THREADS) k_keep(const KeepSource* __restr
     }
     __syncthreads();
     if (MODE == 0) return;
-    uint64_t o = (uint64_t)block_off[blockIdx.x] + w_sum[warp] + inc - cnt;
+    // the block's kept keys in order in shared memory, then out coalesced
+    __shared__ uint64_t s_keep[KEEP_TILE];
+    uint32_t o = w_sum[warp] + inc - cnt;
 #pragma unroll
     for (int k = 0; k < KEEP_ITEMS; k++)
-        if (keep & (1u << k)) {
-            if (o < out_cap) out[o] = keys[k];
-            o++;
-        }
+        if (keep & (1u << k)) s_keep[o++] = keys[k];
+    __shared__ uint32_t s_total;
+    if (threadIdx.x == KEEP_THREADS - 1) s_total = o;
+    __syncthreads();
+    const uint64_t base = block_off[blockIdx.x];
+    for (uint32_t i = threadIdx.x; i < s_total; i += KEEP_THREADS)
+        if (base + i < out_cap) out[base + i] = s_keep[i];
 }
 
 __device__ __forceinline__ uint64_t mkey(uint64_t v) { return v >> 22; }
