@@ -167,3 +167,25 @@ def test_incremental_with_caches_crops_gradients_and_clips(gpu_lib):
         for cl, cache, img in zip((cg, cr), caches, imgs):
             cl.comp.render(img, sc.width, sc.background, crop=crop if seq % 2 else None, layer_cache=cache)
         _assert_same(imgs[0], imgs[1], f"frame {seq}")
+
+
+def test_incremental_full_size(gpu_lib):
+    """Config 2a (65,535 layers, 2560x1600, ~42M segments per frame): incremental
+    frames equal full frames through seeded transform updates of 20% of the
+    layers (no layers added: the 16-bit format has no free ids left)."""
+    import torch
+    sc = scenes.mixed(seed=2, n_layers=65_535, width=2560, height=1600)
+    pool = scenes.mixed(seed=3, n_layers=256, width=2560, height=1600)
+    cg, cr = _pair(sc, pool)
+    outs = [torch.zeros((sc.height, sc.width, 4), dtype=torch.uint8, device="cuda") for _ in range(2)]
+    for seq in range(4):
+        if seq:
+            for cl in (cg, cr):
+                serving.apply_update(cl, 5, seq, changed=0.2, churn=0.0)
+        for cl, out in zip((cg, cr), outs):
+            cl.comp.render(out.data_ptr(), sc.width, sc.background, height=sc.height)
+        assert torch.equal(outs[0], outs[1]), f"frame {seq}"
+        sg, sr = cg.comp.stats(), cr.comp.stats()
+        assert sg["painted_segments"] == sr["painted_segments"] > 40_000_000
+        if seq:
+            assert sg["segments"] < sr["segments"] // 3
