@@ -639,6 +639,9 @@ def main():
                 comp.set_transforms(ids, base)
                 comp.set_incremental(mode == "incremental")
                 comp.render(out.data_ptr(), W, scene.background, height=H)  # the first frame of the mode
+                for k in (-2, -1):  # untimed update frames: the incremental ones size the sync-free form
+                    update(k, frac)
+                    comp.render(out.data_ptr(), W, scene.background, height=H)
                 torch.cuda.synchronize()
                 ms, dev = [], []
                 for k in range(1, args.update_steps + 1):
@@ -651,7 +654,8 @@ def main():
                     dev.append(st_k["total_ms"])
                 res[mode] = {"ms_per_frame": statistics.mean(ms), "device_ms_per_frame": statistics.mean(dev),
                              "segments_rasterized": int(st_k["segments"]),
-                             "graph_replayed": int(st_k["graph_replayed"])}
+                             "graph_replayed": int(st_k["graph_replayed"]),
+                             "incremental_form": int(st_k["incremental_form"])}
             res["speedup"] = res["full"]["ms_per_frame"] / res["incremental"]["ms_per_frame"]
             updates[f"changed_{int(frac * 100)}pct"] = res
         comp.set_incremental(False)

@@ -104,6 +104,8 @@ class CgbStats(ctypes.Structure):
         ("total_ms", ctypes.c_float),
         ("graph_replayed", ctypes.c_uint32),
         ("graphs_cached", ctypes.c_uint32),
+        ("incremental_form", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
     ]
 
     def as_dict(self):

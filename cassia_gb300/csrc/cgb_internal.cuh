@@ -214,11 +214,13 @@ struct DevBuf {
 // consumes one reads it, clamped to the capacity its buffers were sized for;
 // a count above its capacity sets its bit in `overflow` (the painter then
 // paints nothing and the host renders the frame again with larger buffers).
-enum { FC_STEPS = 0, FC_SEGS = 1, FC_TLS = 2, FC_ITEMS = 3 };
+// Sync-free incremental frames also count the kept resident segments
+// (FC_KEPT) and the new ones (FC_NEW); FC_SEGS is then their merge.
+enum { FC_STEPS = 0, FC_SEGS = 1, FC_TLS = 2, FC_ITEMS = 3, FC_KEPT = 4, FC_NEW = 5 };
 struct FrameCounts {
-    uint32_t n[4];
+    uint32_t n[6];
     uint32_t overflow;
-    uint32_t pad[3];
+    uint32_t pad;
     unsigned long long produced;  // segments the rasterizer produced, kept or not
 };
 
@@ -344,9 +346,11 @@ cudaError_t launch_keep(int mode, const KeepSource* srcs, uint32_t n_srcs, uint6
                         uint32_t* block_count, const uint32_t* block_off, uint64_t* out, uint64_t out_cap,
                         cudaStream_t st);
 // Stable merge of two key-sorted arrays (by bits 22..63; a first on ties);
-// split holds merge_tiles(na + nb) + 1 entries.
+// split holds merge_tiles(na + nb) + 1 entries.  With fc, na and nb are
+// capacities (counts fc->n[FC_KEPT], fc->n[FC_NEW]) and fc->n[FC_SEGS]
+// receives the merged count.
 cudaError_t launch_merge(const uint64_t* a, uint32_t na, const uint64_t* b, uint32_t nb, uint32_t* split,
-                         uint64_t* out, cudaStream_t st);
+                         uint64_t* out, cudaStream_t st, FrameCounts* fc = nullptr);
 // ranges[2k], ranges[2k + 1]: the segments of scene scene_ids[k]'s tile rows in the sorted frame.
 cudaError_t launch_scene_ranges(const uint64_t* segs, uint32_t n, const BatchGeom& bg, const uint32_t* scene_ids,
                                 uint32_t n_ids, uint32_t* ranges, cudaStream_t st);

@@ -243,6 +243,13 @@ struct cgb_composition {
     uint32_t resident_rows = 0, resident_row_len = 0;
     // frame-level buffers of an incremental frame (on the handle that renders it)
     DevBuf segs_k, segs_m, d_keep, d_scene_ids, d_ranges, d_extract, merge_split;
+    // sync-free incremental frames: capacities from the earlier incremental
+    // frames (steps and segs: those of the changed layers; tls and items:
+    // the whole frame's), with headroom
+    FrameCaps incr_caps;
+    bool incr_caps_valid = false;
+    uint64_t last_new_segs = 0;  // segments the last staged frame rasterized
+    uint32_t incr_form = 0;      // the last frame: 0 full, 1 incremental staged, 2 incremental sync-free
 
     cgb_status cuda_fail(cudaError_t e, const char* where) {
         if (e == cudaErrorMemoryAllocation && s.over_budget) {
@@ -758,10 +765,12 @@ cgb_status prepare_incremental(cgb_composition* c, SceneInput& in) {
         return CGB_OK;
     }
     const bool valid = c->resident_valid && c->resident_rows == rows && c->resident_row_len == row_len;
+    // from the device-table mirror (32 bytes per layer; touch() keeps it current)
     auto current_order = [&](uint32_t id) -> int32_t {
-        if (id >= c->layers.size()) return -1;
-        const HostLayer& l = c->layers[id];
-        return (l.present && l.enabled) ? (int32_t)(l.has_order ? l.order : id) : -1;
+        if (id >= c->layer_recs.size()) return -1;
+        const LayerRec& r = c->layer_recs[id];
+        const bool live = (r.flags & LAYER_PRESENT) && (r.flags & LAYER_ENABLED);
+        return live ? (int32_t)((r.flags & LAYER_HAS_ORDER) ? r.order : id) : -1;
     };
     if (!valid) {  // every line rasterized; the resident segments are rebuilt after the frame
         c->rast_order.assign(c->layers.size(), -1);
@@ -1024,6 +1033,7 @@ cgb_status staged_frame(cgb_composition* c, const FrameSetup& f, std::vector<Sce
     CK(radix_sort_u64(keys, c->segs_a.as<uint64_t>(), (uint32_t)P, 22, 22 + (int)bg.key_bits,
                       (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &sorted, &passes, true));
     c->stats.sort_passes = passes;
+    c->last_new_segs = P;
     if (f.incremental) {
         cgb_status si = incremental_merge(c, f, scenes, &sorted, &P);
         if (si) return si;
@@ -1168,6 +1178,9 @@ cudaError_t ensure_graph_buffers(cgb_composition* c, const FrameSetup& f, const 
     return e;
 }
 
+cgb_status enqueue_counted_tail(cgb_composition* c, const FrameSetup& f, const FrameCaps& k, uint64_t* sorted,
+                                FrameGraph* g);
+
 // The body of a frame graph: the staged frame's launches with the counts
 // kept on the device (no host synchronization) and every grid sized for
 // the capacities.
@@ -1197,7 +1210,20 @@ cgb_status enqueue_counted_frame(cgb_composition* c, const FrameSetup& f, const 
                       &c->s, err, st, &sorted, &passes, true, fc, FC_SEGS));
     g->sort_passes = (uint32_t)passes;
     CK(stage_mark(c, 3, st, nullptr));
+    return enqueue_counted_tail(c, f, k, sorted, g);
+}
 
+// The device-counted stages after the sort: tile-layer groups, carries,
+// work items and their sort, the painter and the counts readback.  `sorted`
+// holds the frame's sorted segments, at most k.segs of them
+// (fc->n[FC_SEGS]).
+cgb_status enqueue_counted_tail(cgb_composition* c, const FrameSetup& f, const FrameCaps& k, uint64_t* sorted,
+                                FrameGraph* g) {
+    cudaStream_t st = c->stream;
+    const BatchGeom& bg = f.bg;
+    FrameCounts* fc = c->d_counts.as<FrameCounts>();
+    uint32_t* err = c->err.as<uint32_t>();
+    const int rbits = (int)c->tuning.radix_bits;
     CarryBuffers cb{};
     const uint32_t hg = tl_scan_grid(k.segs);
     cb.blk_cover = c->blk_cover.as<uint64_t>();
@@ -1348,6 +1374,138 @@ void post_frame(std::vector<SceneInput>& scenes, const std::vector<uint8_t>& wri
             }
 }
 
+// Capacities of the next sync-free incremental frame: the largest counts of
+// the incremental frames so far, with headroom.
+void note_incremental_counts(cgb_composition* c, uint64_t steps, uint64_t new_segs, uint64_t tls, uint64_t items) {
+    FrameCaps& k = c->incr_caps;
+    const float h = c->graph_headroom;
+    k.steps = std::max(k.steps, with_headroom(steps, h));
+    k.segs = std::max(k.segs, with_headroom(new_segs, h));
+    k.tls = std::max(k.tls, with_headroom(tls, h));
+    k.items = std::max(k.items, with_headroom(items, h));
+    c->incr_caps_valid = true;
+}
+
+// An incremental frame of composition c on its own handle without host
+// synchronization between stages: the changed layers' lines are rasterized
+// and sorted, the resident segments of clean orders kept and merged in, and
+// the device-counted stages of a frame graph finish it; every count stays on
+// the device, grids are sized by the capacities of the earlier incremental
+// frames.  *done is false when a count passed its capacity (nothing was
+// painted; the caller renders the frame stage by stage).
+cgb_status sync_free_incremental(cgb_composition* c, const FrameSetup& f, std::vector<SceneInput>& scenes,
+                                 std::vector<uint8_t>& written, bool* done) {
+    *done = false;
+    const FrameCaps& ic = c->incr_caps;
+    const uint64_t K = c->resident_n;
+    if (K + ic.segs >= (1ull << 30) - 1) return CGB_OK;
+    cudaStream_t st = c->stream;
+    const BatchGeom& bg = f.bg;
+    FrameCaps k;
+    k.steps = ic.steps;
+    k.segs = (uint32_t)(K + ic.segs);  // the merged frame
+    k.tls = ic.tls;
+    k.items = ic.items;
+    const uint32_t L = (uint32_t)bg.total_lines;
+    const uint32_t block = c->tuning.raster_block, items = c->tuning.steps_per_block / block;
+    const uint64_t grid = raster_grid(k.steps, block, items), slots = raster_run_slots(block, items);
+    const uint64_t hg = tl_scan_grid(k.segs), kg = keep_grid(std::max<uint64_t>(K, 1));
+    const uint64_t nb = std::max(std::max(grid, hg), kg) + 1;
+    if (!c->h_counts && cudaMallocHost(&c->h_counts, sizeof(FrameCounts)) != cudaSuccess) {
+        cudaGetLastError();
+        c->h_counts = nullptr;
+        return CGB_OK;
+    }
+    Scratch& sc = c->s;
+    CK(sc.ensure(c->recs, std::max<uint64_t>(L, 1) * sizeof(LineRec)));
+    CK(sc.ensure(c->lengths, std::max<uint64_t>(L, 1) * 4));
+    CK(sc.ensure(c->step_off, ((uint64_t)L + 1) * 4));
+    CK(sc.ensure(c->segs_a, std::max<uint64_t>(grid * slots, ic.segs) * 8));
+    CK(sc.ensure(c->segs_b, (uint64_t)ic.segs * 8));
+    CK(sc.ensure(c->bcounts, nb * 4));
+    CK(sc.ensure(c->boff, nb * 4));
+    CK(sc.ensure(c->blk_cover, (hg + 1) * 8));
+    CK(sc.ensure(c->blk_head, (hg + 1) * 4));
+    CK(sc.ensure(c->segs_k, std::max<uint64_t>(K, 1) * 8));
+    CK(sc.ensure(c->segs_m, (uint64_t)k.segs * 8));
+    CK(sc.ensure(c->merge_split, ((uint64_t)merge_tiles(k.segs) + 1) * 4));
+    CK(sc.ensure(c->tl_start, ((uint64_t)k.tls + 1) * 4));
+    CK(sc.ensure(c->tl_key, (uint64_t)k.tls * 8));
+    CK(sc.ensure(c->tl_cover, (uint64_t)k.tls * 8));
+    CK(sc.ensure(c->tl_carry, (uint64_t)k.tls * 8));
+    CK(sc.ensure(c->tl_flags, (uint64_t)k.tls * 4));
+    CK(sc.ensure(c->item_count, (uint64_t)k.tls * 4));
+    CK(sc.ensure(c->item_off, ((uint64_t)k.tls + 1) * 4));
+    CK(sc.ensure(c->items_a, (uint64_t)k.items * 8));
+    CK(sc.ensure(c->items_b, (uint64_t)k.items * 8));
+    CK(sc.ensure(c->tile_start, (f.tiles + 1) * 4));
+    if (f.features & FEAT_CLIPS) CK(sc.ensure(c->item_state, k.items));
+    CK(sc.ensure(c->d_counts, sizeof(FrameCounts)));
+    CK(sc.ensure(c->d_keep, sizeof(KeepSource)));
+    const uint64_t scan_n = std::max(std::max<uint64_t>(L, grid), std::max<uint64_t>(std::max(hg, kg), k.tls));
+    CK(reserve_frame_scratch(&sc, (uint32_t)std::min<uint64_t>(scan_n, UINT32_MAX), std::max(ic.segs, k.items)));
+
+    FrameCounts* fc = c->d_counts.as<FrameCounts>();
+    uint32_t* err = c->err.as<uint32_t>();
+    const int rbits = (int)c->tuning.radix_bits;
+    const KeepSource src{c->resident.as<uint64_t>(), 0, K, c->d_rast_dirty.as<uint8_t>(), c->max_ids, 0,
+                         c->resident_ob, c->resident_cb};
+    CK(cudaMemsetAsync(fc, 0, sizeof(FrameCounts), st));
+    CK(cudaMemcpyAsync(c->d_keep.p, &src, sizeof(src), cudaMemcpyHostToDevice, st));
+    CK(stage_mark(c, 0, st, "cgb:build_lines"));
+    CK(launch_build_lines(bg, 1, c->recs.as<LineRec>(), c->lengths.as<uint32_t>(), st));
+    CK(scan_u32(c->lengths.as<uint32_t>(), c->step_off.as<uint32_t>(), L, &sc, st, nullptr, &fc->n[FC_STEPS]));
+    CK(stage_mark(c, 1, st, "cgb:rasterize"));
+    CK(launch_rasterize(1, bg, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, k.steps, block, items,
+                        c->segs_a.as<uint64_t>(), c->bcounts.as<uint32_t>(), &fc->produced, st, fc, true));
+    CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), (uint32_t)grid, &sc, st, nullptr,
+                &fc->n[FC_NEW]));
+    CK(radix_gather_hist(c->segs_a.as<uint64_t>(), (uint32_t)slots, c->bcounts.as<uint32_t>(),
+                         c->boff.as<uint32_t>(), (uint32_t)grid, c->segs_b.as<uint64_t>(), 22, 22 + (int)bg.key_bits,
+                         rbits, &sc, st, ic.segs));
+    CK(stage_mark(c, 2, st, "cgb:sort"));
+    uint64_t* sorted_new = nullptr;
+    int passes = 0;
+    CK(radix_sort_u64(c->segs_b.as<uint64_t>(), c->segs_a.as<uint64_t>(), ic.segs, 22, 22 + (int)bg.key_bits, rbits,
+                      &sc, err, st, &sorted_new, &passes, true, fc, FC_NEW));
+    if (K) {
+        CK(launch_keep(0, c->d_keep.as<KeepSource>(), 1, K, bg, c->bcounts.as<uint32_t>(), nullptr, nullptr, 0, st));
+        CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), (uint32_t)kg, &sc, st, nullptr,
+                    &fc->n[FC_KEPT]));
+        CK(launch_keep(1, c->d_keep.as<KeepSource>(), 1, K, bg, nullptr, c->boff.as<uint32_t>(),
+                       c->segs_k.as<uint64_t>(), K, st));
+    }
+    CK(launch_merge(c->segs_k.as<uint64_t>(), (uint32_t)K, sorted_new, ic.segs, c->merge_split.as<uint32_t>(),
+                    c->segs_m.as<uint64_t>(), st, fc));
+    CK(stage_mark(c, 3, st, "cgb:carry"));
+    FrameGraph g;
+    cgb_status s1 = enqueue_counted_tail(c, f, k, c->segs_m.as<uint64_t>(), &g);
+    if (s1) return s1;
+    cgb_status s3 = finish_frame(c, scenes, f, written);
+    if (s3) return s3;
+    const FrameCounts& h = *c->h_counts;
+    if (h.overflow) return CGB_OK;
+    // the merged frame is the resident segments of the next one
+    std::swap(c->resident, c->segs_m);
+    c->resident_n = h.n[FC_SEGS];
+    c->resident_ob = bg.order_bits;
+    c->resident_cb = bg.col_bits;
+    c->resident_valid = true;
+    c->resident_rows = scenes[0].d.rows;
+    c->resident_row_len = scenes[0].d.row_len;
+    c->stats.lines = bg.total_lines;
+    c->stats.steps = h.n[FC_STEPS];
+    c->stats.segments = h.produced;
+    c->stats.painted_segments = h.n[FC_SEGS];
+    c->stats.tile_layers = h.n[FC_TLS];
+    c->stats.work_items = h.n[FC_ITEMS];
+    c->stats.sort_passes = (uint32_t)passes;
+    c->stats.item_sort_passes = g.item_sort_passes;
+    note_incremental_counts(c, h.n[FC_STEPS], h.n[FC_NEW], h.n[FC_TLS], h.n[FC_ITEMS]);
+    *done = true;
+    return CGB_OK;
+}
+
 // Renders every scene of `scenes` in one pipeline on `c`'s stream and
 // buffers: build, rasterize, sort, carries / items, paint.  In graph mode a
 // frame whose signature and buffers match a captured one is replayed from
@@ -1449,6 +1607,24 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
             c->graphs.erase(it);
         }
     }
+    // an incremental frame of a composition on its own handle, once earlier
+    // incremental frames have sized its buffers: no synchronization between stages
+    const bool own_incremental = f.incremental && scenes.size() == 1 && scenes[0].incr == 2 && scenes[0].comp == c;
+    c->incr_form = f.incremental ? 1 : 0;
+    if (own_incremental && c->incr_caps_valid && lines > 0) {
+        bool done = false;
+        cgb_status si = sync_free_incremental(c, f, scenes, written, &done);
+        if (si) {
+            c->resident_valid = false;
+            return si;
+        }
+        if (done) {
+            c->incr_form = 2;
+            post_frame(scenes, written);
+            return CGB_OK;
+        }
+        written.clear();  // a count passed its capacity: nothing was painted
+    }
     cgb_status s2 = staged_frame(c, f, scenes);
     cgb_status s3 = s2 ? s2 : finish_frame(c, scenes, f, written);
     if (s3) {
@@ -1459,6 +1635,8 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
         return s3;
     }
     post_frame(scenes, written);
+    if (own_incremental)  // sizes for the sync-free form of the next frames
+        note_incremental_counts(c, c->stats.steps, c->last_new_segs, c->stats.tile_layers, c->stats.work_items);
     if (graphable) capture_frame_graph(c, f, sig);
     return CGB_OK;
 }
@@ -1904,6 +2082,8 @@ CGB_EXPORT cgb_status cgb_get_stats(cgb_composition* c, cgb_stats* out) {
     *out = c->stats;
     out->graph_replayed = c->last_replayed ? 1u : 0u;
     out->graphs_cached = (uint32_t)c->graphs.size();
+    out->incremental_form = c->incr_form;
+    out->reserved = 0;
     return CGB_OK;
 }
 
@@ -1913,6 +2093,8 @@ CGB_EXPORT cgb_status cgb_set_incremental(cgb_composition* c, int enabled) {
     c->incremental = enabled != 0;
     c->resident_valid = false;
     c->resident_n = 0;
+    c->incr_caps = FrameCaps{};
+    c->incr_caps_valid = false;
     c->rast_ids.clear();
     c->rast_flag.clear();
     c->rast_order.clear();

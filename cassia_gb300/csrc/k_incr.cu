@@ -166,9 +166,15 @@ __device__ __forceinline__ uint32_t merge_split(const uint64_t* a, uint32_t na, 
     return lo;
 }
 
+// With fc (sync-free frames) na and nb are capacities and the counts are
+// fc->n[FC_KEPT] and fc->n[FC_NEW]; thread 0 then records the merged count
+// in fc->n[FC_SEGS] for the stages after the merge.
 __global__ void k_merge_split(const uint64_t* __restrict__ a, uint32_t na, const uint64_t* __restrict__ b,
-                              uint32_t nb, uint32_t n_tiles, uint32_t* __restrict__ split) {
+                              uint32_t nb, uint32_t n_tiles, uint32_t* __restrict__ split, FrameCounts* fc) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    na = fc_count(fc, FC_KEPT, na, false);
+    nb = fc_count(fc, FC_NEW, nb, false);
+    if (fc && t == 0) fc->n[FC_SEGS] = na + nb;
     if (t > n_tiles) return;
     const uint64_t d = min((uint64_t)t * MERGE_TILE, (uint64_t)na + nb);
     split[t] = merge_split(a, na, b, nb, (uint32_t)d);
@@ -180,9 +186,13 @@ __global__ void k_merge_split(const uint64_t* __restrict__ a, uint32_t na, const
 __global__ void __launch_bounds__(MERGE_THREADS) k_merge(const uint64_t* __restrict__ a, uint32_t na,
                                                          const uint64_t* __restrict__ b, uint32_t nb,
                                                          const uint32_t* __restrict__ split,
-                                                         uint64_t* __restrict__ out) {
+                                                         uint64_t* __restrict__ out, const FrameCounts* fc) {
     __shared__ uint64_t s_in[MERGE_TILE];
     __shared__ uint64_t s_out[MERGE_TILE];
+    if (fc) {  // the counts, clamped to the capacities the grid was sized for
+        na = min(fc->n[FC_KEPT], na);
+        nb = min(fc->n[FC_NEW], nb);
+    }
     const uint64_t n = (uint64_t)na + nb;
     const uint64_t d0 = (uint64_t)blockIdx.x * MERGE_TILE;
     if (d0 >= n) return;
@@ -276,12 +286,12 @@ uint32_t keep_grid(uint64_t total) { return (uint32_t)((total + KEEP_TILE - 1) /
 uint32_t merge_tiles(uint64_t n) { return (uint32_t)((n + MERGE_TILE - 1) / MERGE_TILE); }
 
 cudaError_t launch_merge(const uint64_t* a, uint32_t na, const uint64_t* b, uint32_t nb, uint32_t* split,
-                         uint64_t* out, cudaStream_t st) {
+                         uint64_t* out, cudaStream_t st, FrameCounts* fc) {
     const uint32_t tiles = merge_tiles((uint64_t)na + nb);
-    if (tiles == 0) return cudaSuccess;
+    if (tiles == 0 && !fc) return cudaSuccess;
     count_launches(2);
-    k_merge_split<<<(tiles + 1 + 255) / 256, 256, 0, st>>>(a, na, b, nb, tiles, split);
-    k_merge<<<tiles, MERGE_THREADS, 0, st>>>(a, na, b, nb, split, out);
+    k_merge_split<<<(tiles + 1 + 255) / 256, 256, 0, st>>>(a, na, b, nb, tiles, split, fc);
+    if (tiles) k_merge<<<tiles, MERGE_THREADS, 0, st>>>(a, na, b, nb, split, out, fc);
     return cudaGetLastError();
 }
 

@@ -174,6 +174,9 @@ typedef struct cgb_stats {
     float build_ms, rasterize_ms, sort_ms, carry_ms, paint_ms, total_ms;
     uint32_t graph_replayed;   /* 1: the frame was replayed from a frame graph (cgb_set_graph_mode) */
     uint32_t graphs_cached;    /* frame graphs held by the handle */
+    uint32_t incremental_form; /* 0 full frame; incremental frame (cgb_set_incremental): 1 staged,
+                                  2 sync-free (no host synchronization between stages) */
+    uint32_t reserved;
 } cgb_stats;
 
 /* Autotuned knobs (0 keeps the current value).  Every setting renders the
@@ -307,7 +310,10 @@ CGB_EXPORT cgb_status cgb_set_graph_mode(cgb_composition* c, int enabled, float 
  * inserted lines, removal), drops those layers' old segments and merges the
  * rest back in.  Pixels are identical to a full frame.  Works for cgb_render
  * and for the compositions of cgb_render_batch; such frames are staged (no
- * frame graph).  Costs 8 bytes of device memory per segment of the frame. */
+ * frame graph); once earlier incremental frames of a handle rendered on its own
+ * have sized its buffers, they run without host synchronization between
+ * stages (a frame whose counts outgrow them is rendered again stage by
+ * stage).  Costs 8 bytes of device memory per segment of the frame. */
 CGB_EXPORT cgb_status cgb_set_incremental(cgb_composition* c, int enabled);
 CGB_EXPORT cgb_status cgb_set_tuning(cgb_composition* c, const cgb_tuning* tuning);
 CGB_EXPORT cgb_status cgb_get_tuning(cgb_composition* c, cgb_tuning* out);

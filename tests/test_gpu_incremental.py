@@ -189,3 +189,26 @@ def test_incremental_full_size(gpu_lib):
         assert sg["painted_segments"] == sr["painted_segments"] > 40_000_000
         if seq:
             assert sg["segments"] < sr["segments"] // 3
+
+
+def test_sync_free_incremental_frames_and_overflow(gpu_lib):
+    """Incremental frames of a composition on its own handle run without
+    host synchronization once an earlier incremental frame sized the
+    buffers (incremental_form 2); an update larger than the capacities
+    paints nothing and is rendered again stage by stage (form 1), which
+    sizes the buffers for the next ones."""
+    sc = scenes.mixed(seed=101, n_layers=2000, width=512, height=384)
+    pool = scenes.mixed(seed=102, n_layers=32, width=512, height=384)
+    cg, cr = _pair(sc, pool)
+    forms = []
+    for seq, frac in enumerate([0.0, 0.02, 0.02, 0.02, 0.6, 0.6, 0.02]):
+        if seq:
+            for cl in (cg, cr):
+                serving.apply_update(cl, 7, seq, changed=frac, churn=0.0)
+        _assert_same(_render(cg.comp, sc), _render(cr.comp, sc), f"frame {seq}")
+        sg, sr = cg.comp.stats(), cr.comp.stats()
+        for key in ("painted_segments", "tile_layers", "work_items"):
+            assert sg[key] == sr[key], (seq, key)
+        forms.append(sg["incremental_form"])
+        assert sr["incremental_form"] == 0
+    assert forms == [1, 1, 2, 2, 1, 2, 2], forms
