@@ -15,8 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libcassia_gb300.so")
-SOURCES = ["k_lines.cu", "k_sort.cu", "k_paint.cu", "k_incr.cu", "composition.cu"]
-HEADERS = ["cgb_internal.cuh"]
+SOURCES = ["k_lines.cu", "k_sort.cu", "k_paint.cu", "k_incr.cu", "composition.cu", "frame.cu"]
+HEADERS = ["cgb_internal.cuh", "host_state.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",

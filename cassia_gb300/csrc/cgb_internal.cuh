@@ -250,6 +250,8 @@ struct Scratch {
 
 // Process-wide count of kernels launched by this library.
 void count_launches(uint64_t n);
+uint64_t launches_total();
+void uncount_launches(uint64_t n);  // launches captured into a graph, counted when replayed
 
 // k_lines.cu
 cudaError_t launch_flatten(int write, const uint32_t* kinds, const float* points, const uint64_t* cmd_off,

@@ -212,3 +212,28 @@ def test_sync_free_incremental_frames_and_overflow(gpu_lib):
         forms.append(sg["incremental_form"])
         assert sr["incremental_form"] == 0
     assert forms == [1, 1, 2, 2, 1, 2, 2], forms
+
+
+def test_switching_between_incremental_and_graph_frames(gpu_lib):
+    """One composition switched between incremental and full frames: every
+    frame equals a composition that always renders full frames, and the
+    frame form it reports is the form that frame ran in (a replayed graph
+    is a full frame, form 0)."""
+    sc = scenes.mixed(seed=103, n_layers=1200, width=384, height=256)
+    pool = scenes.mixed(seed=104, n_layers=32, width=384, height=256)
+    cg, cr = _pair(sc, pool)
+    cg.comp.set_graph_mode(True)
+    plan = [True, True, True, True, False, False, False, True, True, True]
+    for seq, inc in enumerate(plan):
+        if seq:
+            for cl in (cg, cr):
+                serving.apply_update(cl, 9, seq, changed=0.05, churn=0.0)
+        cg.comp.set_incremental(inc)
+        _assert_same(_render(cg.comp, sc), _render(cr.comp, sc), f"frame {seq}")
+        st = cg.comp.stats()
+        if not inc:
+            assert st["incremental_form"] == 0, (seq, st["incremental_form"])
+        else:
+            assert st["incremental_form"] in (1, 2), (seq, st["incremental_form"])
+        if not inc and seq == 6:  # the third full frame in a row replays its graph
+            assert st["graph_replayed"] == 1
