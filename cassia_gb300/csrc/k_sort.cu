@@ -136,16 +136,37 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const uint32_t* __r
 // radix sort
 // ---------------------------------------------------------------------------
 
-constexpr int RADIX = 512;  // up to 9-bit digits: one digit per thread of a sort CTA
+constexpr int RADIX = 512;  // up to 9-bit digits
 constexpr int MAX_PASSES = 11;
-constexpr int SORT_THREADS = 512;
+#ifndef CGB_SORT_THREADS
+#define CGB_SORT_THREADS 512
+#endif
+#ifndef CGB_SORT_ITEMS
+#define CGB_SORT_ITEMS 8
+#endif
+#ifndef CGB_SORT_MINB
+#define CGB_SORT_MINB 3
+#endif
+constexpr int SORT_THREADS = CGB_SORT_THREADS;
 constexpr int SORT_WARPS = SORT_THREADS / 32;
-constexpr int SORT_ITEMS = 8;
-constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;  // 4096 keys per CTA
+constexpr int SORT_ITEMS = CGB_SORT_ITEMS;
+constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;  // keys per CTA
+constexpr int SORT_DPT = RADIX / SORT_THREADS;       // digits per thread
+constexpr int SORT_MIN_BLOCKS = CGB_SORT_MINB;
+static_assert(SORT_DPT == 1 || SORT_DPT == 2, "one or two digits per thread");
+static_assert(SORT_TILE < 65536, "per-warp digit offsets are 16-bit");
 constexpr uint32_t ST_AGG = 1u << 30;
 constexpr uint32_t ST_INC = 2u << 30;
 constexpr uint32_t ST_VAL = (1u << 30) - 1;
 constexpr uint32_t SPIN_LIMIT = 1u << 22;  // ~ a second with the back-off below
+#ifndef CGB_LB_WINDOW
+#define CGB_LB_WINDOW 4
+#endif
+#ifndef CGB_LB_SLEEP
+#define CGB_LB_SLEEP 32
+#endif
+constexpr int LB_WINDOW = CGB_LB_WINDOW;  // look-back entries loaded per round
+constexpr unsigned LB_SLEEP = CGB_LB_SLEEP;  // back-off (ns) after a round with no published entry
 
 struct PassPlan {
     int n;
@@ -222,16 +243,27 @@ __global__ void __launch_bounds__(RADIX) k_radix_hist_scan(uint32_t* hist) {
     h[threadIdx.x] = ex;
 }
 
-__global__ void __launch_bounds__(SORT_THREADS, 3) k_onesweep(const uint64_t* __restrict__ in, uint64_t* __restrict__ out,
-                                                           uint32_t n, int shift, int bits,
-                                                           const uint32_t* __restrict__ global_off,
-                                                           uint32_t* lookback, uint32_t* tile_counter,
-                                                           uint32_t* err, FrameCounts* fc, int fc_which) {
-    __shared__ uint16_t s_hist[SORT_WARPS][RADIX];  // per-warp counts, then offsets (< 4096)
-    __shared__ uint32_t s_count[RADIX];
-    __shared__ uint32_t s_start[RADIX];
-    __shared__ uint32_t s_base[RADIX];
-    extern __shared__ uint64_t s_keys[];  // SORT_TILE keys (dynamic: the CTA needs > 48 KB)
+// Digit `mask` of a key at bit `shift`: from the high word alone (HI, shift
+// >= 32) or funnel-shifted out of both words.
+template <bool HI>
+__device__ __forceinline__ uint32_t key_digit(uint64_t k, int sh, uint32_t mask) {
+    const uint32_t lo = (uint32_t)k, hi = (uint32_t)(k >> 32);
+    return (HI ? (hi >> sh) : __funnelshift_r(lo, hi, sh)) & mask;
+}
+
+// One LSD pass over a tile of SORT_TILE keys.  HI: the digit lies in the high
+// word (`sh` = shift - 32); else `sh` = shift < 32.
+template <bool HI>
+__global__ void __launch_bounds__(SORT_THREADS, SORT_MIN_BLOCKS)
+    k_onesweep(const uint64_t* __restrict__ in, uint64_t* __restrict__ out, uint32_t n, int sh, int bits,
+               const uint32_t* __restrict__ global_off, uint32_t* lookback, uint32_t* tile_counter, uint32_t* err,
+               FrameCounts* fc, int fc_which) {
+    // per-warp digit counts, then the warp's offsets within each digit; the
+    // column past the digits counts the keys past the end of the last tile
+    __shared__ __align__(16) uint16_t s_hist[SORT_WARPS][RADIX + 2];
+    __shared__ uint32_t s_start[RADIX];  // tile-local start of each digit
+    __shared__ uint32_t s_off[RADIX];    // global start minus tile-local start (mod 2^32)
+    extern __shared__ uint64_t s_keys[];  // SORT_TILE keys
     __shared__ uint32_t s_tile;
     __shared__ uint32_t s_abort;
 
@@ -241,7 +273,10 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) k_onesweep(const uint64_t* __
         s_tile = atomicAdd(tile_counter, 1u);
         s_abort = 0;
     }
-    for (int i = tid; i < SORT_WARPS * RADIX; i += SORT_THREADS) (&s_hist[0][0])[i] = 0;
+    {
+        uint32_t* h = reinterpret_cast<uint32_t*>(&s_hist[0][0]);
+        for (int i = tid; i < SORT_WARPS * (RADIX + 2) / 2; i += SORT_THREADS) h[i] = 0;
+    }
     __syncthreads();
     const uint32_t tile = s_tile;
     const uint64_t base = (uint64_t)tile * SORT_TILE;
@@ -251,50 +286,71 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) k_onesweep(const uint64_t* __
     if (fc && base >= n && tile > 0) return;
 
     uint64_t key[SORT_ITEMS];
-    uint32_t dr[SORT_ITEMS];  // digit (RADIX = none) | rank within the warp << 16
+    uint32_t dr[SORT_ITEMS];  // digit (RADIX = past the end) | rank within the warp << 16
+    const uint64_t wbase = base + (uint64_t)warp * 32 * SORT_ITEMS + lane;
+    if (base + SORT_TILE <= n) {
 #pragma unroll
-    for (int k = 0; k < SORT_ITEMS; k++) {
-        uint64_t idx = base + (uint64_t)warp * 32 * SORT_ITEMS + k * 32 + lane;
-        bool valid = idx < n;
-        key[k] = valid ? in[idx] : 0;
-        dr[k] = valid ? ((uint32_t)(key[k] >> shift) & mask) : RADIX;
+        for (int k = 0; k < SORT_ITEMS; k++) key[k] = in[wbase + k * 32];
+#pragma unroll
+        for (int k = 0; k < SORT_ITEMS; k++) dr[k] = key_digit<HI>(key[k], sh, mask);
+    } else {
+#pragma unroll
+        for (int k = 0; k < SORT_ITEMS; k++) {
+            const bool valid = wbase + k * 32 < n;
+            key[k] = valid ? in[wbase + k * 32] : 0;
+            dr[k] = valid ? key_digit<HI>(key[k], sh, mask) : (uint32_t)RADIX;
+        }
     }
     // Warp-level multi-split ranking, in key order within the warp (stable).
     const uint32_t lt = lanemask_lt();
 #pragma unroll
     for (int k = 0; k < SORT_ITEMS; k++) {
-        uint32_t d = dr[k];
-        uint32_t peers = __match_any_sync(0xffffffffu, d);
-        uint32_t r = __popc(peers & lt);
-        uint32_t cnt = d < RADIX ? s_hist[warp][d] : 0;
+        const uint32_t d = dr[k];
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t r = __popc(peers & lt);
+        const uint32_t cnt = s_hist[warp][d];
         __syncwarp();
-        if (d < RADIX && r == 0) s_hist[warp][d] = (uint16_t)(cnt + __popc(peers));
+        if (r == 0) s_hist[warp][d] = (uint16_t)(cnt + __popc(peers));
         __syncwarp();
         dr[k] = d | ((cnt + r) << 16);
     }
     __syncthreads();
     // Per digit: exclusive offsets across warps and the tile's count.
-    for (int d = tid; d < RADIX; d += SORT_THREADS) {
+    uint32_t cnt[SORT_DPT];
+    const int d0 = tid * SORT_DPT;
+    if constexpr (SORT_DPT == 2) {
+        uint32_t lo = 0, hi = 0;
+#pragma unroll
+        for (int w = 0; w < SORT_WARPS; w++) {
+            uint32_t* p = reinterpret_cast<uint32_t*>(&s_hist[w][d0]);
+            const uint32_t v = *p;
+            *p = lo | (hi << 16);
+            lo += v & 0xFFFFu;
+            hi += v >> 16;
+        }
+        cnt[0] = lo;
+        cnt[1] = hi;
+    } else {
         uint32_t sum = 0;
 #pragma unroll
         for (int w = 0; w < SORT_WARPS; w++) {
-            uint32_t v = s_hist[w][d];
-            s_hist[w][d] = (uint16_t)sum;
+            const uint32_t v = s_hist[w][d0];
+            s_hist[w][d0] = (uint16_t)sum;
             sum += v;
         }
-        s_count[d] = sum;
+        cnt[0] = sum;
     }
-    __syncthreads();
     // The tile's digit counts are published at once (aggregate status; the
     // first tile's are already inclusive), so that later tiles can sum them
     // while this one places its keys in shared memory.
-    const uint32_t my_cnt = tid < RADIX ? s_count[tid] : 0;
-    uint32_t* mine = lookback + (uint64_t)tile * RADIX + tid;
-    if (tid < RADIX) st_relaxed(mine, (tile == 0 ? ST_INC : ST_AGG) | my_cnt);
-    // Tile-local digit starts: exclusive scan of s_count over the RADIX digits.
+    uint32_t* mine = lookback + (uint64_t)tile * RADIX + d0;
+#pragma unroll
+    for (int j = 0; j < SORT_DPT; j++) st_relaxed(mine + j, (tile == 0 ? ST_INC : ST_AGG) | cnt[j]);
+    // Tile-local digit starts: exclusive scan of the counts over the digits.
     {
-        uint32_t ex = block_exclusive_scan<uint32_t>(my_cnt, nullptr);
-        if (tid < RADIX) s_start[tid] = ex;
+        const uint32_t ex = block_exclusive_scan<uint32_t>(SORT_DPT == 2 ? cnt[0] + cnt[SORT_DPT - 1] : cnt[0], nullptr);
+        s_start[d0] = ex;
+        if constexpr (SORT_DPT == 2) s_start[d0 + 1] = ex + cnt[0];
     }
     __syncthreads();
 #pragma unroll
@@ -302,60 +358,78 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) k_onesweep(const uint64_t* __
         const uint32_t d = dr[k] & 0xFFFFu;
         if (d < RADIX) s_keys[s_start[d] + s_hist[warp][d] + (dr[k] >> 16)] = key[k];
     }
-    // Decoupled look-back for the tile's global digit offsets: one thread per
-    // digit walks back over its predecessors four entries per load round,
-    // summing until an inclusive prefix, and publishes its own.
-    if (tid < RADIX) {
-        const int d = tid;
-        uint32_t excl = 0;
-        if (tile > 0) {
-            int64_t t = (int64_t)tile - 1;
-            uint32_t spins = 0;
-            while (t >= 0) {
-                uint32_t v[4];
+    // Decoupled look-back for the tile's global digit offsets: each thread
+    // walks back over the predecessors of its digits, LB_WINDOW entries per
+    // load round, summing until an inclusive prefix, and publishes its own.
+    uint32_t excl[SORT_DPT];
 #pragma unroll
-                for (int k = 0; k < 4; k++)
-                    v[k] = t - k >= 0 ? ld_relaxed(lookback + (uint64_t)(t - k) * RADIX + d) : (ST_INC | 0u);
+    for (int j = 0; j < SORT_DPT; j++) excl[j] = 0;
+    if (tile > 0) {
+        int64_t t[SORT_DPT];
+        bool done[SORT_DPT];
+#pragma unroll
+        for (int j = 0; j < SORT_DPT; j++) {
+            t[j] = (int64_t)tile - 1;
+            done[j] = false;
+        }
+        uint32_t spins = 0;
+        while (true) {
+            bool progress = false, all = true;
+#pragma unroll
+            for (int j = 0; j < SORT_DPT; j++) {
+                if (done[j]) continue;
+                uint32_t v[LB_WINDOW];
+#pragma unroll
+                for (int k = 0; k < LB_WINDOW; k++)
+                    v[k] = t[j] - k >= 0 ? ld_relaxed(lookback + (uint64_t)(t[j] - k) * RADIX + d0 + j) : (ST_INC | 0u);
                 int used = 0;
                 bool inc = false;
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
+                for (int k = 0; k < LB_WINDOW; k++) {
                     if (inc || used < k) break;  // stop at the first inclusive or unpublished entry
                     const uint32_t stt = v[k] & ~ST_VAL;
                     if (stt == 0) break;
-                    excl += v[k] & ST_VAL;
+                    excl[j] += v[k] & ST_VAL;
                     used++;
                     if (stt == ST_INC) inc = true;
                 }
-                if (inc) break;
-                if (used == 0) {
-                    if (++spins > SPIN_LIMIT) {  // a predecessor never published
-                        atomicExch(err, 1u);
-                        s_abort = 1;
-                        break;
-                    }
-                    __nanosleep(32);
-                }
-                t -= used;
+                t[j] -= used;
+                progress |= used > 0;
+                done[j] = inc;
+                all &= inc;
             }
-            st_relaxed(mine, ST_INC | ((excl + my_cnt) & ST_VAL));
+            if (all) break;
+            if (!progress) {
+                if (++spins > SPIN_LIMIT) {  // a predecessor never published
+                    atomicExch(err, 1u);
+                    s_abort = 1;
+                    break;
+                }
+                __nanosleep(LB_SLEEP);
+            }
         }
-        s_base[d] = global_off[d] + excl;
+#pragma unroll
+        for (int j = 0; j < SORT_DPT; j++) st_relaxed(mine + j, ST_INC | ((excl[j] + cnt[j]) & ST_VAL));
     }
+#pragma unroll
+    for (int j = 0; j < SORT_DPT; j++) s_off[d0 + j] = global_off[d0 + j] + excl[j] - s_start[d0 + j];
     __syncthreads();
     if (s_abort) return;  // a predecessor never published: leave the output, the host reports the timeout
     const uint32_t valid = (n - base) < (uint64_t)SORT_TILE ? (uint32_t)(n - base) : (uint32_t)SORT_TILE;
-    for (uint32_t i = tid; i < valid; i += SORT_THREADS) {
-        uint64_t k = s_keys[i];
-        uint32_t d = (uint32_t)(k >> shift) & mask;
-        uint32_t pos = s_base[d] + (i - s_start[d]);
-        if (pos < n) out[pos] = k;
+#pragma unroll
+    for (int k = 0; k < SORT_ITEMS; k++) {
+        const uint32_t i = k * SORT_THREADS + tid;
+        if (i < valid) {
+            const uint64_t v = s_keys[i];
+            const uint32_t pos = s_off[key_digit<HI>(v, sh, mask)] + i;
+            if (pos < n) out[pos] = v;
+        }
     }
 }
 
 constexpr size_t ONESWEEP_DYN_SMEM = SORT_TILE * sizeof(uint64_t);
 
-// Opts the onesweep kernel into its dynamic shared memory (once per device).
+// Opts the onesweep kernels into their dynamic shared memory (once per device).
 cudaError_t onesweep_setup() {
     static std::mutex mu;
     static bool done[64] = {};
@@ -364,11 +438,27 @@ cudaError_t onesweep_setup() {
     if (e != cudaSuccess || dev < 0 || dev >= 64) return e != cudaSuccess ? e : cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(mu);
     if (!done[dev]) {
-        e = cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ONESWEEP_DYN_SMEM);
+        e = cudaFuncSetAttribute(k_onesweep<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)ONESWEEP_DYN_SMEM);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_onesweep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)ONESWEEP_DYN_SMEM);
         if (e != cudaSuccess) return e;
         done[dev] = true;
     }
     return cudaSuccess;
+}
+
+// One onesweep pass over the digit of `bits` bits at bit `shift`.
+void launch_onesweep(uint32_t grid, cudaStream_t st, const uint64_t* in, uint64_t* out, uint32_t n, int shift,
+                     int bits, const uint32_t* global_off, uint32_t* lookback, uint32_t* tile_counter, uint32_t* err,
+                     FrameCounts* fc, int fc_which) {
+    if (shift >= 32)
+        k_onesweep<true><<<grid, SORT_THREADS, ONESWEEP_DYN_SMEM, st>>>(in, out, n, shift - 32, bits, global_off,
+                                                                        lookback, tile_counter, err, fc, fc_which);
+    else
+        k_onesweep<false><<<grid, SORT_THREADS, ONESWEEP_DYN_SMEM, st>>>(in, out, n, shift, bits, global_off,
+                                                                         lookback, tile_counter, err, fc, fc_which);
 }
 
 }  // namespace
@@ -486,9 +576,8 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo
     uint64_t* dst = tmp;
     for (int p = 0; p < plan.n; p++) {
         if ((e = cudaMemsetAsync(lb, 0, (size_t)tiles * RADIX * 4, st)) != cudaSuccess) return e;
-        k_onesweep<<<tiles, SORT_THREADS, ONESWEEP_DYN_SMEM, st>>>(src, dst, n, plan.shift[p], plan.bits[p],
-                                                                   hist + p * RADIX, lb, ctr + p, err_flag, fc,
-                                                                   fc_which);
+        launch_onesweep(tiles, st, src, dst, n, plan.shift[p], plan.bits[p], hist + p * RADIX, lb, ctr + p, err_flag,
+                        fc, fc_which);
         std::swap(src, dst);
     }
     *result = src;
@@ -518,7 +607,7 @@ cudaError_t selftest_bounded_wait(cudaStream_t st, uint32_t* flag_host) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(ctr, &one, 4, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
         count_launches(1);
-        k_onesweep<<<1, SORT_THREADS, ONESWEEP_DYN_SMEM, st>>>(in, out, n, 0, 8, hist, lb, ctr, err, nullptr, 0);
+        launch_onesweep(1, st, in, out, n, 0, 8, hist, lb, ctr, err, nullptr, 0);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(flag_host, err, 4, cudaMemcpyDeviceToHost, st);
@@ -549,7 +638,7 @@ namespace cgb {
 namespace {
 
 constexpr uint32_t NOALLOC_MAX_KEYS = 1u << 24;                    // 16,777,216 keys
-constexpr uint32_t NOALLOC_TILES = NOALLOC_MAX_KEYS / SORT_TILE;    // 4,096 onesweep tiles
+constexpr uint32_t NOALLOC_TILES = (NOALLOC_MAX_KEYS + SORT_TILE - 1) / SORT_TILE;  // onesweep tiles
 constexpr uint32_t NOALLOC_HIST_WORDS = MAX_PASSES * RADIX;
 constexpr uint32_t NOALLOC_CTR_OFF = NOALLOC_HIST_WORDS;            // MAX_PASSES tile counters
 constexpr uint32_t NOALLOC_ERR_OFF = NOALLOC_CTR_OFF + 64;          // error flag
@@ -622,8 +711,8 @@ extern "C" CGB_EXPORT cgb_status cgb_sort_keys_noalloc(uint64_t* keys, uint64_t*
     for (int p = 0; p < plan.n && e == cudaSuccess; p++) {
         e = cudaMemsetAsync(lb, 0, (size_t)tiles * RADIX * 4, st);
         if (e != cudaSuccess) break;
-        k_onesweep<<<tiles, SORT_THREADS, ONESWEEP_DYN_SMEM, st>>>(src, dst, nn, plan.shift[p], plan.bits[p],
-                                                                   hist + p * RADIX, lb, ctr + p, err, nullptr, 0);
+        launch_onesweep(tiles, st, src, dst, nn, plan.shift[p], plan.bits[p], hist + p * RADIX, lb, ctr + p, err,
+                        nullptr, 0);
         e = cudaGetLastError();
         std::swap(src, dst);
     }
