@@ -142,10 +142,10 @@ constexpr int MAX_PASSES = 11;
 #define CGB_SORT_THREADS 512
 #endif
 #ifndef CGB_SORT_ITEMS
-#define CGB_SORT_ITEMS 8
+#define CGB_SORT_ITEMS 14
 #endif
 #ifndef CGB_SORT_MINB
-#define CGB_SORT_MINB 3
+#define CGB_SORT_MINB 2
 #endif
 constexpr int SORT_THREADS = CGB_SORT_THREADS;
 constexpr int SORT_WARPS = SORT_THREADS / 32;
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(RADIX) k_radix_hist_scan(uint32_t* hist) {
 template <bool HI>
 __device__ __forceinline__ uint32_t key_digit(uint64_t k, int sh, uint32_t mask) {
     const uint32_t lo = (uint32_t)k, hi = (uint32_t)(k >> 32);
-    return (HI ? (hi >> sh) : __funnelshift_r(lo, hi, sh)) & mask;
+    return (HI ? __funnelshift_r(hi, 0u, sh) : __funnelshift_r(lo, hi, sh)) & mask;
 }
 
 // One LSD pass over a tile of SORT_TILE keys.  HI: the digit lies in the high
@@ -285,34 +285,35 @@ __global__ void __launch_bounds__(SORT_THREADS, SORT_MIN_BLOCKS)
     n = fc_count(fc, fc_which, n, tile == 0 && tid == 0);
     if (fc && base >= n && tile > 0) return;
 
+    // Keys stay in registers; ranks are packed two per register and digits
+    // recomputed from the keys, which keeps 14 keys per thread unspilled.
     uint64_t key[SORT_ITEMS];
-    uint32_t dr[SORT_ITEMS];  // digit (RADIX = past the end) | rank within the warp << 16
+    uint32_t rk[(SORT_ITEMS + 1) / 2];
     const uint64_t wbase = base + (uint64_t)warp * 32 * SORT_ITEMS + lane;
-    if (base + SORT_TILE <= n) {
+    const bool full = base + SORT_TILE <= n;
+    if (full) {
 #pragma unroll
         for (int k = 0; k < SORT_ITEMS; k++) key[k] = in[wbase + k * 32];
-#pragma unroll
-        for (int k = 0; k < SORT_ITEMS; k++) dr[k] = key_digit<HI>(key[k], sh, mask);
     } else {
 #pragma unroll
-        for (int k = 0; k < SORT_ITEMS; k++) {
-            const bool valid = wbase + k * 32 < n;
-            key[k] = valid ? in[wbase + k * 32] : 0;
-            dr[k] = valid ? key_digit<HI>(key[k], sh, mask) : (uint32_t)RADIX;
-        }
+        for (int k = 0; k < SORT_ITEMS; k++) key[k] = wbase + k * 32 < n ? in[wbase + k * 32] : 0;
     }
-    // Warp-level multi-split ranking, in key order within the warp (stable).
+    // Warp-level multi-split ranking, in key order within the warp (stable);
+    // keys past the end count in the spare digit column.
     const uint32_t lt = lanemask_lt();
 #pragma unroll
     for (int k = 0; k < SORT_ITEMS; k++) {
-        const uint32_t d = dr[k];
+        const uint32_t d = full || wbase + k * 32 < n ? key_digit<HI>(key[k], sh, mask) : (uint32_t)RADIX;
         const uint32_t peers = __match_any_sync(0xffffffffu, d);
         const uint32_t r = __popc(peers & lt);
         const uint32_t cnt = s_hist[warp][d];
         __syncwarp();
         if (r == 0) s_hist[warp][d] = (uint16_t)(cnt + __popc(peers));
         __syncwarp();
-        dr[k] = d | ((cnt + r) << 16);
+        if (k & 1)
+            rk[k >> 1] |= (cnt + r) << 16;
+        else
+            rk[k >> 1] = cnt + r;
     }
     __syncthreads();
     // Per digit: exclusive offsets across warps and the tile's count.
@@ -355,8 +356,9 @@ __global__ void __launch_bounds__(SORT_THREADS, SORT_MIN_BLOCKS)
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < SORT_ITEMS; k++) {
-        const uint32_t d = dr[k] & 0xFFFFu;
-        if (d < RADIX) s_keys[s_start[d] + s_hist[warp][d] + (dr[k] >> 16)] = key[k];
+        const uint32_t d = full || wbase + k * 32 < n ? key_digit<HI>(key[k], sh, mask) : (uint32_t)RADIX;
+        const uint32_t rank = (rk[k >> 1] >> ((k & 1) * 16)) & 0xFFFFu;
+        if (d < RADIX) s_keys[s_start[d] + s_hist[warp][d] + rank] = key[k];
     }
     // Decoupled look-back for the tile's global digit offsets: each thread
     // walks back over the predecessors of its digits, LB_WINDOW entries per
@@ -365,11 +367,11 @@ __global__ void __launch_bounds__(SORT_THREADS, SORT_MIN_BLOCKS)
 #pragma unroll
     for (int j = 0; j < SORT_DPT; j++) excl[j] = 0;
     if (tile > 0) {
-        int64_t t[SORT_DPT];
+        int t[SORT_DPT];  // tiles < 2^30 / SORT_TILE
         bool done[SORT_DPT];
 #pragma unroll
         for (int j = 0; j < SORT_DPT; j++) {
-            t[j] = (int64_t)tile - 1;
+            t[j] = (int)tile - 1;
             done[j] = false;
         }
         uint32_t spins = 0;
@@ -381,7 +383,8 @@ __global__ void __launch_bounds__(SORT_THREADS, SORT_MIN_BLOCKS)
                 uint32_t v[LB_WINDOW];
 #pragma unroll
                 for (int k = 0; k < LB_WINDOW; k++)
-                    v[k] = t[j] - k >= 0 ? ld_relaxed(lookback + (uint64_t)(t[j] - k) * RADIX + d0 + j) : (ST_INC | 0u);
+                    v[k] = t[j] - k >= 0 ? ld_relaxed(lookback + (size_t)(uint32_t)(t[j] - k) * RADIX + d0 + j)
+                                         : (ST_INC | 0u);
                 int used = 0;
                 bool inc = false;
 #pragma unroll
