@@ -447,17 +447,49 @@ __device__ __forceinline__ float2 blend_vec2(float2 d, float s) {
     return add2(fma2(mul2(splat(-2.0f), d), S, d), S);  // EXCLUSION
 }
 
-// blend_at for one lane's pixel pair of a tile row (painter/mod.rs:364-400),
-// specialised per blend mode so that the mode is dispatched once per layer.
+// blend_function! (style.rs:288-418) for the three colour channels of a
+// lane's pixel pair: the only part of blend_at that depends on the mode.  The
+// switch holds just these few operations per mode, so that the painter's hot
+// code stays small when a tile's layers use many modes.
+template <int MODE>
+__device__ __forceinline__ void blend_channels(const float2 (&C)[4], const float4& src, float2 (&B)[3]) {
+    B[0] = blend_vec2<MODE>(C[0], src.x);
+    B[1] = blend_vec2<MODE>(C[1], src.y);
+    B[2] = blend_vec2<MODE>(C[2], src.z);
+}
+
+__device__ __forceinline__ void blend_channels(uint32_t mode, const float2 (&C)[4], const float4& src,
+                                               float2 (&B)[3]) {
+    switch (mode) {
+        case CGB_BLEND_OVER: blend_channels<CGB_BLEND_OVER>(C, src, B); break;
+        case CGB_BLEND_MULTIPLY: blend_channels<CGB_BLEND_MULTIPLY>(C, src, B); break;
+        case CGB_BLEND_SCREEN: blend_channels<CGB_BLEND_SCREEN>(C, src, B); break;
+        case CGB_BLEND_OVERLAY: blend_channels<CGB_BLEND_OVERLAY>(C, src, B); break;
+        case CGB_BLEND_DARKEN: blend_channels<CGB_BLEND_DARKEN>(C, src, B); break;
+        case CGB_BLEND_LIGHTEN: blend_channels<CGB_BLEND_LIGHTEN>(C, src, B); break;
+        case CGB_BLEND_COLOR_DODGE: blend_channels<CGB_BLEND_COLOR_DODGE>(C, src, B); break;
+        case CGB_BLEND_COLOR_BURN: blend_channels<CGB_BLEND_COLOR_BURN>(C, src, B); break;
+        case CGB_BLEND_HARD_LIGHT: blend_channels<CGB_BLEND_HARD_LIGHT>(C, src, B); break;
+        case CGB_BLEND_SOFT_LIGHT: blend_channels<CGB_BLEND_SOFT_LIGHT>(C, src, B); break;
+        case CGB_BLEND_DIFFERENCE: blend_channels<CGB_BLEND_DIFFERENCE>(C, src, B); break;
+        default: blend_channels<CGB_BLEND_EXCLUSION>(C, src, B); break;
+    }
+}
+
+// blend_at for one lane's pixel pair of a tile row (painter/mod.rs:364-400).
 // C[q] holds channel q of the two pixels; a pixel whose column is not blended
-// keeps its color.
-template <int MODE, bool MASKED>
-__device__ __forceinline__ void blend_pixels(float2 (&C)[4], const float4& src, float2 cov, bool col0, bool col1) {
+// keeps its color.  MASKED = false when both columns of every lane are
+// blended (cover-carry-only items: every column has the same per-row coverage).
+template <bool MASKED>
+__device__ __forceinline__ void blend_dispatch(uint32_t mode, float2 (&C)[4], const float4& src, float2 cov,
+                                               bool col0, bool col1) {
+    float2 B[3];
+    blend_channels(mode, C, src, B);
     const float2 al = mul2(splat(src.w), cov);
     const float2 inv = sub2(splat(1.0f), al);
-    const float2 n0 = fma2(C[0], inv, mul2(blend_vec2<MODE>(C[0], src.x), al));
-    const float2 n1 = fma2(C[1], inv, mul2(blend_vec2<MODE>(C[1], src.y), al));
-    const float2 n2 = fma2(C[2], inv, mul2(blend_vec2<MODE>(C[2], src.z), al));
+    const float2 n0 = fma2(C[0], inv, mul2(B[0], al));
+    const float2 n1 = fma2(C[1], inv, mul2(B[1], al));
+    const float2 n2 = fma2(C[2], inv, mul2(B[2], al));
     const float2 n3 = fma2(C[3], inv, al);
     if (MASKED) {
         C[0] = sel2(col0, col1, n0, C[0]);
@@ -469,27 +501,6 @@ __device__ __forceinline__ void blend_pixels(float2 (&C)[4], const float4& src, 
         C[1] = n1;
         C[2] = n2;
         C[3] = n3;
-    }
-}
-
-// MASKED = false when both columns of every lane are blended (cover-carry-only
-// items: every column has the same per-row coverage).
-template <bool MASKED>
-__device__ __forceinline__ void blend_dispatch(uint32_t mode, float2 (&C)[4], const float4& src, float2 cov,
-                                               bool col0, bool col1) {
-    switch (mode) {
-        case CGB_BLEND_OVER: blend_pixels<CGB_BLEND_OVER, MASKED>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_MULTIPLY: blend_pixels<CGB_BLEND_MULTIPLY, MASKED>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_SCREEN: blend_pixels<CGB_BLEND_SCREEN, MASKED>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_OVERLAY: blend_pixels<CGB_BLEND_OVERLAY, MASKED>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_DARKEN: blend_pixels<CGB_BLEND_DARKEN, MASKED>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_LIGHTEN: blend_pixels<CGB_BLEND_LIGHTEN, MASKED>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_COLOR_DODGE: blend_pixels<CGB_BLEND_COLOR_DODGE, MASKED>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_COLOR_BURN: blend_pixels<CGB_BLEND_COLOR_BURN, MASKED>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_HARD_LIGHT: blend_pixels<CGB_BLEND_HARD_LIGHT, MASKED>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_SOFT_LIGHT: blend_pixels<CGB_BLEND_SOFT_LIGHT, MASKED>(C, src, cov, col0, col1); break;
-        case CGB_BLEND_DIFFERENCE: blend_pixels<CGB_BLEND_DIFFERENCE, MASKED>(C, src, cov, col0, col1); break;
-        default: blend_pixels<CGB_BLEND_EXCLUSION, MASKED>(C, src, cov, col0, col1); break;
     }
 }
 
@@ -563,11 +574,41 @@ __device__ float4 gradient_color(const GradRec& g, const GradStop* __restrict__ 
                        __uint_as_float(out[3]));
 }
 
+// blend_function! for a per-pixel source: the three channels of both pixels.
+template <int MODE>
+__device__ __forceinline__ void blend_channels_src(const float2 (&C)[4], const float4 (&src)[2], float (&B)[2][3]) {
+    B[0][0] = blend_vec1<MODE>(C[0].x, src[0].x);
+    B[0][1] = blend_vec1<MODE>(C[1].x, src[0].y);
+    B[0][2] = blend_vec1<MODE>(C[2].x, src[0].z);
+    B[1][0] = blend_vec1<MODE>(C[0].y, src[1].x);
+    B[1][1] = blend_vec1<MODE>(C[1].y, src[1].y);
+    B[1][2] = blend_vec1<MODE>(C[2].y, src[1].z);
+}
+
+__device__ __forceinline__ void blend_channels_src(uint32_t mode, const float2 (&C)[4], const float4 (&src)[2],
+                                                   float (&B)[2][3]) {
+    switch (mode) {
+        case CGB_BLEND_OVER: blend_channels_src<CGB_BLEND_OVER>(C, src, B); break;
+        case CGB_BLEND_MULTIPLY: blend_channels_src<CGB_BLEND_MULTIPLY>(C, src, B); break;
+        case CGB_BLEND_SCREEN: blend_channels_src<CGB_BLEND_SCREEN>(C, src, B); break;
+        case CGB_BLEND_OVERLAY: blend_channels_src<CGB_BLEND_OVERLAY>(C, src, B); break;
+        case CGB_BLEND_DARKEN: blend_channels_src<CGB_BLEND_DARKEN>(C, src, B); break;
+        case CGB_BLEND_LIGHTEN: blend_channels_src<CGB_BLEND_LIGHTEN>(C, src, B); break;
+        case CGB_BLEND_COLOR_DODGE: blend_channels_src<CGB_BLEND_COLOR_DODGE>(C, src, B); break;
+        case CGB_BLEND_COLOR_BURN: blend_channels_src<CGB_BLEND_COLOR_BURN>(C, src, B); break;
+        case CGB_BLEND_HARD_LIGHT: blend_channels_src<CGB_BLEND_HARD_LIGHT>(C, src, B); break;
+        case CGB_BLEND_SOFT_LIGHT: blend_channels_src<CGB_BLEND_SOFT_LIGHT>(C, src, B); break;
+        case CGB_BLEND_DIFFERENCE: blend_channels_src<CGB_BLEND_DIFFERENCE>(C, src, B); break;
+        default: blend_channels_src<CGB_BLEND_EXCLUSION>(C, src, B); break;
+    }
+}
+
 // blend_at with a per-pixel source (gradient fills) and, for clipped layers,
 // the clip mask (alpha = fill alpha * coverage * mask, in that order).
-template <int MODE>
-__device__ __forceinline__ void blend_pixels_src(float2 (&C)[4], const float4 (&src)[2], float2 cov, bool col0,
-                                                 bool col1, bool clipped, float2 mask) {
+__device__ void blend_dispatch_src(uint32_t mode, float2 (&C)[4], const float4 (&src)[2], float2 cov, bool col0,
+                                   bool col1, bool clipped, float2 mask) {
+    float B[2][3];
+    blend_channels_src(mode, C, src, B);
 #pragma unroll
     for (int h = 0; h < 2; h++) {
         const float cv = h ? cov.y : cov.x;
@@ -576,34 +617,14 @@ __device__ __forceinline__ void blend_pixels_src(float2 (&C)[4], const float4 (&
         float al = src[h].w * cv;
         if (clipped) al *= h ? mask.y : mask.x;
         const float inv = 1.0f - al;
-        const float n0 = __fmaf_rn(c[0], inv, blend_vec1<MODE>(c[0], src[h].x) * al);
-        const float n1 = __fmaf_rn(c[1], inv, blend_vec1<MODE>(c[1], src[h].y) * al);
-        const float n2 = __fmaf_rn(c[2], inv, blend_vec1<MODE>(c[2], src[h].z) * al);
+        const float n0 = __fmaf_rn(c[0], inv, B[h][0] * al);
+        const float n1 = __fmaf_rn(c[1], inv, B[h][1] * al);
+        const float n2 = __fmaf_rn(c[2], inv, B[h][2] * al);
         const float n3 = __fmaf_rn(c[3], inv, al);
         if (on) {
             if (h) C[0].y = n0, C[1].y = n1, C[2].y = n2, C[3].y = n3;
             else C[0].x = n0, C[1].x = n1, C[2].x = n2, C[3].x = n3;
         }
-    }
-}
-
-__device__ void blend_dispatch_src(uint32_t mode, float2 (&C)[4], const float4 (&src)[2], float2 cov, bool col0,
-                                   bool col1, bool clipped, float2 mask) {
-    switch (mode) {
-        case CGB_BLEND_OVER: blend_pixels_src<CGB_BLEND_OVER>(C, src, cov, col0, col1, clipped, mask); break;
-        case CGB_BLEND_MULTIPLY: blend_pixels_src<CGB_BLEND_MULTIPLY>(C, src, cov, col0, col1, clipped, mask); break;
-        case CGB_BLEND_SCREEN: blend_pixels_src<CGB_BLEND_SCREEN>(C, src, cov, col0, col1, clipped, mask); break;
-        case CGB_BLEND_OVERLAY: blend_pixels_src<CGB_BLEND_OVERLAY>(C, src, cov, col0, col1, clipped, mask); break;
-        case CGB_BLEND_DARKEN: blend_pixels_src<CGB_BLEND_DARKEN>(C, src, cov, col0, col1, clipped, mask); break;
-        case CGB_BLEND_LIGHTEN: blend_pixels_src<CGB_BLEND_LIGHTEN>(C, src, cov, col0, col1, clipped, mask); break;
-        case CGB_BLEND_COLOR_DODGE:
-            blend_pixels_src<CGB_BLEND_COLOR_DODGE>(C, src, cov, col0, col1, clipped, mask);
-            break;
-        case CGB_BLEND_COLOR_BURN: blend_pixels_src<CGB_BLEND_COLOR_BURN>(C, src, cov, col0, col1, clipped, mask); break;
-        case CGB_BLEND_HARD_LIGHT: blend_pixels_src<CGB_BLEND_HARD_LIGHT>(C, src, cov, col0, col1, clipped, mask); break;
-        case CGB_BLEND_SOFT_LIGHT: blend_pixels_src<CGB_BLEND_SOFT_LIGHT>(C, src, cov, col0, col1, clipped, mask); break;
-        case CGB_BLEND_DIFFERENCE: blend_pixels_src<CGB_BLEND_DIFFERENCE>(C, src, cov, col0, col1, clipped, mask); break;
-        default: blend_pixels_src<CGB_BLEND_EXCLUSION>(C, src, cov, col0, col1, clipped, mask); break;
     }
 }
 
