@@ -153,7 +153,7 @@ struct cgb_composition {
     bool wide = false;
     uint32_t max_ids = 1u << 16;
     Scratch s;
-    cgb_tuning tuning{9, 256, 2048, 4};  // radix bits, raster block, steps per block, painter warps
+    cgb_tuning tuning{9, 256, 2048, 2};  // radix bits, raster block, steps per block, painter warps
     cgb_stats stats{};
 
     // LinesBuilder (device SoA)
