@@ -195,8 +195,9 @@ STAGE_KERNELS = {
 # in profiles/kernels_mixed20k.md.
 STAGE_LIMITERS = {
     "rasterize": "fixed-point step arithmetic and barriers of the per-block runs (55% issue active)",
-    "sort": "latency of the onesweep tile (64% issue active, 2.1 TB/s)",
-    "paint": "instruction issue and dependent-instruction latency (64% of issue slots, fixed-latency "
+    "sort": "instruction issue of the onesweep tile's ranking and scatter (56-59% issue active, "
+            "2.3 TB/s per pass)",
+    "paint": "instruction issue and dependent-instruction latency (74% of issue slots, fixed-latency "
              "waits the top stall; not occupancy: more resident warps did not help); its DRAM traffic "
              "equals its algorithmic input",
 }
