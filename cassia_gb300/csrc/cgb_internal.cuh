@@ -300,9 +300,13 @@ cudaError_t reserve_frame_scratch(Scratch* s, uint32_t scan_n, uint32_t sort_n);
 // hist_ready the digit counts of every pass are already in s->sort_hist
 // (from radix_gather_hist).
 // With fc, n is the capacity of keys and tmp and the key count is fc->n[fc_which].
+// Pass p ranks its tile's keys with warp ballots instead of match.any when bit
+// p of ballot_passes is set: for digits that the lanes of a warp mostly hold
+// distinct (the low digit of the work items' tile field).
 cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo, int bit_hi, int digit_bits,
                            Scratch* s, uint32_t* err_flag, cudaStream_t st, uint64_t** result, int* passes,
-                           bool hist_ready = false, FrameCounts* fc = nullptr, int fc_which = 0);
+                           bool hist_ready = false, FrameCounts* fc = nullptr, int fc_which = 0,
+                           uint32_t ballot_passes = 0);
 // Runs one onesweep CTA whose predecessor tile never publishes; *flag_host
 // receives the kernel's error flag (1 = the bounded wait gave up).
 cudaError_t selftest_bounded_wait(cudaStream_t st, uint32_t* flag_host);

@@ -467,7 +467,8 @@ cgb_status staged_frame(cgb_composition* c, const FrameSetup& f, std::vector<Sce
     int ipasses = 0;
     // stable sort on the tile field: each tile's items stay in order
     CK(radix_sort_u64(cb.items, cb.items_tmp, (uint32_t)W, tile_shift, tile_shift + tile_bits,
-                      (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &items_sorted, &ipasses));
+                      (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &items_sorted, &ipasses, false,
+                      nullptr, 0, 1u));
     c->stats.item_sort_passes = ipasses;
     CK(launch_tile_ranges(items_sorted, (uint32_t)W, (uint32_t)tiles, tile_shift, cb.tile_start, st));
     CK(stage_mark(c, 4, st, "cgb:paint"));
@@ -632,7 +633,7 @@ cgb_status enqueue_counted_tail(cgb_composition* c, const FrameSetup& f, const F
     uint64_t* items_sorted = nullptr;
     int ipasses = 0;
     CK(radix_sort_u64(cb.items, cb.items_tmp, k.items, tile_shift, tile_shift + tile_bits, rbits, &c->s, err, st,
-                      &items_sorted, &ipasses, false, fc, FC_ITEMS));
+                      &items_sorted, &ipasses, false, fc, FC_ITEMS, 1u));
     g->item_sort_passes = (uint32_t)ipasses;
     CK(launch_tile_ranges(items_sorted, k.items, (uint32_t)f.tiles, tile_shift, cb.tile_start, st, fc));
     CK(stage_mark(c, 4, st, nullptr));

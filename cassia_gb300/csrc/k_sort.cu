@@ -251,9 +251,24 @@ __device__ __forceinline__ uint32_t key_digit(uint64_t k, int sh, uint32_t mask)
     return (HI ? __funnelshift_r(hi, 0u, sh) : __funnelshift_r(lo, hi, sh)) & mask;
 }
 
+// The lanes of the warp that hold digit d (d < 1024), from ten ballots: a
+// fixed cost, where match.any slows down when the lanes' digits are mostly
+// distinct.
+__device__ __forceinline__ uint32_t ballot_peers(uint32_t d) {
+    uint32_t peers = 0xffffffffu;
+#pragma unroll
+    for (int b = 0; b < 10; b++) {
+        const bool bit = (d >> b) & 1u;
+        const uint32_t v = __ballot_sync(0xffffffffu, bit);
+        peers &= bit ? v : ~v;
+    }
+    return peers;
+}
+
 // One LSD pass over a tile of SORT_TILE keys.  HI: the digit lies in the high
-// word (`sh` = shift - 32); else `sh` = shift < 32.
-template <bool HI>
+// word (`sh` = shift - 32); else `sh` = shift < 32.  BALLOT: the warp's peers
+// of a digit come from ballots rather than match.any.
+template <bool HI, bool BALLOT>
 __global__ void __launch_bounds__(SORT_THREADS, SORT_MIN_BLOCKS)
     k_onesweep(const uint64_t* __restrict__ in, uint64_t* __restrict__ out, uint32_t n, int sh, int bits,
                const uint32_t* __restrict__ global_off, uint32_t* lookback, uint32_t* tile_counter, uint32_t* err,
@@ -304,7 +319,7 @@ __global__ void __launch_bounds__(SORT_THREADS, SORT_MIN_BLOCKS)
 #pragma unroll
     for (int k = 0; k < SORT_ITEMS; k++) {
         const uint32_t d = full || wbase + k * 32 < n ? key_digit<HI>(key[k], sh, mask) : (uint32_t)RADIX;
-        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t peers = BALLOT ? ballot_peers(d) : __match_any_sync(0xffffffffu, d);
         const uint32_t r = __popc(peers & lt);
         const uint32_t cnt = s_hist[warp][d];
         __syncwarp();
@@ -441,11 +456,10 @@ cudaError_t onesweep_setup() {
     if (e != cudaSuccess || dev < 0 || dev >= 64) return e != cudaSuccess ? e : cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(mu);
     if (!done[dev]) {
-        e = cudaFuncSetAttribute(k_onesweep<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)ONESWEEP_DYN_SMEM);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_onesweep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)ONESWEEP_DYN_SMEM);
+        const void* fns[4] = {(const void*)k_onesweep<false, false>, (const void*)k_onesweep<true, false>,
+                              (const void*)k_onesweep<false, true>, (const void*)k_onesweep<true, true>};
+        for (int i = 0; i < 4 && e == cudaSuccess; i++)
+            e = cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ONESWEEP_DYN_SMEM);
         if (e != cudaSuccess) return e;
         done[dev] = true;
     }
@@ -455,13 +469,13 @@ cudaError_t onesweep_setup() {
 // One onesweep pass over the digit of `bits` bits at bit `shift`.
 void launch_onesweep(uint32_t grid, cudaStream_t st, const uint64_t* in, uint64_t* out, uint32_t n, int shift,
                      int bits, const uint32_t* global_off, uint32_t* lookback, uint32_t* tile_counter, uint32_t* err,
-                     FrameCounts* fc, int fc_which) {
-    if (shift >= 32)
-        k_onesweep<true><<<grid, SORT_THREADS, ONESWEEP_DYN_SMEM, st>>>(in, out, n, shift - 32, bits, global_off,
-                                                                        lookback, tile_counter, err, fc, fc_which);
-    else
-        k_onesweep<false><<<grid, SORT_THREADS, ONESWEEP_DYN_SMEM, st>>>(in, out, n, shift, bits, global_off,
-                                                                         lookback, tile_counter, err, fc, fc_which);
+                     FrameCounts* fc, int fc_which, bool ballot = false) {
+    const bool hi = shift >= 32;
+    const int sh = hi ? shift - 32 : shift;
+    auto k = hi ? (ballot ? k_onesweep<true, true> : k_onesweep<true, false>)
+                : (ballot ? k_onesweep<false, true> : k_onesweep<false, false>);
+    k<<<grid, SORT_THREADS, ONESWEEP_DYN_SMEM, st>>>(in, out, n, sh, bits, global_off, lookback, tile_counter, err,
+                                                      fc, fc_which);
 }
 
 }  // namespace
@@ -551,7 +565,7 @@ cudaError_t radix_gather_hist(const uint64_t* runs, uint32_t run_slots, const ui
 
 cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo, int bit_hi, int digit_bits,
                            Scratch* s, uint32_t* err_flag, cudaStream_t st, uint64_t** result, int* passes,
-                           bool hist_ready, FrameCounts* fc, int fc_which) {
+                           bool hist_ready, FrameCounts* fc, int fc_which, uint32_t ballot_passes) {
     PassPlan plan = make_plan(bit_lo, bit_hi, digit_bits);
     *result = keys;
     if (passes) *passes = plan.n;
@@ -580,7 +594,7 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo
     for (int p = 0; p < plan.n; p++) {
         if ((e = cudaMemsetAsync(lb, 0, (size_t)tiles * RADIX * 4, st)) != cudaSuccess) return e;
         launch_onesweep(tiles, st, src, dst, n, plan.shift[p], plan.bits[p], hist + p * RADIX, lb, ctr + p, err_flag,
-                        fc, fc_which);
+                        fc, fc_which, ((ballot_passes >> p) & 1u) != 0);
         std::swap(src, dst);
     }
     *result = src;
