@@ -272,7 +272,7 @@ cudaError_t launch_build_lines(const BatchGeom& bg, int cull, LineRec* recs, uin
 cudaError_t launch_rasterize(int render, const BatchGeom& bg, const LineRec* recs, const uint32_t* step_off,
                              uint32_t n_lines, uint64_t n_steps, uint32_t block, uint32_t items, uint64_t* runs,
                              uint32_t* run_count, unsigned long long* produced, cudaStream_t st,
-                             FrameCounts* fc = nullptr, bool sparse = false);
+                             FrameCounts* fc, bool sparse, uint32_t* block_lines);
 uint32_t raster_run_slots(uint32_t block, uint32_t items);
 // Keys n reference CompactSegments (cassia_render's input) of scene 0 into
 // runs of import_run_slots() slots per block, as launch_rasterize does.

@@ -435,7 +435,7 @@ CGB_EXPORT cgb_status cgb_composition_free(cgb_composition* c) {
     DeviceGuard g(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     DevBuf* bufs[] = {&c->p0x, &c->p0y, &c->p1x, &c->p1y, &c->lids, &c->d_layers, &c->recs, &c->lengths,
-                      &c->step_off, &c->bcounts, &c->boff, &c->segs_a, &c->segs_b,
+                      &c->step_off, &c->bcounts, &c->boff, &c->segs_a, &c->segs_b, &c->raster_lines,
                       &c->tl_start, &c->tl_key, &c->blk_cover, &c->blk_head, &c->rlb, &c->item_state, &c->d_import, &c->written, &c->tl_cover, &c->tl_carry, &c->tl_flags, &c->item_count, &c->item_off,
                       &c->items_a, &c->items_b, &c->tile_start, &c->d_props, &c->d_grads, &c->d_stops, &c->d_unchanged, &c->out_rgba, &c->err,
                       &c->dflt_t, &c->f_kinds, &c->f_points, &c->f_cmd_off, &c->f_pt_off, &c->f_t9, &c->f_has_t,

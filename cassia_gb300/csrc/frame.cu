@@ -47,11 +47,13 @@ cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& 
     CK(c->s.ensure(c->segs_a, std::max<size_t>((size_t)grid * slots, 1) * 8));
     CK(c->s.ensure(c->bcounts, ((size_t)grid + 1) * 4));
     CK(c->s.ensure(c->boff, ((size_t)grid + 1) * 4));
+    CK(c->s.ensure(c->raster_lines, ((size_t)grid + 1) * 8));
     CK(c->s.ensure(c->rlb, 8));
     CK(cudaMemsetAsync(c->rlb.p, 0, 8, st));
     unsigned long long* produced = c->rlb.as<unsigned long long>();
     CK(launch_rasterize(render, bg, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, S, block, items,
-                        c->segs_a.as<uint64_t>(), c->bcounts.as<uint32_t>(), produced, st, nullptr, sparse));
+                        c->segs_a.as<uint64_t>(), c->bcounts.as<uint32_t>(), produced, st, nullptr, sparse,
+                        c->raster_lines.as<uint32_t>()));
     CK(cudaMemcpyAsync(&c->s.pinned[3], produced, 8, cudaMemcpyDeviceToHost, st));
     uint64_t P = 0;
     if (grid) CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid, &c->s, st, &P));
@@ -504,7 +506,7 @@ std::string frame_signature(const cgb_composition* c, const FrameSetup& f) {
 
 // (pointer, size) of every buffer that a frame graph launches on.
 std::vector<std::pair<const void*, size_t>> graph_buffers(cgb_composition* c) {
-    const DevBuf* b[] = {&c->recs,       &c->lengths,   &c->step_off,  &c->bcounts,         &c->boff,
+    const DevBuf* b[] = {&c->recs,       &c->lengths,   &c->step_off,  &c->bcounts,         &c->boff, &c->raster_lines,
                          &c->segs_a,     &c->segs_b,    &c->blk_cover, &c->blk_head,        &c->tl_start,
                          &c->tl_key,     &c->tl_cover,  &c->tl_carry,  &c->tl_flags,        &c->item_count,
                          &c->item_off,   &c->items_a,   &c->items_b,   &c->tile_start,      &c->item_state,
@@ -533,6 +535,7 @@ cudaError_t ensure_graph_buffers(cgb_composition* c, const FrameSetup& f, const 
     need(c->segs_a, std::max<uint64_t>(grid * slots, k.segs) * 8);
     need(c->segs_b, (uint64_t)k.segs * 8);
     need(c->bcounts, (std::max(grid, hg) + 1) * 4);
+    need(c->raster_lines, (grid + 1) * 8);
     need(c->boff, (std::max(grid, hg) + 1) * 4);
     need(c->blk_cover, (hg + 1) * 8);
     need(c->blk_head, (hg + 1) * 4);
@@ -576,7 +579,8 @@ cgb_status enqueue_counted_frame(cgb_composition* c, const FrameSetup& f, const 
     CK(scan_u32(c->lengths.as<uint32_t>(), c->step_off.as<uint32_t>(), L, &c->s, st, nullptr, &fc->n[FC_STEPS]));
     CK(stage_mark(c, 1, st, nullptr));
     CK(launch_rasterize(1, bg, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, k.steps, block, items,
-                        c->segs_a.as<uint64_t>(), c->bcounts.as<uint32_t>(), &fc->produced, st, fc));
+                        c->segs_a.as<uint64_t>(), c->bcounts.as<uint32_t>(), &fc->produced, st, fc, false,
+                        c->raster_lines.as<uint32_t>()));
     CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid, &c->s, st, nullptr, &fc->n[FC_SEGS]));
     CK(radix_gather_hist(c->segs_a.as<uint64_t>(), slots, c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid,
                          c->segs_b.as<uint64_t>(), 22, 22 + (int)bg.key_bits, rbits, &c->s, st, k.segs));
@@ -800,6 +804,7 @@ cgb_status sync_free_incremental(cgb_composition* c, const FrameSetup& f, std::v
     CK(sc.ensure(c->segs_a, std::max<uint64_t>(grid * slots, ic.segs) * 8));
     CK(sc.ensure(c->segs_b, (uint64_t)ic.segs * 8));
     CK(sc.ensure(c->bcounts, nb * 4));
+    CK(sc.ensure(c->raster_lines, ((uint64_t)grid + 1) * 8));
     CK(sc.ensure(c->boff, nb * 4));
     CK(sc.ensure(c->blk_cover, (hg + 1) * 8));
     CK(sc.ensure(c->blk_head, (hg + 1) * 4));
@@ -834,7 +839,8 @@ cgb_status sync_free_incremental(cgb_composition* c, const FrameSetup& f, std::v
     CK(scan_u32(c->lengths.as<uint32_t>(), c->step_off.as<uint32_t>(), L, &sc, st, nullptr, &fc->n[FC_STEPS]));
     CK(stage_mark(c, 1, st, "cgb:rasterize"));
     CK(launch_rasterize(1, bg, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, k.steps, block, items,
-                        c->segs_a.as<uint64_t>(), c->bcounts.as<uint32_t>(), &fc->produced, st, fc, true));
+                        c->segs_a.as<uint64_t>(), c->bcounts.as<uint32_t>(), &fc->produced, st, fc, true,
+                        c->raster_lines.as<uint32_t>()));
     CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), (uint32_t)grid, &sc, st, nullptr,
                 &fc->n[FC_NEW]));
     CK(radix_gather_hist(c->segs_a.as<uint64_t>(), (uint32_t)slots, c->bcounts.as<uint32_t>(),

@@ -190,6 +190,7 @@ struct cgb_composition {
 
     // frame buffers
     DevBuf recs, lengths, step_off, bcounts, boff, segs_a, segs_b;
+    DevBuf raster_lines;  // [2 * (raster grid + 1)] first and last line of each rasterizer block
     DevBuf tl_start, tl_key, tl_cover, tl_carry, tl_flags, item_count, item_off, items_a, items_b, tile_start;
     DevBuf blk_cover, blk_head, rlb, item_state, written;
     DevBuf d_props, d_grads, d_stops, d_unchanged, out_rgba, err, dflt_t, d_scenes, d_row_scene;

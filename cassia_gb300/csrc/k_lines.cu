@@ -523,6 +523,26 @@ __device__ __forceinline__ uint32_t find_line(const uint32_t* __restrict__ off, 
     return lo;
 }
 
+// The first and the last line of each rasterizer block's steps (per_block
+// steps per block): each line with steps [a, e) records itself for the blocks
+// whose first or last step lies in it.  block_lines[b] = first line of block
+// b, block_lines[nb + 1 + b] = its last line, for the nb blocks of the count.
+__global__ void k_block_lines(const uint32_t* __restrict__ off, uint32_t n_lines, uint64_t n_steps,
+                              uint32_t per_block, uint32_t* __restrict__ block_lines, uint32_t cap_blocks,
+                              FrameCounts* fc) {
+    if (fc) n_steps = fc_count(fc, FC_STEPS, (uint32_t)n_steps, false);
+    const uint32_t nb = (uint32_t)((n_steps + per_block - 1) / per_block);
+    const uint32_t l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= n_lines) return;
+    const uint32_t a = off[l], e = off[l + 1];
+    if (a >= e) return;
+    for (uint32_t b = a / per_block; b < nb && (uint64_t)b * per_block < e; b++) {
+        if ((uint64_t)b * per_block >= a) block_lines[b] = l;
+        const uint64_t last = min((uint64_t)(b + 1) * per_block, n_steps) - 1;
+        if (last >= a && last < e) block_lines[cap_blocks + 1 + b] = l;
+    }
+}
+
 // Every block rasterizes RASTER_ITEMS pixel steps per thread and stores its
 // kept segments, in step order, at the start of its own run of
 // 2 * RASTER_ITEMS * blockDim.x slots (a step yields at most two segments);
@@ -532,23 +552,18 @@ template <int RENDER, int RASTER_ITEMS, bool SPARSE>
 __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ recs, const uint32_t* __restrict__ off,
                                                    uint32_t n_lines, uint64_t n_steps, BatchGeom bg,
                                                    uint64_t* __restrict__ runs, uint32_t* __restrict__ run_count,
-                                                   unsigned long long* __restrict__ produced, FrameCounts* fc) {
+                                                   unsigned long long* __restrict__ produced, FrameCounts* fc,
+                                                   const uint32_t* __restrict__ block_lines) {
     extern __shared__ uint64_t s_out[];  // 2 * RASTER_ITEMS * blockDim.x
     // The line offsets of the block's step range, staged once: two searches
     // over the whole offset array per block instead of one per thread.
     __shared__ uint32_t s_off[RASTER_LINE_STAGE + 1];
-    __shared__ uint32_t s_lines[2];
     if (fc) n_steps = fc_count(fc, FC_STEPS, (uint32_t)n_steps, blockIdx.x == 0 && threadIdx.x == 0);
     const uint64_t bs0 = (uint64_t)blockIdx.x * blockDim.x * RASTER_ITEMS;
     const uint64_t bs1 = min(bs0 + (uint64_t)blockDim.x * RASTER_ITEMS, n_steps);  // exclusive
-    if (bs0 < n_steps) {
-        if (threadIdx.x == 0) s_lines[0] = find_line(off, n_lines, bs0);
-        if (threadIdx.x == 32 % blockDim.x) s_lines[1] = find_line(off, n_lines, bs1 - 1);
-    }
-    __syncthreads();
-    // lines l0..l1 hold the block's steps; off[l0 .. l1 + 1] go to s_off
-    const uint32_t l0 = bs0 < n_steps ? s_lines[0] : 0u;
-    const uint32_t nl = bs0 < n_steps ? s_lines[1] - l0 + 1 : 0u;
+    // lines l0..l1 hold the block's steps (from k_block_lines); off[l0 .. l1 + 1] go to s_off
+    const uint32_t l0 = bs0 < n_steps ? block_lines[blockIdx.x] : 0u;
+    const uint32_t nl = bs0 < n_steps ? block_lines[gridDim.x + 1 + blockIdx.x] - l0 + 1 : 0u;
     const bool staged = nl > 0 && nl <= RASTER_LINE_STAGE;
     if (staged)
         for (uint32_t q = threadIdx.x; q <= nl; q += blockDim.x) s_off[q] = off[l0 + q];
@@ -806,15 +821,19 @@ cudaError_t launch_build_lines(const BatchGeom& bg, int cull, LineRec* recs, uin
 cudaError_t launch_rasterize(int render, const BatchGeom& bg, const LineRec* recs, const uint32_t* step_off,
                              uint32_t n_lines, uint64_t n_steps, uint32_t block, uint32_t items, uint64_t* runs,
                              uint32_t* run_count, unsigned long long* produced, cudaStream_t st,
-                             FrameCounts* fc, bool sparse) {
+                             FrameCounts* fc, bool sparse, uint32_t* block_lines) {
     if (n_steps == 0) return cudaSuccess;
     if (fc && n_steps >= (1ull << 32)) return cudaErrorInvalidValue;
     if (block == 0 || block % 32 || block > 256 || (items != 4 && items != 8)) return cudaErrorInvalidValue;
     const uint32_t grid = raster_grid(n_steps, block, items);
     const size_t smem = (size_t)raster_run_slots(block, items) * sizeof(uint64_t);
-    count_launches(1);
-#define CGB_RASTER(R, I, S) \
-    k_rasterize<R, I, S><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced, fc)
+    count_launches(2);
+    if (n_lines > 0)
+        k_block_lines<<<(n_lines + 255) / 256, 256, 0, st>>>(step_off, n_lines, n_steps, block * items, block_lines,
+                                                               grid, fc);
+#define CGB_RASTER(R, I, S)                                                                                   \
+    k_rasterize<R, I, S><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced, \
+                                                    fc, block_lines)
     if (render && sparse) {
         if (items == 4) CGB_RASTER(1, 4, true);
         else CGB_RASTER(1, 8, true);
