@@ -183,36 +183,59 @@ __device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
     asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// One pass over the keys that histograms every digit of every pass.
+// One pass over the keys that histograms every digit of every pass (passes
+// unrolled as in k_gather_hist; NP = 0: any number).
+template <int NP>
 __global__ void __launch_bounds__(512) k_radix_hist(const uint64_t* __restrict__ keys, uint32_t n, PassPlan plan,
                                                     uint32_t* __restrict__ hist, FrameCounts* fc, int fc_which) {
     __shared__ uint32_t sh[MAX_PASSES][RADIX];
+    const int np = NP > 0 ? NP : plan.n;
     n = fc_count(fc, fc_which, n, false);
-    for (int i = threadIdx.x; i < plan.n * RADIX; i += blockDim.x) (&sh[0][0])[i] = 0;
+    for (int i = threadIdx.x; i < np * RADIX; i += blockDim.x) (&sh[0][0])[i] = 0;
     __syncthreads();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint64_t k = keys[i];
-        for (int p = 0; p < plan.n; p++) {
-            uint32_t d = (uint32_t)(k >> plan.shift[p]) & ((1u << plan.bits[p]) - 1);
+        const uint64_t k = keys[i];
+#pragma unroll
+        for (int p = 0; p < (NP > 0 ? NP : MAX_PASSES); p++) {
+            if (NP == 0 && p >= np) break;
+            const uint32_t d = (uint32_t)(k >> plan.shift[p]) & ((1u << plan.bits[p]) - 1);
             atomicAdd(&sh[p][d], 1u);
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < plan.n * RADIX; i += blockDim.x) {
-        uint32_t v = (&sh[0][0])[i];
+    for (int i = threadIdx.x; i < np * RADIX; i += blockDim.x) {
+        const uint32_t v = (&sh[0][0])[i];
         if (v) atomicAdd(&hist[i], v);
+    }
+}
+
+// Launches k_radix_hist for the plan's number of passes.
+void launch_radix_hist(uint32_t blocks, cudaStream_t st, const uint64_t* keys, uint32_t n, const PassPlan& plan,
+                       uint32_t* hist, FrameCounts* fc, int fc_which) {
+    switch (plan.n) {
+        case 1: k_radix_hist<1><<<blocks, 512, 0, st>>>(keys, n, plan, hist, fc, fc_which); break;
+        case 2: k_radix_hist<2><<<blocks, 512, 0, st>>>(keys, n, plan, hist, fc, fc_which); break;
+        case 3: k_radix_hist<3><<<blocks, 512, 0, st>>>(keys, n, plan, hist, fc, fc_which); break;
+        case 4: k_radix_hist<4><<<blocks, 512, 0, st>>>(keys, n, plan, hist, fc, fc_which); break;
+        case 5: k_radix_hist<5><<<blocks, 512, 0, st>>>(keys, n, plan, hist, fc, fc_which); break;
+        case 6: k_radix_hist<6><<<blocks, 512, 0, st>>>(keys, n, plan, hist, fc, fc_which); break;
+        default: k_radix_hist<0><<<blocks, 512, 0, st>>>(keys, n, plan, hist, fc, fc_which); break;
     }
 }
 
 // Packs the rasterizer's runs into one array and histograms every pass's
 // digits on the way (the counting pass of the sort, fused with the copy).
+// NP > 0: the plan has NP passes, unrolled so that each pass's shift and mask
+// stay in registers; NP = 0: any number of passes.
+template <int NP>
 __global__ void __launch_bounds__(512) k_gather_hist(const uint64_t* __restrict__ runs, uint32_t run_slots,
                                                      const uint32_t* __restrict__ run_count,
                                                      const uint32_t* __restrict__ run_off, uint32_t n_runs,
                                                      uint64_t* __restrict__ out, uint32_t out_cap, PassPlan plan,
                                                      uint32_t* __restrict__ hist) {
     __shared__ uint32_t sh[MAX_PASSES][RADIX];
-    for (int i = threadIdx.x; i < plan.n * RADIX; i += blockDim.x) (&sh[0][0])[i] = 0;
+    const int np = NP > 0 ? NP : plan.n;
+    for (int i = threadIdx.x; i < np * RADIX; i += blockDim.x) (&sh[0][0])[i] = 0;
     __syncthreads();
     for (uint32_t r = blockIdx.x; r < n_runs; r += gridDim.x) {
         const uint32_t o = run_off[r];
@@ -222,14 +245,16 @@ __global__ void __launch_bounds__(512) k_gather_hist(const uint64_t* __restrict_
         for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) {
             const uint64_t k = src[i];
             dst[i] = k;
-            for (int p = 0; p < plan.n; p++) {
+#pragma unroll
+            for (int p = 0; p < (NP > 0 ? NP : MAX_PASSES); p++) {
+                if (NP == 0 && p >= np) break;
                 const uint32_t d = (uint32_t)(k >> plan.shift[p]) & ((1u << plan.bits[p]) - 1);
                 atomicAdd(&sh[p][d], 1u);
             }
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < plan.n * RADIX; i += blockDim.x) {
+    for (int i = threadIdx.x; i < np * RADIX; i += blockDim.x) {
         const uint32_t v = (&sh[0][0])[i];
         if (v) atomicAdd(&hist[i], v);
     }
@@ -559,7 +584,18 @@ cudaError_t radix_gather_hist(const uint64_t* runs, uint32_t run_slots, const ui
     if (n_runs == 0) return cudaSuccess;
     const uint32_t blocks = std::min<uint32_t>(n_runs, (uint32_t)sm_count() * 4);
     count_launches(1);
-    k_gather_hist<<<blocks, 512, 0, st>>>(runs, run_slots, run_count, run_off, n_runs, out, out_cap, plan, hist);
+#define CGB_GATHER(NP) \
+    k_gather_hist<NP><<<blocks, 512, 0, st>>>(runs, run_slots, run_count, run_off, n_runs, out, out_cap, plan, hist)
+    switch (plan.n) {
+        case 1: CGB_GATHER(1); break;
+        case 2: CGB_GATHER(2); break;
+        case 3: CGB_GATHER(3); break;
+        case 4: CGB_GATHER(4); break;
+        case 5: CGB_GATHER(5); break;
+        case 6: CGB_GATHER(6); break;
+        default: CGB_GATHER(0); break;
+    }
+#undef CGB_GATHER
     return cudaGetLastError();
 }
 
@@ -585,7 +621,7 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo
         if ((e = cudaMemsetAsync(hist, 0, (size_t)plan.n * RADIX * 4, st)) != cudaSuccess) return e;
         uint32_t hist_blocks = std::min<uint32_t>((n + 511) / 512, (uint32_t)sm_count() * 4);
         count_launches(1);
-        k_radix_hist<<<hist_blocks, 512, 0, st>>>(keys, n, plan, hist, fc, fc_which);
+        launch_radix_hist(hist_blocks, st, keys, n, plan, hist, fc, fc_which);
     }
     count_launches(1 + plan.n);
     k_radix_hist_scan<<<plan.n, RADIX, 0, st>>>(hist);
@@ -718,7 +754,7 @@ extern "C" CGB_EXPORT cgb_status cgb_sort_keys_noalloc(uint64_t* keys, uint64_t*
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint32_t hist_blocks = std::min<uint32_t>((nn + 511) / 512, (uint32_t)sms * 4);
     if (e == cudaSuccess) {
-        k_radix_hist<<<hist_blocks, 512, 0, st>>>(keys, nn, plan, hist, nullptr, 0);
+        launch_radix_hist(hist_blocks, st, keys, nn, plan, hist, nullptr, 0);
         k_radix_hist_scan<<<plan.n, RADIX, 0, st>>>(hist);
         e = cudaGetLastError();
     }
