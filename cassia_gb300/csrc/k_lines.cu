@@ -554,7 +554,7 @@ __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ r
                                                    uint64_t* __restrict__ runs, uint32_t* __restrict__ run_count,
                                                    unsigned long long* __restrict__ produced, FrameCounts* fc,
                                                    const uint32_t* __restrict__ block_lines) {
-    extern __shared__ uint64_t s_out[];  // 2 * RASTER_ITEMS * blockDim.x
+    extern __shared__ __align__(16) uint64_t s_out[];  // 2 * RASTER_ITEMS * blockDim.x
     // The line offsets of the block's step range, staged once: two searches
     // over the whole offset array per block instead of one per thread.
     __shared__ uint32_t s_off[RASTER_LINE_STAGE + 1];
@@ -567,6 +567,15 @@ __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ r
     const bool staged = nl > 0 && nl <= RASTER_LINE_STAGE;
     if (staged)
         for (uint32_t q = threadIdx.x; q <= nl; q += blockDim.x) s_off[q] = off[l0 + q];
+    // Full frames: the block's line records too, loaded together, into the
+    // output stage (free until the steps are walked); the walk then reads
+    // them from shared memory.  Incremental frames skip it: most of their
+    // lines are empty.
+    LineRec* s_recs = reinterpret_cast<LineRec*>(s_out);
+    const bool recs_staged =
+        !SPARSE && staged && nl * sizeof(LineRec) <= 2 * RASTER_ITEMS * blockDim.x * sizeof(uint64_t);
+    if (recs_staged)
+        for (uint32_t q = threadIdx.x; q < nl; q += blockDim.x) s_recs[q] = recs[l0 + q];
     __syncthreads();
     const uint64_t s0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * RASTER_ITEMS;
     uint64_t segs[2 * RASTER_ITEMS];
@@ -594,7 +603,7 @@ __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ r
         }
         uint32_t cur = staged ? s_off[l - l0] : off[l];
         uint32_t next = staged ? s_off[l - l0 + 1] : off[l + 1];
-        LineRec rec = recs[l];
+        LineRec rec = recs_staged ? s_recs[l - l0] : recs[l];
         uint32_t sc = rec.order_octant >> LINE_SCENE_SHIFT;
         SceneRaster sr{bg.scenes[sc].wide, bg.scenes[sc].rows, bg.scenes[sc].row_len, bg.scenes[sc].row_base};
 #pragma unroll
@@ -626,7 +635,7 @@ __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ r
                         cur = staged ? s_off[l - l0] : off[l];
                         next = staged ? s_off[l - l0 + 1] : off[l + 1];
                     }
-                    rec = recs[l];
+                    rec = recs_staged ? s_recs[l - l0] : recs[l];
                     if ((rec.order_octant >> LINE_SCENE_SHIFT) != sc) {
                         sc = rec.order_octant >> LINE_SCENE_SHIFT;
                         sr = SceneRaster{bg.scenes[sc].wide, bg.scenes[sc].rows, bg.scenes[sc].row_len,
@@ -699,7 +708,7 @@ constexpr int IMPORT_ITEMS = 8;
 __global__ void __launch_bounds__(256) k_import_segments(const uint64_t* __restrict__ in, uint64_t n, BatchGeom bg,
                                                          uint64_t* __restrict__ runs, uint32_t* __restrict__ run_count,
                                                          unsigned long long* __restrict__ produced) {
-    extern __shared__ uint64_t s_out[];  // IMPORT_ITEMS * blockDim.x
+    extern __shared__ __align__(16) uint64_t s_out[];  // IMPORT_ITEMS * blockDim.x
     const SceneDesc& sc = bg.scenes[0];
     const SceneRaster sr{sc.wide, sc.rows, sc.row_len, sc.row_base};
     const uint64_t s0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * IMPORT_ITEMS;
