@@ -194,8 +194,8 @@ STAGE_KERNELS = {
 # What bounds each stage's dominant kernel, from the ncu captures summarised
 # in profiles/kernels_mixed20k.md.
 STAGE_LIMITERS = {
-    "rasterize": "fixed-point step arithmetic and barriers of the per-block runs (55% issue active)",
-    "sort": "instruction issue of the onesweep tile's ranking and scatter (56-59% issue active, "
+    "rasterize": "fixed-point step arithmetic (70% issue active) and the latency of its line loads",
+    "sort": "instruction issue of the onesweep tile's ranking and scatter (53-57% issue active, "
             "2.3 TB/s per pass)",
     "paint": "instruction issue and dependent-instruction latency (74% of issue slots, fixed-latency "
              "waits the top stall; not occupancy: more resident warps did not help); its DRAM traffic "
