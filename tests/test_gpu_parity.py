@@ -256,3 +256,46 @@ def test_render_tile_layer_longer_than_scan_blocks():
     stats_segments = g.stats()["segments"]
     assert stats_segments > 3 * 2048
     _assert_same_image(a, b)
+
+
+def test_lines_across_rasterizer_blocks():
+    """Lines longer than a rasterizer block's 2,048 pixel steps, with runs of
+    culled lines (no steps in a render frame) before, between and after them,
+    so that blocks start and end inside long lines and next to empty ones; the
+    same layers rasterized whole by pixel_segments; and an incremental frame,
+    whose sparse rasterizer walks mostly empty lines."""
+    from cassia_gb300 import Composition
+    W, H = 2600, 48
+    g, o = Composition(), oracle.Composition()
+    for c in (g, o):
+        for k in range(40):
+            lid = c.create_layer()
+            if k % 4 == 3:  # a long thin triangle across the canvas
+                y = 1.5 + k
+                p = Path().line((-3.5, y), (W + 2.5, y + 2.7)).line((W + 2.5, y + 2.7), (W / 2, y + 6.1)).close()
+                props = Props(fill_rule=FillRule(int(k % 8 == 3)), func=Style(fill=(0.2, 0.6, 0.9, 0.7)))
+            else:  # above the canvas
+                x = 10.0 * k
+                p = Path().line((x, -300.0), (x + 900.0, -280.0)).line((x + 900.0, -280.0), (x, -250.0)).close()
+                props = solid((1.0, 0.0, 0.0, 1.0))
+            c.insert_in_layer(lid, p)
+            c.set_props(lid, props)
+    g.set_incremental(True)
+    bg = (1.0, 1.0, 1.0, 1.0)
+    a = np.zeros((H, W, 4), np.uint8)
+    b = np.zeros_like(a)
+    g.render(a, W, bg)
+    o.render(b, W, bg, threads=8)
+    _assert_same_image(a, b)
+    assert g.stats()["steps"] > 8 * 2048
+    t = np.array([[0.999, -0.02, 0.02, 0.999, 1.25, -0.5]], np.float32)
+    for c in (g, o):
+        c.set_transforms(np.array([7], np.uint32), t)
+    g.render(a, W, bg)
+    o.render(b, W, bg, threads=8)
+    _assert_same_image(a, b)
+    assert g.stats()["incremental_form"] in (1, 2)
+    gs, gnone = g.pixel_segments(canonical=True)
+    os_, onone = o.pixel_segments(threads=8)
+    assert gnone == onone
+    assert np.array_equal(gs, os_)
