@@ -138,35 +138,21 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const uint32_t* __r
 
 constexpr int RADIX = 512;  // up to 9-bit digits
 constexpr int MAX_PASSES = 11;
-#ifndef CGB_SORT_THREADS
-#define CGB_SORT_THREADS 512
-#endif
-#ifndef CGB_SORT_ITEMS
-#define CGB_SORT_ITEMS 14
-#endif
-#ifndef CGB_SORT_MINB
-#define CGB_SORT_MINB 2
-#endif
-constexpr int SORT_THREADS = CGB_SORT_THREADS;
+// 512 threads (one digit each) x 14 keys: 7,168-key tiles, 2 CTAs per SM at 64
+// registers.  Measured against 8 keys at 3 CTAs per SM, 12 and 16 keys at 2,
+// and 256-thread CTAs: this shape sorts fastest.
+constexpr int SORT_THREADS = RADIX;
 constexpr int SORT_WARPS = SORT_THREADS / 32;
-constexpr int SORT_ITEMS = CGB_SORT_ITEMS;
+constexpr int SORT_ITEMS = 14;
 constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;  // keys per CTA
-constexpr int SORT_DPT = RADIX / SORT_THREADS;       // digits per thread
-constexpr int SORT_MIN_BLOCKS = CGB_SORT_MINB;
-static_assert(SORT_DPT == 1 || SORT_DPT == 2, "one or two digits per thread");
+constexpr int SORT_MIN_BLOCKS = 2;
 static_assert(SORT_TILE < 65536, "per-warp digit offsets are 16-bit");
 constexpr uint32_t ST_AGG = 1u << 30;
 constexpr uint32_t ST_INC = 2u << 30;
 constexpr uint32_t ST_VAL = (1u << 30) - 1;
 constexpr uint32_t SPIN_LIMIT = 1u << 22;  // ~ a second with the back-off below
-#ifndef CGB_LB_WINDOW
-#define CGB_LB_WINDOW 4
-#endif
-#ifndef CGB_LB_SLEEP
-#define CGB_LB_SLEEP 32
-#endif
-constexpr int LB_WINDOW = CGB_LB_WINDOW;  // look-back entries loaded per round
-constexpr unsigned LB_SLEEP = CGB_LB_SLEEP;  // back-off (ns) after a round with no published entry
+constexpr int LB_WINDOW = 4;      // look-back entries loaded per round
+constexpr unsigned LB_SLEEP = 32;  // back-off (ns) after a round with no published entry
 
 struct PassPlan {
     int n;
@@ -356,43 +342,22 @@ __global__ void __launch_bounds__(SORT_THREADS, SORT_MIN_BLOCKS)
             rk[k >> 1] = cnt + r;
     }
     __syncthreads();
-    // Per digit: exclusive offsets across warps and the tile's count.
-    uint32_t cnt[SORT_DPT];
-    const int d0 = tid * SORT_DPT;
-    if constexpr (SORT_DPT == 2) {
-        uint32_t lo = 0, hi = 0;
+    // Per digit (one per thread): exclusive offsets across warps and the tile's count.
+    const int d0 = tid;
+    uint32_t cnt = 0;
 #pragma unroll
-        for (int w = 0; w < SORT_WARPS; w++) {
-            uint32_t* p = reinterpret_cast<uint32_t*>(&s_hist[w][d0]);
-            const uint32_t v = *p;
-            *p = lo | (hi << 16);
-            lo += v & 0xFFFFu;
-            hi += v >> 16;
-        }
-        cnt[0] = lo;
-        cnt[1] = hi;
-    } else {
-        uint32_t sum = 0;
-#pragma unroll
-        for (int w = 0; w < SORT_WARPS; w++) {
-            const uint32_t v = s_hist[w][d0];
-            s_hist[w][d0] = (uint16_t)sum;
-            sum += v;
-        }
-        cnt[0] = sum;
+    for (int w = 0; w < SORT_WARPS; w++) {
+        const uint32_t v = s_hist[w][d0];
+        s_hist[w][d0] = (uint16_t)cnt;
+        cnt += v;
     }
     // The tile's digit counts are published at once (aggregate status; the
     // first tile's are already inclusive), so that later tiles can sum them
     // while this one places its keys in shared memory.
     uint32_t* mine = lookback + (uint64_t)tile * RADIX + d0;
-#pragma unroll
-    for (int j = 0; j < SORT_DPT; j++) st_relaxed(mine + j, (tile == 0 ? ST_INC : ST_AGG) | cnt[j]);
+    st_relaxed(mine, (tile == 0 ? ST_INC : ST_AGG) | cnt);
     // Tile-local digit starts: exclusive scan of the counts over the digits.
-    {
-        const uint32_t ex = block_exclusive_scan<uint32_t>(SORT_DPT == 2 ? cnt[0] + cnt[SORT_DPT - 1] : cnt[0], nullptr);
-        s_start[d0] = ex;
-        if constexpr (SORT_DPT == 2) s_start[d0 + 1] = ex + cnt[0];
-    }
+    s_start[d0] = block_exclusive_scan<uint32_t>(cnt, nullptr);
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < SORT_ITEMS; k++) {
@@ -401,48 +366,30 @@ __global__ void __launch_bounds__(SORT_THREADS, SORT_MIN_BLOCKS)
         if (d < RADIX) s_keys[s_start[d] + s_hist[warp][d] + rank] = key[k];
     }
     // Decoupled look-back for the tile's global digit offsets: each thread
-    // walks back over the predecessors of its digits, LB_WINDOW entries per
+    // walks back over the predecessors of its digit, LB_WINDOW entries per
     // load round, summing until an inclusive prefix, and publishes its own.
-    uint32_t excl[SORT_DPT];
-#pragma unroll
-    for (int j = 0; j < SORT_DPT; j++) excl[j] = 0;
+    uint32_t excl = 0;
     if (tile > 0) {
-        int t[SORT_DPT];  // tiles < 2^30 / SORT_TILE
-        bool done[SORT_DPT];
-#pragma unroll
-        for (int j = 0; j < SORT_DPT; j++) {
-            t[j] = (int)tile - 1;
-            done[j] = false;
-        }
+        int t = (int)tile - 1;  // tiles < 2^30 / SORT_TILE
         uint32_t spins = 0;
-        while (true) {
-            bool progress = false, all = true;
+        while (t >= 0) {
+            uint32_t v[LB_WINDOW];
 #pragma unroll
-            for (int j = 0; j < SORT_DPT; j++) {
-                if (done[j]) continue;
-                uint32_t v[LB_WINDOW];
+            for (int k = 0; k < LB_WINDOW; k++)
+                v[k] = t - k >= 0 ? ld_relaxed(lookback + (size_t)(uint32_t)(t - k) * RADIX + d0) : (ST_INC | 0u);
+            int used = 0;
+            bool inc = false;
 #pragma unroll
-                for (int k = 0; k < LB_WINDOW; k++)
-                    v[k] = t[j] - k >= 0 ? ld_relaxed(lookback + (size_t)(uint32_t)(t[j] - k) * RADIX + d0 + j)
-                                         : (ST_INC | 0u);
-                int used = 0;
-                bool inc = false;
-#pragma unroll
-                for (int k = 0; k < LB_WINDOW; k++) {
-                    if (inc || used < k) break;  // stop at the first inclusive or unpublished entry
-                    const uint32_t stt = v[k] & ~ST_VAL;
-                    if (stt == 0) break;
-                    excl[j] += v[k] & ST_VAL;
-                    used++;
-                    if (stt == ST_INC) inc = true;
-                }
-                t[j] -= used;
-                progress |= used > 0;
-                done[j] = inc;
-                all &= inc;
+            for (int k = 0; k < LB_WINDOW; k++) {
+                if (inc || used < k) break;  // stop at the first inclusive or unpublished entry
+                const uint32_t stt = v[k] & ~ST_VAL;
+                if (stt == 0) break;
+                excl += v[k] & ST_VAL;
+                used++;
+                if (stt == ST_INC) inc = true;
             }
-            if (all) break;
-            if (!progress) {
+            if (inc) break;
+            if (used == 0) {
                 if (++spins > SPIN_LIMIT) {  // a predecessor never published
                     atomicExch(err, 1u);
                     s_abort = 1;
@@ -450,12 +397,11 @@ __global__ void __launch_bounds__(SORT_THREADS, SORT_MIN_BLOCKS)
                 }
                 __nanosleep(LB_SLEEP);
             }
+            t -= used;
         }
-#pragma unroll
-        for (int j = 0; j < SORT_DPT; j++) st_relaxed(mine + j, ST_INC | ((excl[j] + cnt[j]) & ST_VAL));
+        st_relaxed(mine, ST_INC | ((excl + cnt) & ST_VAL));
     }
-#pragma unroll
-    for (int j = 0; j < SORT_DPT; j++) s_off[d0 + j] = global_off[d0 + j] + excl[j] - s_start[d0 + j];
+    s_off[d0] = global_off[d0] + excl - s_start[d0];
     __syncthreads();
     if (s_abort) return;  // a predecessor never published: leave the output, the host reports the timeout
     const uint32_t valid = (n - base) < (uint64_t)SORT_TILE ? (uint32_t)(n - base) : (uint32_t)SORT_TILE;
