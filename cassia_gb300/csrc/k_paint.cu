@@ -62,6 +62,17 @@ __global__ void __launch_bounds__(HEAD_THREADS, 5) k_tl_scan(const uint64_t* __r
                                                           const uint32_t* __restrict__ block_off, CarryBuffers cb) {
     constexpr int mode = MODE;
     n = fc_count(cb.fc, FC_SEGS, n, false);
+    // (graph frames launch blocks for the capacity: those past the count
+    // hold no segments and are not walked)
+    const uint32_t nb = min(gridDim.x, (uint32_t)((n + HEAD_THREADS * HEAD_ITEMS - 1) / (HEAD_THREADS * HEAD_ITEMS)));
+    // mode 1: the next block's cover sum and head flag, loaded first so that
+    // their latency passes while the segments load
+    uint64_t next_cover = 0;
+    uint32_t next_head = 1;
+    if (mode == 1 && threadIdx.x == 0 && blockIdx.x + 1 < nb) {
+        next_cover = cb.blk_cover[blockIdx.x + 1];
+        next_head = cb.blk_head[blockIdx.x + 1];
+    }
     const uint64_t s0 = ((uint64_t)blockIdx.x * HEAD_THREADS + threadIdx.x) * HEAD_ITEMS;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint64_t key[HEAD_ITEMS];
@@ -134,14 +145,13 @@ __global__ void __launch_bounds__(HEAD_THREADS, 5) k_tl_scan(const uint64_t* __r
     }
     if (lane == 31) w_sums[warp] = inc;
     if (mode == 1 && threadIdx.x == 0) {
-        uint64_t x = 0;
-        // (graph frames launch blocks for the capacity: those past the
-        // count hold no segments and are not walked)
-        const uint32_t nb = min(gridDim.x, (uint32_t)((n + HEAD_THREADS * HEAD_ITEMS - 1) / (HEAD_THREADS * HEAD_ITEMS)));
-        for (uint32_t b = blockIdx.x + 1; b < nb; b++) {
-            x = cover_add(x, cb.blk_cover[b]);
-            if (cb.blk_head[b]) break;
-        }
+        // the covers of the following blocks up to the first with a head
+        uint64_t x = next_cover;
+        if (!next_head)
+            for (uint32_t b = blockIdx.x + 2; b < nb; b++) {
+                x = cover_add(x, cb.blk_cover[b]);
+                if (cb.blk_head[b]) break;
+            }
         s_next = x;
     }
     __syncthreads();
