@@ -5,6 +5,7 @@
 //                  path; a count pass, a scan of the counts, a write pass.
 //   k_build_lines  LinesBuilder::build (surpass/src/segment.rs:91-237): one
 //                  thread per line; writes a packed 32-byte LineRec + length.
+//   k_block_lines  the first and last line of each rasterizer block.
 //   k_rasterize    Rasterizer::rasterize (surpass/src/rasterizer/mod.rs:214-285):
 //                  each thread walks 4 or 8 consecutive pixel steps; each block
 //                  block-scans the per-thread counts, stages its segments in

@@ -3,7 +3,8 @@
 // Replaces Rasterizer::sort (surpass/src/rasterizer/mod.rs:287-290), a rayon
 // par_sort_unstable_by_key over `segment >> 22`.  The GPU sort is an LSD radix
 // sort over a caller-chosen bit range with one "onesweep" kernel per digit:
-// each CTA ranks a tile of keys in shared memory (warp match_any multi-split),
+// each CTA ranks a tile of keys in shared memory (warp multi-split: match.any,
+// or ten ballots for a pass whose digits are mostly distinct within a warp),
 // publishes its digit counts, resolves its global digit offsets with a
 // decoupled look-back over the preceding tiles, and scatters the tile through
 // shared memory so that each digit run is written contiguously.  The sort is
