@@ -389,6 +389,128 @@ cgb_status insert_paths(cgb_composition* c, size_t n_paths, const uint32_t* laye
 
 }  // namespace cgb_host
 
+namespace cgb_host {
+
+// A few persistent host threads for per-layer updates of long id lists (a
+// frame that moves every layer of a large scene).  The calling thread works
+// too; run() returns when every part is done.  After a fork the child has no
+// workers, so run() then does all parts itself.
+class HostPool {
+public:
+    static HostPool& get() {
+        static HostPool* pool = new HostPool();  // never destroyed: its threads wait for work until exit
+        return *pool;
+    }
+    int threads() const { return (int)workers_.size() + 1; }
+    void run(int parts, const std::function<void(int)>& f) {
+        std::lock_guard<std::mutex> one(run_mu_);
+        if (workers_.empty() || getpid() != owner_) {
+            for (int p = 0; p < parts; p++) f(p);
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> g(m_);
+            job_ = &f;
+            parts_ = parts;
+            next_.store(0);
+            pending_ = (int)workers_.size();
+            gen_++;
+        }
+        cv_.notify_all();
+        work();
+        std::unique_lock<std::mutex> g(m_);
+        done_cv_.wait(g, [&] { return pending_ == 0; });
+        job_ = nullptr;
+    }
+
+private:
+    HostPool() : owner_(getpid()) {
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        const unsigned n = std::min(7u, hw - 1);
+        for (unsigned i = 0; i < n; i++) workers_.emplace_back([this] { loop(); });
+    }
+    void work() {
+        for (int p; (p = next_.fetch_add(1)) < parts_;) (*job_)(p);
+    }
+    void loop() {
+        uint64_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> g(m_);
+                cv_.wait(g, [&] { return gen_ != seen; });
+                seen = gen_;
+            }
+            work();
+            std::lock_guard<std::mutex> g(m_);
+            if (--pending_ == 0) done_cv_.notify_one();
+        }
+    }
+    std::vector<std::thread> workers_;
+    pid_t owner_;
+    std::mutex m_, run_mu_;
+    std::condition_variable cv_, done_cv_;
+    const std::function<void(int)>* job_ = nullptr;
+    int parts_ = 0;
+    std::atomic<int> next_{0};
+    int pending_ = 0;
+    uint64_t gen_ = 0;
+};
+
+// cgb_layers_set_transforms over many layers at once: when every item takes
+// the common path (an existing layer whose transform stays a non-identity
+// one, within the scale limit) and the ids strictly increase, the items are
+// checked, then applied, by the host pool; the result equals the sequential
+// loop's.  Returns false, having changed nothing, when that does not hold.
+bool set_transforms_parallel(cgb_composition* c, size_t n, const uint32_t* ids, const float* affine6, bool check) {
+    HostPool& pool = HostPool::get();
+    if (pool.threads() < 2) return false;
+    const int parts = pool.threads() * 4;
+    const size_t chunk = (n + parts - 1) / parts;
+    std::vector<uint8_t> ok(parts, 1);
+    pool.run(parts, [&](int p) {
+        const size_t a = (size_t)p * chunk, b = std::min(n, a + chunk);
+        bool good = true;
+        for (size_t i = a; i < b && good; i++) {
+            const uint32_t id = ids[i];
+            const float* t = affine6 + 6 * i;
+            const HostLayer* l = find_layer(c, id);
+            const bool identity = t[0] == 1 && t[1] == 0 && t[2] == 0 && t[3] == 1 && t[4] == 0 && t[5] == 0;
+            good = (i == 0 || id > ids[i - 1]) && l && !identity && l->has_transform && id < c->layer_recs.size() &&
+                   !(check && (t[0] * t[0] + t[2] * t[2] > 1.001f || t[1] * t[1] + t[3] * t[3] > 1.001f));
+        }
+        ok[p] = good;
+    });
+    for (uint8_t g : ok)
+        if (!g) return false;
+    std::vector<uint32_t> lo(parts, UINT32_MAX), hi(parts, 0);
+    pool.run(parts, [&](int p) {
+        const size_t a = (size_t)p * chunk, b = std::min(n, a + chunk);
+        uint32_t plo = UINT32_MAX, phi = 0;
+        for (size_t i = a; i < b; i++) {
+            const uint32_t id = ids[i];
+            const float* t = affine6 + 6 * i;
+            HostLayer& l = c->layers[id];
+            if (l.t[0] == t[0] && l.t[1] == t[1] && l.t[2] == t[2] && l.t[3] == t[3] && l.t[4] == t[4] &&
+                l.t[5] == t[5])
+                continue;  // equal as f32 (Layer::set_transform compares with ==)
+            l.unchanged = 0;
+            std::memcpy(l.t, t, sizeof(l.t));
+            std::memcpy(c->layer_recs[id].t, t, sizeof(l.t));
+            plo = std::min(plo, id);
+            phi = std::max(phi, id + 1);
+        }
+        lo[p] = plo;  // once per part: the parts' slots share cache lines
+        hi[p] = phi;
+    });
+    for (int p = 0; p < parts; p++) {
+        c->dirty_lo = std::min(c->dirty_lo, lo[p]);
+        c->dirty_hi = std::max(c->dirty_hi, hi[p]);
+    }
+    return true;
+}
+
+}  // namespace cgb_host
+
 #define HANDLE_CHECK()                                                      \
     if (!c) return fail(CGB_ERR_INVALID_ARG, "null composition handle");   \
     DeviceGuard _guard(c->device)
@@ -574,6 +696,9 @@ CGB_EXPORT cgb_status cgb_layers_set_transforms(cgb_composition* c, size_t n, co
     if (!c || (n && (!layer_ids || !affine6))) return fail(CGB_ERR_INVALID_ARG, "null argument");
     const bool check = !(flags & CGB_TRANSFORM_UNCHECKED);
     const bool incremental = c->incremental;
+    // long lists (a frame that moves every layer) on the host pool; the
+    // incremental bookkeeping of changed layers stays sequential
+    if (n >= (1u << 14) && !incremental && set_transforms_parallel(c, n, layer_ids, affine6, check)) return CGB_OK;
     for (size_t i = 0; i < n; i++) {
         const uint32_t id = layer_ids[i];
         const float* t = affine6 + 6 * i;

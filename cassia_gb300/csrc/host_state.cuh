@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -15,8 +16,12 @@
 #include <mutex>
 #include <new>
 #include <set>
+#include <functional>
 #include <string>
+#include <thread>
 #include <vector>
+
+#include <unistd.h>
 
 #include <nvtx3/nvToolsExt.h>
 

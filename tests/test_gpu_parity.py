@@ -299,3 +299,43 @@ def test_lines_across_rasterizer_blocks():
     os_, onone = o.pixel_segments(threads=8)
     assert gnone == onone
     assert np.array_equal(gs, os_)
+
+
+def test_many_transforms_in_one_call():
+    """20,000 layer transforms in one call (split over host threads) render as
+    the same update made in calls of 1,000 layers and as the oracle; an
+    invalid transform in the middle of a call leaves the layers before it
+    moved and the rest as they were, as one call per layer would."""
+    from cassia_gb300 import Composition
+    from cassia_gb300.abi import CassiaError
+    sc = scenes.mixed(seed=27, n_layers=20_000, width=256, height=192)
+    g1, o = _load_both(sc)
+    g2 = Composition(wide=sc.wide)
+    scenes.load(sc, g2)
+    ids = np.arange(sc.n_layers, dtype=np.uint32)
+    t = sc.transforms.copy()
+    t[:, 4] += 0.75
+    t[:, 5] -= 0.5
+
+    def chunked(c, tt, unchecked=True):
+        for k in range(0, len(ids), 1000):
+            c.set_transforms(ids[k:k + 1000], tt[k:k + 1000], unchecked=unchecked)
+
+    g1.set_transforms(ids, t)
+    chunked(g2, t)
+    o.set_transforms(ids, t)
+    a, b = _render_both(sc, g1, o)
+    _assert_same_image(a, b)
+    c2 = np.zeros_like(a)
+    g2.render(c2, sc.width, sc.background)
+    _assert_same_image(c2, a)
+    t2 = t.copy()
+    t2[:, 4] -= 2.0
+    t2[15_000, 0] = 1.5  # scale above 1
+    with pytest.raises(CassiaError):
+        g1.set_transforms(ids, t2, unchecked=False)
+    with pytest.raises(CassiaError):
+        chunked(g2, t2, unchecked=False)
+    g1.render(a, sc.width, sc.background)
+    g2.render(c2, sc.width, sc.background)
+    _assert_same_image(c2, a)
