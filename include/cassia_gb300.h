@@ -247,7 +247,10 @@ CGB_EXPORT cgb_status cgb_layers_set_enabled(cgb_composition* c, size_t n, const
 /* Batched set_props: props[k] applies to layer_ids[k]. */
 CGB_EXPORT cgb_status cgb_layers_set_props(cgb_composition* c, size_t n, const uint32_t* layer_ids,
                                            const cgb_props* props);
-/* Batched set_transform for n layers (6 floats each); flags as above. */
+/* Batched set_transform for n layers (6 floats each); flags as above.  The
+ * result equals n set_transform calls in order (up to the first error).  A
+ * long list (16,384 ids or more) of existing layers with increasing ids is
+ * checked and applied by a process-wide pool of host threads. */
 CGB_EXPORT cgb_status cgb_layers_set_transforms(cgb_composition* c, size_t n,
                                                 const uint32_t* layer_ids, const float* affine6,
                                                 uint32_t flags);
