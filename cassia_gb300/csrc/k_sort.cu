@@ -629,7 +629,7 @@ cudaError_t selftest_bounded_wait(cudaStream_t st, uint32_t* flag_host) {
 // histograms, tile counters, the look-back table and the error flag) lives in
 // one file-scope device array instead, sized for at most
 // NOALLOC_MAX_KEYS keys; every GPU that loads this library holds it (about
-// 4 MB) until the process exits.  Every call shares that array and leaves its
+// 5 MB) until the process exits.  Every call shares that array and leaves its
 // contents behind: each call clears what must start at zero, and calls whose
 // work overlaps on the GPU (two streams, or two host threads) race on it.
 // ---------------------------------------------------------------------------

@@ -340,7 +340,7 @@ CGB_EXPORT uint64_t cgb_kernel_launches(void);
  * the sort ping-pongs between it and `out` (n u64), which receives the sorted
  * keys; both are on the current device and must not overlap.  At most
  * 16,777,216 keys (larger n returns CGB_ERR_CAPACITY before any work).  The
- * scratch is one static device array of about 8 MB held by every GPU that
+ * scratch is one static device array of about 5 MB held by every GPU that
  * loads the library; the first call on a device looks up its address, so make
  * that first call before any stream capture.  Calls share the array: calls
  * whose work overlaps on the GPU race, so serialize them.  Runs on `stream`
