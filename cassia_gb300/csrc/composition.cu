@@ -1024,7 +1024,9 @@ CGB_EXPORT cgb_status cgb_selftest_bounded_wait(void) {
         return fail(CGB_ERR_DEVICE, "selftest: stream");
     uint32_t flag = 0;
     cudaError_t e = selftest_bounded_wait(st, &flag);
-    // the context must still work: sort a few keys the normal way
+    // the context must still work: sort a few keys with the pipeline's sort,
+    // on scratch of its own (not the allocation-free entry point's shared
+    // array, which a caller's call on another stream may be using)
     bool sorted_ok = false;
     if (e == cudaSuccess) {
         const uint32_t n_keys = 10000;
@@ -1035,14 +1037,27 @@ CGB_EXPORT cgb_status cgb_selftest_bounded_wait(void) {
             v = x;
         }
         uint64_t* d = nullptr;
-        if (cudaMalloc(&d, 2 * n_keys * 8) == cudaSuccess) {
-            cudaMemcpyAsync(d, host.data(), n_keys * 8, cudaMemcpyHostToDevice, st);
-            cgb_status s = cgb_sort_keys_noalloc(d, d + n_keys, n_keys, 0, 64, st);
+        if (cudaMalloc(&d, 2 * n_keys * 8 + 64) == cudaSuccess) {
+            uint32_t* err = reinterpret_cast<uint32_t*>(d + 2 * n_keys);
+            Scratch scratch;
+            uint64_t* result = nullptr;
+            uint32_t err_host = 0;
+            cudaError_t es = cudaMemsetAsync(err, 0, 4, st);
+            if (es == cudaSuccess) es = cudaMemcpyAsync(d, host.data(), n_keys * 8, cudaMemcpyHostToDevice, st);
+            if (es == cudaSuccess)
+                es = radix_sort_u64(d, d + n_keys, n_keys, 0, 64, 8, &scratch, err, st, &result, nullptr, false,
+                                    nullptr, 0, 0);
             std::vector<uint64_t> back(n_keys);
-            cudaMemcpyAsync(back.data(), d + n_keys, n_keys * 8, cudaMemcpyDeviceToHost, st);
+            if (es == cudaSuccess)
+                es = cudaMemcpyAsync(back.data(), result, n_keys * 8, cudaMemcpyDeviceToHost, st);
+            if (es == cudaSuccess) es = cudaMemcpyAsync(&err_host, err, 4, cudaMemcpyDeviceToHost, st);
             e = cudaStreamSynchronize(st);
             std::sort(host.begin(), host.end());
-            sorted_ok = s == CGB_OK && e == cudaSuccess && back == host;
+            sorted_ok = es == cudaSuccess && e == cudaSuccess && err_host == 0 && back == host;
+            scratch.release(scratch.sort_hist);
+            scratch.release(scratch.sort_lookback);
+            scratch.release(scratch.sort_counter);
+            scratch.release(scratch.scan_sums);
             cudaFree(d);
         }
     }

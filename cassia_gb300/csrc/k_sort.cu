@@ -678,8 +678,19 @@ extern "C" CGB_EXPORT cgb_status cgb_sort_keys_noalloc(uint64_t* keys, uint64_t*
     using namespace cgb;
     if (n > NOALLOC_MAX_KEYS) return CGB_ERR_CAPACITY;
     if (bit_lo >= bit_hi || bit_hi > 64) return CGB_ERR_INVALID_ARG;
-    if (n > 0 && (!keys || !out || keys == out)) return CGB_ERR_INVALID_ARG;
+    if (n > 0 && (!keys || !out)) return CGB_ERR_INVALID_ARG;
+    // the two buffers ping-pong, so any overlap of [keys, keys+n) and [out, out+n) would corrupt the keys
+    if (n > 0 && (uintptr_t)keys < (uintptr_t)(out + n) && (uintptr_t)out < (uintptr_t)(keys + n))
+        return CGB_ERR_INVALID_ARG;
     cudaStream_t st = (cudaStream_t)stream;
+    // The call reads its error flag back and waits for the stream, neither of
+    // which a capturing stream allows: refuse it before any work.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        return CGB_ERR_INVALID_ARG;
+    }
+    if (cap != cudaStreamCaptureStatusNone) return CGB_ERR_INVALID_ARG;
     if (n <= 1) {
         if (n == 1 && cudaMemcpyAsync(out, keys, 8, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
             return CGB_ERR_DEVICE;
@@ -701,7 +712,9 @@ extern "C" CGB_EXPORT cgb_status cgb_sort_keys_noalloc(uint64_t* keys, uint64_t*
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint32_t hist_blocks = std::min<uint32_t>((nn + 511) / 512, (uint32_t)sms * 4);
     if (e == cudaSuccess) {
+        count_launches(1);
         launch_radix_hist(hist_blocks, st, keys, nn, plan, hist, nullptr, 0);
+        count_launches(1 + plan.n);
         k_radix_hist_scan<<<plan.n, RADIX, 0, st>>>(hist);
         e = cudaGetLastError();
     }

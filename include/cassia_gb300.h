@@ -338,14 +338,16 @@ CGB_EXPORT uint64_t cgb_kernel_launches(void);
  * render loop, or owned by another allocator, where cudaMalloc fails or, like
  * cudaFree, synchronizes the device).  `keys` (input, n u64) is overwritten:
  * the sort ping-pongs between it and `out` (n u64), which receives the sorted
- * keys; both are on the current device and must not overlap.  At most
- * 16,777,216 keys (larger n returns CGB_ERR_CAPACITY before any work).  The
- * scratch is one static device array of about 5 MB held by every GPU that
- * loads the library; the first call on a device looks up its address, so make
- * that first call before any stream capture.  Calls share the array: calls
- * whose work overlaps on the GPU race, so serialize them.  Runs on `stream`
- * (a cudaStream_t, NULL for the default stream) and returns once the sort is
- * complete. */
+ * keys; both are on the current device and must not overlap (overlapping
+ * ranges return CGB_ERR_INVALID_ARG).  At most 16,777,216 keys (larger n
+ * returns CGB_ERR_CAPACITY before any work).  The scratch is one static device
+ * array of about 5 MB held by every GPU that loads the library; the first call
+ * on a device looks up its address, so make that first call before any stream
+ * capture.  Calls share the array: calls whose work overlaps on the GPU race,
+ * so serialize them.  Runs on `stream` (a cudaStream_t, NULL for the default
+ * stream) and returns once the sort is complete: it reads an error flag back
+ * and waits for the stream, so a call on a stream that is capturing returns
+ * CGB_ERR_INVALID_ARG before any work. */
 CGB_EXPORT cgb_status cgb_sort_keys_noalloc(uint64_t* keys, uint64_t* out, size_t n, uint32_t bit_lo,
                                             uint32_t bit_hi, void* stream);
 

@@ -65,3 +65,45 @@ def test_noalloc_sort_key_bits_and_limits(gpu_lib):
     assert np.array_equal(np.sort(got), expected)
     # sizes beyond the stated maximum are rejected before any device work
     assert lib.cgb_sort_keys_noalloc(None, None, MAX_KEYS + 1, 0, 64, None) == abi.ERR_CAPACITY
+
+
+SORT_TILE = 7168  # keys one onesweep tile ranks
+
+
+@pytest.mark.parametrize("n", [1, SORT_TILE + 1, MAX_KEYS])
+def test_noalloc_sort_sizes_twice(gpu_lib, n):
+    """One key, one key past a tile, and the stated maximum (where the
+    look-back table uses every tile of the static array), each twice in a row
+    with different keys, against numpy's sort."""
+    from cassia_gb300 import abi
+    lib = abi.load_library()
+    rng = np.random.default_rng(n)
+    for _ in range(2):
+        keys = rng.integers(0, np.iinfo(np.uint64).max, size=n, dtype=np.uint64, endpoint=True)
+        st, got = _sort_noalloc(lib, keys)
+        assert st == abi.OK, abi.STATUS_NAMES.get(st)
+        assert np.array_equal(got, np.sort(keys))
+
+
+def test_noalloc_sort_rejects_overlap_and_capture(gpu_lib):
+    """Overlapping buffers and a capturing stream are refused before any work;
+    the next ordinary call still sorts."""
+    import torch
+    from cassia_gb300 import abi
+    lib = abi.load_library()
+    n = 5000
+    buf = torch.zeros(2 * n, dtype=torch.int64, device="cuda")
+    base = buf.data_ptr()
+    assert lib.cgb_sort_keys_noalloc(ctypes.c_void_p(base), ctypes.c_void_p(base + 8 * (n // 2)), n, 0, 64,
+                                     None) == abi.ERR_INVALID_ARG
+    side = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=side):
+        buf.add_(1)  # something to capture
+        st = lib.cgb_sort_keys_noalloc(ctypes.c_void_p(base), ctypes.c_void_p(base + 8 * n), n, 0, 64,
+                                       ctypes.c_void_p(side.cuda_stream))
+    assert st == abi.ERR_INVALID_ARG
+    keys = np.random.default_rng(5).integers(0, 1 << 62, size=n, dtype=np.uint64)
+    st, got = _sort_noalloc(lib, keys)
+    assert st == abi.OK
+    assert np.array_equal(got, np.sort(keys))
