@@ -11,6 +11,12 @@ default frames are replayed from a captured CUDA graph (the library's graph
 mode: counts stay on the device); --frame-mode staged enqueues each stage and
 reads the counts back between stages.
 
+The default run (mixed100k) then measures the batched form (the 256-scene
+batch workload: one pipeline per group of scenes against one render call per
+scene) and the served form (64 clients, Poisson arrivals, continuous batching
+against one full render per request) and reports them as the "batched" and
+"served" sub-objects of the same JSON line (--no-forms skips them).
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--frame-mode staged|graph]
 
 --impl reference times the CPU restatement of the reference path (the
@@ -380,8 +386,8 @@ def run_batch(args, rank, world, local):
                     "d2h_bytes_per_step": int(sum(s.width * s.height * 4 for s in sset)), "ms_per_step": te * 1e3},
             "gpu_launches": launches, "clocks": clk.summary(), "setup_s": {"scene_gen": gen_s},
         }
-        print(json.dumps(line))
-    return 0
+        return line
+    return None
 
 
 def run_serve(args, rank, world, local):
@@ -454,8 +460,15 @@ def run_serve(args, rank, world, local):
             "speedup_vs_plain": b["frames_per_s_all_ranks"] / p["frames_per_s_all_ranks"],
             "gpu_launches": b["gpu_launches"], "clocks": b["clocks"],
         }
-        print(json.dumps(line))
-    return 0
+        return line
+    return None
+
+
+def scene_config(workload, scene, world):
+    """The workload as both arms name it: the scene, not what a run measured."""
+    return {"workload": workload, "canvas": [scene.width, scene.height], "layers": scene.n_layers,
+            "segment_format": "wide (17-bit layer)" if scene.wide else "reference u16",
+            "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"}
 
 
 def run_reference(args, rank, world):
@@ -468,7 +481,7 @@ def run_reference(args, rank, world):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+int (fixed point)",
         "data": "synthetic (seeded)",
-        "config": {"workload": args.workload, "canvas": [scene.width, scene.height], "layers": scene.n_layers},
+        "config": scene_config(args.workload, scene, world),
         "frames_per_s": r["frames_per_s"],
         "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": r["value"], "unit": "Msegments/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -494,6 +507,8 @@ def main():
     ap.add_argument("--serve-workers", type=int, default=3,
                     help="render workers of the served form (3 measured best: 2 leave the GPU idle during "
                          "host updates, 4 contend for the interpreter)")
+    ap.add_argument("--no-forms", dest="forms", action="store_false",
+                    help="mixed100k: skip the batched (batch256) and served (serve) sub-objects")
     ap.add_argument("--cpu-budget", type=float, default=150.0,
                     help="seconds of host work the reference arm's samples are sized to")
     args = ap.parse_args()
@@ -518,10 +533,12 @@ def main():
     torch.cuda.set_device(local)
     if WORKLOADS[args.workload]["kind"] in ("batch", "serve"):
         fn = run_batch if WORKLOADS[args.workload]["kind"] == "batch" else run_serve
-        rc = fn(args, rank, world, local)
+        line = fn(args, rank, world, local)
+        if line is not None:
+            print(json.dumps(line))
         if dist:
             dist.destroy_process_group()
-        return rc
+        return 0
     from cassia_gb300 import Composition, scenes
     from cassia_gb300.composition import kernel_launches
 
@@ -674,15 +691,12 @@ def main():
             "metric": "Msegments/s", "value": value, "unit": "Msegments/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+int (fixed point)", "data": "synthetic (seeded)",
-            "config": {"workload": args.workload, "canvas": [W, H], "layers": scene.n_layers,
-                       "lines": st["lines"], "segments_per_frame": segs,
-                       "segments_rasterized": st["segments"],
-                       "painted_segments": st["painted_segments"], "tile_layers": st["tile_layers"],
-                       "work_items": st["work_items"],
-                       "segment_format": "wide (17-bit layer)" if scene.wide else "reference u16",
-                       "l2": "inputs larger than L2 (lines %d MB, segments %d MB)" % (
-                           st["lines"] * 20 // 2**20, segs * 8 // 2**20),
-                       "parallelism": f"replicas x{world}"},
+            "config": scene_config(args.workload, scene, world),
+            "frame_counts": {"lines": st["lines"], "segments_per_frame": segs,
+                             "segments_rasterized": st["segments"],
+                             "painted_segments": st["painted_segments"], "tile_layers": st["tile_layers"],
+                             "work_items": st["work_items"], "lines_mb": st["lines"] * 20 // 2**20,
+                             "segments_mb": segs * 8 // 2**20},
             "frames_per_s": world * 1e3 / ms_step,
             "frame_mode": args.frame_mode, "graph_replayed": int(st.get("graph_replayed", 0)),
             "stage_ms": stage_ms,
@@ -700,8 +714,33 @@ def main():
             "clocks": clk.summary(),
             "setup_s": {"scene_gen": gen_s, "load_insert_paths": load_s},
         }
-        print(json.dumps(line))
     comp.close()
+    del out
+    torch.cuda.empty_cache()
+    if args.forms and args.workload == "mixed100k":
+        # the batched (256 scenes) and served (64 clients) forms, each as a
+        # sub-object of the headline line
+        fa = argparse.Namespace(**vars(args))
+        fa.workload, fa.steps, fa.warmup = "batch256", 3, 3
+        b = run_batch(fa, rank, world, local)
+        torch.cuda.empty_cache()
+        fa.workload = "serve"
+        v = run_serve(fa, rank, world, local)
+        torch.cuda.empty_cache()
+        if rank == 0:
+            line["batched"] = {k: b[k] for k in (
+                "metric", "value", "unit", "ms_per_step", "steps", "warmup", "config", "speedup_vs_plain",
+                "speedup_vs_plain_graph", "speedup_vs_plain_staged", "plain_graph_ms_per_pass",
+                "plain_staged_ms_per_pass", "bit_exact_batched_vs_plain", "tuning", "e2e", "gpu_launches", "clocks")}
+            line["served"] = {
+                "metric": v["metric"], "value": v["value"], "unit": v["unit"], "config": v["config"],
+                "p50_ms": v["p50_ms"], "p99_ms": v["p99_ms"], "speedup_vs_plain": v["speedup_vs_plain"],
+                "plain_frames_per_s": v["plain"]["frames_per_s_all_ranks"],
+                "sustained": v["sustained"], "mix_equals_alone_sampled": v["batched"]["mix_equals_alone_sampled"],
+                "requests": v["batched"]["requests"], "mean_batch": v["batched"]["mean_batch"],
+                "gpu_launches": v["gpu_launches"], "clocks": v["clocks"]}
+    if rank == 0:
+        print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
     return 0
