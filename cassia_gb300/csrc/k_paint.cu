@@ -380,39 +380,31 @@ __device__ __forceinline__ float from_area(int32_t area, uint32_t fill_rule) {
 // Packed pixel pairs.  Each lane holds two pixels of a tile row, so every
 // per-pixel operation of the blend is issued as one f32x2 instruction; each
 // element is rounded exactly as the scalar f32 operation (.rn, no flush).
-__device__ __forceinline__ unsigned long long f2u(float2 v) {
-    unsigned long long r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(v.x), "f"(v.y));
-    return r;
-}
-__device__ __forceinline__ float2 u2f(unsigned long long r) {
-    float2 v;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
-    return v;
-}
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
-    unsigned long long d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(f2u(a)), "l"(f2u(b)), "l"(f2u(c)));
-    return u2f(d);
-}
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
-    unsigned long long d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2u(a)), "l"(f2u(b)));
-    return u2f(d);
-}
-__device__ __forceinline__ float2 add2(float2 a, float2 b) {
-    unsigned long long d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2u(a)), "l"(f2u(b)));
-    return u2f(d);
-}
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
-    unsigned long long d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2u(a)), "l"(f2u(b)));
-    return u2f(d);
-}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+// a - b is a + (-b) in IEEE arithmetic: the negation is exact
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
 __device__ __forceinline__ float2 splat(float v) { return make_float2(v, v); }
 __device__ __forceinline__ float2 sel2(bool a, bool b, float2 x, float2 y) {
     return make_float2(a ? x.x : y.x, b ? x.y : y.y);
+}
+
+// SoftLight's per-channel constants of a source colour (style.rs:365-418):
+// (s (1 - s), d - s) with d = ((16 s - 12) s + 4) s for s <= 1/4, else sqrt(s).
+// They depend on the item alone, so the stage computes them once per item.
+__device__ __forceinline__ void soft_light_consts(const float4& c, float4 (&k)[2]) {
+    float sk[3], dk[3];
+    const float sv[3] = {c.x, c.y, c.z};
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const float s = sv[q];
+        const float dd = s <= 0.25f ? __fmaf_rn(__fmaf_rn(16.0f, s, -12.0f), s, 4.0f) * s : sqrtf(s);
+        sk[q] = s * (1.0f - s);
+        dk[q] = dd - s;
+    }
+    k[0] = make_float4(sk[0], sk[1], sk[2], dk[0]);
+    k[1] = make_float4(dk[1], dk[2], 0.0f, 0.0f);
 }
 
 // blend_function! (style.rs:288-418) for a pixel pair
@@ -468,8 +460,25 @@ __device__ __forceinline__ void blend_channels(const float2 (&C)[4], const float
     B[2] = blend_vec2<MODE>(C[2], src.z);
 }
 
+// SoftLight from the item's constants (soft_light_consts): the vector
+// formula's operations on the pixel pair.
+__device__ __forceinline__ void blend_soft_light(const float2 (&C)[4], const float4& src, const float4* hk,
+                                                 float2 (&B)[3]) {
+    const float4 k0 = hk[0], k1 = hk[1];
+    const float sk[3] = {k0.x, k0.y, k0.z}, dk[3] = {k0.w, k1.x, k1.y}, sv[3] = {src.x, src.y, src.z};
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const float2 d = C[q];
+        const float2 k = fma2(splat(2.0f), d, splat(-1.0f));
+        const float2 lo = fma2(splat(sk[q]), k, splat(sv[q]));
+        const float2 hi = fma2(splat(dk[q]), k, splat(sv[q]));
+        B[q] = sel2(d.x <= 0.5f, d.y <= 0.5f, lo, hi);
+    }
+}
+
+// hk: the item's SoftLight constants (read only for that mode).
 __device__ __forceinline__ void blend_channels(uint32_t mode, const float2 (&C)[4], const float4& src,
-                                               float2 (&B)[3]) {
+                                               const float4* hk, float2 (&B)[3]) {
     switch (mode) {
         case CGB_BLEND_OVER: blend_channels<CGB_BLEND_OVER>(C, src, B); break;
         case CGB_BLEND_MULTIPLY: blend_channels<CGB_BLEND_MULTIPLY>(C, src, B); break;
@@ -480,7 +489,7 @@ __device__ __forceinline__ void blend_channels(uint32_t mode, const float2 (&C)[
         case CGB_BLEND_COLOR_DODGE: blend_channels<CGB_BLEND_COLOR_DODGE>(C, src, B); break;
         case CGB_BLEND_COLOR_BURN: blend_channels<CGB_BLEND_COLOR_BURN>(C, src, B); break;
         case CGB_BLEND_HARD_LIGHT: blend_channels<CGB_BLEND_HARD_LIGHT>(C, src, B); break;
-        case CGB_BLEND_SOFT_LIGHT: blend_channels<CGB_BLEND_SOFT_LIGHT>(C, src, B); break;
+        case CGB_BLEND_SOFT_LIGHT: blend_soft_light(C, src, hk, B); break;
         case CGB_BLEND_DIFFERENCE: blend_channels<CGB_BLEND_DIFFERENCE>(C, src, B); break;
         default: blend_channels<CGB_BLEND_EXCLUSION>(C, src, B); break;
     }
@@ -490,12 +499,12 @@ __device__ __forceinline__ void blend_channels(uint32_t mode, const float2 (&C)[
 // C[q] holds channel q of the two pixels; a pixel whose column is not blended
 // keeps its color.  MASKED = false when both columns of every lane are
 // blended (cover-carry-only items: every column has the same per-row coverage).
+// al = src.w * coverage, the pixel pair's alpha; hk: the item's SoftLight constants.
 template <bool MASKED>
-__device__ __forceinline__ void blend_dispatch(uint32_t mode, float2 (&C)[4], const float4& src, float2 cov,
-                                               bool col0, bool col1) {
+__device__ __forceinline__ void blend_dispatch_al(uint32_t mode, float2 (&C)[4], const float4& src,
+                                                  const float4* hk, float2 al, bool col0, bool col1) {
     float2 B[3];
-    blend_channels(mode, C, src, B);
-    const float2 al = mul2(splat(src.w), cov);
+    blend_channels(mode, C, src, hk, B);
     const float2 inv = sub2(splat(1.0f), al);
     const float2 n0 = fma2(C[0], inv, mul2(B[0], al));
     const float2 n1 = fma2(C[1], inv, mul2(B[1], al));
@@ -512,6 +521,12 @@ __device__ __forceinline__ void blend_dispatch(uint32_t mode, float2 (&C)[4], co
         C[2] = n2;
         C[3] = n3;
     }
+}
+
+template <bool MASKED>
+__device__ __forceinline__ void blend_dispatch(uint32_t mode, float2 (&C)[4], const float4& src, const float4* hk,
+                                               float2 cov, bool col0, bool col1) {
+    blend_dispatch_al<MASKED>(mode, C, src, hk, mul2(splat(src.w), cov), col0, col1);
 }
 
 // blend_function! (style.rs:288-418) for one pixel: blend_vec2's operations
@@ -733,7 +748,8 @@ constexpr uint8_t ISTATE_SKIP_CLIP = 2;  // clipped, but its clip is full: drawn
 // Per-warp staging of 32 work items.
 struct WarpStage {
     float4 color[32];
-    float4 rowcov[32][2];  // carry-only items: coverage of each tile row
+    float4 rowcov[32][2];  // carry-only items: coverage (FULL) or alpha of each tile row
+    float4 hoist[32][2];   // SoftLight items: soft_light_consts of the colour
     uint64_t carry[32];    // cover entering the tile (TL items)
     uint32_t meta[32];     // blend_mode | fill_rule << 4 | META_*
     uint32_t order[32];    // the item's layer order
@@ -765,6 +781,7 @@ __device__ __forceinline__ void stage_items(const PaintArgs& a, const SceneDesc&
         const uint32_t co = (fl & ITEM_CARRY) ? 1u : 0u;
         const uint32_t fr = hdr.x & 1u;
         meta = (hdr.y & 15u) | (fr << 4);
+        if ((hdr.y & 15u) == CGB_BLEND_SOFT_LIGHT) soft_light_consts(col, S.hoist[lane]);
         if (FULL) {
             if (hdr.z & PROPS_CLIP) {
                 // `layer + *layers as u16` (mold's u16 arithmetic; 17 bits in the widened format)
@@ -786,12 +803,15 @@ __device__ __forceinline__ void stage_items(const PaintArgs& a, const SceneDesc&
             if (with_segments) {
                 // every pixel of a tile row has the row's coverage; the
                 // layer's columns are blended iff some row is covered
+                // (the plain painter stores each row's alpha, fill alpha x
+                // coverage, the first product of blend_at)
                 float rc[8];
                 bool any = false;
 #pragma unroll
                 for (int yy = 0; yy < 8; yy++) {
                     rc[yy] = from_area(PIXEL_WIDTH * cover_lane(carry, yy), fr);
                     any |= rc[yy] != 0.0f;
+                    if (!FULL) rc[yy] = col.w * rc[yy];
                 }
                 S.rowcov[lane][0] = make_float4(rc[0], rc[1], rc[2], rc[3]);
                 S.rowcov[lane][1] = make_float4(rc[4], rc[5], rc[6], rc[7]);
@@ -1075,6 +1095,13 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
                 float2 cov;
                 bool col0, col1;
                 if (meta & META_CARRY_ONLY) {
+                    if (!FULL) {
+                        if (!(meta & META_ACTIVE)) continue;
+                        blend_dispatch_al<false>(mode, C, S.color[q], S.hoist[q],
+                                                 splat(reinterpret_cast<const float*>(&S.rowcov[q][0])[y]), true,
+                                                 true);
+                        continue;
+                    }
                     cov = splat(reinterpret_cast<const float*>(&S.rowcov[q][0])[y]);
                     if (clips && (meta & META_CLIP)) {
                         if (!has_clip) {
@@ -1094,7 +1121,7 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
                         }
                         blend_dispatch_src(mode, C, src, cov, true, true, apply, clip_mask);
                     } else {
-                        blend_dispatch<false>(mode, C, S.color[q], cov, true, true);
+                        blend_dispatch<false>(mode, C, S.color[q], S.hoist[q], cov, true, true);
                     }
                     continue;
                 } else {
@@ -1153,7 +1180,7 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
                     }
                     blend_dispatch_src(mode, C, src, cov, col0, col1, apply, clip_mask);
                 } else {
-                    blend_dispatch<true>(mode, C, S.color[q], cov, col0, col1);
+                    blend_dispatch<true>(mode, C, S.color[q], S.hoist[q], cov, col0, col1);
                 }
             }
             __syncwarp();
