@@ -207,6 +207,14 @@ extern "C" {
     ) -> cgb_status;
     pub fn cgb_insert_lines(c: *mut cgb_composition, layer_id: u32, segments: *const f32, n_lines: usize) -> cgb_status;
 
+    pub fn cgb_insert_layer_copies(
+        c: *mut cgb_composition,
+        n: usize,
+        layer_ids: *const u32,
+        src: *mut cgb_composition,
+        src_layer_ids: *const u32,
+    ) -> cgb_status;
+
     pub fn cgb_layer_set_enabled(c: *mut cgb_composition, layer_id: u32, enabled: c_int) -> cgb_status;
     pub fn cgb_layer_set_transform(c: *mut cgb_composition, layer_id: u32, affine6: *const f32, flags: u32) -> cgb_status;
     pub fn cgb_layer_set_order(c: *mut cgb_composition, layer_id: u32, order: u32) -> cgb_status;
@@ -257,6 +265,7 @@ extern "C" {
     pub fn cgb_get_tuning(c: *mut cgb_composition, out: *mut cgb_tuning) -> cgb_status;
     pub fn cgb_synchronize(c: *mut cgb_composition) -> cgb_status;
     pub fn cgb_get_stream(c: *mut cgb_composition, out_stream: *mut *mut c_void) -> cgb_status;
+    pub fn cgb_get_memory(c: *mut cgb_composition, device_bytes: *mut u64) -> cgb_status;
     pub fn cgb_kernel_launches() -> u64;
 
     pub fn cgb_sort_keys_noalloc(

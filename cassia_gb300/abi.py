@@ -167,6 +167,8 @@ def _declare(lib):
         "cgb_insert_in_layer": ([handle, u32, P(u32), sz, fp, sz, fp], i32),
         "cgb_insert_paths": ([handle, sz, P(u32), P(u64), P(u32), P(u64), fp, fp, P(ctypes.c_uint8)], i32),
         "cgb_insert_lines": ([handle, u32, fp, sz], i32),
+        "cgb_insert_layer_copies": ([handle, sz, P(u32), handle, P(u32)], i32),
+        "cgb_get_memory": ([handle, P(u64)], i32),
         "cgb_layer_set_enabled": ([handle, u32, ctypes.c_int], i32),
         "cgb_layer_set_transform": ([handle, u32, fp, u32], i32),
         "cgb_layer_set_order": ([handle, u32, u32], i32),

@@ -136,6 +136,23 @@ class Composition:
         segs = np.ascontiguousarray(np.asarray(segs, np.float32).reshape(-1, 4))
         _check(self._lib, self._lib.cgb_insert_lines(self._h, layer_id, _fp(segs), len(segs)), "insert_lines")
 
+    def insert_layer_copies(self, layer_ids, src: "Composition", src_layer_ids):
+        """insert_in_layer of paths already flattened into `src`: layer
+        layer_ids[k] gets a copy of the lines src holds for src_layer_ids[k]
+        (device to device, no flattening, no wait)."""
+        ids = np.ascontiguousarray(layer_ids, np.uint32)
+        sids = np.ascontiguousarray(src_layer_ids, np.uint32)
+        if len(ids) != len(sids):
+            raise ValueError("layer_ids and src_layer_ids differ in length")
+        _check(self._lib, self._lib.cgb_insert_layer_copies(self._h, len(ids), _u32p(ids), src._h, _u32p(sids)),
+               "insert_layer_copies")
+
+    def device_bytes(self) -> int:
+        """Device memory the handle holds (what its HBM budget is checked against)."""
+        out = ctypes.c_uint64()
+        _check(self._lib, self._lib.cgb_get_memory(self._h, ctypes.byref(out)), "get_memory")
+        return out.value
+
     def set_enabled(self, layer_id: int, enabled: bool):
         _check(self._lib, self._lib.cgb_layer_set_enabled(self._h, layer_id, int(bool(enabled))), "set_enabled")
 

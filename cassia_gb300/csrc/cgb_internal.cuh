@@ -284,6 +284,12 @@ uint32_t raster_grid(uint64_t n_steps, uint32_t block, uint32_t items);
 cudaError_t launch_compact_lines(const float* in4[4], const uint32_t* lid_in, uint32_t n, const LayerRec* layers,
                                  uint32_t n_layer_recs, float* out4[4], uint32_t* lid_out, uint32_t* flags,
                                  uint32_t* offsets, Scratch* s, cudaStream_t st, uint32_t* n_out_host);
+// Appends copies of n line runs: run k starts at src4[*][src_first[k]] and
+// lands at dst4[*][dst_off[k] .. dst_off[k + 1]) with layer id dst_ids[k];
+// total = dst_off[n].
+cudaError_t launch_copy_lines(const float* const src4[4], const uint64_t* src_first, const uint64_t* dst_off,
+                              const uint32_t* dst_ids, uint32_t n, uint64_t total, float* const dst4[4],
+                              uint32_t* dst_lids, cudaStream_t st);
 
 // k_sort.cu
 // Exclusive scan of n u32 values; out has n+1 entries (out[n] = total mod 2^32).

@@ -164,12 +164,21 @@ void release_id(cgb_composition* c, uint32_t id) {
 }
 
 // insert_segments bookkeeping (mold/src/composition.rs:58-79)
-void insert_bookkeeping(cgb_composition* c, uint32_t id, uint64_t n) {
+// n lines were appended to layer `id` at builder position `first`.
+void insert_bookkeeping(cgb_composition* c, uint32_t id, uint64_t n, uint64_t first) {
     if (id >= c->layers.size()) c->layers.resize((size_t)id + 1);
     HostLayer& l = c->layers[id];
     if (!l.present) {
         l = HostLayer();
         l.present = true;
+    }
+    if (n > 0) {
+        if (l.len == 0) {
+            l.first_line = first;
+            l.contiguous = true;
+        } else if (l.first_line + l.len != first) {
+            l.contiguous = false;
+        }
     }
     const uint64_t before = l.enabled ? l.len : 0;
     l.has_order = true;
@@ -290,6 +299,7 @@ cgb_status remove_disabled(cgb_composition* c) {
             CK(cudaMemcpyAsync(arrs[k]->p, c->g_tmp[k].p, (size_t)kept * 4, cudaMemcpyDeviceToDevice, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         c->n_lines = kept;
+        for (HostLayer& l : c->layers) l.contiguous = false;  // the kept lines moved
     }
     for (uint32_t id = 0; id < c->layers.size(); id++) {
         HostLayer& l = c->layers[id];
@@ -383,7 +393,11 @@ cgb_status insert_paths(cgb_composition* c, size_t n_paths, const uint32_t* laye
     CK(cudaMemcpyAsync(counts.data(), c->f_counts.p, n_paths * 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     c->n_lines += total;
-    for (size_t k = 0; k < n_paths; k++) insert_bookkeeping(c, layer_ids[k], counts[k]);
+    uint64_t at = base;
+    for (size_t k = 0; k < n_paths; k++) {
+        insert_bookkeeping(c, layer_ids[k], counts[k], at);
+        at += counts[k];
+    }
     return CGB_OK;
 }
 
@@ -643,7 +657,57 @@ CGB_EXPORT cgb_status cgb_insert_lines(cgb_composition* c, uint32_t layer_id, co
         CK(cudaStreamSynchronize(c->stream));
     }
     c->n_lines += n_lines;
-    insert_bookkeeping(c, layer_id, n_lines);
+    insert_bookkeeping(c, layer_id, n_lines, c->n_lines - n_lines);
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_insert_layer_copies(cgb_composition* c, size_t n, const uint32_t* layer_ids,
+                                              cgb_composition* src, const uint32_t* src_layer_ids) {
+    HANDLE_CHECK();
+    if (n == 0) return CGB_OK;
+    if (!src || !layer_ids || !src_layer_ids) return fail(CGB_ERR_INVALID_ARG, "insert_layer_copies: null argument");
+    if (src->device != c->device) return fail(CGB_ERR_INVALID_ARG, "insert_layer_copies: handles on two devices");
+    if (n >= (1u << 31)) return fail(CGB_ERR_INVALID_ARG, "insert_layer_copies: too many layers");
+    // runs: the source's first line of each copy, then each copy's offset in the appended lines
+    std::vector<uint64_t> runs(2 * n + 1);
+    uint64_t total = 0;
+    for (size_t k = 0; k < n; k++) {
+        if (layer_ids[k] >= c->max_ids) return fail(CGB_ERR_LAYER_LIMIT, "insert_layer_copies: layer id out of range");
+        const HostLayer* l = find_layer(src, src_layer_ids[k]);
+        if (!l) return fail(CGB_ERR_NOT_FOUND, "insert_layer_copies: unknown source layer");
+        if (l->len > 0 && !l->contiguous)
+            return fail(CGB_ERR_INVALID_ARG, "insert_layer_copies: the source layer's lines are not one run");
+        runs[k] = l->first_line;
+        runs[n + k] = total;
+        total += l->len;
+    }
+    runs[2 * n] = total;
+    if (c->n_lines + total >= (1ull << 32)) return fail(CGB_ERR_LAYER_LIMIT, "insert_layer_copies: too many lines");
+    // (when src == c, growing the arrays keeps the old lines in place)
+    CK(ensure_lines(c, c->n_lines + total));
+    const float* src4[4] = {src->p0x.as<float>(), src->p0y.as<float>(), src->p1x.as<float>(), src->p1y.as<float>()};
+    const uint64_t base = c->n_lines;
+    float* dst4[4] = {c->p0x.as<float>() + base, c->p0y.as<float>() + base, c->p1x.as<float>() + base,
+                      c->p1y.as<float>() + base};
+    CK(c->s.ensure(c->f_cmd_off, runs.size() * 8));
+    CK(c->s.ensure(c->f_path_layer, n * 4));
+    uint64_t* d_runs = c->f_cmd_off.as<uint64_t>();
+    CK(cudaMemcpyAsync(d_runs, runs.data(), runs.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->f_path_layer.p, layer_ids, n * 4, cudaMemcpyHostToDevice, c->stream));
+    if (src != c) {  // the source's lines are complete before they are copied
+        CK(cudaEventRecord(c->ev[7], src->stream));
+        CK(cudaStreamWaitEvent(c->stream, c->ev[7], 0));
+    }
+    CK(launch_copy_lines(src4, d_runs, d_runs + n, c->f_path_layer.as<uint32_t>(), (uint32_t)n, total, dst4,
+                         c->lids.as<uint32_t>() + base, c->stream));
+    c->n_lines += total;
+    for (size_t k = 0; k < n; k++) insert_bookkeeping(c, layer_ids[k], runs[n + k + 1] - runs[n + k], base + runs[n + k]);
+    return CGB_OK;
+}
+
+CGB_EXPORT cgb_status cgb_get_memory(cgb_composition* c, uint64_t* device_bytes) {
+    if (!c || !device_bytes) return fail(CGB_ERR_INVALID_ARG, "null argument");
+    *device_bytes = c->s.used;
     return CGB_OK;
 }
 

@@ -77,6 +77,10 @@ struct alignas(64) HostLayer {
     float t[6] = {1, 0, 0, 1, 0, 0};
     uint64_t len = 0;
     HostProps props = default_props();
+    // Where the layer's lines sit in the builder: one run [first_line,
+    // first_line + len) while `contiguous` (cgb_insert_layer_copies reads it).
+    uint64_t first_line = 0;
+    bool contiguous = true;
 };
 
 struct CacheState {

@@ -879,6 +879,42 @@ cudaError_t launch_import_segments(const uint64_t* segs, uint64_t n, const Batch
 uint32_t import_grid(uint64_t n) { return (uint32_t)((n + 256 * IMPORT_ITEMS - 1) / (256 * IMPORT_ITEMS)); }
 uint32_t import_run_slots() { return 256 * IMPORT_ITEMS; }
 
+// Line copies for cgb_insert_layer_copies: one thread per copied line finds
+// its run by a binary search over the run offsets.
+__global__ void k_copy_lines(const float* __restrict__ sx0, const float* __restrict__ sy0,
+                             const float* __restrict__ sx1, const float* __restrict__ sy1,
+                             const uint64_t* __restrict__ src_first, const uint64_t* __restrict__ dst_off,
+                             const uint32_t* __restrict__ dst_ids, uint32_t n, uint64_t total, float* __restrict__ dx0,
+                             float* __restrict__ dy0, float* __restrict__ dx1, float* __restrict__ dy1,
+                             uint32_t* __restrict__ dlid) {
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < total;
+         j += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = n;  // the last run k with dst_off[k] <= j
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (dst_off[mid] <= j) lo = mid;
+            else hi = mid;
+        }
+        const uint64_t s = src_first[lo] + (j - dst_off[lo]);
+        dx0[j] = sx0[s];
+        dy0[j] = sy0[s];
+        dx1[j] = sx1[s];
+        dy1[j] = sy1[s];
+        dlid[j] = dst_ids[lo];
+    }
+}
+
+cudaError_t launch_copy_lines(const float* const src4[4], const uint64_t* src_first, const uint64_t* dst_off,
+                              const uint32_t* dst_ids, uint32_t n, uint64_t total, float* const dst4[4],
+                              uint32_t* dst_lids, cudaStream_t st) {
+    if (total == 0 || n == 0) return cudaSuccess;
+    const uint64_t blocks = std::min<uint64_t>((total + 255) / 256, 4096);
+    count_launches(1);
+    k_copy_lines<<<(uint32_t)blocks, 256, 0, st>>>(src4[0], src4[1], src4[2], src4[3], src_first, dst_off, dst_ids,
+                                                   n, total, dst4[0], dst4[1], dst4[2], dst4[3], dst_lids);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_compact_lines(const float* in4[4], const uint32_t* lid_in, uint32_t n, const LayerRec* layers,
                                  uint32_t n_layer_recs, float* out4[4], uint32_t* lid_out, uint32_t* flags,
                                  uint32_t* offsets, Scratch* s, cudaStream_t st, uint32_t* n_out_host) {

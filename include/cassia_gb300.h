@@ -234,6 +234,18 @@ CGB_EXPORT cgb_status cgb_insert_paths(cgb_composition* c, size_t n_paths,
 CGB_EXPORT cgb_status cgb_insert_lines(cgb_composition* c, uint32_t layer_id,
                                        const float* segments, size_t n_lines);
 
+/* Composition::insert_in_layer (mold/src/composition.rs:58-94) of a path
+ * that is already flattened: appends to layer layer_ids[k] a copy of the lines
+ * that `src` holds for its layer src_layer_ids[k] (src may be `c`), device to
+ * device, without flattening again and without waiting for the device.  A
+ * source layer's lines must be one run: lines inserted by one call (or by
+ * consecutive calls with nothing inserted in between), not moved since by
+ * cgb_remove_disabled's garbage collection (CGB_ERR_INVALID_ARG otherwise).
+ * Both handles are on one device; `src` must not be used by another thread
+ * during the call. */
+CGB_EXPORT cgb_status cgb_insert_layer_copies(cgb_composition* c, size_t n, const uint32_t* layer_ids,
+                                              cgb_composition* src, const uint32_t* src_layer_ids);
+
 /* Layer setters (mold/src/layer.rs:158-231).  set_transform(NULL) = identity. */
 CGB_EXPORT cgb_status cgb_layer_set_enabled(cgb_composition* c, uint32_t layer_id, int enabled);
 CGB_EXPORT cgb_status cgb_layer_set_transform(cgb_composition* c, uint32_t layer_id,
@@ -327,6 +339,10 @@ CGB_EXPORT cgb_status cgb_synchronize(cgb_composition* c);
 /* The cudaStream_t the handle launches on (for callers that order their own
  * work or timing events after a render). */
 CGB_EXPORT cgb_status cgb_get_stream(cgb_composition* c, void** out_stream);
+
+/* Device memory the handle holds (its lines, layer tables, frame buffers,
+ * resident segments): what its HBM budget is checked against. */
+CGB_EXPORT cgb_status cgb_get_memory(cgb_composition* c, uint64_t* device_bytes);
 
 /* Kernels this library has launched in the process (all handles). */
 CGB_EXPORT uint64_t cgb_kernel_launches(void);
