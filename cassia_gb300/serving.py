@@ -48,6 +48,7 @@ class Client:
     done_seq: int = -1
     pool: Optional[scenes.Scene] = None  # shapes new layers are drawn from
     pool_next: int = 0
+    pool_comp: Optional[Composition] = None  # the pool's shapes flattened once, layer k = shape k
 
 
 def poisson_arrivals(rate: float, n_clients: int, duration: float, seed: int = 0) -> List[Request]:
@@ -86,14 +87,21 @@ def make_clients(n_clients: int, seed: int, device_out: bool = True, max_layers:
         else:
             out = np.zeros((sc.height, sc.width, 4), np.uint8)
         pool = scenes.mixed(seed=seed * 7919 + k, n_layers=256, width=sc.width, height=sc.height)
-        clients.append(Client(c, sc, out, np.ones(sc.n_layers, bool), sc.transforms.copy(), pool=pool))
+        # the pool's shapes flattened once on the device: an added layer takes
+        # a copy of its shape's lines instead of flattening the path again
+        pool_comp = Composition()
+        pool_comp.create_layers(pool.n_layers)
+        pool_comp.insert_paths(pool)
+        clients.append(Client(c, sc, out, np.ones(sc.n_layers, bool), sc.transforms.copy(), pool=pool,
+                              pool_comp=pool_comp))
     return clients
 
 
-def _mix64(ids: np.ndarray, salt: int) -> np.ndarray:
-    """splitmix64 of each id and a salt, vectorized (array integer arithmetic
-    wraps silently)."""
-    z = ids.astype(np.uint64) * np.uint64(0x9E3779B97F4A7C15) + np.uint64(salt & 0xFFFFFFFFFFFFFFFF)
+def _mix64(ids: np.ndarray, salt) -> np.ndarray:
+    """splitmix64 of each id and a salt (a scalar or one per id), vectorized
+    (array integer arithmetic wraps silently)."""
+    salt = np.asarray(salt, np.uint64) if np.ndim(salt) else np.uint64(salt & 0xFFFFFFFFFFFFFFFF)
+    z = ids.astype(np.uint64) * np.uint64(0x9E3779B97F4A7C15) + salt
     z ^= z >> np.uint64(30)
     z *= np.uint64(0xBF58476D1CE4E5B9)
     z ^= z >> np.uint64(27)
@@ -112,37 +120,67 @@ def _u01(ids: np.ndarray, salt: int) -> np.ndarray:
     return _bits01(_mix64(ids, salt), 11, 53)
 
 
+def _salt(client_id: int, seq: int) -> int:
+    return ((client_id << 40) ^ (seq * 0x9E3779B1)) & 0xFFFFFFFFFFFFFFFF
+
+
 def apply_update(cl: Client, client_id: int, seq: int, changed: float = 0.2, churn: float = 0.01):
-    """The scene update of frame `seq`: each enabled layer gets a new affine
-    with probability `changed` and is removed with probability `churn`
-    (seeded per client and frame); as many layers as were removed are added."""
-    live = np.flatnonzero(cl.enabled).astype(np.uint32)
-    if len(live) == 0:
+    """The scene update of frame `seq` of one client (apply_updates of one)."""
+    apply_updates([(cl, client_id, seq)], changed, churn)
+
+
+def apply_updates(items, changed: float = 0.2, churn: float = 0.01):
+    """The scene updates of a batch, one (client, client id, frame seq) per
+    distinct client: each enabled layer gets a new affine with probability
+    `changed` and is removed with probability `churn` (seeded per client and
+    frame); as many layers as were removed are added.  The random draws of
+    the whole batch are made by a few array operations over all its clients
+    (integer hashing and IEEE float32 arithmetic only, so each client's
+    update is the same whether it is drawn alone or in a batch); then each
+    client's calls are made."""
+    assert len({id(cl) for cl, _, _ in items}) == len(items), "one update per client"
+    lives = [np.flatnonzero(cl.enabled).astype(np.uint32) for cl, _, _ in items]
+    items = [it for it, live in zip(items, lives) if len(live)]
+    lives = [live for live in lives if len(live)]
+    if not items:
         return
-    salt = (client_id << 40) ^ (seq * 0x9E3779B1)
+    lens = np.array([len(x) for x in lives])
+    salts = np.array([_salt(cid, seq) for _, cid, seq in items], np.uint64)
     # one hash per live layer: 24 bits decide the new affine, 24 others the removal
-    z = _mix64(live, salt)
-    ids = live[_bits01(z, 40, 24) < changed]
-    if len(ids) == 0:
-        ids = live[:1]
-    # one hash per changed layer: rotation U[-0.05, 0.05), shift U[-3, 3)^2
-    w = _mix64(ids, salt ^ 0x2545F4914F6CDD1D)
-    th = ((_bits01(w, 42, 21) - 0.5) * 0.1).astype(np.float32)
-    t = cl.transforms[ids]
-    c, s = np.cos(th), np.sin(th)
+    z = _mix64(np.concatenate(lives), np.repeat(salts, lens))
+    chg = _bits01(z, 40, 24) < changed
+    rem = _bits01(z, 16, 24) < churn
+    offs = np.concatenate([[0], np.cumsum(lens)])
+    ids = []
+    for k, live in enumerate(lives):
+        sel = live[chg[offs[k]:offs[k + 1]]]
+        ids.append(sel if len(sel) else live[:1])
+    # one hash per changed layer: a rotation by 2 atan(u), u U[-0.025, 0.025),
+    # as the rational (1 - u^2, 2u) / (1 + u^2), and a shift U[-3, 3)^2
+    nid = np.array([len(x) for x in ids])
+    w = _mix64(np.concatenate(ids), np.repeat(salts ^ np.uint64(0x2545F4914F6CDD1D), nid))
+    u = ((_bits01(w, 42, 21) - 0.5) * 0.05).astype(np.float32)
+    uu = u * u
+    den = np.float32(1.0) + uu
+    c = (np.float32(1.0) - uu) / den
+    s = (np.float32(2.0) * u) / den
+    t = np.concatenate([cl.transforms[x] for (cl, _, _), x in zip(items, ids)])
     a, b, cc, d = t[:, 0].copy(), t[:, 1].copy(), t[:, 2].copy(), t[:, 3].copy()
     t[:, 0], t[:, 1] = c * a - s * cc, c * b - s * d
     t[:, 2], t[:, 3] = s * a + c * cc, s * b + c * d
     t[:, 4] += ((_bits01(w, 21, 21) - 0.5) * 6.0).astype(np.float32)
     t[:, 5] += ((_bits01(w, 0, 21) - 0.5) * 6.0).astype(np.float32)
-    cl.transforms[ids] = t
-    cl.comp.set_transforms(ids, t)
-    gone = live[_bits01(z, 16, 24) < churn]
-    if len(gone):
-        cl.comp.set_enabled_many(gone, np.zeros(len(gone), np.uint8))
-        cl.enabled[gone] = False
-        cl.comp.remove_disabled()  # mold's GC: drops the disabled layers at 50% garbage
-        add_layers(cl, len(gone))
+    toff = np.concatenate([[0], np.cumsum(nid)])
+    for k, (cl, _, _) in enumerate(items):
+        tk = t[toff[k]:toff[k + 1]]
+        cl.transforms[ids[k]] = tk
+        cl.comp.set_transforms(ids[k], tk)
+        gone = lives[k][rem[offs[k]:offs[k + 1]]]
+        if len(gone):
+            cl.comp.set_enabled_many(gone, np.zeros(len(gone), np.uint8))
+            cl.enabled[gone] = False
+            cl.comp.remove_disabled()  # mold's GC: drops the disabled layers at 50% garbage
+            add_layers(cl, len(gone))
 
 
 def _pool_runs(start: int, n: int, size: int):
@@ -158,12 +196,31 @@ def _pool_runs(start: int, n: int, size: int):
 
 def add_layers(cl: Client, n: int):
     """Adds n layers drawn in turn from the client's shape pool (one path
-    per pool layer), with one insert call."""
+    per pool layer), with one insert call: copies of the shapes' lines from
+    the pool's composition when the client has one, else the paths (the
+    same lines: the flattening is deterministic)."""
     p = cl.pool
     ids = cl.comp.create_layers(n)
     runs = _pool_runs(cl.pool_next, n, p.n_layers)
     picks = np.concatenate([np.arange(a, b) for a, b in runs])
     cl.pool_next += n
+    if cl.pool_comp is not None:
+        cl.comp.insert_layer_copies(ids, cl.pool_comp, picks.astype(np.uint32))
+    else:
+        _insert_pool_paths(cl, ids, runs)
+    cl.comp.set_layers_solid(ids, p.fill_rule[picks], p.blend_mode[picks], p.color[picks])
+    cl.comp.set_transforms(ids, p.transforms[picks])
+    top = int(ids.max()) + 1
+    if top > len(cl.enabled):
+        grow = top - len(cl.enabled)
+        cl.enabled = np.concatenate([cl.enabled, np.zeros(grow, bool)])
+        cl.transforms = np.concatenate([cl.transforms, np.zeros((grow, 6), np.float32)])
+    cl.enabled[ids] = True
+    cl.transforms[ids] = p.transforms[picks]
+
+
+def _insert_pool_paths(cl: Client, ids, runs):
+    p = cl.pool
     co = [np.zeros(1, np.uint64)]
     po = [np.zeros(1, np.uint64)]
     kinds, pts = [], []
@@ -179,15 +236,6 @@ def add_layers(cl: Client, n: int):
     sub = scenes.Scene("add", p.width, p.height, p.background, p.wide, len(ids), ids, co,
                        np.concatenate(kinds).astype(np.uint32), po, np.concatenate(pts).astype(np.float32))
     cl.comp.insert_paths(sub)
-    cl.comp.set_layers_solid(ids, p.fill_rule[picks], p.blend_mode[picks], p.color[picks])
-    cl.comp.set_transforms(ids, p.transforms[picks])
-    top = int(ids.max()) + 1
-    if top > len(cl.enabled):
-        grow = top - len(cl.enabled)
-        cl.enabled = np.concatenate([cl.enabled, np.zeros(grow, bool)])
-        cl.transforms = np.concatenate([cl.transforms, np.zeros((grow, 6), np.float32)])
-    cl.enabled[ids] = True
-    cl.transforms[ids] = p.transforms[picks]
 
 
 def frame_bytes(st: dict) -> int:
@@ -197,6 +245,16 @@ def frame_bytes(st: dict) -> int:
 
 
 class Server:
+    """The HBM budget covers the clients' resident device memory (their lines,
+    layer tables and resident segments) and the frame buffers of the batches
+    in flight.  What the clients hold when the server starts is set aside;
+    each worker's batch context gets an equal share of the rest as its
+    library budget, so the library refuses (CGB_ERR_OVER_BUDGET) a batch
+    whose frame would not fit: the worker then renders the batch in halves,
+    and a single request that fits no share on the client's own handle
+    (counted in `refused_alone`).  Requests are first admitted by an estimate
+    of their frame size, kept current from the sizes of the frames rendered."""
+
     def __init__(self, clients: List[Client], mode: str = "batched", workers: int = 2, max_batch: int = 16,
                  hbm_budget: float = 40e9):
         assert mode in ("batched", "plain")
@@ -205,9 +263,17 @@ class Server:
         self.workers = 1 if mode == "plain" else workers
         self.max_batch = 1 if mode == "plain" else max_batch
         self.budget = hbm_budget
+        resident = sum(cl.comp.device_bytes() + (cl.pool_comp.device_bytes() if cl.pool_comp else 0)
+                       for cl in clients)
+        # at least what a handle holds when it is created (a budget of 0
+        # would mean "unlimited" to the library)
+        self.ctx_budget = max(1 << 20, int((hbm_budget - resident) // self.workers))
         # batch renders run at low priority so that the clients' small update
-        # kernels (path flattening) are not queued behind them
-        self.ctx = [Composition(priority="low") for _ in range(self.workers)] if mode == "batched" else []
+        # kernels are not queued behind them
+        self.ctx = ([Composition(priority="low", hbm_budget=self.ctx_budget) for _ in range(self.workers)]
+                    if mode == "batched" else [])
+        self.refused_batches = 0  # batches the library refused for the budget (then split)
+        self.refused_alone = 0    # single requests rendered on their own handle
         self.cv = threading.Condition()
         self.pending: Dict[int, collections.deque] = collections.defaultdict(collections.deque)
         self.busy = set()
@@ -250,7 +316,7 @@ class Server:
                 ts = time.perf_counter() - t0
                 for r in batch:
                     r.t_start = ts
-                    apply_update(self.clients[r.client], r.client, r.seq)
+                apply_updates([(self.clients[r.client], r.client, r.seq) for r in batch])
                 tr = time.perf_counter() - t0
                 for r in batch:
                     r.t_render = tr
@@ -260,14 +326,15 @@ class Server:
                     _render_one(cl)
                 else:
                     cls = [self.clients[r.client] for r in batch]
-                    _render_many(self.ctx[wid], cls)
+                    self._render_within_budget(self.ctx[wid], cls)
                 td = time.perf_counter() - t0
                 for r in batch:
                     r.t_done = td
                     r.batch_size = len(batch)
                     cl = self.clients[r.client]
                     cl.done_seq = r.seq
-                    cl.est_bytes = frame_bytes(cl.comp.stats()) if self.mode == "plain" else cl.est_bytes
+                    if self.mode == "plain":
+                        cl.est_bytes = frame_bytes(cl.comp.stats())
             except BaseException as e:  # surface to the caller
                 with self.cv:
                     self.errors.append(e)
@@ -279,6 +346,33 @@ class Server:
                 self.inflight_bytes -= mem
                 self.completed += len(batch)
                 self.cv.notify_all()
+
+    def _render_within_budget(self, ctx: Composition, cls: List[Client]):
+        """Renders a batch on `ctx`; a batch the library refuses for the
+        budget is rendered in halves, a single client on its own handle."""
+        from .abi import ERR_OVER_BUDGET, CassiaError
+        try:
+            _render_many(ctx, cls)
+        except CassiaError as e:
+            if e.status != ERR_OVER_BUDGET:
+                raise
+            with self.cv:
+                self.refused_batches += 1
+            if len(cls) == 1:
+                with self.cv:
+                    self.refused_alone += 1
+                _render_one(cls[0])
+                return
+            h = len(cls) // 2
+            self._render_within_budget(ctx, cls[:h])
+            self._render_within_budget(ctx, cls[h:])
+            return
+        # size estimates from this frame: its buffers per line, times each client's lines
+        st = ctx.stats()
+        if st.get("lines", 0) > 0:
+            per_line = frame_bytes(st) / st["lines"]
+            for cl in cls:
+                cl.est_bytes = int(per_line * cl.comp.lens()[0])
 
     def _next_arrival(self):
         if self._cursor < len(self._requests):

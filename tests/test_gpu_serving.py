@@ -56,3 +56,89 @@ def test_admission_respects_budget(gpu_lib):
     srv = serving.Server(clients, mode="batched", workers=2, max_batch=8, hbm_budget=1)
     done = srv.run(reqs)
     assert max(r.batch_size for r in done) == 1
+
+
+def _alone(cl):
+    import torch
+    img = torch.zeros_like(cl.out)
+    cl.comp.render(img.data_ptr(), cl.scene.width, cl.scene.background, height=cl.scene.height)
+    return img
+
+
+def test_library_refuses_an_over_budget_batch(gpu_lib):
+    """The worker contexts' HBM budget is enforced by the library: a batch
+    whose frame buffers do not fit is refused with CGB_ERR_OVER_BUDGET, and
+    the server then renders it in halves; every result still equals the
+    client's frame rendered alone."""
+    import torch
+    from cassia_gb300 import Composition, abi, serving
+    from cassia_gb300.composition import render_batch
+    clients = serving.make_clients(4, seed=44, device_out=True, max_layers=300)
+    # the largest single client's frame buffers on a batch context
+    single = 0
+    for cl in clients:
+        ctx = Composition()
+        render_batch(ctx, [cl.comp], [cl.out.data_ptr()], [cl.scene.width], [cl.scene.background],
+                     heights=[cl.scene.height])
+        single = max(single, ctx.device_bytes())
+        ctx.close()
+    share = int(1.3 * single)
+    # the library itself refuses the four together
+    ctx = Composition(hbm_budget=share)
+    with pytest.raises(abi.CassiaError) as ex:
+        render_batch(ctx, [cl.comp for cl in clients], [cl.out.data_ptr() for cl in clients],
+                     [cl.scene.width for cl in clients], [cl.scene.background for cl in clients],
+                     heights=[cl.scene.height for cl in clients])
+    assert ex.value.status == abi.ERR_OVER_BUDGET
+    ctx.close()
+    # a server whose estimates admit whole batches: the library's refusal splits them
+    resident = sum(cl.comp.device_bytes() + cl.pool_comp.device_bytes() for cl in clients)
+    for cl in clients:
+        cl.est_bytes = 1
+    srv = serving.Server(clients, mode="batched", workers=1, max_batch=4, hbm_budget=resident + share)
+    assert srv.ctx_budget == share
+    reqs = serving.poisson_arrivals(rate=2000.0, n_clients=len(clients), duration=0.02, seed=3)
+    srv.run(reqs)
+    assert srv.refused_batches > 0
+    assert srv.ctx[0].device_bytes() <= share
+    for k, cl in enumerate(clients):
+        assert torch.equal(cl.out, _alone(cl)), f"client {k}: mix != alone"
+
+
+def test_added_layers_copy_pool_lines(gpu_lib):
+    """insert_layer_copies gives the same lines, segments and pixels as
+    inserting (and flattening) the same paths."""
+    from cassia_gb300 import Composition, scenes
+    pool = scenes.mixed(seed=45, n_layers=64, width=256, height=256)
+    src = Composition()
+    src.create_layers(pool.n_layers)
+    src.insert_paths(pool)
+    picks = np.array([5, 0, 63, 17, 17, 40], np.uint32)
+    a, b = Composition(), Composition()
+    ids_a = a.create_layers(len(picks))
+    ids_b = b.create_layers(len(picks))
+    a.insert_layer_copies(ids_a, src, picks)
+    co = np.diff(pool.cmd_offsets)[picks]
+    po = np.diff(pool.point_offsets)[picks]
+    sub = scenes.Scene("sub", pool.width, pool.height, pool.background, False, len(picks), ids_b,
+                       np.concatenate([[0], np.cumsum(co)]).astype(np.uint64),
+                       np.concatenate([pool.kinds[pool.cmd_offsets[p]:pool.cmd_offsets[p + 1]] for p in picks]),
+                       np.concatenate([[0], np.cumsum(po)]).astype(np.uint64),
+                       np.concatenate([pool.points[pool.point_offsets[p]:pool.point_offsets[p + 1]] for p in picks]))
+    b.insert_paths(sub)
+    for c, ids in ((a, ids_a), (b, ids_b)):
+        c.set_layers_solid(ids, pool.fill_rule[picks], pool.blend_mode[picks], pool.color[picks])
+        c.set_transforms(ids, pool.transforms[picks])
+    assert a.lens() == b.lens()
+    sa, na = a.pixel_segments()
+    sb, nb = b.pixel_segments()
+    assert na == nb and np.array_equal(sa, sb)
+    ia = np.zeros((256, 256, 4), np.uint8)
+    ib = np.zeros_like(ia)
+    a.render(ia, 256, (1.0, 1.0, 1.0, 1.0))
+    b.render(ib, 256, (1.0, 1.0, 1.0, 1.0))
+    assert np.array_equal(ia, ib)
+    # a layer whose lines are no longer one run is refused as a source
+    a.insert_layer_copies(ids_a[:1], src, picks[:1])
+    with pytest.raises(Exception):
+        b.insert_layer_copies(ids_b[:1], a, ids_a[:1])
