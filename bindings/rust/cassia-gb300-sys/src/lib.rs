@@ -168,6 +168,26 @@ pub struct cgb_cassia_styling {
     pub _padding: [u32; 2],
 }
 
+/// One composition's changes between two frames (cgb_update_layers).
+#[repr(C)]
+#[derive(Clone, Copy, Debug)]
+pub struct cgb_layer_update {
+    pub comp: *mut cgb_composition,
+    pub n_transforms: usize,
+    pub transform_ids: *const u32,
+    pub transforms: *const f32,
+    pub transform_flags: u32,
+    pub reserved: u32,
+    pub n_removed: usize,
+    pub removed_ids: *const u32,
+    pub n_added: usize,
+    pub added_from: *mut cgb_composition,
+    pub added_from_ids: *const u32,
+    pub added_props: *const cgb_props,
+    pub added_transforms: *const f32,
+    pub added_ids: *mut u32,
+}
+
 /// Opaque composition handle.
 #[repr(C)]
 pub struct cgb_composition {
@@ -229,6 +249,7 @@ extern "C" {
         flags: u32,
     ) -> cgb_status;
 
+    pub fn cgb_update_layers(n: usize, updates: *const cgb_layer_update) -> cgb_status;
     pub fn cgb_remove_disabled(c: *mut cgb_composition) -> cgb_status;
     pub fn cgb_lines_len(c: *mut cgb_composition, builder_len: *mut u64, actual_len: *mut u64) -> cgb_status;
 

@@ -55,6 +55,25 @@ class CgbProps(ctypes.Structure):
     ]
 
 
+class CgbLayerUpdate(ctypes.Structure):
+    _fields_ = [
+        ("comp", ctypes.c_void_p),
+        ("n_transforms", ctypes.c_size_t),
+        ("transform_ids", ctypes.POINTER(ctypes.c_uint32)),
+        ("transforms", ctypes.POINTER(ctypes.c_float)),
+        ("transform_flags", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
+        ("n_removed", ctypes.c_size_t),
+        ("removed_ids", ctypes.POINTER(ctypes.c_uint32)),
+        ("n_added", ctypes.c_size_t),
+        ("added_from", ctypes.c_void_p),
+        ("added_from_ids", ctypes.POINTER(ctypes.c_uint32)),
+        ("added_props", ctypes.POINTER(CgbProps)),
+        ("added_transforms", ctypes.POINTER(ctypes.c_float)),
+        ("added_ids", ctypes.POINTER(ctypes.c_uint32)),
+    ]
+
+
 # cgb_flush_fn: (user, pixels, n_pixels)
 FLUSH_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t)
 
@@ -169,6 +188,7 @@ def _declare(lib):
         "cgb_insert_lines": ([handle, u32, fp, sz], i32),
         "cgb_insert_layer_copies": ([handle, sz, P(u32), handle, P(u32)], i32),
         "cgb_get_memory": ([handle, P(u64)], i32),
+        "cgb_update_layers": ([sz, P(CgbLayerUpdate)], i32),
         "cgb_layer_set_enabled": ([handle, u32, ctypes.c_int], i32),
         "cgb_layer_set_transform": ([handle, u32, fp, u32], i32),
         "cgb_layer_set_order": ([handle, u32, u32], i32),

@@ -69,6 +69,63 @@ def render_batch(ctx, scenes, pixels, widths, backgrounds, crops=None, heights=N
     return pixels
 
 
+def solid_props(fill_rules, blend_modes, colors):
+    """A cgb_props array of Solid Draw props, one per entry."""
+    fr = np.asarray(fill_rules, np.uint32)
+    n = len(fr)
+    arr = (abi.CgbProps * max(n, 1))()
+    view = np.frombuffer(arr, dtype=np.uint8).reshape(max(n, 1), ctypes.sizeof(abi.CgbProps))
+    u32 = view[:, :40].view(np.uint32)
+    u32[:n, 0] = fr
+    u32[:n, 1] = abi.FUNC_DRAW
+    u32[:n, 4] = np.asarray(blend_modes, np.uint32)
+    u32[:n, 5] = abi.FILL_SOLID
+    view[:n, 24:40].view(np.float32)[:] = np.asarray(colors, np.float32).reshape(-1, 4)
+    return arr
+
+
+def update_layers(updates):
+    """cgb_update_layers: each update is a dict with `comp` and any of
+    `transform_ids` + `transforms` (n x 6), `removed_ids`, and `added_from`
+    (a Composition) + `added_from_ids` + `added_props` (a cgb_props array, as
+    solid_props makes) + `added_transforms` (n x 6).  Returns, per update,
+    the new layers' ids (uint32 array).  Transforms are stored unchecked."""
+    lib = abi.load_library()
+    n = len(updates)
+    arr = (abi.CgbLayerUpdate * max(n, 1))()
+    keep, outs = [], []
+    for k, u in enumerate(updates):
+        r = arr[k]
+        r.comp = u["comp"]._h.value
+        r.transform_flags = abi.TRANSFORM_UNCHECKED
+        if u.get("transform_ids") is not None and len(u["transform_ids"]):
+            ids = np.ascontiguousarray(u["transform_ids"], np.uint32)
+            t = np.ascontiguousarray(u["transforms"], np.float32)
+            keep += [ids, t]
+            r.n_transforms, r.transform_ids, r.transforms = len(ids), _u32p(ids), _fp(t)
+        if u.get("removed_ids") is not None and len(u["removed_ids"]):
+            ids = np.ascontiguousarray(u["removed_ids"], np.uint32)
+            keep.append(ids)
+            r.n_removed, r.removed_ids = len(ids), _u32p(ids)
+        out = np.zeros(0, np.uint32)
+        if u.get("added_from_ids") is not None and len(u["added_from_ids"]):
+            src = np.ascontiguousarray(u["added_from_ids"], np.uint32)
+            out = np.zeros(len(src), np.uint32)
+            keep += [src, out]
+            r.n_added, r.added_from, r.added_from_ids, r.added_ids = len(src), u["added_from"]._h.value, _u32p(src), \
+                _u32p(out)
+            if u.get("added_props") is not None:
+                keep.append(u["added_props"])
+                r.added_props = ctypes.cast(u["added_props"], ctypes.POINTER(abi.CgbProps))
+            if u.get("added_transforms") is not None:
+                t = np.ascontiguousarray(u["added_transforms"], np.float32)
+                keep.append(t)
+                r.added_transforms = _fp(t)
+        outs.append(out)
+    _check(lib, lib.cgb_update_layers(n, arr), "update_layers")
+    return outs
+
+
 def kernel_launches() -> int:
     """Kernels launched by the native library in this process."""
     return int(abi.load_library().cgb_kernel_launches())
@@ -185,18 +242,7 @@ class Composition:
     def set_layers_solid(self, ids, fill_rules, blend_modes, colors):
         ids = np.ascontiguousarray(ids, np.uint32)
         n = len(ids)
-        arr = (abi.CgbProps * max(n, 1))()
-        fr = np.asarray(fill_rules, np.uint32)
-        bm = np.asarray(blend_modes, np.uint32)
-        col = np.asarray(colors, np.float32).reshape(-1, 4)
-        # fill the struct array through a numpy view of its bytes
-        view = np.frombuffer(arr, dtype=np.uint8).reshape(max(n, 1), ctypes.sizeof(abi.CgbProps))
-        u32 = view[:, :40].view(np.uint32)
-        u32[:n, 0] = fr
-        u32[:n, 1] = abi.FUNC_DRAW
-        u32[:n, 4] = bm
-        u32[:n, 5] = abi.FILL_SOLID
-        view[:n, 24:40].view(np.float32)[:] = col
+        arr = solid_props(fill_rules, blend_modes, colors)
         st = self._lib.cgb_layers_set_props(self._h, n, _u32p(ids), arr)
         _check(self._lib, st, "set_layers_solid")
 

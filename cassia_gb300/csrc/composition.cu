@@ -1132,6 +1132,35 @@ CGB_EXPORT cgb_status cgb_selftest_bounded_wait(void) {
     return fail(CGB_ERR_DEVICE_TIMEOUT, "selftest: the bounded wait expired as designed");
 }
 
+CGB_EXPORT cgb_status cgb_update_layers(size_t n, const cgb_layer_update* updates) {
+    if (n && !updates) return fail(CGB_ERR_INVALID_ARG, "update_layers: null updates");
+    std::vector<uint8_t> off;
+    for (size_t k = 0; k < n; k++) {
+        const cgb_layer_update& u = updates[k];
+        cgb_composition* c = u.comp;
+        if (!c) return fail(CGB_ERR_INVALID_ARG, "update_layers: null composition");
+        cgb_status st = CGB_OK;
+        if (u.n_transforms)
+            st = cgb_layers_set_transforms(c, u.n_transforms, u.transform_ids, u.transforms, u.transform_flags);
+        if (!st && u.n_removed) {
+            off.assign(u.n_removed, 0);
+            st = cgb_layers_set_enabled(c, u.n_removed, u.removed_ids, off.data());
+            if (!st) st = cgb_remove_disabled(c);
+        }
+        if (!st && u.n_added) {
+            if (!u.added_ids || !u.added_from || !u.added_from_ids)
+                return fail(CGB_ERR_INVALID_ARG, "update_layers: added layers need ids and sources");
+            st = cgb_create_layers(c, u.n_added, u.added_ids);
+            if (!st) st = cgb_insert_layer_copies(c, u.n_added, u.added_ids, u.added_from, u.added_from_ids);
+            if (!st && u.added_props) st = cgb_layers_set_props(c, u.n_added, u.added_ids, u.added_props);
+            if (!st && u.added_transforms)
+                st = cgb_layers_set_transforms(c, u.n_added, u.added_ids, u.added_transforms, u.transform_flags);
+        }
+        if (st) return fail(st, "update_layers: update " + std::to_string(k) + ": " + g_last_error);
+    }
+    return CGB_OK;
+}
+
 CGB_EXPORT cgb_status cgb_composition_clear(cgb_composition* c) {
     if (!c) return fail(CGB_ERR_INVALID_ARG, "null composition handle");
     c->n_lines = 0;

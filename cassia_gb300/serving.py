@@ -23,7 +23,7 @@ from typing import Dict, List, Optional
 import numpy as np
 
 from . import scenes
-from .composition import Composition, render_batch
+from .composition import Composition, render_batch, solid_props, update_layers
 
 
 @dataclass
@@ -171,16 +171,33 @@ def apply_updates(items, changed: float = 0.2, churn: float = 0.01):
     t[:, 4] += ((_bits01(w, 21, 21) - 0.5) * 6.0).astype(np.float32)
     t[:, 5] += ((_bits01(w, 0, 21) - 0.5) * 6.0).astype(np.float32)
     toff = np.concatenate([[0], np.cumsum(nid)])
+    batch = []  # clients whose calls go to the library in one cgb_update_layers
     for k, (cl, _, _) in enumerate(items):
         tk = t[toff[k]:toff[k + 1]]
         cl.transforms[ids[k]] = tk
-        cl.comp.set_transforms(ids[k], tk)
         gone = lives[k][rem[offs[k]:offs[k + 1]]]
+        if cl.pool_comp is not None and isinstance(cl.comp, Composition):
+            u = {"comp": cl.comp, "transform_ids": ids[k], "transforms": tk}
+            if len(gone):
+                cl.enabled[gone] = False
+                picks = _pool_picks(cl, len(gone))
+                p = cl.pool
+                u.update(removed_ids=gone, added_from=cl.pool_comp, added_from_ids=picks.astype(np.uint32),
+                         added_props=solid_props(p.fill_rule[picks], p.blend_mode[picks], p.color[picks]),
+                         added_transforms=p.transforms[picks])
+            batch.append((cl, u))
+            continue
+        cl.comp.set_transforms(ids[k], tk)
         if len(gone):
             cl.comp.set_enabled_many(gone, np.zeros(len(gone), np.uint8))
             cl.enabled[gone] = False
             cl.comp.remove_disabled()  # mold's GC: drops the disabled layers at 50% garbage
             add_layers(cl, len(gone))
+    if batch:
+        # the same calls in the same order, in one library call for the batch
+        for (cl, u), new_ids in zip(batch, update_layers([u for _, u in batch])):
+            if len(new_ids):
+                _note_added(cl, new_ids, u["added_from_ids"])
 
 
 def _pool_runs(start: int, n: int, size: int):
@@ -194,6 +211,13 @@ def _pool_runs(start: int, n: int, size: int):
     return runs
 
 
+def _pool_picks(cl: Client, n: int) -> np.ndarray:
+    """The next n shapes of the client's pool (taken in turn)."""
+    runs = _pool_runs(cl.pool_next, n, cl.pool.n_layers)
+    cl.pool_next += n
+    return np.concatenate([np.arange(a, b) for a, b in runs])
+
+
 def add_layers(cl: Client, n: int):
     """Adds n layers drawn in turn from the client's shape pool (one path
     per pool layer), with one insert call: copies of the shapes' lines from
@@ -201,15 +225,19 @@ def add_layers(cl: Client, n: int):
     same lines: the flattening is deterministic)."""
     p = cl.pool
     ids = cl.comp.create_layers(n)
-    runs = _pool_runs(cl.pool_next, n, p.n_layers)
-    picks = np.concatenate([np.arange(a, b) for a, b in runs])
-    cl.pool_next += n
+    picks = _pool_picks(cl, n)
     if cl.pool_comp is not None:
         cl.comp.insert_layer_copies(ids, cl.pool_comp, picks.astype(np.uint32))
     else:
-        _insert_pool_paths(cl, ids, runs)
+        _insert_pool_paths(cl, ids, picks)
     cl.comp.set_layers_solid(ids, p.fill_rule[picks], p.blend_mode[picks], p.color[picks])
     cl.comp.set_transforms(ids, p.transforms[picks])
+    _note_added(cl, ids, picks)
+
+
+def _note_added(cl: Client, ids, picks):
+    """The client's mirror of its new layers: enabled, with their transforms."""
+    p = cl.pool
     top = int(ids.max()) + 1
     if top > len(cl.enabled):
         grow = top - len(cl.enabled)
@@ -219,20 +247,12 @@ def add_layers(cl: Client, n: int):
     cl.transforms[ids] = p.transforms[picks]
 
 
-def _insert_pool_paths(cl: Client, ids, runs):
+def _insert_pool_paths(cl: Client, ids, picks):
     p = cl.pool
-    co = [np.zeros(1, np.uint64)]
-    po = [np.zeros(1, np.uint64)]
-    kinds, pts = [], []
-    for a, b in runs:
-        c0, c1 = int(p.cmd_offsets[a]), int(p.cmd_offsets[b])
-        q0, q1 = int(p.point_offsets[a]), int(p.point_offsets[b])
-        kinds.append(p.kinds[c0:c1])
-        pts.append(p.points[q0:q1])
-        co.append(np.diff(p.cmd_offsets[a:b + 1]))
-        po.append(np.diff(p.point_offsets[a:b + 1]))
-    co = np.cumsum(np.concatenate(co)).astype(np.uint64)
-    po = np.cumsum(np.concatenate(po)).astype(np.uint64)
+    kinds = [p.kinds[int(p.cmd_offsets[k]):int(p.cmd_offsets[k + 1])] for k in picks]
+    pts = [p.points[int(p.point_offsets[k]):int(p.point_offsets[k + 1])] for k in picks]
+    co = np.concatenate([[0], np.cumsum(np.diff(p.cmd_offsets)[picks])]).astype(np.uint64)
+    po = np.concatenate([[0], np.cumsum(np.diff(p.point_offsets)[picks])]).astype(np.uint64)
     sub = scenes.Scene("add", p.width, p.height, p.background, p.wide, len(ids), ids, co,
                        np.concatenate(kinds).astype(np.uint32), po, np.concatenate(pts).astype(np.float32))
     cl.comp.insert_paths(sub)
@@ -310,8 +330,8 @@ class Server:
                             self.busy.add(r.client)
                         self.inflight_bytes += mem
                         break
-                    nxt = self._next_arrival()
-                    self.cv.wait(timeout=0.002 if nxt is None else max(0.0, min(0.002, nxt - now)))
+                    # arrivals and finished batches notify; the timeout is a safety net
+                    self.cv.wait(timeout=0.05)
             try:
                 ts = time.perf_counter() - t0
                 for r in batch:
@@ -374,11 +394,6 @@ class Server:
             for cl in cls:
                 cl.est_bytes = int(per_line * cl.comp.lens()[0])
 
-    def _next_arrival(self):
-        if self._cursor < len(self._requests):
-            return self._requests[self._cursor].arrival
-        return None
-
     def run(self, requests: List[Request]) -> List[Request]:
         """Serves `requests` (sorted by arrival) in real time; returns them
         with start / completion times filled in."""
@@ -398,11 +413,14 @@ class Server:
         while self._cursor < len(requests):
             now = time.perf_counter() - t0
             with self.cv:
+                fed = 0
                 while self._cursor < len(requests) and requests[self._cursor].arrival <= now:
                     r = requests[self._cursor]
                     self.pending[r.client].append(r)
                     self._cursor += 1
-                self.cv.notify_all()
+                    fed += 1
+                if fed:  # wake the workers only when there is new work
+                    self.cv.notify_all()
                 if self.errors:
                     break
             if self._cursor < len(requests):

@@ -267,6 +267,39 @@ CGB_EXPORT cgb_status cgb_layers_set_transforms(cgb_composition* c, size_t n,
                                                 const uint32_t* layer_ids, const float* affine6,
                                                 uint32_t flags);
 
+/* One composition's changes between two frames, as a client sends them: new
+ * transforms for some layers (Layer::set_transform, mold/src/layer.rs:180-197),
+ * layers removed (Layer::disable, then Composition::remove_disabled,
+ * mold/src/composition.rs:124-142), and layers added (Composition::create_layer
+ * and insert_in_layer, composition.rs:54-94) whose paths are already
+ * flattened in layers of `added_from` (as cgb_insert_layer_copies), with their
+ * props and transforms (either may be NULL).  `transform_flags` apply to both
+ * transform lists.  The new layers' ids are written to `added_ids`. */
+typedef struct cgb_layer_update {
+    cgb_composition* comp;
+    size_t n_transforms;
+    const uint32_t* transform_ids;
+    const float* transforms; /* 6 floats per id */
+    uint32_t transform_flags;
+    uint32_t reserved;
+    size_t n_removed;
+    const uint32_t* removed_ids;
+    size_t n_added;
+    cgb_composition* added_from;
+    const uint32_t* added_from_ids;
+    const cgb_props* added_props;
+    const float* added_transforms; /* 6 floats per added layer */
+    uint32_t* added_ids;           /* out: n_added ids */
+} cgb_layer_update;
+
+/* Applies n updates in order, each exactly as the separate calls would
+ * (cgb_layers_set_transforms, cgb_layers_set_enabled + cgb_remove_disabled,
+ * cgb_create_layers + cgb_insert_layer_copies + cgb_layers_set_props +
+ * cgb_layers_set_transforms), in one call: a server applies the updates of a
+ * whole batch of clients at once.  Stops at the first failing update (the
+ * message names it). */
+CGB_EXPORT cgb_status cgb_update_layers(size_t n, const cgb_layer_update* updates);
+
 /* Composition::remove_disabled (mold/src/composition.rs:124-142). */
 CGB_EXPORT cgb_status cgb_remove_disabled(cgb_composition* c);
 /* LinesBuilder::len and Composition::actual_len (composition.rs:116-121). */

@@ -152,7 +152,8 @@ def test_every_function_declared_with_the_same_signature():
 def test_every_struct_has_the_same_fields_in_order():
     _, cs, _, cflush = _c_header()
     _, rs, _, rflush = _rust_lib()
-    for name in ("cgb_props", "cgb_buffer", "cgb_rect", "cgb_stats", "cgb_tuning", "cgb_cassia_styling"):
+    for name in ("cgb_props", "cgb_buffer", "cgb_rect", "cgb_stats", "cgb_tuning", "cgb_cassia_styling",
+                 "cgb_layer_update"):
         assert name in cs and name in rs, name
         assert rs[name] == cs[name], (name, rs[name], cs[name])
     # the buffer's flusher callback: fields present and the callback's own signature
