@@ -507,6 +507,8 @@ def main():
     ap.add_argument("--serve-workers", type=int, default=3,
                     help="render workers of the served form (3 measured best: 2 leave the GPU idle during "
                          "host updates, 4 contend for the interpreter)")
+    ap.add_argument("--blend-mode", type=int, default=None, choices=range(12),
+                    help="give every layer this blend mode (the cost of one mode; changes the scene)")
     ap.add_argument("--no-forms", dest="forms", action="store_false",
                     help="mixed100k: skip the batched (batch256) and served (serve) sub-objects")
     ap.add_argument("--cpu-budget", type=float, default=150.0,
@@ -544,6 +546,8 @@ def main():
 
     t0 = time.time()
     scene = make_scene(args.workload)
+    if args.blend_mode is not None:
+        scene.blend_mode[:] = args.blend_mode
     gen_s = time.time() - t0
     comp = Composition(wide=scene.wide)
     t0 = time.time()
@@ -691,7 +695,8 @@ def main():
             "metric": "Msegments/s", "value": value, "unit": "Msegments/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+int (fixed point)", "data": "synthetic (seeded)",
-            "config": scene_config(args.workload, scene, world),
+            "config": dict(scene_config(args.workload, scene, world),
+                           **({} if args.blend_mode is None else {"blend_mode": args.blend_mode})),
             "frame_counts": {"lines": st["lines"], "segments_per_frame": segs,
                              "segments_rasterized": st["segments"],
                              "painted_segments": st["painted_segments"], "tile_layers": st["tile_layers"],
@@ -717,7 +722,7 @@ def main():
     comp.close()
     del out
     torch.cuda.empty_cache()
-    if args.forms and args.workload == "mixed100k":
+    if args.forms and args.workload == "mixed100k" and args.blend_mode is None:
         # the batched (256 scenes) and served (64 clients) forms, each as a
         # sub-object of the headline line
         fa = argparse.Namespace(**vars(args))
