@@ -398,9 +398,10 @@ def run_serve(args, rank, world, local):
     incremental frames (each client's sorted segments stay resident; only
     changed layers are rasterized) against the plain loop (one full render
     call per request), on identical request streams.
-    The offered rate saturates the server (its latency then grows with the
-    run), so the batched server is also run at 75% of the throughput it
-    reached ("sustained": p50/p99 of a server that keeps up)."""
+    A server that keeps up serves the offered rate and no more, so the
+    batched server is also run at twice the offered rate ("capacity": the
+    frames/s it sustains when saturated), beside the plain loop's, which
+    saturates at the offered rate."""
     import torch
     from cassia_gb300 import serving
     from cassia_gb300.composition import kernel_launches
@@ -408,12 +409,11 @@ def run_serve(args, rank, world, local):
     reqs_b = serving.poisson_arrivals(w["rate"], w["n_clients"], w["duration"], seed=w["seed"] + rank)
     reqs_p = serving.poisson_arrivals(w["rate"], w["n_clients"], w["duration"], seed=w["seed"] + rank)
     out = {}
-    runs = [("batched", reqs_b), ("plain", reqs_p), ("sustained", None)]
+    runs = [("batched", reqs_b), ("plain", reqs_p), ("capacity", None)]
     for mode, reqs in runs:
-        if mode == "sustained":
-            # the batched server at 75% of the throughput it reached at the
-            # offered rate: latency of a server that keeps up with its load
-            rate = 0.75 * out["batched"]["frames_per_s"]
+        if mode == "capacity":
+            # the batched server offered twice the configured rate: what it sustains when saturated
+            rate = 2.0 * w["rate"]
             reqs = serving.poisson_arrivals(rate, w["n_clients"], w["duration"], seed=w["seed"] + rank + 1)
         # the served form keeps each client's segments resident and
         # re-rasterizes only changed layers; the plain loop re-renders in full
@@ -426,7 +426,7 @@ def run_serve(args, rank, world, local):
             done = srv.run(reqs)
         torch.cuda.synchronize()
         s = serving.latency_summary(done, w["duration"])
-        if mode == "sustained":
+        if mode == "capacity":
             s["offered_rate"] = rate
         # whole-job rate: the frames of every replica over the slowest replica's span
         span = over_ranks(s["requests"] / s["frames_per_s"])
@@ -455,9 +455,11 @@ def run_serve(args, rank, world, local):
                        "duration_s": w["duration"], "hbm_budget_gb": 40, "max_batch": 16, "workers": args.serve_workers,
                        "served": "continuous batching, incremental frames", "plain": "one full render per request"},
             "p50_ms": b["p50_ms"], "p99_ms": b["p99_ms"], "batched": b, "plain": p,
-            "sustained": {k: out["sustained"][k] for k in ("offered_rate", "frames_per_s", "p50_ms", "p99_ms",
-                                                           "mean_batch")},
+            "capacity": {k: out["capacity"][k] for k in ("offered_rate", "frames_per_s", "frames_per_s_all_ranks",
+                                                         "p50_ms", "p99_ms", "mean_batch")},
             "speedup_vs_plain": b["frames_per_s_all_ranks"] / p["frames_per_s_all_ranks"],
+            "capacity_speedup_vs_plain": (out["capacity"]["frames_per_s_all_ranks"] /
+                                          p["frames_per_s_all_ranks"]),
             "gpu_launches": b["gpu_launches"], "clocks": b["clocks"],
         }
         return line
@@ -741,7 +743,8 @@ def main():
                 "metric": v["metric"], "value": v["value"], "unit": v["unit"], "config": v["config"],
                 "p50_ms": v["p50_ms"], "p99_ms": v["p99_ms"], "speedup_vs_plain": v["speedup_vs_plain"],
                 "plain_frames_per_s": v["plain"]["frames_per_s_all_ranks"],
-                "sustained": v["sustained"], "mix_equals_alone_sampled": v["batched"]["mix_equals_alone_sampled"],
+                "capacity": v["capacity"], "capacity_speedup_vs_plain": v["capacity_speedup_vs_plain"],
+                "mix_equals_alone_sampled": v["batched"]["mix_equals_alone_sampled"],
                 "requests": v["batched"]["requests"], "mean_batch": v["batched"]["mean_batch"],
                 "gpu_launches": v["gpu_launches"], "clocks": v["clocks"]}
     if rank == 0:
