@@ -394,7 +394,7 @@ def run_serve(args, rank, world, local):
     """Serving workload: 64 clients with resident compositions (batched-workload
     distribution), Poisson arrivals at 2,000 requests/s; each frame gives 20%
     of a client's layers a new affine and adds/removes 1%.  Continuous
-    batching (3 workers, batches of up to 16, 40 GB HBM budget) of
+    batching (4 workers, batches of up to 16, 40 GB HBM budget) of
     incremental frames (each client's sorted segments stay resident; only
     changed layers are rasterized) against the plain loop (one full render
     call per request), on identical request streams.
@@ -506,9 +506,9 @@ def main():
     ap.add_argument("--quiet", action="store_true")
     ap.add_argument("--frame-mode", default="graph", choices=["staged", "graph"],
                     help="graph: frames replayed from a captured CUDA graph (cgb_set_graph_mode)")
-    ap.add_argument("--serve-workers", type=int, default=3,
-                    help="render workers of the served form (3 measured best: 2 leave the GPU idle during "
-                         "host updates, 4 contend for the interpreter)")
+    ap.add_argument("--serve-workers", type=int, default=4,
+                    help="render workers of the served form (4 measured best: 3 leave the GPU idle during "
+                         "host updates, 6 add nothing)")
     ap.add_argument("--blend-mode", type=int, default=None, choices=range(12),
                     help="give every layer this blend mode (the cost of one mode; changes the scene)")
     ap.add_argument("--no-forms", dest="forms", action="store_false",

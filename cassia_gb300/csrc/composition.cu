@@ -475,6 +475,10 @@ private:
 // one, within the scale limit) and the ids strictly increase, the items are
 // checked, then applied, by the host pool; the result equals the sequential
 // loop's.  Returns false, having changed nothing, when that does not hold.
+void host_parallel(int parts, const std::function<void(int)>& f) { HostPool::get().run(parts, f); }
+
+int host_threads() { return HostPool::get().threads(); }
+
 bool set_transforms_parallel(cgb_composition* c, size_t n, const uint32_t* ids, const float* affine6, bool check) {
     HostPool& pool = HostPool::get();
     if (pool.threads() < 2) return false;

@@ -158,16 +158,37 @@ cgb_status prepare_incremental(cgb_composition* c, SceneInput& in) {
         in.incr = 1;
         return CGB_OK;
     }
-    c->h_rast_dirty.assign(c->max_ids, 0);
-    for (uint32_t o = c->n_orders; o < c->max_ids; o++) c->h_rast_dirty[o] = 1;  // orders no layer holds
-    if (c->rast_order.size() < c->layers.size()) c->rast_order.resize(c->layers.size(), -1);
-    for (uint32_t id : c->rast_ids) {
-        if (id < c->rast_order.size() && c->rast_order[id] >= 0) c->h_rast_dirty[(uint32_t)c->rast_order[id]] = 1;
-        const int32_t cur = current_order(id);
-        if (cur >= 0 && (uint32_t)cur < c->max_ids) c->h_rast_dirty[(uint32_t)cur] = 1;
-        if (id >= c->rast_order.size()) c->rast_order.resize((size_t)id + 1, -1);
-        c->rast_order[id] = cur;
-        c->rast_flag[id] = 0;
+    c->h_rast_dirty.resize(c->max_ids);
+    uint8_t* dirty = c->h_rast_dirty.data();
+    const uint32_t held = std::min(c->n_orders, c->max_ids);
+    std::memset(dirty, 0, held);
+    std::memset(dirty + held, 1, c->max_ids - held);  // orders no layer holds
+    size_t need = c->layers.size();
+    for (uint32_t id : c->rast_ids) need = std::max<size_t>(need, (size_t)id + 1);
+    if (c->rast_order.size() < need) c->rast_order.resize(need, -1);
+    // every listed layer marks its old and its new order (marks are idempotent
+    // byte stores, so parts of a long list run on the host pool)
+    int32_t* rorder = c->rast_order.data();
+    uint8_t* rflag = c->rast_flag.data();
+    const uint32_t* list = c->rast_ids.data();
+    const size_t n_ids = c->rast_ids.size();
+    auto mark = [&](size_t lo, size_t hi) {
+        for (size_t k = lo; k < hi; k++) {
+            const uint32_t id = list[k];
+            const int32_t old = rorder[id];
+            if (old >= 0 && (uint32_t)old < c->max_ids) __atomic_store_n(&dirty[(uint32_t)old], (uint8_t)1, __ATOMIC_RELAXED);
+            const int32_t cur = current_order(id);
+            if (cur >= 0 && (uint32_t)cur < c->max_ids) __atomic_store_n(&dirty[(uint32_t)cur], (uint8_t)1, __ATOMIC_RELAXED);
+            rorder[id] = cur;
+            rflag[id] = 0;
+        }
+    };
+    if (n_ids >= 16384 && host_threads() > 1) {
+        const int parts = host_threads() * 2;
+        const size_t chunk = (n_ids + parts - 1) / parts;
+        host_parallel(parts, [&](int p) { mark(std::min(n_ids, p * chunk), std::min(n_ids, (p + 1) * chunk)); });
+    } else {
+        mark(0, n_ids);
     }
     c->rast_ids.clear();
     CK(c->s.ensure(c->d_rast_dirty, c->max_ids));

@@ -278,6 +278,11 @@ struct SceneInput {
     int incr = 0;
 };
 
+// composition.cu: the process-wide host thread pool (the caller works too;
+// returns when every part is done; one run at a time)
+void host_parallel(int parts, const std::function<void(int)>& f);
+int host_threads();
+
 // composition.cu: mold's per-frame host work
 cgb_status upload_layers(cgb_composition* c);
 void rebuild_props(cgb_composition* c);
