@@ -290,8 +290,9 @@ def group_scenes(comps, sset, line_budget=16_000_000, key_bits=36):
 def run_batch(args, rank, world, local):
     """Batched workload: 256 independent scenes (layer count log-U[10, 50,000],
     canvas side in {256, 512, 1024, 2048}).  Batched = the scenes rendered
-    together, a few pipelines per pass (grouped by a line budget); plain = one
-    render call per scene.  Outputs are compared bit for bit."""
+    together, a few pipelines per pass (grouped by a line budget), the groups
+    on --batch-streams contexts at once; plain = one render call per scene.
+    Outputs are compared bit for bit."""
     import torch
     from cassia_gb300 import Composition, scenes
     from cassia_gb300.composition import kernel_launches, render_batch
@@ -308,11 +309,33 @@ def run_batch(args, rank, world, local):
     outs_p = [torch.zeros_like(o) for o in outs_b]
     ctx = Composition()
     groups = group_scenes(comps, sset)
+    # groups are rendered on args.batch_streams contexts at once (one stream and
+    # one host thread each), so that one group's tail overlaps the next group
+    ctxs = [ctx] + [Composition() for _ in range(max(1, args.batch_streams) - 1)]
+
+    def render_groups(contexts, outs, with_heights=True):
+        def part(j):
+            for gi, g in enumerate(groups):
+                if gi % len(contexts) == j:
+                    render_batch(contexts[j], [comps[k] for k in g], [outs[k] for k in g], [sset[k].width for k in g],
+                                 [sset[k].background for k in g],
+                                 heights=[sset[k].height for k in g] if with_heights else None)
+        if len(contexts) == 1:
+            part(0)
+            return
+        threads = [threading.Thread(target=part, args=(j,)) for j in range(len(contexts))]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+
+    ptrs_b = [o.data_ptr() for o in outs_b]
+
+    def batched_one():  # one context (what the autotuner times on its stream)
+        render_groups(ctxs[:1], ptrs_b)
 
     def batched():
-        for g in groups:
-            render_batch(ctx, [comps[k] for k in g], [outs_b[k].data_ptr() for k in g], [sset[k].width for k in g],
-                         [sset[k].background for k in g], heights=[sset[k].height for k in g])
+        render_groups(ctxs, ptrs_b)
 
     def plain():
         for k, sc in enumerate(sset):
@@ -332,11 +355,14 @@ def run_batch(args, rank, world, local):
     # per-scene composition so that the comparison isolates batching
     from cassia_gb300 import autotune
     t_tune = time.time()
-    tuning, trials = autotune.tune(ctx, batched, snapshot=lambda: [o.clone() for o in outs_b],
+    tuning, trials = autotune.tune(ctx, batched_one, snapshot=lambda: [o.clone() for o in outs_b],
                                    same=lambda a, b: all(torch.equal(x, y) for x, y in zip(a, b)), reps=2)
     tune_s = time.time() - t_tune
+    for c in ctxs[1:]:
+        c.set_tuning(**tuning)
     if args.frame_mode == "graph":  # after tuning: each tuning is a new frame geometry
-        ctx.set_graph_mode(True)
+        for c in ctxs:
+            c.set_graph_mode(True)
     for c in comps:
         c.set_tuning(**tuning)
     for _ in range(args.warmup):
@@ -362,9 +388,7 @@ def run_batch(args, rank, world, local):
     host = [torch.zeros((sc.height, sc.width, 4), dtype=torch.uint8).pin_memory().numpy() for sc in sset]
 
     def batched_host():
-        for g in groups:
-            render_batch(ctx, [comps[k] for k in g], [host[k] for k in g], [sset[k].width for k in g],
-                         [sset[k].background for k in g])
+        render_groups(ctxs, host, with_heights=False)
 
     batched_host()
     te = timed(batched_host, max(1, args.steps // 2))
@@ -375,6 +399,7 @@ def run_batch(args, rank, world, local):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+int (fixed point)", "data": "synthetic (seeded)",
             "config": {"workload": args.workload, "scenes": len(sset), "layers": int(sum(s.n_layers for s in sset)),
                        "frames_per_pass": len(groups), "segments_per_pass": int(segs),
+                       "contexts": len(ctxs),
                        "l2": "inputs larger than L2"},
             "plain_scenes_per_s": world * len(sset) / tp_ref, "plain_ms_per_pass": tp_ref * 1e3,
             "speedup_vs_plain": tp_ref / tb, "bit_exact_batched_vs_plain": bool(exact), "frame_mode": args.frame_mode,
@@ -511,6 +536,8 @@ def main():
                          "host updates, 6 add nothing)")
     ap.add_argument("--blend-mode", type=int, default=None, choices=range(12),
                     help="give every layer this blend mode (the cost of one mode; changes the scene)")
+    ap.add_argument("--batch-streams", type=int, default=2,
+                    help="batch256: contexts (streams) the groups of scenes are rendered on at once")
     ap.add_argument("--no-forms", dest="forms", action="store_false",
                     help="mixed100k: skip the batched (batch256) and served (serve) sub-objects")
     ap.add_argument("--cpu-budget", type=float, default=150.0,
