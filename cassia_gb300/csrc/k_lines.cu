@@ -468,12 +468,12 @@ __device__ __forceinline__ bool render_key(const SceneRaster& sr, const BatchGeo
     return true;
 }
 
-// One pixel step (rasterizer/mod.rs:233-281): one or two segments, of which
-// the kept ones (all of them outside render mode) go to out; `produced`
-// counts both.
+// One pixel step (rasterizer/mod.rs:233-281): one or two segments, at out[0]
+// and out[1]; returns the mask of those kept (all of them outside render
+// mode); `produced` counts both.
 template <int RENDER>
-__device__ __forceinline__ int raster_step(const SceneRaster& sr, const BatchGeom& bg, const LineRec& l, int32_t pi,
-                                           uint64_t out[2], int& produced) {
+__device__ __forceinline__ uint32_t raster_step(const SceneRaster& sr, const BatchGeom& bg, const LineRec& l,
+                                                int32_t pi, uint64_t out[2], int& produced) {
     const uint32_t oct = l.order_octant & 7, layer = (l.order_octant >> 3) & ((1u << (LINE_SCENE_SHIFT - 3)) - 1);
     const int32_t x0i = wadd(l.start, pi);
     const int32_t x1i = wadd(x0i, 1);
@@ -488,26 +488,28 @@ __device__ __forceinline__ int raster_step(const SceneRaster& sr, const BatchGeo
     const int32_t ys = (int32_t)((uint32_t)(max(y0s, y1s) >> PIXEL_SHIFT) << PIXEL_SHIFT);
     const int32_t xs = to_sub_pixel(__fmaf_rn(l.slope_recip, (float)(max(y0s, y1s) >> PIXEL_SHIFT), l.px_slope_recip_py));
     const int32_t ex = inter ? xs : x1s, ey = inter ? ys : y1s;
-    int m = 0;
+    uint32_t mask = 0;
     {
         const SegFields f = seg_fields(x0s, ex, y0s, ey, border_x, min(ey, y0s) >> PIXEL_SHIFT, oct);
         if (RENDER) {
-            if (render_key(sr, bg, layer, f, out[m])) m++;
+            if (render_key(sr, bg, layer, f, out[0])) mask |= 1u;
         } else {
-            out[m++] = pack_fields(sr.wide, layer, f);
+            out[0] = pack_fields(sr.wide, layer, f);
+            mask |= 1u;
         }
     }
     produced += 1;
     if (inter) {
         const SegFields f = seg_fields(xs, x1s, ys, y1s, border_x, min(ys, y1s) >> PIXEL_SHIFT, oct);
         if (RENDER) {
-            if (render_key(sr, bg, layer, f, out[m])) m++;
+            if (render_key(sr, bg, layer, f, out[1])) mask |= 2u;
         } else {
-            out[m++] = pack_fields(sr.wide, layer, f);
+            out[1] = pack_fields(sr.wide, layer, f);
+            mask |= 2u;
         }
         produced += 1;
     }
-    return m;
+    return mask;
 }
 
 
@@ -579,7 +581,10 @@ __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ r
         for (uint32_t q = threadIdx.x; q < nl; q += blockDim.x) s_recs[q] = recs[l0 + q];
     __syncthreads();
     const uint64_t s0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * RASTER_ITEMS;
+    // step k's segments at fixed positions 2k, 2k + 1 (constant indices keep
+    // the array in registers); `kept` marks the positions that hold one
     uint64_t segs[2 * RASTER_ITEMS];
+    uint32_t kept = 0;
     int n = 0, total = 0;
     if (s0 < n_steps) {
         uint32_t l;
@@ -643,11 +648,9 @@ __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ r
                                          bg.scenes[sc].row_base};
                     }
                 }
-                uint64_t o[2];
-                const int m = raster_step<RENDER>(sr, bg, rec, (int32_t)(s - cur), o, total);
-#pragma unroll
-                for (int q = 0; q < 2; q++)
-                    if (q < m) segs[n++] = o[q];
+                const uint32_t m = raster_step<RENDER>(sr, bg, rec, (int32_t)(s - cur), &segs[2 * k], total);
+                kept |= m << (2 * k);
+                n += __popc(m);
             }
         }
     }
@@ -693,7 +696,9 @@ __global__ void __launch_bounds__(256) k_rasterize(const LineRec* __restrict__ r
     __syncthreads();
     const uint32_t local = warp_sums[warp] + inc - n;
     const uint32_t btotal = warp_tot[0];
-    for (int q = 0; q < n; q++) s_out[local + q] = segs[q];
+#pragma unroll
+    for (int q = 0; q < 2 * RASTER_ITEMS; q++)
+        if ((kept >> q) & 1u) s_out[local + __popc(kept & ((1u << q) - 1u))] = segs[q];
     __syncthreads();
     uint64_t* dst = runs + (uint64_t)blockIdx.x * (2 * RASTER_ITEMS * blockDim.x);
     for (uint32_t i = threadIdx.x; i < btotal; i += blockDim.x) dst[i] = s_out[i];
