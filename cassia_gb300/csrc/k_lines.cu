@@ -718,7 +718,8 @@ __global__ void __launch_bounds__(256) k_import_segments(const uint64_t* __restr
     const SceneDesc& sc = bg.scenes[0];
     const SceneRaster sr{sc.wide, sc.rows, sc.row_len, sc.row_base};
     const uint64_t s0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * IMPORT_ITEMS;
-    uint64_t keys[IMPORT_ITEMS];
+    uint64_t keys[IMPORT_ITEMS];  // segment k's key at slot k (constant indices: registers)
+    uint32_t mask = 0;
     int kept = 0, real = 0;
 #pragma unroll
     for (int k = 0; k < IMPORT_ITEMS; k++) {
@@ -740,7 +741,11 @@ __global__ void __launch_bounds__(256) k_import_segments(const uint64_t* __restr
         f.low = (uint32_t)(v & 0x3FFFFFu);
         real++;
         uint64_t key;
-        if (layer < sc.n_orders && render_key(sr, bg, layer, f, key)) keys[kept++] = key;
+        if (layer < sc.n_orders && render_key(sr, bg, layer, f, key)) {
+            keys[k] = key;
+            mask |= 1u << k;
+            kept++;
+        }
     }
     __shared__ uint32_t warp_sums[32];
     __shared__ uint32_t warp_tot[32];
@@ -782,7 +787,9 @@ __global__ void __launch_bounds__(256) k_import_segments(const uint64_t* __restr
     __syncthreads();
     const uint32_t local = warp_sums[warp] + inc - kept;
     const uint32_t btotal = warp_tot[0];
-    for (int q = 0; q < kept; q++) s_out[local + q] = keys[q];
+#pragma unroll
+    for (int q = 0; q < IMPORT_ITEMS; q++)
+        if ((mask >> q) & 1u) s_out[local + __popc(mask & ((1u << q) - 1u))] = keys[q];
     __syncthreads();
     uint64_t* dst = runs + (uint64_t)blockIdx.x * (IMPORT_ITEMS * blockDim.x);
     for (uint32_t i = threadIdx.x; i < btotal; i += blockDim.x) dst[i] = s_out[i];
