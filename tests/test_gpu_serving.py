@@ -142,3 +142,69 @@ def test_added_layers_copy_pool_lines(gpu_lib):
     a.insert_layer_copies(ids_a[:1], src, picks[:1])
     with pytest.raises(Exception):
         b.insert_layer_copies(ids_b[:1], a, ids_a[:1])
+
+
+def test_update_layers_equals_separate_calls(gpu_lib):
+    """cgb_update_layers applies each composition's transforms, removals
+    (with remove_disabled) and added copies exactly as the separate calls
+    do: same new ids, same lines, same pixels."""
+    from cassia_gb300 import Composition, scenes
+    from cassia_gb300.composition import solid_props, update_layers
+    sc = scenes.mixed(seed=46, n_layers=120, width=256, height=192)
+    pool = scenes.mixed(seed=47, n_layers=32, width=256, height=192)
+    src = Composition()
+    src.create_layers(pool.n_layers)
+    src.insert_paths(pool)
+    a, b = Composition(), Composition()
+    for c in (a, b):
+        scenes.load(sc, c)
+    rng = np.random.default_rng(48)
+    live = np.arange(sc.n_layers, dtype=np.uint32)
+    for step in range(3):
+        pick = rng.permutation(len(live))
+        ids = np.sort(live[pick[:25]])
+        gone = np.sort(live[pick[25:31 + 20 * step]])
+        t = np.tile(np.array([[1.0, 0.0, 0.0, 1.0, 0.0, 0.0]], np.float32), (len(ids), 1))
+        t[:, 0] = t[:, 3] = rng.uniform(0.8, 1.2, len(ids)).astype(np.float32)
+        t[:, 4:] = rng.uniform(-20, 20, (len(ids), 2)).astype(np.float32)
+        picks = rng.integers(0, pool.n_layers, len(gone)).astype(np.uint32)
+        props = solid_props(pool.fill_rule[picks], pool.blend_mode[picks], pool.color[picks])
+        new_a = update_layers([{"comp": a, "transform_ids": ids, "transforms": t, "removed_ids": gone,
+                                "added_from": src, "added_from_ids": picks, "added_props": props,
+                                "added_transforms": pool.transforms[picks]}])[0]
+        b.set_transforms(ids, t)
+        b.set_enabled_many(gone, np.zeros(len(gone), np.uint8))
+        b.remove_disabled()
+        new_b = b.create_layers(len(gone))
+        b.insert_layer_copies(new_b, src, picks)
+        b.set_layers_solid(new_b, pool.fill_rule[picks], pool.blend_mode[picks], pool.color[picks])
+        b.set_transforms(new_b, pool.transforms[picks])
+        live = np.concatenate([np.setdiff1d(live, gone), new_b]).astype(np.uint32)
+        assert np.array_equal(new_a, new_b)
+        assert a.lens() == b.lens()
+        ia = np.zeros((sc.height, sc.width, 4), np.uint8)
+        ib = np.zeros_like(ia)
+        a.render(ia, sc.width, sc.background)
+        b.render(ib, sc.width, sc.background)
+        assert np.array_equal(ia, ib), f"step {step}"
+
+
+def test_copies_refused_after_compaction(gpu_lib):
+    """remove_disabled's garbage collection moves the kept lines, after which
+    a source layer's lines are no longer known to be one run."""
+    from cassia_gb300 import Composition, abi, scenes
+    pool = scenes.mixed(seed=49, n_layers=20, width=128, height=128)
+    src = Composition()
+    src.create_layers(pool.n_layers)
+    src.insert_paths(pool)
+    dst = Composition()
+    ids = dst.create_layers(2)
+    last = np.array([pool.n_layers - 1], np.uint32)
+    dst.insert_layer_copies(ids[:1], src, last)  # one run: accepted
+    before = src.lens()[0]
+    src.set_enabled_many(np.arange(pool.n_layers - 1, dtype=np.uint32), np.zeros(pool.n_layers - 1, np.uint8))
+    src.remove_disabled()  # more than half the lines are garbage: compaction
+    assert src.lens()[0] < before
+    with pytest.raises(abi.CassiaError) as ex:
+        dst.insert_layer_copies(ids[1:], src, last)
+    assert ex.value.status == abi.ERR_INVALID_ARG
