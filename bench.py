@@ -313,21 +313,31 @@ def run_batch(args, rank, world, local):
     # one host thread each), so that one group's tail overlaps the next group
     ctxs = [ctx] + [Composition() for _ in range(max(1, args.batch_streams) - 1)]
 
-    def render_groups(contexts, outs, with_heights=True):
+    def render_groups(contexts, outs, with_heights=True, mapped=False):
         def part(j):
             for gi, g in enumerate(groups):
                 if gi % len(contexts) == j:
                     render_batch(contexts[j], [comps[k] for k in g], [outs[k] for k in g], [sset[k].width for k in g],
                                  [sset[k].background for k in g],
-                                 heights=[sset[k].height for k in g] if with_heights else None)
+                                 heights=[sset[k].height for k in g] if with_heights else None, mapped=mapped)
         if len(contexts) == 1:
             part(0)
             return
-        threads = [threading.Thread(target=part, args=(j,)) for j in range(len(contexts))]
+        errors = []
+
+        def guarded(j):
+            try:
+                part(j)
+            except BaseException as e:  # re-raised below: a failed group must fail the run
+                errors.append(e)
+
+        threads = [threading.Thread(target=guarded, args=(j,)) for j in range(len(contexts))]
         for t in threads:
             t.start()
         for t in threads:
             t.join()
+        if errors:
+            raise errors[0]
 
     ptrs_b = [o.data_ptr() for o in outs_b]
 
@@ -387,8 +397,8 @@ def run_batch(args, rank, world, local):
     # e2e: the same batched pass into pinned host buffers (RGBA8 read back each pass)
     host = [torch.zeros((sc.height, sc.width, 4), dtype=torch.uint8).pin_memory().numpy() for sc in sset]
 
-    def batched_host():
-        render_groups(ctxs, host, with_heights=False)
+    def batched_host():  # page-locked host buffers, written by the painter directly
+        render_groups(ctxs, host, with_heights=False, mapped=True)
 
     batched_host()
     te = timed(batched_host, max(1, args.steps // 2))
@@ -524,7 +534,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="mixed100k", choices=list(WORKLOADS))
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--update-steps", type=int, default=5,
                     help="frames re-transforming 20%% / 5%% of the layers, full vs incremental (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -640,17 +650,21 @@ def main():
         ids = np.arange(scene.n_layers, dtype=np.uint32)
         tr = torch.from_numpy(scene.transforms if scene.transforms is not None
                               else np.tile(np.array([[1, 0, 0, 1, 0, 0]], np.float32), (scene.n_layers, 1)))
-        tr = tr.pin_memory().numpy()
-        comp.set_transforms(ids, tr)
-        comp.render(host_img, W, scene.background)
+        # two placements prepared before the timed steps (the caller's input of
+        # a frame), alternated so that every frame moves every layer
+        tr = [tr.pin_memory().numpy() for _ in range(2)]
+        tr[1][:, 4] += np.float32(0.25)
+        # the frame goes to page-locked host memory that the painter writes
+        # directly (CGB_MEMORY_HOST_MAPPED): no device staging and copy back
+        comp.set_transforms(ids, tr[0])
+        comp.render(host_img, W, scene.background, mapped=True)
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
         t0 = time.perf_counter()
         for k in range(args.e2e_steps):
-            tr[:, 4] += np.float32(0.25 if k % 2 == 0 else -0.25)  # a new placement each frame
-            comp.set_transforms(ids, tr)
-            comp.render(host_img, W, scene.background)
+            comp.set_transforms(ids, tr[(k + 1) % 2])
+            comp.render(host_img, W, scene.background, mapped=True)
         torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t0) / args.e2e_steps
         e2e_s = over_ranks(e2e_s)

@@ -76,6 +76,7 @@ pub const CGB_SORT_CANONICAL: u32 = 0;
 pub const CGB_SORT_KEY: u32 = 1;
 pub const CGB_MEMORY_HOST: u32 = 0;
 pub const CGB_MEMORY_DEVICE: u32 = 1;
+pub const CGB_MEMORY_HOST_MAPPED: u32 = 2;
 
 // ---- plain-data types ------------------------------------------------------------
 

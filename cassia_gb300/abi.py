@@ -35,7 +35,7 @@ COMPOSITION_PRIORITY_HIGH = 2
 COMPOSITION_PRIORITY_LOW = 4
 TRANSFORM_UNCHECKED = 1
 SORT_CANONICAL, SORT_KEY = 0, 1
-MEMORY_HOST, MEMORY_DEVICE = 0, 1
+MEMORY_HOST, MEMORY_DEVICE, MEMORY_HOST_MAPPED = 0, 1, 2
 
 
 class CgbProps(ctypes.Structure):

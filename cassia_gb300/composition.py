@@ -32,14 +32,16 @@ def _fp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
 
 
-def _buffer(pixels, width, layer_cache=-1, width_stride=None, height=None):
+def _buffer(pixels, width, layer_cache=-1, width_stride=None, height=None, mapped=False):
+    """mapped: `pixels` (a numpy array) is page-locked host memory the device
+    writes directly (CGB_MEMORY_HOST_MAPPED), e.g. a pinned torch tensor's numpy view."""
     stride = width_stride or width
     b = abi.CgbBuffer()
     if isinstance(pixels, np.ndarray):
         assert pixels.dtype == np.uint8 and pixels.flags.c_contiguous
         b.pixels = pixels.ctypes.data
         b.height = pixels.size // (4 * stride)
-        b.memory = abi.MEMORY_HOST
+        b.memory = abi.MEMORY_HOST_MAPPED if mapped else abi.MEMORY_HOST
     else:
         b.pixels = int(pixels)
         b.height = int(height)
@@ -50,16 +52,18 @@ def _buffer(pixels, width, layer_cache=-1, width_stride=None, height=None):
     return b
 
 
-def render_batch(ctx, scenes, pixels, widths, backgrounds, crops=None, heights=None, layer_caches=None):
+def render_batch(ctx, scenes, pixels, widths, backgrounds, crops=None, heights=None, layer_caches=None,
+                 mapped=False):
     """Renders several Compositions in one pipeline (cgb_render_batch) on
-    `ctx`'s stream.  pixels[k] is a host numpy RGBA8 array or a device
-    pointer (then heights[k] is required)."""
+    `ctx`'s stream.  pixels[k] is a host numpy RGBA8 array (page-locked and
+    written directly with `mapped`) or a device pointer (then heights[k] is
+    required)."""
     lib = abi.load_library()
     n = len(scenes)
     bufs = (abi.CgbBuffer * max(n, 1))()
     for k in range(n):
         bufs[k] = _buffer(pixels[k], widths[k], layer_cache=-1 if layer_caches is None else layer_caches[k],
-                          height=None if heights is None else heights[k])
+                          height=None if heights is None else heights[k], mapped=mapped)
     handles = (ctypes.c_void_p * max(n, 1))(*[s._h.value for s in scenes])
     bg = (ctypes.c_float * (4 * max(n, 1)))(*[float(v) for b in backgrounds for v in b])
     cr = None
@@ -264,12 +268,13 @@ class Composition:
 
     # ---- frames -----------------------------------------------------------------
     def render(self, pixels, width, background, crop=None, layer_cache=-1, width_stride=None, height=None,
-               flusher=None):
+               flusher=None, mapped=False):
         """Composition::render.  `pixels` is a host uint8 numpy array of shape
-        (height, width_stride, 4), or a device pointer (int) with `height` given.
+        (height, width_stride, 4) (page-locked and written directly by the
+        device with `mapped`), or a device pointer (int) with `height` given.
         `flusher(view)` (host buffers) is called with an (n, 4) uint8 view of
         each row slice of every tile written, as mold's Buffer::flusher."""
-        b = _buffer(pixels, width, layer_cache, width_stride, height)
+        b = _buffer(pixels, width, layer_cache, width_stride, height, mapped)
         cb = None
         if flusher is not None:
             def _flush(user, ptr, n):

@@ -207,11 +207,32 @@ cgb_status prepare_scene(cgb_composition* c, SceneInput& in) {
     const cgb_buffer* buf = in.buf;
     if (!buf || !in.bg || !buf->pixels || buf->width == 0 || buf->height == 0)
         return fail(CGB_ERR_INVALID_ARG, "render: empty buffer");
-    if (buf->flusher && buf->memory != CGB_MEMORY_HOST)
+    if (buf->memory > CGB_MEMORY_HOST_MAPPED) return fail(CGB_ERR_INVALID_ARG, "render: unknown buffer memory kind");
+    if (buf->flusher && buf->memory == CGB_MEMORY_DEVICE)
         return fail(CGB_ERR_INVALID_ARG, "render: a flusher needs a host buffer");
     const uint64_t stride = buf->width_stride ? buf->width_stride : buf->width;
     if (stride < buf->width || buf->width > (1u << 20) || buf->height > (1u << 20))
         return fail(CGB_ERR_INVALID_ARG, "render: bad width/stride/height");
+    in.mapped = nullptr;
+    if (buf->memory == CGB_MEMORY_HOST_MAPPED) {
+        // page-locked host memory the device reaches directly (its first and
+        // last byte checked; the caller vouches for the range between)
+        const size_t last = ((size_t)(buf->height - 1) * stride + buf->width) * 4 - 1;
+        cudaPointerAttributes a0{}, a1{};
+        // the device addresses are those of the current context: make the
+        // device's primary context current on this thread first
+        const bool ok = cudaSetDevice(c->device) == cudaSuccess &&
+                        cudaPointerGetAttributes(&a0, buf->pixels) == cudaSuccess &&
+                        cudaPointerGetAttributes(&a1, buf->pixels + last) == cudaSuccess &&
+                        a0.type == cudaMemoryTypeHost && a1.type == cudaMemoryTypeHost && a0.devicePointer &&
+                        a1.devicePointer &&
+                        (uint8_t*)a1.devicePointer - (uint8_t*)a0.devicePointer == (ptrdiff_t)last;
+        if (!ok) {
+            cudaGetLastError();
+            return fail(CGB_ERR_INVALID_ARG, "render: a mapped buffer must be page-locked host memory");
+        }
+        in.mapped = (uint8_t*)a0.devicePointer;
+    }
     const uint32_t rows = (uint32_t)((buf->height + 7) / 8), row_len = (uint32_t)((buf->width + 7) / 8);
     const uint64_t n_tiles = (uint64_t)rows * row_len;
     in.cache = nullptr;
@@ -964,6 +985,8 @@ cgb_status render_frame(cgb_composition* c, std::vector<SceneInput>& scenes) {
             if (in.cache || in.crop)  // tiles that are not repainted keep the caller's pixels
                 CK(cudaMemcpy2DAsync(in.d.out, (size_t)in.d.stride * 4, in.buf->pixels, (size_t)in.d.stride * 4,
                                      (size_t)in.d.width * 4, in.d.height, cudaMemcpyHostToDevice, st));
+        } else if (in.buf->memory == CGB_MEMORY_HOST_MAPPED) {
+            in.d.out = in.mapped;  // the painter writes the caller's pages directly
         } else {
             in.d.out = in.buf->pixels;
         }

@@ -273,6 +273,7 @@ struct SceneInput {
     CacheState* cache;
     SceneDesc d;
     size_t staging_off;  // offset in the frame's host-output staging buffer
+    uint8_t* mapped = nullptr;  // CGB_MEMORY_HOST_MAPPED: the buffer's device address
     // incremental frames: 0 no; 1 all lines rasterized, the resident
     // segments rebuilt; 2 only changed layers rasterized, the resident ones kept
     int incr = 0;

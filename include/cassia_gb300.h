@@ -136,6 +136,13 @@ typedef struct cgb_props {
  * `width_stride` RGBA8 pixels of which the first `width` are painted. */
 #define CGB_MEMORY_HOST 0u
 #define CGB_MEMORY_DEVICE 1u
+/* Page-locked host memory the device can address (cudaHostAlloc,
+ * cudaHostRegister): the painter writes the pixels into it directly over the
+ * host link, without a device staging buffer and a copy back.  The whole
+ * buffer must lie in one page-locked allocation (its first and last byte are
+ * checked: CGB_ERR_INVALID_ARG otherwise).  Flushers work as for host
+ * buffers. */
+#define CGB_MEMORY_HOST_MAPPED 2u
 /* surpass Flusher::flush (surpass/src/painter/buffer_layout.rs:52-54): called
  * with each row slice (at most 8 pixels) of every tile the render wrote. */
 typedef void (*cgb_flush_fn)(void* user, uint8_t* pixels, size_t n_pixels);
@@ -146,7 +153,7 @@ typedef struct cgb_buffer {
     uint64_t height;
     uint64_t width_stride; /* 0 means width */
     int32_t layer_cache;   /* BufferLayerCache id, or -1 */
-    uint32_t memory;       /* CGB_MEMORY_HOST | CGB_MEMORY_DEVICE */
+    uint32_t memory;       /* CGB_MEMORY_HOST | CGB_MEMORY_DEVICE | CGB_MEMORY_HOST_MAPPED */
     /* mold Buffer::flusher (mold/src/buffer.rs:19-25), host buffers only:
      * after the frame, called on the host for the row slices of every tile
      * written (not for tiles left unchanged by a layer cache or outside the
