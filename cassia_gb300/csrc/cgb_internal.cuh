@@ -108,9 +108,11 @@ struct SceneDesc {
 
 // Frame-wide geometry of the render-mode segment key, bit fields from high
 // to low:
-//   key = global tile row | order | tile column + 1
-// (order_bits and col_bits wide), with n_orders and row_len the maxima over
-// the frame's scenes.
+//   key = global tile row | tile column + 1 | order
+// (col_bits and order_bits wide), with n_orders and row_len the maxima over
+// the frame's scenes.  Sorted, the segments are tile-major: each tile's
+// tile-layer groups are contiguous and in paint order, as the reference's
+// `u64 >> 22` sort key orders them (tile_j, tile_i, layer).
 struct BatchGeom {
     const SceneDesc* scenes;     // device array
     const uint32_t* row_scene;   // device: scene of each global tile row
@@ -124,18 +126,22 @@ struct BatchGeom {
 
 __host__ __device__ __forceinline__ uint64_t make_render_key(const BatchGeom& bg, uint32_t grow, uint32_t order,
                                                              uint32_t col1) {
-    return ((((uint64_t)grow << bg.order_bits) | order) << bg.col_bits) | col1;
+    return ((((uint64_t)grow << bg.col_bits) | col1) << bg.order_bits) | order;
 }
-// (row, order) run of a key, its tile column + 1, its order and row
-__host__ __device__ __forceinline__ uint64_t key_run(uint64_t key, uint32_t col_bits) { return key >> col_bits; }
-__host__ __device__ __forceinline__ uint32_t key_col1(uint64_t key, uint32_t col_bits) {
-    return (uint32_t)(key & ((1ull << col_bits) - 1));
+// The fields of a key (bits 22..63 of a segment) in a layout of order_bits /
+// col_bits: its row, tile column + 1 and order, and its (row, order) run
+// (row << order_bits | order), along which cover carries flow.
+__host__ __device__ __forceinline__ uint32_t key_order(uint64_t key, uint32_t order_bits) {
+    return (uint32_t)(key & ((1ull << order_bits) - 1));
 }
-__host__ __device__ __forceinline__ uint32_t run_order(uint64_t run, uint32_t order_bits) {
-    return (uint32_t)(run & ((1ull << order_bits) - 1));
+__host__ __device__ __forceinline__ uint32_t key_col1(uint64_t key, uint32_t order_bits, uint32_t col_bits) {
+    return (uint32_t)((key >> order_bits) & ((1ull << col_bits) - 1));
 }
-__host__ __device__ __forceinline__ uint32_t run_row(uint64_t run, uint32_t order_bits) {
-    return (uint32_t)(run >> order_bits);
+__host__ __device__ __forceinline__ uint32_t key_row(uint64_t key, uint32_t order_bits, uint32_t col_bits) {
+    return (uint32_t)(key >> (order_bits + col_bits));
+}
+__host__ __device__ __forceinline__ uint64_t key_run(uint64_t key, uint32_t order_bits, uint32_t col_bits) {
+    return ((uint64_t)key_row(key, order_bits, col_bits) << order_bits) | key_order(key, order_bits);
 }
 
 // LineRec.order_octant packing: scene << 20 | order << 3 | octant
@@ -259,7 +265,11 @@ cudaError_t launch_flatten(int write, const uint32_t* kinds, const float* points
                            const uint32_t* path_layer, uint32_t n_paths, uint32_t* counts, const uint32_t* out_off,
                            float* p0x, float* p0y, float* p1x, float* p1y, uint32_t* lids, cudaStream_t st);
 // cull != 0 (render mode) drops lines whose segments the painter never reads.
-cudaError_t launch_build_lines(const BatchGeom& bg, int cull, LineRec* recs, uint32_t* lengths, cudaStream_t st);
+// order_flag (zeroed by the caller), if given, is set to 1 when some line of
+// a scene has a lower order than the line before it; while it stays 0 the
+// rasterizer's segments come out in non-decreasing order within each scene.
+cudaError_t launch_build_lines(const BatchGeom& bg, int cull, LineRec* recs, uint32_t* lengths, cudaStream_t st,
+                               uint32_t* order_flag = nullptr);
 // mode: 0 = count, 1 = write.  render != 0: culled, re-keyed render format;
 // else the reference segment format of the (single) scene.
 // Rasterizes every pixel step (`items` consecutive steps per thread, 4 or 8);
@@ -301,7 +311,18 @@ cudaError_t scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, Scratch* s, 
 // sorts of up to sort_n keys (before a frame graph is captured: nothing may
 // allocate while a stream captures).
 cudaError_t reserve_frame_scratch(Scratch* s, uint32_t scan_n, uint32_t sort_n);
-// Sort n u64 keys by bits [bit_lo, bit_hi).  `keys` and `tmp` hold n keys;
+// The key bits a sort orders by, [lo, hi), with the digit passes planned
+// separately for [lo, mid) and for [mid, hi).  With skip_flag, the passes of
+// [lo, mid) are skipped on the device while *skip_flag == 0: the caller's
+// guarantee that wherever bits [mid, hi) tie the keys already come in
+// non-decreasing [lo, mid) order, so that those stable passes would move no
+// key (the result is bit for bit the full sort's).
+struct SortBits {
+    int lo, mid, hi;
+    const uint32_t* skip_flag;
+};
+inline SortBits sort_bits(int lo, int hi) { return SortBits{lo, lo, hi, nullptr}; }
+// Sort n u64 keys by bits [sb.lo, sb.hi).  `keys` and `tmp` hold n keys;
 // on return *result points at the sorted array (keys or tmp).  With
 // hist_ready the digit counts of every pass are already in s->sort_hist
 // (from radix_gather_hist).
@@ -309,8 +330,8 @@ cudaError_t reserve_frame_scratch(Scratch* s, uint32_t scan_n, uint32_t sort_n);
 // Pass p ranks its tile's keys with warp ballots instead of match.any when bit
 // p of ballot_passes is set: for digits that the lanes of a warp mostly hold
 // distinct (the low digit of the work items' tile field).
-cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo, int bit_hi, int digit_bits,
-                           Scratch* s, uint32_t* err_flag, cudaStream_t st, uint64_t** result, int* passes,
+cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, SortBits sb, int digit_bits, Scratch* s,
+                           uint32_t* err_flag, cudaStream_t st, uint64_t** result, int* passes,
                            bool hist_ready = false, FrameCounts* fc = nullptr, int fc_which = 0,
                            uint32_t ballot_passes = 0);
 // Runs one onesweep CTA whose predecessor tile never publishes; *flag_host
@@ -318,16 +339,22 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo
 cudaError_t selftest_bounded_wait(cudaStream_t st, uint32_t* flag_host);
 // Packs runs of keys (run r: run_count[r] keys at runs[r * run_slots...],
 // placed at run_off[r] of out) and counts the digits of every pass of the sort
-// by bits [bit_lo, bit_hi) into s->sort_hist, for radix_sort_u64(hist_ready).
+// by `sb` into s->sort_hist, for radix_sort_u64(hist_ready) with the same sb.
 // Keys placed at or beyond out_cap are dropped (a graph frame whose segment
 // count passed its capacity; the sort reports the overflow).
 cudaError_t radix_gather_hist(const uint64_t* runs, uint32_t run_slots, const uint32_t* run_count,
-                              const uint32_t* run_off, uint32_t n_runs, uint64_t* out, int bit_lo, int bit_hi,
-                              int digit_bits, Scratch* s, cudaStream_t st, uint32_t out_cap = 0xFFFFFFFFu);
+                              const uint32_t* run_off, uint32_t n_runs, uint64_t* out, SortBits sb, int digit_bits,
+                              Scratch* s, cudaStream_t st, uint32_t out_cap = 0xFFFFFFFFu);
+// The sort of a frame's render keys (bits 22..63 of its segments): bits
+// [22, 22 + order_bits) hold the order, the passes that order_flag lets the
+// frame skip.
+inline SortBits render_sort_bits(const BatchGeom& bg, const uint32_t* order_flag) {
+    return SortBits{22, 22 + (int)bg.order_bits, 22 + (int)bg.key_bits, order_flag};
+}
 
 // k_incr.cu: incremental frames
 // Local key layout of a composition's resident segments after a batched
-// frame (bits 22..63): tile row (12 bits) | order (17) | tile column + 1 (13).
+// frame (bits 22..63): tile row (12 bits) | tile column + 1 (13) | order (17).
 // After a frame of the composition alone they stay in that frame's layout.
 constexpr int LOCAL_ORDER_BITS = 17;
 constexpr int LOCAL_COL_BITS = 13;
@@ -370,20 +397,31 @@ cudaError_t launch_extract(const uint64_t* segs, const ExtractTarget* tg, uint32
                            const BatchGeom& bg, cudaStream_t st);
 
 // k_paint.cu
+// The run-record sort ranks its first two passes (the order's digits) by
+// warp ballots: consecutive TLs of a tile hold distinct, increasing orders.
+constexpr uint32_t TL_SORT_BALLOT_PASSES = 3u;
+// TLs (tile-layer groups) are numbered in segment order, which is
+// tile-major; tl_rec lists them along the (row, order) runs that carry
+// cover from tile to tile: entry s = run << idx_bits | TL index, sorted by
+// run (stably, so each run's TLs go left to right).
 struct CarryBuffers {
     uint32_t* tl_start;   // [G + 1] first segment of each tile-layer group (TL)
     uint64_t* tl_key;     // [G] its segment key (bits 22..63)
     uint64_t* tl_cover;   // [G] lane-wise cover sum of its segments
     uint64_t* tl_carry;   // [G] cover entering it along its (row, order) run
-    uint32_t* tl_flags;   // [G] 1 = first TL of its run
-    uint32_t* item_count; // [G]
+    uint64_t* tl_rec;     // [G] run << idx_bits | TL: written unsorted by the TL scan, then sorted
+    uint64_t* tl_skey;    // [G] by position in tl_rec: the TL's key
+    uint64_t* tl_sout;    // [G] by position in tl_rec: the cover leaving the TL
+    uint32_t* item_count; // [G] by position in tl_rec
     uint32_t* item_off;   // [G + 1]
     uint64_t* items;      // [W]
     uint64_t* items_tmp;  // [W]
     uint32_t* tile_start; // [tiles + 1]
     uint64_t* blk_cover;  // [tl_scan_grid] per block: cover sum before its first TL head
     uint32_t* blk_head;   // [tl_scan_grid] per block: holds a TL head
-    int order_bits;       // width of the order field of an item
+    int order_bits;       // width of the order field of keys and items
+    int col_bits;         // width of the tile column field of keys
+    int idx_bits;         // width of the TL index in tl_rec and in items
     // graph frames: the device counts, and the TL and item capacities (TL
     // and item writes at or beyond them are dropped); without fc, the exact
     // G and W bound every write
@@ -391,7 +429,7 @@ struct CarryBuffers {
     uint32_t tl_cap, items_cap;
 };
 // n: the segment count (with cb.fc, the capacity of the segment arrays).
-cudaError_t launch_tl_scan(int mode, const uint64_t* segs, uint32_t n, uint32_t col_bits, uint32_t* block_counts,
+cudaError_t launch_tl_scan(int mode, const uint64_t* segs, uint32_t n, uint32_t* block_counts,
                            const uint32_t* block_off, const CarryBuffers& cb, cudaStream_t st);
 uint32_t tl_scan_grid(uint32_t n);
 // Also sets tl_start[G] = P.  G, P: the counts (with cb.fc, the capacities).

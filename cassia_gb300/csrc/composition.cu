@@ -576,7 +576,7 @@ CGB_EXPORT cgb_status cgb_composition_free(cgb_composition* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     DevBuf* bufs[] = {&c->p0x, &c->p0y, &c->p1x, &c->p1y, &c->lids, &c->d_layers, &c->recs, &c->lengths,
                       &c->step_off, &c->bcounts, &c->boff, &c->segs_a, &c->segs_b, &c->raster_lines,
-                      &c->tl_start, &c->tl_key, &c->blk_cover, &c->blk_head, &c->rlb, &c->item_state, &c->d_import, &c->written, &c->tl_cover, &c->tl_carry, &c->tl_flags, &c->item_count, &c->item_off,
+                      &c->tl_start, &c->tl_key, &c->blk_cover, &c->blk_head, &c->rlb, &c->item_state, &c->d_import, &c->written, &c->tl_cover, &c->tl_carry, &c->tl_rec_a, &c->tl_rec_b, &c->tl_skey, &c->tl_sout, &c->order_flag, &c->item_count, &c->item_off,
                       &c->items_a, &c->items_b, &c->tile_start, &c->d_props, &c->d_grads, &c->d_stops, &c->d_unchanged, &c->out_rgba, &c->err,
                       &c->dflt_t, &c->f_kinds, &c->f_points, &c->f_cmd_off, &c->f_pt_off, &c->f_t9, &c->f_has_t,
                       &c->f_path_layer, &c->f_counts, &c->f_off, &c->g_flags, &c->g_off, &c->s.scan_sums,
@@ -983,12 +983,12 @@ CGB_EXPORT cgb_status cgb_pixel_segments(cgb_composition* c, uint64_t* out, size
     bg.total_lines = c->n_lines;
     const int lo = order == CGB_SORT_CANONICAL ? 0 : 22;
     uint64_t* keys = nullptr;
-    cgb_status s2 = build_and_rasterize(c, 0, bg, lo, 64, &P, &PT, &keys);
+    cgb_status s2 = build_and_rasterize(c, 0, bg, sort_bits(lo, 64), nullptr, &P, &PT, &keys);
     if (s2) return s2;
     uint64_t* sorted = keys;
     int passes = 0;
-    CK(radix_sort_u64(keys, c->segs_a.as<uint64_t>(), (uint32_t)P, lo, 64, (int)c->tuning.radix_bits, &c->s,
-                      c->err.as<uint32_t>(), c->stream, &sorted, &passes, true));
+    CK(radix_sort_u64(keys, c->segs_a.as<uint64_t>(), (uint32_t)P, sort_bits(lo, 64), (int)c->tuning.radix_bits,
+                      &c->s, c->err.as<uint32_t>(), c->stream, &sorted, &passes, true));
     c->stats.sort_passes = passes;
     CK(stage_mark(c, 3, c->stream, nullptr));
     *out_len = P;
@@ -1113,8 +1113,8 @@ CGB_EXPORT cgb_status cgb_selftest_bounded_wait(void) {
             cudaError_t es = cudaMemsetAsync(err, 0, 4, st);
             if (es == cudaSuccess) es = cudaMemcpyAsync(d, host.data(), n_keys * 8, cudaMemcpyHostToDevice, st);
             if (es == cudaSuccess)
-                es = radix_sort_u64(d, d + n_keys, n_keys, 0, 64, 8, &scratch, err, st, &result, nullptr, false,
-                                    nullptr, 0, 0);
+                es = radix_sort_u64(d, d + n_keys, n_keys, sort_bits(0, 64), 8, &scratch, err, st, &result, nullptr,
+                                    false, nullptr, 0, 0);
             std::vector<uint64_t> back(n_keys);
             if (es == cudaSuccess)
                 es = cudaMemcpyAsync(back.data(), result, n_keys * 8, cudaMemcpyDeviceToHost, st);

@@ -24,7 +24,7 @@ cudaError_t stage_mark(cgb_composition* c, int k, cudaStream_t st, const char* n
 // *keys (segs_b; segs_a is free for the sort) with the digit histogram of the
 // sort by bits [sort_lo, sort_hi) counted.  sparse: only changed layers'
 // lines have steps (an incremental frame).
-cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& bg, int sort_lo, int sort_hi,
+cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& bg, SortBits sb, uint32_t* order_flag,
                                uint64_t* n_segs, uint64_t* n_total, uint64_t** keys, bool sparse) {
     cudaStream_t st = c->stream;
     if (bg.total_lines >= (1ull << 32)) return fail(CGB_ERR_LAYER_LIMIT, "more than 2^32 lines in a frame");
@@ -34,7 +34,8 @@ cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& 
     CK(c->s.ensure(c->lengths, std::max<size_t>(L, 1) * 4));
     CK(c->s.ensure(c->step_off, ((size_t)L + 1) * 4));
     CK(stage_mark(c, 0, st, "cgb:build_lines"));
-    CK(launch_build_lines(bg, render, c->recs.as<LineRec>(), c->lengths.as<uint32_t>(), st));
+    if (order_flag) CK(cudaMemsetAsync(order_flag, 0, 4, st));
+    CK(launch_build_lines(bg, render, c->recs.as<LineRec>(), c->lengths.as<uint32_t>(), st, order_flag));
     uint64_t S = 0;
     CK(scan_u32(c->lengths.as<uint32_t>(), c->step_off.as<uint32_t>(), L, &c->s, st, &S));
     CK(stage_mark(c, 1, st, "cgb:rasterize"));
@@ -61,7 +62,7 @@ cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& 
     if (P >= (1ull << 30) - 1) return fail(CGB_ERR_LAYER_LIMIT, "more than 2^30 pixel segments");
     CK(c->s.ensure(c->segs_b, std::max<size_t>(P, 1) * 8));
     CK(radix_gather_hist(c->segs_a.as<uint64_t>(), slots, c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid,
-                         c->segs_b.as<uint64_t>(), sort_lo, sort_hi, (int)c->tuning.radix_bits, &c->s, st));
+                         c->segs_b.as<uint64_t>(), sb, (int)c->tuning.radix_bits, &c->s, st));
     CK(stage_mark(c, 2, st, "cgb:sort"));
     *n_segs = P;
     *n_total = PT;
@@ -72,7 +73,7 @@ cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& 
 
 // cassia_render's segments (host memory) into packed keys of scene 0, with
 // the sort's digit histogram counted, like build_and_rasterize.
-cgb_status import_segments(cgb_composition* c, const BatchGeom& bg, int sort_lo, int sort_hi, uint64_t* n_segs,
+cgb_status import_segments(cgb_composition* c, const BatchGeom& bg, SortBits sb, uint64_t* n_segs,
                            uint64_t* n_total, uint64_t** keys) {
     cudaStream_t st = c->stream;
     const uint64_t n = c->import_n;
@@ -99,7 +100,7 @@ cgb_status import_segments(cgb_composition* c, const BatchGeom& bg, int sort_lo,
     if (P >= (1ull << 30) - 1) return fail(CGB_ERR_LAYER_LIMIT, "more than 2^30 pixel segments");
     CK(c->s.ensure(c->segs_b, std::max<size_t>(P, 1) * 8));
     CK(radix_gather_hist(c->segs_a.as<uint64_t>(), slots, c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid,
-                         c->segs_b.as<uint64_t>(), sort_lo, sort_hi, (int)c->tuning.radix_bits, &c->s, st));
+                         c->segs_b.as<uint64_t>(), sb, (int)c->tuning.radix_bits, &c->s, st));
     CK(stage_mark(c, 2, st, "cgb:sort"));
     *n_segs = P;
     *n_total = n ? c->s.pinned[3] : 0;
@@ -443,15 +444,19 @@ cgb_status staged_frame(cgb_composition* c, const FrameSetup& f, std::vector<Sce
     uint64_t* keys = nullptr;
     bool sparse = false;  // some scene rasterizes only its changed layers
     for (const SceneInput& in : scenes) sparse |= in.incr == 2;
-    cgb_status s2 = c->import_segs ? import_segments(c, bg, 22, 22 + (int)bg.key_bits, &P, &PT, &keys)
-                                   : build_and_rasterize(c, 1, bg, 22, 22 + (int)bg.key_bits, &P, &PT, &keys, sparse);
+    CK(c->s.ensure(c->order_flag, 4));
+    uint32_t* order_flag = c->order_flag.as<uint32_t>();
+    // imported segments come in any order: every pass runs
+    const SortBits sb = render_sort_bits(bg, c->import_segs ? nullptr : order_flag);
+    cgb_status s2 = c->import_segs ? import_segments(c, bg, sb, &P, &PT, &keys)
+                                   : build_and_rasterize(c, 1, bg, sb, order_flag, &P, &PT, &keys, sparse);
     if (s2) return s2;
     c->stats.painted_segments = P;
-    // sort by (global row, order, tile column)
+    // sort tile-major: by (global row, tile column, order)
     uint64_t* sorted = keys;
     int passes = 0;
-    CK(radix_sort_u64(keys, c->segs_a.as<uint64_t>(), (uint32_t)P, 22, 22 + (int)bg.key_bits,
-                      (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &sorted, &passes, true));
+    CK(radix_sort_u64(keys, c->segs_a.as<uint64_t>(), (uint32_t)P, sb, (int)c->tuning.radix_bits, &c->s,
+                      c->err.as<uint32_t>(), st, &sorted, &passes, true));
     c->stats.sort_passes = passes;
     c->last_new_segs = P;
     if (f.incremental) {
@@ -470,32 +475,45 @@ cgb_status staged_frame(cgb_composition* c, const FrameSetup& f, std::vector<Sce
     CK(c->s.ensure(c->blk_head, ((size_t)hg + 1) * 4));
     cb.blk_cover = c->blk_cover.as<uint64_t>();
     cb.blk_head = c->blk_head.as<uint32_t>();
-    CK(launch_tl_scan(0, sorted, (uint32_t)P, bg.col_bits, c->bcounts.as<uint32_t>(), nullptr, cb, st));
+    cb.order_bits = (int)bg.order_bits;
+    cb.col_bits = (int)bg.col_bits;
+    CK(launch_tl_scan(0, sorted, (uint32_t)P, c->bcounts.as<uint32_t>(), nullptr, cb, st));
     uint64_t G = 0;
     if (P) CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), hg, &c->s, st, &G));
     c->stats.tile_layers = G;
+    const int idx_bits = bits_for(std::max<uint64_t>(G, 1) - 1);
+    const int run_bits = (int)(bg.key_bits - bg.col_bits);
+    if (idx_bits + run_bits > 64) return fail(CGB_ERR_LAYER_LIMIT, "render: too many tile-layer groups");
     CK(c->s.ensure(c->tl_start, (G + 1) * 4));
     CK(c->s.ensure(c->tl_key, std::max<uint64_t>(G, 1) * 8));
     CK(c->s.ensure(c->tl_cover, std::max<uint64_t>(G, 1) * 8));
     CK(c->s.ensure(c->tl_carry, std::max<uint64_t>(G, 1) * 8));
-    CK(c->s.ensure(c->tl_flags, std::max<uint64_t>(G, 1) * 4));
+    CK(c->s.ensure(c->tl_rec_a, std::max<uint64_t>(G, 1) * 8));
+    CK(c->s.ensure(c->tl_rec_b, std::max<uint64_t>(G, 1) * 8));
+    CK(c->s.ensure(c->tl_skey, std::max<uint64_t>(G, 1) * 8));
+    CK(c->s.ensure(c->tl_sout, std::max<uint64_t>(G, 1) * 8));
     CK(c->s.ensure(c->item_count, std::max<uint64_t>(G, 1) * 4));
     CK(c->s.ensure(c->item_off, (G + 1) * 4));
     cb.tl_start = c->tl_start.as<uint32_t>();
     cb.tl_key = c->tl_key.as<uint64_t>();
     cb.tl_cover = c->tl_cover.as<uint64_t>();
     cb.tl_carry = c->tl_carry.as<uint64_t>();
-    cb.tl_flags = c->tl_flags.as<uint32_t>();
+    cb.tl_rec = c->tl_rec_a.as<uint64_t>();
+    cb.tl_skey = c->tl_skey.as<uint64_t>();
+    cb.tl_sout = c->tl_sout.as<uint64_t>();
     cb.item_count = c->item_count.as<uint32_t>();
     cb.item_off = c->item_off.as<uint32_t>();
-    cb.order_bits = (int)bg.order_bits;
-    CK(launch_tl_scan(1, sorted, (uint32_t)P, bg.col_bits, nullptr, c->boff.as<uint32_t>(), cb, st));
+    cb.idx_bits = idx_bits;
+    CK(launch_tl_scan(1, sorted, (uint32_t)P, nullptr, c->boff.as<uint32_t>(), cb, st));
+    // the (row, order) runs: the TLs' run records sorted by run
+    CK(radix_sort_u64(cb.tl_rec, c->tl_rec_b.as<uint64_t>(), (uint32_t)G, sort_bits(idx_bits, idx_bits + run_bits),
+                      (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &cb.tl_rec, nullptr, false, nullptr,
+                      0, TL_SORT_BALLOT_PASSES));
     CK(launch_tl_carry((uint32_t)G, (uint32_t)P, cb, st));
     CK(launch_items(0, (uint32_t)G, bg, cb, 0, st));
     uint64_t W = 0;
     if (G) CK(scan_u32(cb.item_count, cb.item_off, (uint32_t)G, &c->s, st, &W));
     c->stats.work_items = W;
-    const int idx_bits = bits_for(std::max<uint64_t>(G, 1) - 1);
     const int tile_bits = bits_for(std::max<uint64_t>(tiles, 1) - 1);
     const int tile_shift = idx_bits + 3 + cb.order_bits;  // TL index, item flags, order, then the tile
     if (tile_shift + tile_bits > 64 || W >= (1ull << 30))
@@ -510,7 +528,7 @@ cgb_status staged_frame(cgb_composition* c, const FrameSetup& f, std::vector<Sce
     uint64_t* items_sorted = cb.items;
     int ipasses = 0;
     // stable sort on the tile field: each tile's items stay in order
-    CK(radix_sort_u64(cb.items, cb.items_tmp, (uint32_t)W, tile_shift, tile_shift + tile_bits,
+    CK(radix_sort_u64(cb.items, cb.items_tmp, (uint32_t)W, sort_bits(tile_shift, tile_shift + tile_bits),
                       (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &items_sorted, &ipasses, false,
                       nullptr, 0, 1u));
     c->stats.item_sort_passes = ipasses;
@@ -550,7 +568,8 @@ std::string frame_signature(const cgb_composition* c, const FrameSetup& f) {
 std::vector<std::pair<const void*, size_t>> graph_buffers(cgb_composition* c) {
     const DevBuf* b[] = {&c->recs,       &c->lengths,   &c->step_off,  &c->bcounts,         &c->boff, &c->raster_lines,
                          &c->segs_a,     &c->segs_b,    &c->blk_cover, &c->blk_head,        &c->tl_start,
-                         &c->tl_key,     &c->tl_cover,  &c->tl_carry,  &c->tl_flags,        &c->item_count,
+                         &c->tl_key,     &c->tl_cover,  &c->tl_carry,  &c->tl_rec_a,        &c->tl_rec_b,
+                         &c->tl_skey,    &c->tl_sout,   &c->order_flag, &c->item_count,
                          &c->item_off,   &c->items_a,   &c->items_b,   &c->tile_start,      &c->item_state,
                          &c->written,    &c->d_scenes,  &c->d_row_scene, &c->err,           &c->d_counts,
                          &c->s.scan_sums, &c->s.sort_hist, &c->s.sort_lookback, &c->s.sort_counter};
@@ -585,7 +604,11 @@ cudaError_t ensure_graph_buffers(cgb_composition* c, const FrameSetup& f, const 
     need(c->tl_key, (uint64_t)k.tls * 8);
     need(c->tl_cover, (uint64_t)k.tls * 8);
     need(c->tl_carry, (uint64_t)k.tls * 8);
-    need(c->tl_flags, (uint64_t)k.tls * 4);
+    need(c->tl_rec_a, (uint64_t)k.tls * 8);
+    need(c->tl_rec_b, (uint64_t)k.tls * 8);
+    need(c->tl_skey, (uint64_t)k.tls * 8);
+    need(c->tl_sout, (uint64_t)k.tls * 8);
+    need(c->order_flag, 4);
     need(c->item_count, (uint64_t)k.tls * 4);
     need(c->item_off, ((uint64_t)k.tls + 1) * 4);
     need(c->items_a, (uint64_t)k.items * 8);
@@ -615,9 +638,12 @@ cgb_status enqueue_counted_frame(cgb_composition* c, const FrameSetup& f, const 
     const uint32_t block = c->tuning.raster_block, items = c->tuning.steps_per_block / block;
     const uint32_t grid = raster_grid(k.steps, block, items), slots = raster_run_slots(block, items);
     const int rbits = (int)c->tuning.radix_bits;
+    uint32_t* order_flag = c->order_flag.as<uint32_t>();
+    const SortBits sb = render_sort_bits(bg, order_flag);
     CK(cudaMemsetAsync(fc, 0, sizeof(FrameCounts), st));
+    CK(cudaMemsetAsync(order_flag, 0, 4, st));
     CK(stage_mark(c, 0, st, nullptr));
-    CK(launch_build_lines(bg, 1, c->recs.as<LineRec>(), c->lengths.as<uint32_t>(), st));
+    CK(launch_build_lines(bg, 1, c->recs.as<LineRec>(), c->lengths.as<uint32_t>(), st, order_flag));
     CK(scan_u32(c->lengths.as<uint32_t>(), c->step_off.as<uint32_t>(), L, &c->s, st, nullptr, &fc->n[FC_STEPS]));
     CK(stage_mark(c, 1, st, nullptr));
     CK(launch_rasterize(1, bg, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, k.steps, block, items,
@@ -625,12 +651,12 @@ cgb_status enqueue_counted_frame(cgb_composition* c, const FrameSetup& f, const 
                         c->raster_lines.as<uint32_t>()));
     CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid, &c->s, st, nullptr, &fc->n[FC_SEGS]));
     CK(radix_gather_hist(c->segs_a.as<uint64_t>(), slots, c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), grid,
-                         c->segs_b.as<uint64_t>(), 22, 22 + (int)bg.key_bits, rbits, &c->s, st, k.segs));
+                         c->segs_b.as<uint64_t>(), sb, rbits, &c->s, st, k.segs));
     CK(stage_mark(c, 2, st, nullptr));
     uint64_t* sorted = nullptr;
     int passes = 0;
-    CK(radix_sort_u64(c->segs_b.as<uint64_t>(), c->segs_a.as<uint64_t>(), k.segs, 22, 22 + (int)bg.key_bits, rbits,
-                      &c->s, err, st, &sorted, &passes, true, fc, FC_SEGS));
+    CK(radix_sort_u64(c->segs_b.as<uint64_t>(), c->segs_a.as<uint64_t>(), k.segs, sb, rbits, &c->s, err, st, &sorted,
+                      &passes, true, fc, FC_SEGS));
     g->sort_passes = (uint32_t)passes;
     CK(stage_mark(c, 3, st, nullptr));
     return enqueue_counted_tail(c, f, k, sorted, g);
@@ -655,31 +681,39 @@ cgb_status enqueue_counted_tail(cgb_composition* c, const FrameSetup& f, const F
     cb.tl_key = c->tl_key.as<uint64_t>();
     cb.tl_cover = c->tl_cover.as<uint64_t>();
     cb.tl_carry = c->tl_carry.as<uint64_t>();
-    cb.tl_flags = c->tl_flags.as<uint32_t>();
+    cb.tl_rec = c->tl_rec_a.as<uint64_t>();
+    cb.tl_skey = c->tl_skey.as<uint64_t>();
+    cb.tl_sout = c->tl_sout.as<uint64_t>();
     cb.item_count = c->item_count.as<uint32_t>();
     cb.item_off = c->item_off.as<uint32_t>();
     cb.items = c->items_a.as<uint64_t>();
     cb.items_tmp = c->items_b.as<uint64_t>();
     cb.tile_start = c->tile_start.as<uint32_t>();
     cb.order_bits = (int)bg.order_bits;
+    cb.col_bits = (int)bg.col_bits;
     cb.fc = fc;
     cb.tl_cap = k.tls;
     cb.items_cap = k.items;
-    CK(launch_tl_scan(0, sorted, k.segs, bg.col_bits, c->bcounts.as<uint32_t>(), nullptr, cb, st));
+    const int idx_bits = bits_for((uint64_t)k.tls - 1);
+    const int run_bits = (int)(bg.key_bits - bg.col_bits);
+    if (idx_bits + run_bits > 64) return fail(CGB_ERR_LAYER_LIMIT, "render: frame graph run record too wide");
+    cb.idx_bits = idx_bits;
+    CK(launch_tl_scan(0, sorted, k.segs, c->bcounts.as<uint32_t>(), nullptr, cb, st));
     CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), hg, &c->s, st, nullptr, &fc->n[FC_TLS]));
-    CK(launch_tl_scan(1, sorted, k.segs, bg.col_bits, nullptr, c->boff.as<uint32_t>(), cb, st));
+    CK(launch_tl_scan(1, sorted, k.segs, nullptr, c->boff.as<uint32_t>(), cb, st));
+    CK(radix_sort_u64(cb.tl_rec, c->tl_rec_b.as<uint64_t>(), k.tls, sort_bits(idx_bits, idx_bits + run_bits), rbits,
+                      &c->s, err, st, &cb.tl_rec, nullptr, false, fc, FC_TLS, TL_SORT_BALLOT_PASSES));
     CK(launch_tl_carry(k.tls, k.segs, cb, st));
     CK(launch_items(0, k.tls, bg, cb, 0, st));
     CK(scan_u32(cb.item_count, cb.item_off, k.tls, &c->s, st, nullptr, &fc->n[FC_ITEMS]));
-    const int idx_bits = bits_for((uint64_t)k.tls - 1);
     const int tile_bits = bits_for(std::max<uint64_t>(f.tiles, 1) - 1);
     const int tile_shift = idx_bits + 3 + cb.order_bits;
     if (tile_shift + tile_bits > 64) return fail(CGB_ERR_LAYER_LIMIT, "render: frame graph item key too wide");
     CK(launch_items(1, k.tls, bg, cb, idx_bits, st));
     uint64_t* items_sorted = nullptr;
     int ipasses = 0;
-    CK(radix_sort_u64(cb.items, cb.items_tmp, k.items, tile_shift, tile_shift + tile_bits, rbits, &c->s, err, st,
-                      &items_sorted, &ipasses, false, fc, FC_ITEMS, 1u));
+    CK(radix_sort_u64(cb.items, cb.items_tmp, k.items, sort_bits(tile_shift, tile_shift + tile_bits), rbits, &c->s,
+                      err, st, &items_sorted, &ipasses, false, fc, FC_ITEMS, 1u));
     g->item_sort_passes = (uint32_t)ipasses;
     CK(launch_tile_ranges(items_sorted, k.items, (uint32_t)f.tiles, tile_shift, cb.tile_start, st, fc));
     CK(stage_mark(c, 4, st, nullptr));
@@ -857,7 +891,11 @@ cgb_status sync_free_incremental(cgb_composition* c, const FrameSetup& f, std::v
     CK(sc.ensure(c->tl_key, (uint64_t)k.tls * 8));
     CK(sc.ensure(c->tl_cover, (uint64_t)k.tls * 8));
     CK(sc.ensure(c->tl_carry, (uint64_t)k.tls * 8));
-    CK(sc.ensure(c->tl_flags, (uint64_t)k.tls * 4));
+    CK(sc.ensure(c->tl_rec_a, (uint64_t)k.tls * 8));
+    CK(sc.ensure(c->tl_rec_b, (uint64_t)k.tls * 8));
+    CK(sc.ensure(c->tl_skey, (uint64_t)k.tls * 8));
+    CK(sc.ensure(c->tl_sout, (uint64_t)k.tls * 8));
+    CK(sc.ensure(c->order_flag, 4));
     CK(sc.ensure(c->item_count, (uint64_t)k.tls * 4));
     CK(sc.ensure(c->item_off, ((uint64_t)k.tls + 1) * 4));
     CK(sc.ensure(c->items_a, (uint64_t)k.items * 8));
@@ -874,10 +912,13 @@ cgb_status sync_free_incremental(cgb_composition* c, const FrameSetup& f, std::v
     const int rbits = (int)c->tuning.radix_bits;
     const KeepSource src{c->resident.as<uint64_t>(), 0, K, c->d_rast_dirty.as<uint8_t>(), c->max_ids, 0,
                          c->resident_ob, c->resident_cb};
+    uint32_t* order_flag = c->order_flag.as<uint32_t>();
+    const SortBits sb = render_sort_bits(bg, order_flag);
     CK(cudaMemsetAsync(fc, 0, sizeof(FrameCounts), st));
+    CK(cudaMemsetAsync(order_flag, 0, 4, st));
     CK(cudaMemcpyAsync(c->d_keep.p, &src, sizeof(src), cudaMemcpyHostToDevice, st));
     CK(stage_mark(c, 0, st, "cgb:build_lines"));
-    CK(launch_build_lines(bg, 1, c->recs.as<LineRec>(), c->lengths.as<uint32_t>(), st));
+    CK(launch_build_lines(bg, 1, c->recs.as<LineRec>(), c->lengths.as<uint32_t>(), st, order_flag));
     CK(scan_u32(c->lengths.as<uint32_t>(), c->step_off.as<uint32_t>(), L, &sc, st, nullptr, &fc->n[FC_STEPS]));
     CK(stage_mark(c, 1, st, "cgb:rasterize"));
     CK(launch_rasterize(1, bg, c->recs.as<LineRec>(), c->step_off.as<uint32_t>(), L, k.steps, block, items,
@@ -886,13 +927,12 @@ cgb_status sync_free_incremental(cgb_composition* c, const FrameSetup& f, std::v
     CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), (uint32_t)grid, &sc, st, nullptr,
                 &fc->n[FC_NEW]));
     CK(radix_gather_hist(c->segs_a.as<uint64_t>(), (uint32_t)slots, c->bcounts.as<uint32_t>(),
-                         c->boff.as<uint32_t>(), (uint32_t)grid, c->segs_b.as<uint64_t>(), 22, 22 + (int)bg.key_bits,
-                         rbits, &sc, st, ic.segs));
+                         c->boff.as<uint32_t>(), (uint32_t)grid, c->segs_b.as<uint64_t>(), sb, rbits, &sc, st, ic.segs));
     CK(stage_mark(c, 2, st, "cgb:sort"));
     uint64_t* sorted_new = nullptr;
     int passes = 0;
-    CK(radix_sort_u64(c->segs_b.as<uint64_t>(), c->segs_a.as<uint64_t>(), ic.segs, 22, 22 + (int)bg.key_bits, rbits,
-                      &sc, err, st, &sorted_new, &passes, true, fc, FC_NEW));
+    CK(radix_sort_u64(c->segs_b.as<uint64_t>(), c->segs_a.as<uint64_t>(), ic.segs, sb, rbits, &sc, err, st,
+                      &sorted_new, &passes, true, fc, FC_NEW));
     if (K) {
         CK(launch_keep(0, c->d_keep.as<KeepSource>(), 1, K, bg, c->bcounts.as<uint32_t>(), nullptr, nullptr, 0, st));
         CK(scan_u32(c->bcounts.as<uint32_t>(), c->boff.as<uint32_t>(), (uint32_t)kg, &sc, st, nullptr,

@@ -200,7 +200,9 @@ struct cgb_composition {
     // frame buffers
     DevBuf recs, lengths, step_off, bcounts, boff, segs_a, segs_b;
     DevBuf raster_lines;  // [2 * (raster grid + 1)] first and last line of each rasterizer block
-    DevBuf tl_start, tl_key, tl_cover, tl_carry, tl_flags, item_count, item_off, items_a, items_b, tile_start;
+    DevBuf tl_start, tl_key, tl_cover, tl_carry, tl_rec_a, tl_rec_b, tl_skey, tl_sout, item_count, item_off, items_a,
+        items_b, tile_start;
+    DevBuf order_flag;  // u32: 1 = some scene's lines are not in non-decreasing layer order
     DevBuf blk_cover, blk_head, rlb, item_state, written;
     DevBuf d_props, d_grads, d_stops, d_unchanged, out_rgba, err, dflt_t, d_scenes, d_row_scene;
     // flatten staging
@@ -291,7 +293,9 @@ cgb_status remove_disabled(cgb_composition* c);
 
 // frame.cu: the frame pipeline
 cudaError_t stage_mark(cgb_composition* c, int k, cudaStream_t st, const char* next);
-cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& bg, int sort_lo, int sort_hi,
+// sb: the sort the gathered keys get (its digit counts are taken on the way);
+// order_flag: render mode's order check of the lines (see launch_build_lines), or null.
+cgb_status build_and_rasterize(cgb_composition* c, int render, const BatchGeom& bg, SortBits sb, uint32_t* order_flag,
                                uint64_t* n_segs, uint64_t* n_total, uint64_t** keys, bool sparse = false);
 cgb_status check_device_error(cgb_composition* c);
 float elapsed(cudaEvent_t a, cudaEvent_t b);

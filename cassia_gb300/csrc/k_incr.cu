@@ -4,11 +4,12 @@
 // frame on the device ("resident" segments): after a frame of its own, that
 // frame's sorted segments as they are (a buffer swap); after a batched
 // frame, its range of the batch re-keyed to a fixed local layout, bits
-// 22..63 = row:12 | order:17 | tile column + 1:13.  The next
+// 22..63 = row:12 | tile column + 1:13 | order:17.  The next
 // frame rasterizes only the lines of changed layers (their orders are marked
 // dirty; a layer whose order changed marks both orders), sorts those
 // segments, keeps the resident segments of clean orders, re-keys them into
-// the frame's key space and merges the two sorted streams.  Keys of one
+// the frame's key space and merges the two sorted streams (re-keying keeps
+// the tile-major order: row, tile column, order).  Keys of one
 // order never come from both streams, so the merge needs no tie rule beyond
 // "kept first"; within one tile-layer group the order of segments does not
 // change any pixel (their areas and covers are summed).  Afterwards the
@@ -40,7 +41,7 @@ constexpr int MERGE_ITEMS = 4;
 constexpr int MERGE_TILE = MERGE_THREADS * MERGE_ITEMS;
 
 __device__ __forceinline__ uint64_t local_key(uint32_t row, uint32_t order, uint32_t col1) {
-    return ((uint64_t)row << (LOCAL_ORDER_BITS + LOCAL_COL_BITS)) | ((uint64_t)order << LOCAL_COL_BITS) | col1;
+    return ((uint64_t)row << (LOCAL_ORDER_BITS + LOCAL_COL_BITS)) | ((uint64_t)col1 << LOCAL_ORDER_BITS) | order;
 }
 
 // The resident source of flattened index g: the last descriptor whose start is <= g.
@@ -58,9 +59,9 @@ __device__ __forceinline__ uint32_t keep_source(const KeepSource* s, uint32_t n,
 // and its key re-packed into the frame's layout.
 __device__ __forceinline__ bool keep_segment(const KeepSource& src, const BatchGeom& bg, uint64_t v, uint64_t* out) {
     const uint64_t k = v >> 22;
-    const uint32_t col1 = (uint32_t)(k & ((1ull << src.col_bits) - 1));
-    const uint32_t order = (uint32_t)((k >> src.col_bits) & ((1ull << src.order_bits) - 1));
-    const uint32_t row = (uint32_t)(k >> (src.order_bits + src.col_bits));
+    const uint32_t col1 = key_col1(k, src.order_bits, src.col_bits);
+    const uint32_t order = key_order(k, src.order_bits);
+    const uint32_t row = key_row(k, src.order_bits, src.col_bits);
     if (order >= src.n_dirty || src.dirty[order]) return false;
     *out = (make_render_key(bg, src.row_base + row, order, col1) << 22) | (v & 0x3FFFFFull);
     return true;
@@ -259,9 +260,8 @@ __global__ void k_extract(const uint64_t* __restrict__ segs, const ExtractTarget
     if (i >= T.n || i >= T.cap) return;
     const uint64_t v = segs[T.first + i];
     const uint64_t k = v >> 22;
-    const uint32_t col1 = key_col1(k, bg.col_bits);
-    const uint64_t run = key_run(k, bg.col_bits);
-    const uint32_t order = run_order(run, bg.order_bits), row = run_row(run, bg.order_bits) - T.row_base;
+    const uint32_t col1 = key_col1(k, bg.order_bits, bg.col_bits);
+    const uint32_t order = key_order(k, bg.order_bits), row = key_row(k, bg.order_bits, bg.col_bits) - T.row_base;
     T.dst[i] = (local_key(row, order, col1) << 22) | (v & 0x3FFFFFull);
 }
 

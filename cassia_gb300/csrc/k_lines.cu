@@ -4,7 +4,9 @@
 //                  Transform (mold/src/path/transform.rs:56-94): one thread per
 //                  path; a count pass, a scan of the counts, a write pass.
 //   k_build_lines  LinesBuilder::build (surpass/src/segment.rs:91-237): one
-//                  thread per line; writes a packed 32-byte LineRec + length.
+//                  thread per line; writes a packed 32-byte LineRec + length,
+//                  and flags a scene whose lines are not in non-decreasing
+//                  layer order (the sort may skip its order passes otherwise).
 //   k_block_lines  the first and last line of each rasterizer block.
 //   k_rasterize    Rasterizer::rasterize (surpass/src/rasterizer/mod.rs:214-285):
 //                  each thread walks 4 or 8 consecutive pixel steps; each block
@@ -309,7 +311,8 @@ __device__ __forceinline__ uint32_t scene_of_line(const uint64_t* base, uint32_t
     return lo;
 }
 
-__global__ void k_build_lines(BatchGeom bg, int cull, LineRec* __restrict__ recs, uint32_t* __restrict__ lengths) {
+__global__ void k_build_lines(BatchGeom bg, int cull, LineRec* __restrict__ recs, uint32_t* __restrict__ lengths,
+                              uint32_t* __restrict__ order_flag) {
     __shared__ uint64_t s_base[MAX_SMEM_SCENES];
     const uint32_t ns = min(bg.n_scenes, (uint32_t)MAX_SMEM_SCENES);
     for (uint32_t k = threadIdx.x; k < ns; k += blockDim.x) s_base[k] = bg.scenes[k].line_base;
@@ -330,8 +333,19 @@ __global__ void k_build_lines(BatchGeom bg, int cull, LineRec* __restrict__ recs
     if (lid < n_layer_recs) lrec = layers[lid];
     const uint32_t flags = lrec.flags, lorder = lrec.order;
     const bool present = (flags & LAYER_PRESENT) != 0;
+    const uint32_t order = (present && (flags & LAYER_HAS_ORDER)) ? lorder : lid;
+    if (order_flag && i > 0) {
+        // the scene's lines in non-decreasing order?  (The line before is
+        // mostly of the same layer, whose record is already cached.)
+        const uint32_t plid = S.lids[i - 1];
+        uint32_t porder = plid;
+        if (plid < n_layer_recs) {
+            const uint2 h = *reinterpret_cast<const uint2*>(&layers[plid]);
+            if ((h.x & LAYER_PRESENT) && (h.x & LAYER_HAS_ORDER)) porder = h.y;
+        }
+        if (order < porder) *order_flag = 1u;
+    }
     if (!(present && !(flags & LAYER_ENABLED))) {
-        const uint32_t order = (present && (flags & LAYER_HAS_ORDER)) ? lorder : lid;
         // the layer's affine, else the builder's default (segment.rs:130-142)
         bool has_t = false;
         float t0 = 0.f, t1 = 0.f, t2 = 0.f, t3 = 0.f, t4 = 0.f, t5 = 0.f;
@@ -832,11 +846,12 @@ cudaError_t launch_flatten(int write, const uint32_t* kinds, const float* points
     return cudaGetLastError();
 }
 
-cudaError_t launch_build_lines(const BatchGeom& bg, int cull, LineRec* recs, uint32_t* lengths, cudaStream_t st) {
+cudaError_t launch_build_lines(const BatchGeom& bg, int cull, LineRec* recs, uint32_t* lengths, cudaStream_t st,
+                               uint32_t* order_flag) {
     if (bg.total_lines == 0) return cudaSuccess;
     if (bg.n_scenes > MAX_SMEM_SCENES) return cudaErrorInvalidValue;
     count_launches(1);
-    k_build_lines<<<(uint32_t)((bg.total_lines + 255) / 256), 256, 0, st>>>(bg, cull, recs, lengths);
+    k_build_lines<<<(uint32_t)((bg.total_lines + 255) / 256), 256, 0, st>>>(bg, cull, recs, lengths, order_flag);
     return cudaGetLastError();
 }
 

@@ -4,9 +4,11 @@
 // surpass/src/painter/mod.rs:495-596) and carries each layer's per-row cover
 // from tile to tile through LayerWorkbench's queue
 // (surpass/src/painter/layer_workbench.rs:134-198, 430-486).  Here the segments
-// arrive sorted by (tile row j, order L, tile column i), so every (j, L) run of
-// "tile-layer" groups (TLs) is contiguous and the carry into a TL is an
-// exclusive prefix of the runs' cover sums (8 x i8 lanes, wrapping).
+// arrive sorted tile-major, by (tile row j, tile column i, order L), as the
+// reference's sort key orders them, so every "tile-layer" group (TL) is
+// contiguous.  The TLs' (j, L) run records, sorted by run, list each run's
+// TLs left to right, and the carry into a TL is an exclusive prefix of its
+// run's cover sums (8 x i8 lanes, wrapping).
 //
 // A layer L is painted in tile i of row j (is in the workbench's `ids`) iff
 //   - L has segments in (j, i), or
@@ -19,9 +21,9 @@
 // multiples of 32 for EvenOdd (whose tests are mod 32) and exactly for NonZero,
 // so every decision and coverage below is bit-identical.
 //
-// Work items are (tile, order) pairs, written in (row, order, column) order
-// and sorted by tile with the (stable) radix sort, which leaves each tile's
-// items in order.  The painter gives each tile one warp (2 pixels per lane), replicates
+// Work items are (tile, order) pairs, written along the sorted run records
+// ((row, order, column) order) and sorted by tile with the (stable) radix
+// sort, which leaves each tile's items in order.  The painter gives each tile one warp (2 pixels per lane), replicates
 // tile_unchanged_pass and skip_fully_covered_layers (:200-222, :310-388),
 // paints the surviving layers bottom-up in f32 with the reference's vector
 // blend formulas, and writes RGBA8 with 128-bit stores.  Frames with gradient
@@ -55,10 +57,11 @@ __device__ __forceinline__ uint64_t seg_cover(uint32_t low) {
 // (blk_cover, written by the counting pass) and whether the block holds a head.
 //
 // mode 0: per block, the TL count, blk_cover and blk_head.
-// mode 1: per TL g, its first segment, key, cover sum and run-start flag.
+// mode 1: per TL g, its first segment, key, cover sum and run record
+// (tl_rec[g] = (row, order) run << idx_bits | g, sorted afterwards).
 template <int MODE>
 __global__ void __launch_bounds__(HEAD_THREADS, 5) k_tl_scan(const uint64_t* __restrict__ segs, uint32_t n,
-                                                          uint32_t col_bits, uint32_t* __restrict__ block_counts,
+                                                          uint32_t* __restrict__ block_counts,
                                                           const uint32_t* __restrict__ block_off, CarryBuffers cb) {
     constexpr int mode = MODE;
     n = fc_count(cb.fc, FC_SEGS, n, false);
@@ -80,7 +83,6 @@ __global__ void __launch_bounds__(HEAD_THREADS, 5) k_tl_scan(const uint64_t* __r
     uint32_t flags = 0, cnt = 0;
     uint64_t prev = ~0ull;
     if (s0 < n && s0 > 0) prev = segs[s0 - 1] >> 22;
-    const uint64_t first_prev = prev;
     // the thread's segments as 16-byte pairs (s0 is a multiple of HEAD_ITEMS)
     uint64_t sv[HEAD_ITEMS];
     if (s0 + HEAD_ITEMS <= n) {
@@ -182,7 +184,6 @@ __global__ void __launch_bounds__(HEAD_THREADS, 5) k_tl_scan(const uint64_t* __r
     if (!flags) return;
     const uint32_t cap = cb.fc ? cb.tl_cap : 0xFFFFFFFFu;
     uint32_t o = block_off[blockIdx.x] + w_sums[warp] + inc - cnt;
-    uint64_t pk = first_prev;
     uint64_t acc = 0;
     int open = -1;
 #pragma unroll
@@ -197,33 +198,92 @@ __global__ void __launch_bounds__(HEAD_THREADS, 5) k_tl_scan(const uint64_t* __r
             if (o < cap) {
                 cb.tl_start[o] = (uint32_t)(s0 + k);
                 cb.tl_key[o] = key[k];
-                // a run is one (row, order) pair: a new run starts unless the
-                // previous segment is in the same row and order
-                cb.tl_flags[o] = (pk == ~0ull || key_run(pk, col_bits) != key_run(key[k], col_bits)) ? 1u : 0u;
+                cb.tl_rec[o] = (key_run(key[k], cb.order_bits, cb.col_bits) << cb.idx_bits) | o;
             }
         }
         if (s0 + k < n) acc = cover_add(acc, seg_cover(low[k]));
-        pk = key[k];
     }
     if (o < cap) cb.tl_cover[o] = cover_add(acc, cont);
 }
 
-// Exclusive prefix of the cover sums along each (j, L) run: one thread walks
-// each run (runs are a layer's few tile groups in one tile row).  Thread 0
-// also closes the TL segment ranges: tl_start[G] = P.
-__global__ void k_tl_carry(uint32_t G, uint32_t P, CarryBuffers cb) {
+// Exclusive prefix of the cover sums along each (j, L) run, taken in the
+// sorted run records (runs are a layer's tile groups in one tile row, left
+// to right): one thread per record, a segmented scan across the warp, and
+// for a run that began before the warp, the sum of its earlier records,
+// taken 32 at a time by the warp.  Each TL's entering cover goes to the
+// TL's own index, where the painter reads it; the key and the leaving cover
+// go to the record's position (tl_skey, tl_sout), where the item expansion
+// reads them in sequence.  Thread 0 also closes the TL segment ranges:
+// tl_start[G] = P.
+__global__ void __launch_bounds__(256) k_tl_carry(uint32_t G, uint32_t P, CarryBuffers cb) {
     G = fc_count(cb.fc, FC_TLS, G, blockIdx.x == 0 && threadIdx.x == 0);
     P = fc_count(cb.fc, FC_SEGS, P, false);
-    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g == 0) cb.tl_start[G] = P;
-    if (g >= G || !cb.tl_flags[g]) return;
-    uint64_t acc = 0;
-    uint32_t h = g;
-    do {
-        cb.tl_carry[h] = acc;
-        acc = cover_add(acc, cb.tl_cover[h]);
-        h++;
-    } while (h < G && !cb.tl_flags[h]);
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    if (s == 0) cb.tl_start[G] = P;
+    const uint32_t s0 = s - lane;  // the warp's first record
+    if (s0 >= G) return;           // (whole warps only: the shuffles below take every lane)
+    const int ib = cb.idx_bits;
+    const uint64_t mask = (1ull << ib) - 1;
+    const bool valid = s < G;
+    uint64_t run = ~0ull, cov = 0, key = ~0ull;  // no row: no items (g beyond G only after a failed sort)
+    uint32_t g = 0xFFFFFFFFu;
+    if (valid) {
+        const uint64_t r = cb.tl_rec[s];
+        run = r >> ib;
+        g = (uint32_t)(r & mask);
+        if (g < G) {
+            key = cb.tl_key[g];
+            cov = cb.tl_cover[g];
+        }
+    }
+    uint64_t prev_run = __shfl_up_sync(0xffffffffu, run, 1);
+    if (lane == 0) prev_run = s > 0 ? (cb.tl_rec[s - 1] >> ib) : ~run;
+    const bool head = run != prev_run;
+    // segmented inclusive scan of the covers (restart at each head)
+    uint64_t incl = cov;
+    bool f = head;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t tv = __shfl_up_sync(0xffffffffu, incl, o);
+        const bool tf = __shfl_up_sync(0xffffffffu, f ? 1 : 0, o) != 0;
+        if (lane >= o) {
+            if (!f) incl = cover_add(tv, incl);
+            f = f || tf;
+        }
+    }
+    // the run open at the warp's start: its records before the warp
+    uint64_t pre = 0;
+    const uint64_t run0 = __shfl_sync(0xffffffffu, run, 0);
+    if (!__shfl_sync(0xffffffffu, head ? 1 : 0, 0)) {
+        int64_t h0 = (int64_t)s0 - 1;
+        while (true) {
+            const int64_t h = h0 - lane;
+            bool in = false;
+            uint64_t c = 0;
+            if (h >= 0) {
+                const uint64_t r = cb.tl_rec[h];
+                in = (r >> ib) == run0;
+                const uint64_t hg = r & mask;
+                if (in && hg < G) c = cb.tl_cover[hg];
+            }
+            const uint32_t m = __ballot_sync(0xffffffffu, in);
+            const int n_in = m == 0xffffffffu ? 32 : __ffs(~m) - 1;  // the run's records are lanes [0, n_in)
+            if (lane >= n_in) c = 0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) c = cover_add(c, __shfl_xor_sync(0xffffffffu, c, o));
+            pre = cover_add(pre, c);
+            if (n_in < 32) break;
+            h0 -= 32;
+        }
+    }
+    const uint64_t incl_prev = __shfl_up_sync(0xffffffffu, incl, 1);
+    uint64_t carry = (head || lane == 0) ? 0 : incl_prev;
+    if (!f && !head) carry = cover_add(carry, pre);  // still in the warp's open run
+    if (!valid) return;
+    if (g < G) cb.tl_carry[g] = carry;
+    cb.tl_skey[s] = key;
+    cb.tl_sout[s] = cover_add(carry, cov);
 }
 
 // Work-item payload bits above the TL index: the item holds only a cover carry;
@@ -243,33 +303,40 @@ struct TlItems {
     int32_t ta, tb;     // the carry-only items' tile columns (none if ta >= tb)
     uint32_t flags;     // the carry-only items' flags
     uint32_t L;
+    uint32_t g;         // the TL (its index in segment order)
     __device__ __forceinline__ uint32_t count() const {
         return (own >= 0 ? 1u : 0u) + (tb > ta ? (uint32_t)(tb - ta) : 0u);
     }
 };
 
-__device__ __forceinline__ TlItems tl_items(uint32_t g, uint32_t G, const CarryBuffers& cb, const BatchGeom& bg) {
-    TlItems r{0, -1, 0, 0, 0, 0};
-    const uint64_t key = cb.tl_key[g];
-    const int32_t i = (int32_t)key_col1(key, bg.col_bits) - 1;
-    const uint64_t run = key_run(key, bg.col_bits);
-    const uint32_t L = run_order(run, bg.order_bits);
-    const uint32_t grow = run_row(run, bg.order_bits);
+// s: the TL's position in the sorted run records.
+__device__ __forceinline__ TlItems tl_items(uint32_t s, uint32_t G, const CarryBuffers& cb, const BatchGeom& bg) {
+    TlItems r{0, -1, 0, 0, 0, 0, 0};
+    const int ib = cb.idx_bits;
+    const uint64_t rec = cb.tl_rec[s];
+    const uint32_t g = (uint32_t)(rec & ((1ull << ib) - 1));
     // fields out of range only come from a sort that gave up (its error
     // flag is reported after the frame): no items rather than a stray access
+    if (g >= G) return r;
+    r.g = g;
+    const uint64_t key = cb.tl_skey[s];
+    const int32_t i = (int32_t)key_col1(key, bg.order_bits, bg.col_bits) - 1;
+    const uint32_t L = key_order(key, bg.order_bits);
+    const uint32_t grow = key_row(key, bg.order_bits, bg.col_bits);
     if (grow >= bg.total_rows) return r;
     const SceneDesc& S = bg.scenes[bg.row_scene[grow]];
     const uint32_t j = grow - S.row_base;
     if (j < S.crop_v0 || j >= S.crop_v1 || L >= S.n_orders) return r;
     r.L = L;
     r.row_tile = (uint64_t)S.tile_base + (uint64_t)j * S.row_len;
-    int32_t next = (int32_t)S.row_len;
-    if (g + 1 < G && !cb.tl_flags[g + 1]) next = (int32_t)key_col1(cb.tl_key[g + 1], bg.col_bits) - 1;
+    int32_t next = (int32_t)S.row_len;  // the column of the run's next TL
+    if (s + 1 < G && (cb.tl_rec[s + 1] >> ib) == (rec >> ib))
+        next = (int32_t)key_col1(cb.tl_skey[s + 1], bg.order_bits, bg.col_bits) - 1;
     const int32_t h0 = (int32_t)S.crop_h0, h1 = (int32_t)S.crop_h1;
     if (next > h1) next = h1;
     if (i >= h0 && i < h1) r.own = i;  // a layer with segments is never "full" (layer_workbench.rs:164-175)
     if (next <= i + 1) return r;
-    const uint64_t carry_out = cover_add(cb.tl_carry[g], cb.tl_cover[g]);
+    const uint64_t carry_out = cb.tl_sout[s];
     const PaintProps pp = S.props[L];
     const bool nonempty = !cover_is_empty(carry_out, pp.fill_rule);
     // payload of a cover-carry-only item: its layer_is_full and the opaque
@@ -301,10 +368,11 @@ __global__ void k_items_count(uint32_t G, CarryBuffers cb, BatchGeom bg) {
 }
 
 // Item = tile | order | flags | TL index, high to low; the tile field is the
-// sort key.  The items of a tile are written in ascending order (the TLs
-// are sorted by row, then order), so a stable sort on the tile alone leaves
-// each tile's items in paint order.  Each block expands the items of its 256
-// TLs together: thread t writes items t, t + 256, ... of the block's range.
+// sort key.  The items of a tile are written in ascending order (they are
+// written along the sorted run records: by row, then order), so a stable
+// sort on the tile alone leaves each tile's items in paint order.  Each
+// block expands the items of 256 run records together: thread t writes
+// items t, t + 256, ... of the block's range.
 constexpr int IW_THREADS = 256;
 
 __global__ void __launch_bounds__(IW_THREADS) k_items_write(uint32_t G, CarryBuffers cb, BatchGeom bg, int idx_bits) {
@@ -312,6 +380,7 @@ __global__ void __launch_bounds__(IW_THREADS) k_items_write(uint32_t G, CarryBuf
     __shared__ uint64_t s_row[IW_THREADS];
     __shared__ int32_t s_own[IW_THREADS], s_ta[IW_THREADS];
     __shared__ uint32_t s_lf[IW_THREADS];  // order << 3 | carry-only flags
+    __shared__ uint32_t s_g[IW_THREADS];   // the TL
     G = fc_count(cb.fc, FC_TLS, G, false);
     const uint32_t g0 = blockIdx.x * IW_THREADS, g = g0 + threadIdx.x;
     if (g0 >= G) return;  // graph frames: blocks past the TL count
@@ -325,6 +394,7 @@ __global__ void __launch_bounds__(IW_THREADS) k_items_write(uint32_t G, CarryBuf
         s_own[threadIdx.x] = r.own;
         s_ta[threadIdx.x] = r.ta;
         s_lf[threadIdx.x] = (r.L << ITEM_FLAG_BITS) | r.flags;
+        s_g[threadIdx.x] = r.g;
     }
     if (threadIdx.x == 0) s_off[nt] = cb.item_off[g0 + nt] - base;
     __syncthreads();
@@ -352,7 +422,7 @@ __global__ void __launch_bounds__(IW_THREADS) k_items_write(uint32_t G, CarryBuf
         }
         const uint64_t tile = s_row[lo] + (uint64_t)col;
         const uint64_t key = (((tile << ob) | (lf >> ITEM_FLAG_BITS)) << ITEM_FLAG_BITS) | fl;
-        if (base + idx < icap) cb.items[base + idx] = (key << idx_bits) | (g0 + lo);
+        if (base + idx < icap) cb.items[base + idx] = (key << idx_bits) | s_g[lo];
     }
 }
 
@@ -839,11 +909,27 @@ __device__ __forceinline__ void stage_items(const PaintArgs& a, const SceneDesc&
     S.soff[lane] = inc - cnt;
     __syncwarp();
     if (!with_segments) return;
-    // Staged segment s belongs to the last item q with soff[q] <= s among the
-    // items with segments: mark each such item at its offset, take a running
-    // maximum over the offsets, then copy 32 segments per round.
     const uint32_t staged = min(total, (uint32_t)SEGCAP);
     const uint32_t soff = inc - cnt;
+    // Segments are sorted tile-major, so a tile's TLs, in order, are
+    // consecutive TLs with consecutive segment ranges: the chunk's segments
+    // are then one run from its first TL item's first segment.
+    {
+        const uint32_t with = __ballot_sync(0xffffffffu, cnt > 0);
+        const uint32_t base = __shfl_sync(0xffffffffu, sb, with ? __ffs(with) - 1 : 0);
+        if (__all_sync(0xffffffffu, cnt == 0 || sb == base + soff)) {
+#pragma unroll
+            for (int r = 0; r < SEGCAP / 32; r++) {
+                const uint32_t pos = lane + 32 * r;
+                if (pos < staged) S.seg[pos] = (uint32_t)a.segs[base + pos];
+            }
+            __syncwarp();
+            return;
+        }
+    }
+    // Otherwise staged segment s belongs to the last item q with soff[q] <= s
+    // among the items with segments: mark each such item at its offset, take
+    // a running maximum over the offsets, then copy 32 segments per round.
     *reinterpret_cast<uint2*>(&S.owner[8 * lane]) = make_uint2(0u, 0u);
     __syncwarp();
     if (cnt > 0 && soff < (uint32_t)SEGCAP) S.owner[soff] = (uint8_t)lane;
@@ -1210,14 +1296,14 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
 
 }  // namespace
 
-cudaError_t launch_tl_scan(int mode, const uint64_t* segs, uint32_t n, uint32_t col_bits, uint32_t* block_counts,
+cudaError_t launch_tl_scan(int mode, const uint64_t* segs, uint32_t n, uint32_t* block_counts,
                            const uint32_t* block_off, const CarryBuffers& cb, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     count_launches(1);
     if (mode == 0)
-        k_tl_scan<0><<<tl_scan_grid(n), HEAD_THREADS, 0, st>>>(segs, n, col_bits, block_counts, block_off, cb);
+        k_tl_scan<0><<<tl_scan_grid(n), HEAD_THREADS, 0, st>>>(segs, n, block_counts, block_off, cb);
     else
-        k_tl_scan<1><<<tl_scan_grid(n), HEAD_THREADS, 0, st>>>(segs, n, col_bits, block_counts, block_off, cb);
+        k_tl_scan<1><<<tl_scan_grid(n), HEAD_THREADS, 0, st>>>(segs, n, block_counts, block_off, cb);
     return cudaGetLastError();
 }
 

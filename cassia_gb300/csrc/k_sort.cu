@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const uint32_t* __r
 // ---------------------------------------------------------------------------
 
 constexpr int RADIX = 512;  // up to 9-bit digits
-constexpr int MAX_PASSES = 11;
+constexpr int MAX_PASSES = 12;  // 42 key bits in 4-bit digits, split in two groups
 // 512 threads (one digit each) x 14 keys: 7,168-key tiles, 2 CTAs per SM at 64
 // registers.  Measured against 8 keys at 3 CTAs per SM, 12 and 16 keys at 2,
 // and 256-thread CTAs: this shape sorts fastest.
@@ -157,6 +157,7 @@ constexpr unsigned LB_SLEEP = 32;  // back-off (ns) after a round with no publis
 
 struct PassPlan {
     int n;
+    int skip;  // the first `skip` passes may be skipped (SortBits::skip_flag)
     int shift[MAX_PASSES];
     int bits[MAX_PASSES];
 };
@@ -219,9 +220,11 @@ __global__ void __launch_bounds__(512) k_gather_hist(const uint64_t* __restrict_
                                                      const uint32_t* __restrict__ run_count,
                                                      const uint32_t* __restrict__ run_off, uint32_t n_runs,
                                                      uint64_t* __restrict__ out, uint32_t out_cap, PassPlan plan,
-                                                     uint32_t* __restrict__ hist) {
+                                                     uint32_t* __restrict__ hist, const uint32_t* skip_flag) {
     __shared__ uint32_t sh[MAX_PASSES][RADIX];
     const int np = NP > 0 ? NP : plan.n;
+    // passes the sort will skip need no digit counts
+    const int p0 = (skip_flag && *skip_flag == 0) ? plan.skip : 0;
     for (int i = threadIdx.x; i < np * RADIX; i += blockDim.x) (&sh[0][0])[i] = 0;
     __syncthreads();
     for (uint32_t r = blockIdx.x; r < n_runs; r += gridDim.x) {
@@ -235,6 +238,7 @@ __global__ void __launch_bounds__(512) k_gather_hist(const uint64_t* __restrict_
 #pragma unroll
             for (int p = 0; p < (NP > 0 ? NP : MAX_PASSES); p++) {
                 if (NP == 0 && p >= np) break;
+                if (p < p0) continue;
                 const uint32_t d = (uint32_t)(k >> plan.shift[p]) & ((1u << plan.bits[p]) - 1);
                 atomicAdd(&sh[p][d], 1u);
             }
@@ -280,11 +284,24 @@ __device__ __forceinline__ uint32_t ballot_peers(uint32_t d) {
 // One LSD pass over a tile of SORT_TILE keys.  HI: the digit lies in the high
 // word (`sh` = shift - 32); else `sh` = shift < 32.  BALLOT: the warp's peers
 // of a digit come from ballots rather than match.any.
+// skip_mode 1: while *skip_flag == 0 the pass is skipped (it would move no
+// key); skip_mode 2: likewise, but the tile is copied to `out` (the last of
+// an odd number of skipped passes, so the keys end in the buffer the next
+// pass reads).
 template <bool HI, bool BALLOT>
 __global__ void __launch_bounds__(SORT_THREADS, SORT_MIN_BLOCKS)
     k_onesweep(const uint64_t* __restrict__ in, uint64_t* __restrict__ out, uint32_t n, int sh, int bits,
                const uint32_t* __restrict__ global_off, uint32_t* lookback, uint32_t* tile_counter, uint32_t* err,
-               FrameCounts* fc, int fc_which) {
+               FrameCounts* fc, int fc_which, const uint32_t* skip_flag, int skip_mode) {
+    if (skip_mode && *skip_flag == 0) {
+        if (skip_mode == 2) {
+            const uint32_t nk = fc_count(fc, fc_which, n, false);
+            const uint64_t b = (uint64_t)blockIdx.x * SORT_TILE;
+            for (uint32_t i = threadIdx.x; i < SORT_TILE; i += SORT_THREADS)
+                if (b + i < nk) out[b + i] = in[b + i];
+        }
+        return;
+    }
     // per-warp digit counts, then the warp's offsets within each digit; the
     // column past the digits counts the keys past the end of the last tile
     __shared__ __align__(16) uint16_t s_hist[SORT_WARPS][RADIX + 2];
@@ -441,13 +458,14 @@ cudaError_t onesweep_setup() {
 // One onesweep pass over the digit of `bits` bits at bit `shift`.
 void launch_onesweep(uint32_t grid, cudaStream_t st, const uint64_t* in, uint64_t* out, uint32_t n, int shift,
                      int bits, const uint32_t* global_off, uint32_t* lookback, uint32_t* tile_counter, uint32_t* err,
-                     FrameCounts* fc, int fc_which, bool ballot = false) {
+                     FrameCounts* fc, int fc_which, bool ballot = false, const uint32_t* skip_flag = nullptr,
+                     int skip_mode = 0) {
     const bool hi = shift >= 32;
     const int sh = hi ? shift - 32 : shift;
     auto k = hi ? (ballot ? k_onesweep<true, true> : k_onesweep<true, false>)
                 : (ballot ? k_onesweep<false, true> : k_onesweep<false, false>);
     k<<<grid, SORT_THREADS, ONESWEEP_DYN_SMEM, st>>>(in, out, n, sh, bits, global_off, lookback, tile_counter, err,
-                                                      fc, fc_which);
+                                                      fc, fc_which, skip_flag, skip_flag ? skip_mode : 0);
 }
 
 }  // namespace
@@ -493,6 +511,7 @@ cudaError_t scan_block_counts(const uint32_t* counts, uint32_t* offsets, uint32_
 
 static PassPlan make_plan(int bit_lo, int bit_hi, int digit_bits) {
     PassPlan p{};
+    p.skip = 0;
     int bits = std::max(0, bit_hi - bit_lo);
     digit_bits = std::min(9, std::max(1, digit_bits));
     p.n = (bits + digit_bits - 1) / digit_bits;
@@ -504,6 +523,18 @@ static PassPlan make_plan(int bit_lo, int bit_hi, int digit_bits) {
         p.bits[i] = b;
         sh += b;
     }
+    return p;
+}
+
+// The passes of [lo, mid), then those of [mid, hi); the first group may be skipped.
+static PassPlan make_plan(const SortBits& sb, int digit_bits) {
+    const PassPlan a = make_plan(sb.lo, sb.mid, digit_bits), b = make_plan(sb.mid, sb.hi, digit_bits);
+    PassPlan p = a;
+    for (int i = 0; i < b.n && p.n < MAX_PASSES; i++, p.n++) {
+        p.shift[p.n] = b.shift[i];
+        p.bits[p.n] = b.bits[i];
+    }
+    p.skip = sb.skip_flag ? a.n : 0;
     return p;
 }
 
@@ -521,9 +552,9 @@ static int sm_count() {
 }
 
 cudaError_t radix_gather_hist(const uint64_t* runs, uint32_t run_slots, const uint32_t* run_count,
-                              const uint32_t* run_off, uint32_t n_runs, uint64_t* out, int bit_lo, int bit_hi,
-                              int digit_bits, Scratch* s, cudaStream_t st, uint32_t out_cap) {
-    const PassPlan plan = make_plan(bit_lo, bit_hi, digit_bits);
+                              const uint32_t* run_off, uint32_t n_runs, uint64_t* out, SortBits sb, int digit_bits,
+                              Scratch* s, cudaStream_t st, uint32_t out_cap) {
+    const PassPlan plan = make_plan(sb, digit_bits);
     cudaError_t e = s->ensure(s->sort_hist, (size_t)MAX_PASSES * RADIX * 4);
     if (e != cudaSuccess) return e;
     uint32_t* hist = s->sort_hist.as<uint32_t>();
@@ -532,7 +563,8 @@ cudaError_t radix_gather_hist(const uint64_t* runs, uint32_t run_slots, const ui
     const uint32_t blocks = std::min<uint32_t>(n_runs, (uint32_t)sm_count() * 4);
     count_launches(1);
 #define CGB_GATHER(NP) \
-    k_gather_hist<NP><<<blocks, 512, 0, st>>>(runs, run_slots, run_count, run_off, n_runs, out, out_cap, plan, hist)
+    k_gather_hist<NP><<<blocks, 512, 0, st>>>(runs, run_slots, run_count, run_off, n_runs, out, out_cap, plan, hist, \
+                                              sb.skip_flag)
     switch (plan.n) {
         case 1: CGB_GATHER(1); break;
         case 2: CGB_GATHER(2); break;
@@ -546,10 +578,10 @@ cudaError_t radix_gather_hist(const uint64_t* runs, uint32_t run_slots, const ui
     return cudaGetLastError();
 }
 
-cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo, int bit_hi, int digit_bits,
-                           Scratch* s, uint32_t* err_flag, cudaStream_t st, uint64_t** result, int* passes,
-                           bool hist_ready, FrameCounts* fc, int fc_which, uint32_t ballot_passes) {
-    PassPlan plan = make_plan(bit_lo, bit_hi, digit_bits);
+cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, SortBits sb, int digit_bits, Scratch* s,
+                           uint32_t* err_flag, cudaStream_t st, uint64_t** result, int* passes, bool hist_ready,
+                           FrameCounts* fc, int fc_which, uint32_t ballot_passes) {
+    const PassPlan plan = make_plan(sb, digit_bits);
     *result = keys;
     if (passes) *passes = plan.n;
     if (n <= 1 || plan.n == 0) return cudaSuccess;
@@ -576,8 +608,10 @@ cudaError_t radix_sort_u64(uint64_t* keys, uint64_t* tmp, uint32_t n, int bit_lo
     uint64_t* dst = tmp;
     for (int p = 0; p < plan.n; p++) {
         if ((e = cudaMemsetAsync(lb, 0, (size_t)tiles * RADIX * 4, st)) != cudaSuccess) return e;
+        // skippable passes: the last of an odd number copies its keys across
+        const int skip_mode = p < plan.skip ? (p == plan.skip - 1 && (plan.skip & 1) ? 2 : 1) : 0;
         launch_onesweep(tiles, st, src, dst, n, plan.shift[p], plan.bits[p], hist + p * RADIX, lb, ctr + p, err_flag,
-                        fc, fc_which, ((ballot_passes >> p) & 1u) != 0);
+                        fc, fc_which, ((ballot_passes >> p) & 1u) != 0, sb.skip_flag, skip_mode);
         std::swap(src, dst);
     }
     *result = src;
