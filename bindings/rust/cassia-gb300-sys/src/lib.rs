@@ -146,7 +146,7 @@ pub struct cgb_stats {
     pub graph_replayed: u32,
     pub graphs_cached: u32,
     pub incremental_form: u32,
-    pub reserved: u32,
+    pub sort_passes_skipped: u32,
 }
 
 /// Autotuned knobs (0 keeps the current value).

@@ -124,7 +124,7 @@ class CgbStats(ctypes.Structure):
         ("graph_replayed", ctypes.c_uint32),
         ("graphs_cached", ctypes.c_uint32),
         ("incremental_form", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32),
+        ("sort_passes_skipped", ctypes.c_uint32),
     ]
 
     def as_dict(self):

@@ -990,6 +990,7 @@ CGB_EXPORT cgb_status cgb_pixel_segments(cgb_composition* c, uint64_t* out, size
     CK(radix_sort_u64(keys, c->segs_a.as<uint64_t>(), (uint32_t)P, sort_bits(lo, 64), (int)c->tuning.radix_bits,
                       &c->s, c->err.as<uint32_t>(), c->stream, &sorted, &passes, true));
     c->stats.sort_passes = passes;
+    c->stats.sort_passes_skipped = 0;
     CK(stage_mark(c, 3, c->stream, nullptr));
     *out_len = P;
     *out_none = 2 * c->stats.steps - P;
@@ -1013,7 +1014,6 @@ CGB_EXPORT cgb_status cgb_get_stats(cgb_composition* c, cgb_stats* out) {
     out->graph_replayed = c->last_replayed ? 1u : 0u;
     out->graphs_cached = (uint32_t)c->graphs.size();
     out->incremental_form = c->incr_form;
-    out->reserved = 0;
     return CGB_OK;
 }
 

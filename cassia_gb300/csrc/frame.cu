@@ -796,8 +796,14 @@ cgb_status finish_frame(cgb_composition* c, std::vector<SceneInput>& scenes, con
         written.resize(f.tiles);
         CK(cudaMemcpyAsync(written.data(), c->written.p, f.tiles, cudaMemcpyDeviceToHost, st));
     }
+    uint32_t* flag_host = reinterpret_cast<uint32_t*>(&c->s.pinned[5]);
+    *flag_host = 1;
+    if (!c->import_segs && c->order_flag.p) CK(cudaMemcpyAsync(flag_host, c->order_flag.p, 4, cudaMemcpyDeviceToHost, st));
     cgb_status s3 = check_device_error(c);
     if (s3) return s3;
+    // the passes of the order digits (SortBits [22, 22 + order_bits)) the sort skipped
+    const uint32_t d = std::min(9u, std::max(1u, c->tuning.radix_bits));
+    c->stats.sort_passes_skipped = *flag_host == 0 ? (f.bg.order_bits + d - 1) / d : 0u;
     c->stats.build_ms = elapsed(c->ev[0], c->ev[1]);
     c->stats.rasterize_ms = elapsed(c->ev[1], c->ev[2]);
     c->stats.sort_ms = elapsed(c->ev[2], c->ev[3]);

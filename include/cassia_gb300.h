@@ -183,7 +183,9 @@ typedef struct cgb_stats {
     uint32_t graphs_cached;    /* frame graphs held by the handle */
     uint32_t incremental_form; /* 0 full frame; incremental frame (cgb_set_incremental): 1 staged,
                                   2 sync-free (no host synchronization between stages) */
-    uint32_t reserved;
+    uint32_t sort_passes_skipped; /* of sort_passes, those of the order digits that the frame skipped:
+                                     every scene's lines were in non-decreasing layer order, so
+                                     those stable passes would have moved no segment */
 } cgb_stats;
 
 /* Autotuned knobs (0 keeps the current value).  Every setting renders the
