@@ -7,6 +7,8 @@ serving workload's seeded updates), swap layer orders, disable and re-enable
 layers and change the canvas; single renders, batched renders and the oracle;
 and with layer caches, crops, gradient fills and clip layers in the painter.
 """
+from types import SimpleNamespace
+
 import numpy as np
 import pytest
 
@@ -237,3 +239,62 @@ def test_switching_between_incremental_and_graph_frames(gpu_lib):
             assert st["incremental_form"] in (1, 2), (seq, st["incremental_form"])
         if not inc and seq == 6:  # the third full frame in a row replays its graph
             assert st["graph_replayed"] == 1
+
+
+def test_more_new_than_resident_segments(gpu_lib):
+    # A frame whose new segments outnumber the kept ones twenty to one, and
+    # the frames around it with few new segments: every frame equals a
+    # composition rendered in full and the oracle.
+    from cassia_gb300 import Composition
+    big = scenes.mixed(seed=131, n_layers=1200, width=480, height=320)
+    few = 60
+    comps = []
+    for inc in (True, False):
+        c = Composition()
+        for _ in range(big.n_layers):
+            c.create_layer()
+        if inc:
+            c.set_incremental(True)
+        comps.append(c)
+    o = oracle.Composition()
+    for _ in range(big.n_layers):
+        o.create_layer()
+
+    def load(lo, hi):
+        # the paths of layers [lo, hi) (a scene lists its paths layer by layer)
+        k = np.flatnonzero((big.path_layer >= lo) & (big.path_layer < hi))
+        k0, k1 = int(k[0]), int(k[-1]) + 1
+        assert k1 - k0 == len(k)
+        c0, c1 = int(big.cmd_offsets[k0]), int(big.cmd_offsets[k1])
+        p0, p1 = int(big.point_offsets[k0]), int(big.point_offsets[k1])
+        part = SimpleNamespace(n_paths=k1 - k0, path_layer=np.ascontiguousarray(big.path_layer[k0:k1]),
+                               cmd_offsets=np.ascontiguousarray(big.cmd_offsets[k0:k1 + 1] - np.uint64(c0)),
+                               kinds=np.ascontiguousarray(big.kinds[c0:c1]),
+                               point_offsets=np.ascontiguousarray(big.point_offsets[k0:k1 + 1] - np.uint64(p0)),
+                               points=np.ascontiguousarray(big.points[p0:p1]))
+        ids = np.arange(lo, hi, dtype=np.uint32)
+        for c in comps + [o]:
+            c.insert_paths(part)
+            c.set_layers_solid(ids, big.fill_rule[lo:hi], big.blend_mode[lo:hi], big.color[lo:hi])
+            c.set_transforms(ids, big.transforms[lo:hi], unchecked=True)
+
+    def frame(what):
+        a, b = _render(comps[0], big), _render(comps[1], big)
+        _assert_same(a, b, what)
+        ref = np.zeros_like(a)
+        o.render(ref, big.width, big.background, threads=8)
+        _assert_same(a, ref, what + " (oracle)")
+        return comps[0].stats()
+
+    load(0, few)
+    frame("few layers")
+    frame("unchanged")
+    load(few, big.n_layers)  # twenty times the layers: mostly new segments
+    st = frame("many layers added")
+    assert st["incremental_form"] >= 1
+    ids = np.arange(0, big.n_layers, 7, dtype=np.uint32)
+    t = big.transforms[ids].copy()
+    t[:, 4] += 3.25
+    for c in comps + [o]:
+        c.set_transforms(ids, t, unchecked=True)
+    frame("one layer in seven moved")
