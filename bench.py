@@ -60,6 +60,51 @@ def make_scene(name):
     return scenes.glyphs(seed=w["seed"], n_layers=w["n_layers"], width=w["width"], height=w["height"])
 
 
+def measure_frames(name, steps, warmup, local):
+    """Device time per frame of one seeded scene, replayed from its frame
+    graph (CUDA events on the library's stream), with its counts and stage
+    times: the single-frame configurations beside the headline one."""
+    import torch
+    from cassia_gb300 import Composition, scenes
+    scene = make_scene(name)
+    comp = Composition(wide=scene.wide)
+    scenes.load(scene, comp)
+    ref_segments, _ = comp.count_segments()
+    comp.set_graph_mode(True)
+    H, W = scene.height, scene.width
+    out = torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.ExternalStream(comp.stream())
+    for _ in range(warmup):
+        comp.render(out.data_ptr(), W, scene.background, height=H)
+    comp.synchronize()
+    torch.cuda.synchronize()
+    stats = []
+    with ClockSampler(local) as clk:
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(steps):
+            comp.render(out.data_ptr(), W, scene.background, height=H)
+            stats.append(comp.stats())
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    st = stats[-1]
+    comp.close()
+    config = scene_config(name, scene, 1)
+    # line records and the sorted segment arrays against the 129 MB L2
+    if st["lines"] * 52 + st["painted_segments"] * 16 < 129e6:
+        config["l2"] = "inputs within L2 (not flushed between frames)"
+    return {"metric": "Msegments/s", "value": ref_segments / (ms / 1e3) / 1e6, "unit": "Msegments/s",
+            "ms_per_step": ms, "steps": steps, "warmup": warmup, "config": config,
+            "frame_counts": {"lines": st["lines"], "segments_per_frame": ref_segments,
+                             "painted_segments": st["painted_segments"], "tile_layers": st["tile_layers"],
+                             "work_items": st["work_items"]},
+            "stage_ms": {k: statistics.mean(x[k + "_ms"] for x in stats) for k in
+                         ("build", "rasterize", "sort", "carry", "paint", "total")},
+            "sort_passes": int(st["sort_passes"]), "sort_passes_skipped": int(st["sort_passes_skipped"]),
+            "graph_replayed": int(st["graph_replayed"]), "clocks": clk.summary()}
+
+
 def over_ranks(x, op="max"):
     """x reduced over the replicas of a multi-process run ("max" for times,
     "sum" for counts); x itself without a process group.  NCCL groups reduce
@@ -747,6 +792,7 @@ def main():
                              "segments_mb": segs * 8 // 2**20},
             "frames_per_s": world * 1e3 / ms_step,
             "frame_mode": args.frame_mode, "graph_replayed": int(st.get("graph_replayed", 0)),
+            "sort_passes": int(st["sort_passes"]), "sort_passes_skipped": int(st["sort_passes_skipped"]),
             "stage_ms": stage_ms,
             "roofline": {"bound": "hbm", "kernel": STAGE_KERNELS[dom], "stage": dom, "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
@@ -766,8 +812,11 @@ def main():
     del out
     torch.cuda.empty_cache()
     if args.forms and args.workload == "mixed100k" and args.blend_mode is None:
-        # the batched (256 scenes) and served (64 clients) forms, each as a
-        # sub-object of the headline line
+        # the other single-frame configurations (the 50,000-glyph and the
+        # 1,000-circle scenes), then the batched (256 scenes) and served (64
+        # clients) forms, each as a sub-object of the headline line
+        others = {name: measure_frames(name, steps=20, warmup=3, local=local) for name in ("glyphs", "circles")}
+        torch.cuda.empty_cache()
         fa = argparse.Namespace(**vars(args))
         fa.workload, fa.steps, fa.warmup = "batch256", 3, 3
         b = run_batch(fa, rank, world, local)
@@ -776,6 +825,7 @@ def main():
         v = run_serve(fa, rank, world, local)
         torch.cuda.empty_cache()
         if rank == 0:
+            line["workloads"] = others
             line["batched"] = {k: b[k] for k in (
                 "metric", "value", "unit", "ms_per_step", "steps", "warmup", "config", "speedup_vs_plain",
                 "speedup_vs_plain_graph", "speedup_vs_plain_staged", "plain_graph_ms_per_pass",
