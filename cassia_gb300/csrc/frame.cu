@@ -184,7 +184,8 @@ cgb_status prepare_incremental(cgb_composition* c, SceneInput& in) {
             rflag[id] = 0;
         }
     };
-    if (n_ids >= 16384 && host_threads() > 1) {
+    // (each id costs a few host cache misses: 5,000 ids on one thread took 0.38 ms)
+    if (n_ids >= 1024 && host_threads() > 1) {
         const int parts = host_threads() * 2;
         const size_t chunk = (n_ids + parts - 1) / parts;
         host_parallel(parts, [&](int p) { mark(std::min(n_ids, p * chunk), std::min(n_ids, (p + 1) * chunk)); });

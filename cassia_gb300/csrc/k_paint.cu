@@ -39,6 +39,7 @@ namespace {
 constexpr int HEAD_THREADS = 256;
 constexpr int HEAD_ITEMS = 8;
 constexpr int HEAD_WARPS = HEAD_THREADS / 32;
+constexpr int TL_STAGE = 64;  // TLs per warp staged for the TL scan's writes
 
 // The cover of one segment as a packed 8 x i8 value (its row's lane).
 __device__ __forceinline__ uint64_t seg_cover(uint32_t low) {
@@ -181,21 +182,33 @@ __global__ void __launch_bounds__(HEAD_THREADS, 5) k_tl_scan(const uint64_t* __r
     const uint64_t R = stop ? r : cover_add(r, w_carry[warp]);
     const uint64_t r_next_lane = __shfl_down_sync(0xffffffffu, R, 1);
     const uint64_t cont = lane == 31 ? w_carry[warp] : r_next_lane;  // R(t + 1)
-    if (!flags) return;
     const uint32_t cap = cb.fc ? cb.tl_cap : 0xFFFFFFFFu;
-    uint32_t o = block_off[blockIdx.x] + w_sums[warp] + inc - cnt;
+    // The warp's TLs are consecutive from o0: staged in shared memory, then
+    // written by the warp together (a thread's own TLs are few and sparse
+    // across the lanes); a warp with more TLs than the stage writes directly.
+    __shared__ uint32_t st_start[HEAD_WARPS][TL_STAGE];
+    __shared__ uint64_t st_key[HEAD_WARPS][TL_STAGE], st_cover[HEAD_WARPS][TL_STAGE];
+    const uint32_t o0 = block_off[blockIdx.x] + w_sums[warp];
+    const uint32_t wn = __shfl_sync(0xffffffffu, inc, 31);  // the warp's TL count
+    const bool staged = wn <= (uint32_t)TL_STAGE;
+    uint32_t i = inc - cnt;  // the thread's first TL, counted from o0
     uint64_t acc = 0;
     int open = -1;
 #pragma unroll
     for (int k = 0; k < HEAD_ITEMS; k++) {
         if (flags & (1u << k)) {
             if (open >= 0) {
-                if (o < cap) cb.tl_cover[o] = acc;
-                o++;
+                if (staged) st_cover[warp][i] = acc;
+                else if (o0 + i < cap) cb.tl_cover[o0 + i] = acc;
+                i++;
             }
             open = k;
             acc = 0;
-            if (o < cap) {
+            if (staged) {
+                st_start[warp][i] = (uint32_t)(s0 + k);
+                st_key[warp][i] = key[k];
+            } else if (o0 + i < cap) {
+                const uint32_t o = o0 + i;
                 cb.tl_start[o] = (uint32_t)(s0 + k);
                 cb.tl_key[o] = key[k];
                 cb.tl_rec[o] = (key_run(key[k], cb.order_bits, cb.col_bits) << cb.idx_bits) | o;
@@ -203,7 +216,21 @@ __global__ void __launch_bounds__(HEAD_THREADS, 5) k_tl_scan(const uint64_t* __r
         }
         if (s0 + k < n) acc = cover_add(acc, seg_cover(low[k]));
     }
-    if (o < cap) cb.tl_cover[o] = cover_add(acc, cont);
+    if (flags) {
+        if (staged) st_cover[warp][i] = cover_add(acc, cont);
+        else if (o0 + i < cap) cb.tl_cover[o0 + i] = cover_add(acc, cont);
+    }
+    if (!staged) return;
+    __syncwarp();
+    for (uint32_t t = lane; t < wn; t += 32) {
+        const uint32_t o = o0 + t;
+        if (o >= cap) break;
+        const uint64_t k = st_key[warp][t];
+        cb.tl_start[o] = st_start[warp][t];
+        cb.tl_key[o] = k;
+        cb.tl_rec[o] = (key_run(k, cb.order_bits, cb.col_bits) << cb.idx_bits) | o;
+        cb.tl_cover[o] = st_cover[warp][t];
+    }
 }
 
 // Exclusive prefix of the cover sums along each (j, L) run, taken in the
