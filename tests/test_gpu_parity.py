@@ -339,3 +339,42 @@ def test_many_transforms_in_one_call():
     g1.render(a, sc.width, sc.background)
     g2.render(c2, sc.width, sc.background)
     _assert_same_image(c2, a)
+
+
+def test_render_many_small_tile_layer_groups():
+    # 20,000 squares of 0.4-2 px, packed on a 256x256 canvas: a group of a
+    # tile and a layer holds 2-8 segments, so many warps of the tile-layer
+    # scan hold more groups than its shared-memory stage (they write their
+    # groups directly) and others fewer; pixels and segments equal the oracle's.
+    from cassia_gb300 import Composition
+    rng = np.random.default_rng(913)
+    n, size = 20000, 256
+    g, o = Composition(), oracle.Composition()
+    for c in (g, o):
+        for _ in range(n):
+            c.create_layer()
+    x = rng.uniform(-1, size + 1, n).astype(np.float32)
+    y = rng.uniform(-1, size + 1, n).astype(np.float32)
+    s = rng.uniform(0.4, 2.0, n).astype(np.float32)
+    for i in range(n):
+        a, b, e = float(x[i]), float(y[i]), float(s[i])
+        segs = [[a, b, a + e, b], [a + e, b, a + e, b + e], [a + e, b + e, a, b + e], [a, b + e, a, b]]
+        for c in (g, o):
+            c.insert_lines(i, segs)
+    ids = np.arange(n, dtype=np.uint32)
+    fr = rng.integers(0, 2, n).astype(np.uint32)
+    bm = rng.integers(0, 12, n).astype(np.uint32)
+    col = rng.uniform(0, 1, (n, 4)).astype(np.float32)
+    col[:, 3] = rng.uniform(0.2, 1, n)
+    for c in (g, o):
+        c.set_layers_solid(ids, fr, bm, col)
+    a = np.zeros((size, size, 4), np.uint8)
+    g.render(a, size, (1.0, 1.0, 1.0, 1.0))
+    b = np.zeros_like(a)
+    o.render(b, size, (1.0, 1.0, 1.0, 1.0), threads=8)
+    assert np.array_equal(a, b)
+    st = g.stats()
+    assert st["painted_segments"] < 4 * st["tile_layers"]  # groups of a few segments
+    gs, gn = g.pixel_segments()
+    os_, on = o.pixel_segments(threads=8)
+    assert gn == on and np.array_equal(gs, os_)
