@@ -182,24 +182,21 @@ __device__ __forceinline__ uint64_t cover_add(uint64_t a, uint64_t b) {
     return ((a & ~H) + (b & ~H)) ^ ((a ^ b) & H);
 }
 __device__ __forceinline__ int32_t cover_lane(uint64_t c, int y) { return (int32_t)(int8_t)(uint8_t)(c >> (8 * y)); }
-__device__ __forceinline__ int32_t abs8(int32_t v) {  // wrapping i8 abs
-    return (int32_t)(int8_t)(uint8_t)(v < 0 ? (uint32_t)(-v) : (uint32_t)v);
-}
-// Cover::is_empty / is_full (painter/mod.rs:164-189, D2)
+// Cover::is_empty / is_full (painter/mod.rs:164-189, D2), all 8 lanes at
+// once.  A lane's wrapping |v| has its low 5 bits zero iff v is a multiple
+// of 32 and equal to 16 iff v is 16 modulo 32, since -v = v modulo 32 for
+// those values; NonZero's |v| == 16 holds iff the byte is 0x10 or 0xF0 (after
+// XOR 0x10: 0x00 or 0xE0, whose low 5 bits are zero and bits 5..7 equal).
 __device__ __forceinline__ bool cover_is_empty(uint64_t c, uint32_t fill_rule) {
     if (fill_rule == CGB_FILL_NONZERO) return c == 0;
-#pragma unroll
-    for (int y = 0; y < 8; y++)
-        if ((abs8(cover_lane(c, y)) & 31) != 0) return false;
-    return true;
+    return (c & 0x1F1F1F1F1F1F1F1Full) == 0;
 }
 __device__ __forceinline__ bool cover_is_full(uint64_t c, uint32_t fill_rule) {
-#pragma unroll
-    for (int y = 0; y < 8; y++) {
-        int32_t a = abs8(cover_lane(c, y));
-        if (fill_rule == CGB_FILL_NONZERO ? a != PIXEL_WIDTH : (a & 31) != 16) return false;
+    if (fill_rule == CGB_FILL_NONZERO) {
+        const uint64_t t = c ^ 0x1010101010101010ull;
+        return (t & 0x1F1F1F1F1F1F1F1Full) == 0 && ((t ^ (t >> 1)) & 0x6060606060606060ull) == 0;
     }
-    return true;
+    return (c & 0x1F1F1F1F1F1F1F1Full) == 0x1010101010101010ull;
 }
 
 // ---------------------------------------------------------------------------
@@ -397,9 +394,10 @@ cudaError_t launch_extract(const uint64_t* segs, const ExtractTarget* tg, uint32
                            const BatchGeom& bg, cudaStream_t st);
 
 // k_paint.cu
-// The run-record sort ranks its first two passes (the order's digits) by
-// warp ballots: consecutive TLs of a tile hold distinct, increasing orders.
-constexpr uint32_t TL_SORT_BALLOT_PASSES = 3u;
+// The run-record sort ranks its first pass (the order's low digit) by warp
+// ballots: consecutive TLs of a tile hold distinct, increasing orders, whose
+// low bits differ (their high bits repeat: match.any ranks those).
+constexpr uint32_t TL_SORT_BALLOT_PASSES = 1u;
 // TLs (tile-layer groups) are numbered in segment order, which is
 // tile-major; tl_rec lists them along the (row, order) runs that carry
 // cover from tile to tile: entry s = run << idx_bits | TL index, sorted by

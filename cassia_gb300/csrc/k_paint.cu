@@ -401,6 +401,8 @@ __global__ void k_items_count(uint32_t G, CarryBuffers cb, BatchGeom bg) {
 // block expands the items of 256 run records together: thread t writes
 // items t, t + 256, ... of the block's range.
 constexpr int IW_THREADS = 256;
+constexpr int IW_PER = 8;                      // items built per thread and chunk
+constexpr int IW_CHUNK = IW_THREADS * IW_PER;  // items per chunk
 
 __global__ void __launch_bounds__(IW_THREADS) k_items_write(uint32_t G, CarryBuffers cb, BatchGeom bg, int idx_bits) {
     __shared__ uint32_t s_off[IW_THREADS + 1];  // item offsets of the block's TLs, from its first item
@@ -427,29 +429,46 @@ __global__ void __launch_bounds__(IW_THREADS) k_items_write(uint32_t G, CarryBuf
     __syncthreads();
     const uint32_t total = s_off[nt];
     const int ob = cb.order_bits;
-    for (uint32_t idx = threadIdx.x; idx < total; idx += IW_THREADS) {
-        // the TL q with s_off[q] <= idx < s_off[q + 1] (the last one with s_off[q] <= idx)
-        uint32_t lo = 0, hi = nt;
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (s_off[mid] <= idx) lo = mid;
-            else hi = mid;
+    // Chunks of IW_CHUNK items: each thread builds IW_PER consecutive items
+    // (one search for the TL of the first, then a walk), into shared memory;
+    // the block then writes the chunk out together.
+    __shared__ uint64_t s_items[IW_CHUNK];
+    for (uint32_t c0 = 0; c0 < total; c0 += IW_CHUNK) {
+        const uint32_t cn = min((uint32_t)IW_CHUNK, total - c0);
+        const uint32_t i0 = threadIdx.x * IW_PER;
+        if (i0 < cn) {
+            uint32_t idx = c0 + i0;
+            // the TL q with s_off[q] <= idx < s_off[q + 1] (the last one with s_off[q] <= idx)
+            uint32_t lo = 0, hi = nt;
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (s_off[mid] <= idx) lo = mid;
+                else hi = mid;
+            }
+            const uint32_t iend = min(i0 + (uint32_t)IW_PER, cn);
+            for (uint32_t i = i0; i < iend; i++, idx++) {
+                while (s_off[lo + 1] <= idx) lo++;  // (past TLs without items too)
+                const uint32_t k = idx - s_off[lo];
+                const int32_t own = s_own[lo];
+                const uint32_t lf = s_lf[lo];
+                int32_t col;
+                uint32_t fl;
+                if (own >= 0 && k == 0) {
+                    col = own;
+                    fl = ITEM_OWN;
+                } else {
+                    col = s_ta[lo] + (int32_t)(k - (own >= 0 ? 1u : 0u));
+                    fl = lf & 7u;
+                }
+                const uint64_t tile = s_row[lo] + (uint64_t)col;
+                const uint64_t key = (((tile << ob) | (lf >> ITEM_FLAG_BITS)) << ITEM_FLAG_BITS) | fl;
+                s_items[i] = (key << idx_bits) | s_g[lo];
+            }
         }
-        const uint32_t k = idx - s_off[lo];
-        const int32_t own = s_own[lo];
-        const uint32_t lf = s_lf[lo];
-        int32_t col;
-        uint32_t fl;
-        if (own >= 0 && k == 0) {
-            col = own;
-            fl = ITEM_OWN;
-        } else {
-            col = s_ta[lo] + (int32_t)(k - (own >= 0 ? 1u : 0u));
-            fl = lf & 7u;
-        }
-        const uint64_t tile = s_row[lo] + (uint64_t)col;
-        const uint64_t key = (((tile << ob) | (lf >> ITEM_FLAG_BITS)) << ITEM_FLAG_BITS) | fl;
-        if (base + idx < icap) cb.items[base + idx] = (key << idx_bits) | s_g[lo];
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < cn; i += IW_THREADS)
+            if (base + c0 + i < icap) cb.items[base + c0 + i] = s_items[i];
+        __syncthreads();
     }
 }
 
