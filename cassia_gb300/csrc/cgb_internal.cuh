@@ -430,10 +430,12 @@ struct CarryBuffers {
 cudaError_t launch_tl_scan(int mode, const uint64_t* segs, uint32_t n, uint32_t* block_counts,
                            const uint32_t* block_off, const CarryBuffers& cb, cudaStream_t st);
 uint32_t tl_scan_grid(uint32_t n);
-// Also sets tl_start[G] = P.  G, P: the counts (with cb.fc, the capacities).
-cudaError_t launch_tl_carry(uint32_t G, uint32_t P, const CarryBuffers& cb, cudaStream_t st);
-cudaError_t launch_items(int mode, uint32_t G, const BatchGeom& bg, const CarryBuffers& cb, int idx_bits,
-                         cudaStream_t st);
+// Carries along the sorted run records and each record's work-item count
+// (cb.item_count); also sets tl_start[G] = P.  G, P: the counts (with cb.fc,
+// the capacities).
+cudaError_t launch_tl_carry(uint32_t G, uint32_t P, const CarryBuffers& cb, const BatchGeom& bg, cudaStream_t st);
+// The work items at cb.item_off (the scan of cb.item_count).
+cudaError_t launch_items(uint32_t G, const BatchGeom& bg, const CarryBuffers& cb, int idx_bits, cudaStream_t st);
 cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_tiles, int tile_shift,
                                uint32_t* tile_start, cudaStream_t st, FrameCounts* fc = nullptr);
 // full: some scene of the frame has gradient fills or clips (selects the

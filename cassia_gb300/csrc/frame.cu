@@ -510,8 +510,7 @@ cgb_status staged_frame(cgb_composition* c, const FrameSetup& f, std::vector<Sce
     CK(radix_sort_u64(cb.tl_rec, c->tl_rec_b.as<uint64_t>(), (uint32_t)G, sort_bits(idx_bits, idx_bits + run_bits),
                       (int)c->tuning.radix_bits, &c->s, c->err.as<uint32_t>(), st, &cb.tl_rec, nullptr, false, nullptr,
                       0, TL_SORT_BALLOT_PASSES));
-    CK(launch_tl_carry((uint32_t)G, (uint32_t)P, cb, st));
-    CK(launch_items(0, (uint32_t)G, bg, cb, 0, st));
+    CK(launch_tl_carry((uint32_t)G, (uint32_t)P, cb, bg, st));
     uint64_t W = 0;
     if (G) CK(scan_u32(cb.item_count, cb.item_off, (uint32_t)G, &c->s, st, &W));
     c->stats.work_items = W;
@@ -525,7 +524,7 @@ cgb_status staged_frame(cgb_composition* c, const FrameSetup& f, std::vector<Sce
     cb.items = c->items_a.as<uint64_t>();
     cb.items_tmp = c->items_b.as<uint64_t>();
     cb.tile_start = c->tile_start.as<uint32_t>();
-    CK(launch_items(1, (uint32_t)G, bg, cb, idx_bits, st));
+    CK(launch_items((uint32_t)G, bg, cb, idx_bits, st));
     uint64_t* items_sorted = cb.items;
     int ipasses = 0;
     // stable sort on the tile field: each tile's items stay in order
@@ -704,13 +703,12 @@ cgb_status enqueue_counted_tail(cgb_composition* c, const FrameSetup& f, const F
     CK(launch_tl_scan(1, sorted, k.segs, nullptr, c->boff.as<uint32_t>(), cb, st));
     CK(radix_sort_u64(cb.tl_rec, c->tl_rec_b.as<uint64_t>(), k.tls, sort_bits(idx_bits, idx_bits + run_bits), rbits,
                       &c->s, err, st, &cb.tl_rec, nullptr, false, fc, FC_TLS, TL_SORT_BALLOT_PASSES));
-    CK(launch_tl_carry(k.tls, k.segs, cb, st));
-    CK(launch_items(0, k.tls, bg, cb, 0, st));
+    CK(launch_tl_carry(k.tls, k.segs, cb, bg, st));
     CK(scan_u32(cb.item_count, cb.item_off, k.tls, &c->s, st, nullptr, &fc->n[FC_ITEMS]));
     const int tile_bits = bits_for(std::max<uint64_t>(f.tiles, 1) - 1);
     const int tile_shift = idx_bits + 3 + cb.order_bits;
     if (tile_shift + tile_bits > 64) return fail(CGB_ERR_LAYER_LIMIT, "render: frame graph item key too wide");
-    CK(launch_items(1, k.tls, bg, cb, idx_bits, st));
+    CK(launch_items(k.tls, bg, cb, idx_bits, st));
     uint64_t* items_sorted = nullptr;
     int ipasses = 0;
     CK(radix_sort_u64(cb.items, cb.items_tmp, k.items, sort_bits(tile_shift, tile_shift + tile_bits), rbits, &c->s,

@@ -233,6 +233,84 @@ __global__ void __launch_bounds__(HEAD_THREADS, 5) k_tl_scan(const uint64_t* __r
     }
 }
 
+// Work-item payload bits above the TL index: the item holds only a cover carry;
+// its layer is full in the tile; and it is also an opaque Solid Over layer.
+constexpr uint32_t ITEM_OWN = 0u;
+constexpr uint32_t ITEM_OPAQUE = 1u;
+constexpr uint32_t ITEM_FULL = 2u;
+constexpr uint32_t ITEM_CARRY = 4u;
+constexpr int ITEM_FLAG_BITS = 3;
+
+// The work items of TL g: its own (tile, order) pair, when its tile is
+// painted, and cover-carry-only items for the tiles [ta, tb) of its row, up
+// to the next TL of its (row, order) run.
+struct TlItems {
+    uint64_t row_tile;  // global index of the first tile of the TL's row
+    int32_t own;        // tile column of the own item, or -1
+    int32_t ta, tb;     // the carry-only items' tile columns (none if ta >= tb)
+    uint32_t flags;     // the carry-only items' flags
+    uint32_t L;
+    uint32_t g;         // the TL (its index in segment order)
+    __device__ __forceinline__ uint32_t count() const {
+        return (own >= 0 ? 1u : 0u) + (tb > ta ? (uint32_t)(tb - ta) : 0u);
+    }
+};
+
+// The work items of TL g, of key `key` and leaving cover `carry_out`;
+// next_col: the column of the next TL of its run, or -1 at the run's end.
+__device__ __forceinline__ TlItems tl_items_of(uint32_t g, uint64_t key, uint64_t carry_out, int32_t next_col,
+                                               const BatchGeom& bg) {
+    TlItems r{0, -1, 0, 0, 0, 0, 0};
+    r.g = g;
+    const int32_t i = (int32_t)key_col1(key, bg.order_bits, bg.col_bits) - 1;
+    const uint32_t L = key_order(key, bg.order_bits);
+    const uint32_t grow = key_row(key, bg.order_bits, bg.col_bits);
+    // fields out of range only come from a sort that gave up (its error
+    // flag is reported after the frame): no items rather than a stray access
+    if (grow >= bg.total_rows) return r;
+    const SceneDesc& S = bg.scenes[bg.row_scene[grow]];
+    const uint32_t j = grow - S.row_base;
+    if (j < S.crop_v0 || j >= S.crop_v1 || L >= S.n_orders) return r;
+    r.L = L;
+    r.row_tile = (uint64_t)S.tile_base + (uint64_t)j * S.row_len;
+    int32_t next = next_col >= 0 ? next_col : (int32_t)S.row_len;
+    const int32_t h0 = (int32_t)S.crop_h0, h1 = (int32_t)S.crop_h1;
+    if (next > h1) next = h1;
+    if (i >= h0 && i < h1) r.own = i;  // a layer with segments is never "full" (layer_workbench.rs:164-175)
+    if (next <= i + 1) return r;
+    const PaintProps pp = S.props[L];
+    const bool nonempty = !cover_is_empty(carry_out, pp.fill_rule);
+    // payload of a cover-carry-only item: its layer_is_full and the opaque
+    // Solid Over test of skip_fully_covered_layers (:335-356)
+    const bool full = cover_is_full(carry_out, pp.fill_rule);
+    r.flags = ITEM_CARRY | (full ? ITEM_FULL : 0u) | (full && (pp.flags & PROPS_OPAQUE_OVER) ? ITEM_OPAQUE : 0u);
+    if (i < h0) {
+        // the first painted tile of the row holds every layer with segments
+        // to its left, empty or not
+        if (next <= h0) return r;
+        r.ta = h0;
+        r.tb = nonempty ? next : h0 + 1;
+        return r;
+    }
+    if (nonempty) {
+        r.ta = i + 1;
+        r.tb = next;
+    }
+    return r;
+}
+
+// The work items of the TL at position s of the sorted run records.
+__device__ __forceinline__ TlItems tl_items(uint32_t s, uint32_t G, const CarryBuffers& cb, const BatchGeom& bg) {
+    const int ib = cb.idx_bits;
+    const uint64_t rec = cb.tl_rec[s];
+    const uint32_t g = (uint32_t)(rec & ((1ull << ib) - 1));
+    if (g >= G) return TlItems{0, -1, 0, 0, 0, 0, 0};
+    int32_t next_col = -1;
+    if (s + 1 < G && (cb.tl_rec[s + 1] >> ib) == (rec >> ib))
+        next_col = (int32_t)key_col1(cb.tl_skey[s + 1], bg.order_bits, bg.col_bits) - 1;
+    return tl_items_of(g, cb.tl_skey[s], cb.tl_sout[s], next_col, bg);
+}
+
 // Exclusive prefix of the cover sums along each (j, L) run, taken in the
 // sorted run records (runs are a layer's tile groups in one tile row, left
 // to right): one thread per record, a segmented scan across the warp, and
@@ -240,14 +318,18 @@ __global__ void __launch_bounds__(HEAD_THREADS, 5) k_tl_scan(const uint64_t* __r
 // taken 32 at a time by the warp.  Each TL's entering cover goes to the
 // TL's own index, where the painter reads it; the key and the leaving cover
 // go to the record's position (tl_skey, tl_sout), where the item expansion
-// reads them in sequence.  Thread 0 also closes the TL segment ranges:
+// reads them in sequence, and each record's count of work items (TlItems)
+// goes to item_count.  Thread 0 also closes the TL segment ranges:
 // tl_start[G] = P.
-__global__ void __launch_bounds__(256) k_tl_carry(uint32_t G, uint32_t P, CarryBuffers cb) {
+__global__ void __launch_bounds__(256) k_tl_carry(uint32_t G, uint32_t P, CarryBuffers cb, BatchGeom bg) {
+    const uint32_t Gcap = G;
     G = fc_count(cb.fc, FC_TLS, G, blockIdx.x == 0 && threadIdx.x == 0);
     P = fc_count(cb.fc, FC_SEGS, P, false);
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     if (s == 0) cb.tl_start[G] = P;
+    // graph frames: the item counts past the device count stay zero for the scan over the capacity
+    if (s >= G && s < Gcap) cb.item_count[s] = 0;
     const uint32_t s0 = s - lane;  // the warp's first record
     if (s0 >= G) return;           // (whole warps only: the shuffles below take every lane)
     const int ib = cb.idx_bits;
@@ -307,91 +389,27 @@ __global__ void __launch_bounds__(256) k_tl_carry(uint32_t G, uint32_t P, CarryB
     const uint64_t incl_prev = __shfl_up_sync(0xffffffffu, incl, 1);
     uint64_t carry = (head || lane == 0) ? 0 : incl_prev;
     if (!f && !head) carry = cover_add(carry, pre);  // still in the warp's open run
+    // the run's next TL: the next lane's, or (last lane) loaded
+    const uint64_t next_run = __shfl_down_sync(0xffffffffu, run, 1);
+    uint64_t next_key = __shfl_down_sync(0xffffffffu, key, 1);
+    bool more = lane < 31 ? next_run == run : false;
+    if (lane == 31 && valid && s + 1 < G) {
+        const uint64_t r = cb.tl_rec[s + 1];
+        const uint64_t ng = r & mask;
+        more = (r >> ib) == run && ng < G;
+        if (more) next_key = cb.tl_key[ng];
+    }
     if (!valid) return;
+    const uint64_t out = cover_add(carry, cov);
     if (g < G) cb.tl_carry[g] = carry;
     cb.tl_skey[s] = key;
-    cb.tl_sout[s] = cover_add(carry, cov);
-}
-
-// Work-item payload bits above the TL index: the item holds only a cover carry;
-// its layer is full in the tile; and it is also an opaque Solid Over layer.
-constexpr uint32_t ITEM_OWN = 0u;
-constexpr uint32_t ITEM_OPAQUE = 1u;
-constexpr uint32_t ITEM_FULL = 2u;
-constexpr uint32_t ITEM_CARRY = 4u;
-constexpr int ITEM_FLAG_BITS = 3;
-
-// The work items of TL g: its own (tile, order) pair, when its tile is
-// painted, and cover-carry-only items for the tiles [ta, tb) of its row, up
-// to the next TL of its (row, order) run.
-struct TlItems {
-    uint64_t row_tile;  // global index of the first tile of the TL's row
-    int32_t own;        // tile column of the own item, or -1
-    int32_t ta, tb;     // the carry-only items' tile columns (none if ta >= tb)
-    uint32_t flags;     // the carry-only items' flags
-    uint32_t L;
-    uint32_t g;         // the TL (its index in segment order)
-    __device__ __forceinline__ uint32_t count() const {
-        return (own >= 0 ? 1u : 0u) + (tb > ta ? (uint32_t)(tb - ta) : 0u);
+    cb.tl_sout[s] = out;
+    uint32_t items = 0;
+    if (g < G) {
+        const int32_t next_col = more ? (int32_t)key_col1(next_key, bg.order_bits, bg.col_bits) - 1 : -1;
+        items = tl_items_of(g, key, out, next_col, bg).count();
     }
-};
-
-// s: the TL's position in the sorted run records.
-__device__ __forceinline__ TlItems tl_items(uint32_t s, uint32_t G, const CarryBuffers& cb, const BatchGeom& bg) {
-    TlItems r{0, -1, 0, 0, 0, 0, 0};
-    const int ib = cb.idx_bits;
-    const uint64_t rec = cb.tl_rec[s];
-    const uint32_t g = (uint32_t)(rec & ((1ull << ib) - 1));
-    // fields out of range only come from a sort that gave up (its error
-    // flag is reported after the frame): no items rather than a stray access
-    if (g >= G) return r;
-    r.g = g;
-    const uint64_t key = cb.tl_skey[s];
-    const int32_t i = (int32_t)key_col1(key, bg.order_bits, bg.col_bits) - 1;
-    const uint32_t L = key_order(key, bg.order_bits);
-    const uint32_t grow = key_row(key, bg.order_bits, bg.col_bits);
-    if (grow >= bg.total_rows) return r;
-    const SceneDesc& S = bg.scenes[bg.row_scene[grow]];
-    const uint32_t j = grow - S.row_base;
-    if (j < S.crop_v0 || j >= S.crop_v1 || L >= S.n_orders) return r;
-    r.L = L;
-    r.row_tile = (uint64_t)S.tile_base + (uint64_t)j * S.row_len;
-    int32_t next = (int32_t)S.row_len;  // the column of the run's next TL
-    if (s + 1 < G && (cb.tl_rec[s + 1] >> ib) == (rec >> ib))
-        next = (int32_t)key_col1(cb.tl_skey[s + 1], bg.order_bits, bg.col_bits) - 1;
-    const int32_t h0 = (int32_t)S.crop_h0, h1 = (int32_t)S.crop_h1;
-    if (next > h1) next = h1;
-    if (i >= h0 && i < h1) r.own = i;  // a layer with segments is never "full" (layer_workbench.rs:164-175)
-    if (next <= i + 1) return r;
-    const uint64_t carry_out = cb.tl_sout[s];
-    const PaintProps pp = S.props[L];
-    const bool nonempty = !cover_is_empty(carry_out, pp.fill_rule);
-    // payload of a cover-carry-only item: its layer_is_full and the opaque
-    // Solid Over test of skip_fully_covered_layers (:335-356)
-    const bool full = cover_is_full(carry_out, pp.fill_rule);
-    r.flags = ITEM_CARRY | (full ? ITEM_FULL : 0u) | (full && (pp.flags & PROPS_OPAQUE_OVER) ? ITEM_OPAQUE : 0u);
-    if (i < h0) {
-        // the first painted tile of the row holds every layer with segments
-        // to its left, empty or not
-        if (next <= h0) return r;
-        r.ta = h0;
-        r.tb = nonempty ? next : h0 + 1;
-        return r;
-    }
-    if (nonempty) {
-        r.ta = i + 1;
-        r.tb = next;
-    }
-    return r;
-}
-
-// G: the TL count, or with cb.fc the TL capacity (the entries past the
-// device count are zeroed for the scan over the capacity).
-__global__ void k_items_count(uint32_t G, CarryBuffers cb, BatchGeom bg) {
-    const uint32_t Gd = fc_count(cb.fc, FC_TLS, G, false);
-    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= G) return;
-    cb.item_count[g] = g < Gd ? tl_items(g, Gd, cb, bg).count() : 0u;
+    cb.item_count[s] = items;
 }
 
 // Item = tile | order | flags | TL index, high to low; the tile field is the
@@ -1355,20 +1373,16 @@ cudaError_t launch_tl_scan(int mode, const uint64_t* segs, uint32_t n, uint32_t*
 
 uint32_t tl_scan_grid(uint32_t n) { return (n + HEAD_THREADS * HEAD_ITEMS - 1) / (HEAD_THREADS * HEAD_ITEMS); }
 
-cudaError_t launch_tl_carry(uint32_t G, uint32_t P, const CarryBuffers& cb, cudaStream_t st) {
+cudaError_t launch_tl_carry(uint32_t G, uint32_t P, const CarryBuffers& cb, const BatchGeom& bg, cudaStream_t st) {
     count_launches(1);
-    k_tl_carry<<<std::max<uint32_t>(1, (G + 255) / 256), 256, 0, st>>>(G, P, cb);
+    k_tl_carry<<<std::max<uint32_t>(1, (G + 255) / 256), 256, 0, st>>>(G, P, cb, bg);
     return cudaGetLastError();
 }
 
-cudaError_t launch_items(int mode, uint32_t G, const BatchGeom& bg, const CarryBuffers& cb, int idx_bits,
-                         cudaStream_t st) {
+cudaError_t launch_items(uint32_t G, const BatchGeom& bg, const CarryBuffers& cb, int idx_bits, cudaStream_t st) {
     if (G == 0) return cudaSuccess;
     count_launches(1);
-    if (mode == 0)
-        k_items_count<<<(G + 255) / 256, 256, 0, st>>>(G, cb, bg);
-    else
-        k_items_write<<<(G + IW_THREADS - 1) / IW_THREADS, IW_THREADS, 0, st>>>(G, cb, bg, idx_bits);
+    k_items_write<<<(G + IW_THREADS - 1) / IW_THREADS, IW_THREADS, 0, st>>>(G, cb, bg, idx_bits);
     return cudaGetLastError();
 }
 
