@@ -490,14 +490,33 @@ __global__ void __launch_bounds__(IW_THREADS) k_items_write(uint32_t G, CarryBuf
     }
 }
 
+// tile_start from the items sorted by tile: each thread takes TR_ITEMS
+// consecutive items (two 16-byte loads) and writes the start of every tile
+// from the one before its first item's up to each item's tile.
+constexpr int TR_ITEMS = 4;
 __global__ void k_tile_ranges(const uint64_t* __restrict__ items, uint32_t W, uint32_t n_tiles, int tile_shift,
                               uint32_t* __restrict__ tile_start, FrameCounts* fc) {
     W = fc_count(fc, FC_ITEMS, W, blockIdx.x == 0 && threadIdx.x == 0);
-    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k > W) return;
-    int64_t cur = k < W ? (int64_t)min(items[k] >> tile_shift, (uint64_t)n_tiles) : (int64_t)n_tiles;
-    int64_t prev = k > 0 ? (int64_t)min(items[k - 1] >> tile_shift, (uint64_t)n_tiles) : -1;
-    for (int64_t t = prev + 1; t <= cur; t++) tile_start[t] = k;
+    const uint64_t k0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * TR_ITEMS;
+    if (k0 > W) return;
+    uint64_t v[TR_ITEMS];
+    if (k0 + TR_ITEMS <= W) {
+        const ulonglong2* p2 = reinterpret_cast<const ulonglong2*>(items + k0);
+        const ulonglong2 a = p2[0], b = p2[1];
+        v[0] = a.x, v[1] = a.y, v[2] = b.x, v[3] = b.y;
+    } else {
+#pragma unroll
+        for (int j = 0; j < TR_ITEMS; j++) v[j] = k0 + j < W ? items[k0 + j] : 0;
+    }
+    int64_t prev = k0 > 0 ? (int64_t)min(items[k0 - 1] >> tile_shift, (uint64_t)n_tiles) : -1;
+#pragma unroll
+    for (int j = 0; j < TR_ITEMS; j++) {
+        const uint64_t k = k0 + j;
+        if (k > W) break;
+        const int64_t cur = k < W ? (int64_t)min(v[j] >> tile_shift, (uint64_t)n_tiles) : (int64_t)n_tiles;
+        for (int64_t t = prev + 1; t <= cur; t++) tile_start[t] = (uint32_t)k;
+        prev = cur;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1389,7 +1408,8 @@ cudaError_t launch_items(uint32_t G, const BatchGeom& bg, const CarryBuffers& cb
 cudaError_t launch_tile_ranges(const uint64_t* items, uint32_t W, uint32_t n_tiles, int tile_shift,
                                uint32_t* tile_start, cudaStream_t st, FrameCounts* fc) {
     count_launches(1);
-    k_tile_ranges<<<(W + 1 + 255) / 256, 256, 0, st>>>(items, W, n_tiles, tile_shift, tile_start, fc);
+    k_tile_ranges<<<(W + 1 + 256 * TR_ITEMS - 1) / (256 * TR_ITEMS), 256, 0, st>>>(items, W, n_tiles, tile_shift,
+                                                                                   tile_start, fc);
     return cudaGetLastError();
 }
 
