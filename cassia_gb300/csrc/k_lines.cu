@@ -544,19 +544,34 @@ __device__ __forceinline__ uint32_t find_line(const uint32_t* __restrict__ off, 
 // steps per block): each line with steps [a, e) records itself for the blocks
 // whose first or last step lies in it.  block_lines[b] = first line of block
 // b, block_lines[nb + 1 + b] = its last line, for the nb blocks of the count.
+constexpr int BL_LINES = 4;  // lines per thread of k_block_lines (one 16-byte load of their offsets)
 __global__ void k_block_lines(const uint32_t* __restrict__ off, uint32_t n_lines, uint64_t n_steps,
                               uint32_t per_block, uint32_t* __restrict__ block_lines, uint32_t cap_blocks,
                               FrameCounts* fc) {
     if (fc) n_steps = fc_count(fc, FC_STEPS, (uint32_t)n_steps, false);
     const uint32_t nb = (uint32_t)((n_steps + per_block - 1) / per_block);
-    const uint32_t l = blockIdx.x * blockDim.x + threadIdx.x;
-    if (l >= n_lines) return;
-    const uint32_t a = off[l], e = off[l + 1];
-    if (a >= e) return;
-    for (uint32_t b = a / per_block; b < nb && (uint64_t)b * per_block < e; b++) {
-        if ((uint64_t)b * per_block >= a) block_lines[b] = l;
-        const uint64_t last = min((uint64_t)(b + 1) * per_block, n_steps) - 1;
-        if (last >= a && last < e) block_lines[cap_blocks + 1 + b] = l;
+    const uint64_t l0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * BL_LINES;
+    if (l0 >= n_lines) return;
+    uint32_t o[BL_LINES + 1];
+    if (l0 + BL_LINES <= n_lines) {
+        const uint4 v = *reinterpret_cast<const uint4*>(off + l0);
+        o[0] = v.x, o[1] = v.y, o[2] = v.z, o[3] = v.w;
+        o[BL_LINES] = off[l0 + BL_LINES];
+    } else {
+#pragma unroll
+        for (int j = 0; j <= BL_LINES; j++) o[j] = l0 + j <= n_lines ? off[l0 + j] : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < BL_LINES; j++) {
+        const uint32_t l = (uint32_t)l0 + j;
+        if (l >= n_lines) break;
+        const uint32_t a = o[j], e = o[j + 1];
+        if (a >= e) continue;
+        for (uint32_t b = a / per_block; b < nb && (uint64_t)b * per_block < e; b++) {
+            if ((uint64_t)b * per_block >= a) block_lines[b] = l;
+            const uint64_t last = min((uint64_t)(b + 1) * per_block, n_steps) - 1;
+            if (last >= a && last < e) block_lines[cap_blocks + 1 + b] = l;
+        }
     }
 }
 
@@ -866,8 +881,8 @@ cudaError_t launch_rasterize(int render, const BatchGeom& bg, const LineRec* rec
     const size_t smem = (size_t)raster_run_slots(block, items) * sizeof(uint64_t);
     count_launches(2);
     if (n_lines > 0)
-        k_block_lines<<<(n_lines + 255) / 256, 256, 0, st>>>(step_off, n_lines, n_steps, block * items, block_lines,
-                                                               grid, fc);
+        k_block_lines<<<(n_lines + 256 * BL_LINES - 1) / (256 * BL_LINES), 256, 0, st>>>(
+            step_off, n_lines, n_steps, block * items, block_lines, grid, fc);
 #define CGB_RASTER(R, I, S)                                                                                   \
     k_rasterize<R, I, S><<<grid, block, smem, st>>>(recs, step_off, n_lines, n_steps, bg, runs, run_count, produced, \
                                                     fc, block_lines)
