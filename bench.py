@@ -445,7 +445,8 @@ def run_batch(args, rank, world, local):
     def batched_host():  # page-locked host buffers, written by the painter directly
         render_groups(ctxs, host, with_heights=False, mapped=True)
 
-    batched_host()
+    for _ in range(args.warmup):
+        batched_host()
     te = timed(batched_host, max(1, args.steps // 2))
     if rank == 0:
         line = {
@@ -701,14 +702,15 @@ def main():
         tr[1][:, 4] += np.float32(0.25)
         # the frame goes to page-locked host memory that the painter writes
         # directly (CGB_MEMORY_HOST_MAPPED): no device staging and copy back
-        comp.set_transforms(ids, tr[0])
-        comp.render(host_img, W, scene.background, mapped=True)
+        for k in range(args.warmup):
+            comp.set_transforms(ids, tr[k % 2])
+            comp.render(host_img, W, scene.background, mapped=True)
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
         t0 = time.perf_counter()
         for k in range(args.e2e_steps):
-            comp.set_transforms(ids, tr[(k + 1) % 2])
+            comp.set_transforms(ids, tr[(args.warmup + k) % 2])
             comp.render(host_img, W, scene.background, mapped=True)
         torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t0) / args.e2e_steps
