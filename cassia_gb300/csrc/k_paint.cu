@@ -114,11 +114,48 @@ __global__ void __launch_bounds__(HEAD_THREADS, 5) k_tl_scan(const uint64_t* __r
             prev = key[k];
         }
     }
-    // pre(t): covers before the thread's first head (all of them without one)
-    uint64_t pre = 0;
+    // TL counts: inclusive scan within the warp
+    uint32_t inc = cnt;
 #pragma unroll
-    for (int k = 0; k < HEAD_ITEMS; k++)
-        if ((flags & ((2u << k) - 1)) == 0) pre = cover_add(pre, seg_cover(low[k]));
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t a = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += a;
+    }
+    // mode 1: the warp's TLs are consecutive from its first: staged in shared
+    // memory and written by the warp together after the scans (a thread's own
+    // TLs are few and sparse across the lanes); a warp with more TLs than the
+    // stage writes them directly once its offset is known.
+    __shared__ uint32_t st_start[HEAD_WARPS][TL_STAGE];
+    __shared__ uint64_t st_key[HEAD_WARPS][TL_STAGE], st_cover[HEAD_WARPS][TL_STAGE];
+    const uint32_t wn = __shfl_sync(0xffffffffu, inc, 31);  // the warp's TL count
+    const bool staged = mode == 1 && wn <= (uint32_t)TL_STAGE;
+    // pre(t): covers before the thread's first head (all of them without
+    // one); staged: acc = covers since its last head, whose cover is closed
+    // once the following covers are known
+    uint64_t pre = 0, acc = 0;
+    uint32_t last = 0;  // staged: the stage index of the thread's last TL
+    if (staged) {
+        uint32_t i = inc - cnt;
+        bool open = false;
+#pragma unroll
+        for (int k = 0; k < HEAD_ITEMS; k++) {
+            if (flags & (1u << k)) {
+                if (open) st_cover[warp][i++] = acc;
+                else pre = acc;
+                open = true;
+                acc = 0;
+                st_start[warp][i] = (uint32_t)(s0 + k);
+                st_key[warp][i] = key[k];
+            }
+            if (s0 + k < n) acc = cover_add(acc, seg_cover(low[k]));
+        }
+        if (!open) pre = acc;
+        last = i;
+    } else {
+#pragma unroll
+        for (int k = 0; k < HEAD_ITEMS; k++)
+            if ((flags & ((2u << k) - 1)) == 0) pre = cover_add(pre, seg_cover(low[k]));
+    }
 
     // reverse segmented scan of (pre, has head) within the warp
     uint64_t r = pre;
@@ -131,13 +168,6 @@ __global__ void __launch_bounds__(HEAD_THREADS, 5) k_tl_scan(const uint64_t* __r
             r = cover_add(r, nr);
             stop = ns;
         }
-    }
-    // TL counts: inclusive scan within the warp
-    uint32_t inc = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t a = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += a;
     }
     __shared__ uint64_t w_r[HEAD_WARPS], w_carry[HEAD_WARPS];
     __shared__ uint32_t w_stop[HEAD_WARPS], w_sums[HEAD_WARPS];
@@ -183,44 +213,33 @@ __global__ void __launch_bounds__(HEAD_THREADS, 5) k_tl_scan(const uint64_t* __r
     const uint64_t r_next_lane = __shfl_down_sync(0xffffffffu, R, 1);
     const uint64_t cont = lane == 31 ? w_carry[warp] : r_next_lane;  // R(t + 1)
     const uint32_t cap = cb.fc ? cb.tl_cap : 0xFFFFFFFFu;
-    // The warp's TLs are consecutive from o0: staged in shared memory, then
-    // written by the warp together (a thread's own TLs are few and sparse
-    // across the lanes); a warp with more TLs than the stage writes directly.
-    __shared__ uint32_t st_start[HEAD_WARPS][TL_STAGE];
-    __shared__ uint64_t st_key[HEAD_WARPS][TL_STAGE], st_cover[HEAD_WARPS][TL_STAGE];
     const uint32_t o0 = block_off[blockIdx.x] + w_sums[warp];
-    const uint32_t wn = __shfl_sync(0xffffffffu, inc, 31);  // the warp's TL count
-    const bool staged = wn <= (uint32_t)TL_STAGE;
-    uint32_t i = inc - cnt;  // the thread's first TL, counted from o0
-    uint64_t acc = 0;
-    int open = -1;
+    if (!staged) {
+        // the thread's TLs from o0 + its first, written directly
+        uint32_t i = inc - cnt;
+        bool open = false;
 #pragma unroll
-    for (int k = 0; k < HEAD_ITEMS; k++) {
-        if (flags & (1u << k)) {
-            if (open >= 0) {
-                if (staged) st_cover[warp][i] = acc;
-                else if (o0 + i < cap) cb.tl_cover[o0 + i] = acc;
-                i++;
+        for (int k = 0; k < HEAD_ITEMS; k++) {
+            if (flags & (1u << k)) {
+                if (open) {
+                    if (o0 + i < cap) cb.tl_cover[o0 + i] = acc;
+                    i++;
+                }
+                open = true;
+                acc = 0;
+                if (o0 + i < cap) {
+                    const uint32_t o = o0 + i;
+                    cb.tl_start[o] = (uint32_t)(s0 + k);
+                    cb.tl_key[o] = key[k];
+                    cb.tl_rec[o] = (key_run(key[k], cb.order_bits, cb.col_bits) << cb.idx_bits) | o;
+                }
             }
-            open = k;
-            acc = 0;
-            if (staged) {
-                st_start[warp][i] = (uint32_t)(s0 + k);
-                st_key[warp][i] = key[k];
-            } else if (o0 + i < cap) {
-                const uint32_t o = o0 + i;
-                cb.tl_start[o] = (uint32_t)(s0 + k);
-                cb.tl_key[o] = key[k];
-                cb.tl_rec[o] = (key_run(key[k], cb.order_bits, cb.col_bits) << cb.idx_bits) | o;
-            }
+            if (s0 + k < n) acc = cover_add(acc, seg_cover(low[k]));
         }
-        if (s0 + k < n) acc = cover_add(acc, seg_cover(low[k]));
+        if (flags && o0 + i < cap) cb.tl_cover[o0 + i] = cover_add(acc, cont);
+        return;
     }
-    if (flags) {
-        if (staged) st_cover[warp][i] = cover_add(acc, cont);
-        else if (o0 + i < cap) cb.tl_cover[o0 + i] = cover_add(acc, cont);
-    }
-    if (!staged) return;
+    if (flags) st_cover[warp][last] = cover_add(acc, cont);
     __syncwarp();
     for (uint32_t t = lane; t < wn; t += 32) {
         const uint32_t o = o0 + t;
