@@ -287,7 +287,8 @@ __device__ __forceinline__ TlItems tl_items_of(uint32_t g, uint64_t key, uint64_
     // fields out of range only come from a sort that gave up (its error
     // flag is reported after the frame): no items rather than a stray access
     if (grow >= bg.total_rows) return r;
-    const SceneDesc& S = bg.scenes[bg.row_scene[grow]];
+    // (one scene: no row-to-scene lookup on the way to the scene's fields)
+    const SceneDesc& S = bg.scenes[bg.n_scenes == 1 ? 0u : bg.row_scene[grow]];
     const uint32_t j = grow - S.row_base;
     if (j < S.crop_v0 || j >= S.crop_v1 || L >= S.n_orders) return r;
     r.L = L;
@@ -321,13 +322,18 @@ __device__ __forceinline__ TlItems tl_items_of(uint32_t g, uint64_t key, uint64_
 // The work items of the TL at position s of the sorted run records.
 __device__ __forceinline__ TlItems tl_items(uint32_t s, uint32_t G, const CarryBuffers& cb, const BatchGeom& bg) {
     const int ib = cb.idx_bits;
+    // every load issued before any is used (the next record's key whether or
+    // not it continues the run)
+    const bool has_next = s + 1 < G;
     const uint64_t rec = cb.tl_rec[s];
+    const uint64_t rec1 = has_next ? cb.tl_rec[s + 1] : 0;
+    const uint64_t key1 = has_next ? cb.tl_skey[s + 1] : 0;
+    const uint64_t key = cb.tl_skey[s], sout = cb.tl_sout[s];
     const uint32_t g = (uint32_t)(rec & ((1ull << ib) - 1));
     if (g >= G) return TlItems{0, -1, 0, 0, 0, 0, 0};
     int32_t next_col = -1;
-    if (s + 1 < G && (cb.tl_rec[s + 1] >> ib) == (rec >> ib))
-        next_col = (int32_t)key_col1(cb.tl_skey[s + 1], bg.order_bits, bg.col_bits) - 1;
-    return tl_items_of(g, cb.tl_skey[s], cb.tl_sout[s], next_col, bg);
+    if (has_next && (rec1 >> ib) == (rec >> ib)) next_col = (int32_t)key_col1(key1, bg.order_bits, bg.col_bits) - 1;
+    return tl_items_of(g, key, sout, next_col, bg);
 }
 
 // Exclusive prefix of the cover sums along each (j, L) run, taken in the
