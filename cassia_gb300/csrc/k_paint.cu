@@ -1277,7 +1277,10 @@ __global__ void __launch_bounds__(PAINT_WARPS * 32) k_paint(PaintArgs a) {
             const uint32_t n = min(32u, e - c0);
             stage_items<FULL>(a, p, S, c0, n, lane, true);
             for (uint32_t q = 0; q < n; q++) {
-                const uint32_t meta = S.meta[q];
+                // every lane reads the same word; the warp reduction makes
+                // that visible to the compiler (a uniform value), so the
+                // item's branches need no convergence barriers
+                const uint32_t meta = __reduce_or_sync(0xffffffffu, S.meta[q]);
                 const uint32_t mode = meta & 15u, fr = (meta >> 4) & 1u;
                 bool apply = false;
                 if (clips) {
